@@ -1,0 +1,199 @@
+"""CPU oracle for the discovery-barrier graph path -- TEST INFRASTRUCTURE.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline legs may
+import this package, as the checker (or as the timed CPU baseline).  The
+product path never does.
+
+* ``oracle.c`` restates each reference kernel in plain C (citations inside).
+* ``refshim/`` compiles the reference's own OpenCL C kernels as C++ into
+  ``_ref/libgdbref.so`` where the reference checkout exists, to pin the
+  restatement (tests/test_oracle_golden.py, tests/golden/make_golden.py).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LONESTAR_INF = 1_000_000_000
+PANNOTIA_BIG = 99_999_999
+
+_u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+
+_ORC = None
+_REF = None
+
+
+def _nz(a: np.ndarray, dtype=np.uint32) -> np.ndarray:
+    """ctypes needs a non-empty buffer even for E == 0."""
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a if a.size else np.zeros(1, dtype=dtype)
+
+
+def lib() -> C.CDLL:
+    global _ORC
+    if _ORC is None:
+        path = HERE / "_build" / "liboracle.so"
+        if not path.exists():
+            import sys
+            sys.path.insert(0, str(HERE.parent))
+            from gpu_discovery_barrier_gb300 import build
+            build.build_oracle()
+        L = C.CDLL(str(path))
+        U32, P = C.c_uint32, C.c_void_p
+        L.orc_bfs.argtypes = [U32, _u32p, _u32p, U32, _u32p]
+        L.orc_sssp_worklist.argtypes = [U32, _u32p, _u32p, _u32p, U32, _u32p]
+        L.orc_sssp_jacobi.argtypes = [U32, _u32p, _u32p, _u32p, U32, _i32p, C.POINTER(U32)]
+        L.orc_sssp_dijkstra_int.argtypes = [U32, _u32p, _u32p, _u32p, U32, _i32p]
+        L.orc_mis.argtypes = [U32, _u32p, _u32p, _f32p, _i32p, C.POINTER(U32)]
+        L.orc_color.argtypes = [U32, _u32p, _u32p, _f32p, _i32p, C.POINTER(U32)]
+        L.orc_bc_f32.argtypes = [U32, _u32p, _u32p, _u32p, _u32p, _u32p, U32, _f32p]
+        L.orc_bc_f64.argtypes = [U32, _u32p, _u32p, _u32p, U32, _f64p]
+        L.orc_mst.argtypes = [U32, _u32p, _u32p, _u32p, C.POINTER(C.c_uint64), C.POINTER(U32),
+                              C.POINTER(U32), C.POINTER(U32), P]
+        L.orc_verify_dist.restype = C.c_uint64
+        L.orc_verify_dist.argtypes = [U32, _u32p, _u32p, P, _u32p]
+        L.orc_bfs_reached_arcs.restype = C.c_uint64
+        L.orc_bfs_reached_arcs.argtypes = [U32, _u32p, _u32p, U32, C.POINTER(U32)]
+        L.orc_par_threads.restype = C.c_int
+        L.orc_par_bfs.argtypes = [U32, _u32p, _u32p, U32, _u32p]
+        _ORC = L
+    return _ORC
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"oracle {what} failed with {rc}")
+
+
+def bfs(g, src: int) -> np.ndarray:
+    d = np.empty(g.V, dtype=np.uint32)
+    _check(lib().orc_bfs(g.V, g.row_ptr, _nz(g.col), src, d), "bfs")
+    return d
+
+
+def par_bfs(g, src: int) -> np.ndarray:
+    d = np.empty(g.V, dtype=np.uint32)
+    _check(lib().orc_par_bfs(g.V, g.row_ptr, _nz(g.col), src, d), "par_bfs")
+    return d
+
+
+def par_threads() -> int:
+    return int(lib().orc_par_threads())
+
+
+def sssp_worklist(g, src: int) -> np.ndarray:
+    d = np.empty(g.V, dtype=np.uint32)
+    _check(lib().orc_sssp_worklist(g.V, g.row_ptr, _nz(g.col), _nz(g.w), src, d), "sssp")
+    return d
+
+
+def sssp_jacobi(g, src: int, literal: bool = False) -> np.ndarray:
+    """Pannotia Jacobi SSSP costs; `literal` runs the iteration itself
+    (O(diameter * E)), otherwise the same fixed point via Dijkstra."""
+    c = np.empty(g.V, dtype=np.int32)
+    if literal:
+        it = C.c_uint32()
+        _check(lib().orc_sssp_jacobi(g.V, g.row_ptr, _nz(g.col), _nz(g.w), src, c,
+                                     C.byref(it)), "jacobi")
+    else:
+        _check(lib().orc_sssp_dijkstra_int(g.V, g.row_ptr, _nz(g.col), _nz(g.w), src, c),
+               "jacobi")
+    return c
+
+
+def mis(g, prio: np.ndarray) -> tuple[np.ndarray, int]:
+    s = np.empty(g.V, dtype=np.int32)
+    r = C.c_uint32()
+    _check(lib().orc_mis(g.V, g.row_ptr, _nz(g.col), np.ascontiguousarray(prio, np.float32), s,
+                         C.byref(r)), "mis")
+    return s, r.value
+
+
+def color(g, prio: np.ndarray) -> tuple[np.ndarray, int]:
+    c = np.empty(g.V, dtype=np.int32)
+    r = C.c_uint32()
+    _check(lib().orc_color(g.V, g.row_ptr, _nz(g.col), np.ascontiguousarray(prio, np.float32),
+                           c, C.byref(r)), "color")
+    return c, r.value
+
+
+def bc_f32(g, gt, srcs) -> np.ndarray:
+    bc = np.zeros(g.V, dtype=np.float32)
+    s = np.ascontiguousarray(srcs, dtype=np.uint32)
+    _check(lib().orc_bc_f32(g.V, g.row_ptr, _nz(g.col), gt.row_ptr, _nz(gt.col), _nz(s), len(s),
+                            bc), "bc_f32")
+    return bc
+
+
+def bc_f64(g, srcs) -> np.ndarray:
+    bc = np.zeros(g.V, dtype=np.float64)
+    s = np.ascontiguousarray(srcs, dtype=np.uint32)
+    _check(lib().orc_bc_f64(g.V, g.row_ptr, _nz(g.col), _nz(s), len(s), bc), "bc_f64")
+    return bc
+
+
+def mst(g) -> dict:
+    w64 = C.c_uint64()
+    w32, comps, edges = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    flags = np.zeros(max(g.E, 1), dtype=np.uint8)
+    _check(lib().orc_mst(g.V, g.row_ptr, _nz(g.col), _nz(g.w), C.byref(w64), C.byref(w32),
+                         C.byref(comps), C.byref(edges), flags.ctypes.data), "mst")
+    return {"weight64": w64.value, "weight32": w32.value, "components": comps.value,
+            "edges": edges.value, "arc_in_mst": flags[: g.E]}
+
+
+def verify_dist(g, dist: np.ndarray, weighted: bool) -> int:
+    w = _nz(g.w) if weighted else None
+    return int(lib().orc_verify_dist(g.V, g.row_ptr, _nz(g.col),
+                                     w.ctypes.data if w is not None else None,
+                                     np.ascontiguousarray(dist, np.uint32)))
+
+
+def reached_arcs(g, dist: np.ndarray, inf: int) -> tuple[int, int]:
+    r = C.c_uint32()
+    arcs = lib().orc_bfs_reached_arcs(g.V, g.row_ptr, np.ascontiguousarray(dist, np.uint32),
+                                      inf, C.byref(r))
+    return int(arcs), r.value
+
+
+def mst_edge_set(g, arc_flags: np.ndarray) -> set:
+    """Normalised {(min, max)} undirected edge set from per-arc flags."""
+    src = np.repeat(np.arange(g.V, dtype=np.uint32), np.diff(g.row_ptr.astype(np.int64)))
+    sel = np.nonzero(arc_flags[: g.E])[0]
+    a, b = src[sel], g.col[sel]
+    return set(zip(np.minimum(a, b).tolist(), np.maximum(a, b).tolist()))
+
+
+# ---------------------------------------------------------------- reference
+
+
+def ref_available() -> bool:
+    return (HERE / "_ref" / "libgdbref.so").exists()
+
+
+def ref() -> C.CDLL:
+    """The reference's own kernels (oracle/_ref/libgdbref.so)."""
+    global _REF
+    if _REF is None:
+        L = C.CDLL(str(HERE / "_ref" / "libgdbref.so"))
+        U32 = C.c_uint32
+        L.ref_bfs_lonestar.argtypes = [U32, _u32p, _u32p, U32, _u32p]
+        L.ref_sssp_lonestar.argtypes = [U32, _u32p, _u32p, _u32p, U32, _u32p]
+        L.ref_sssp_pannotia.argtypes = [U32, _u32p, _u32p, _u32p, U32, _i32p]
+        L.ref_mis_pannotia.argtypes = [U32, _u32p, _u32p, _f32p, _i32p]
+        L.ref_color_pannotia.argtypes = [U32, _u32p, _u32p, _f32p, _i32p]
+        L.ref_bc_pannotia_gb.argtypes = [U32, _u32p, _u32p, _u32p, _u32p, _f32p]
+        L.ref_bc_pannotia_sources.argtypes = [U32, _u32p, _u32p, _u32p, _u32p, _u32p, U32, _f32p]
+        L.ref_mst_lonestar.argtypes = [U32, _u32p, _u32p, _u32p, C.POINTER(U32), C.POINTER(U32),
+                                       C.POINTER(U32)]
+        L.ref_discovery_threads.argtypes = [C.c_int, C.c_int, _i32p, C.POINTER(C.c_int),
+                                            C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        _REF = L
+    return _REF
