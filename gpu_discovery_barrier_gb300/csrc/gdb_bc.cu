@@ -1,0 +1,433 @@
+// Betweenness centrality (Brandes) over a list of sources, float32 output.
+//
+// Semantics of Pannotia mega_bc_kernel (pannotia/graph_app/bc/kernel/bc_kernel.cl:431-513):
+// per source s, BFS levels d, shortest-path counts rho (forward,
+// mega_bfs_kernel_func :295-371), dependencies sigma with
+// sigma[w] += rho[w]/rho[i] * (1 + sigma[i]) for every predecessor w of i
+// (backward, mega_backtrack_kernel_func :373-428), and bc[i] += sigma[i]
+// for i != s; no halving for undirected graphs.
+//
+// GB300 form, one persistent kernel for all sources, one XF barrier per
+// level:
+//  * forward, level L: every vertex of the level walks its arcs once,
+//    claiming unvisited neighbours for level L+1 (CAS on d) and pulling the
+//    path counts of its level L-1 neighbours into rho -- the push of the
+//    reference's float CAS-loop atomics becomes a per-vertex pull;
+//  * backward, level L (deepest first): every vertex of the level pulls
+//    rho[v]/rho[u] * (1 + sigma[u]) from its level L+1 neighbours;
+//  * each vertex's sum is accumulated in FP64 and rounded to float once,
+//    so the result does not depend on thread order; heavy vertices sum
+//    their chunks with FP64 atomics and the last chunk to finish (a
+//    countdown) writes the vertex;
+//  * levels are kept as segments of one light list and one heavy list, so
+//    the backward pass visits exactly the reached vertices, and only those
+//    are reset between sources.
+// The pull form reads in-arcs forward and out-arcs backward; on the
+// symmetric graphs this library targets both are the CSR itself.
+#include <algorithm>
+
+#include "gdb_internal.h"
+
+namespace {
+
+using namespace gdb;
+
+struct BcWs {
+  int32_t* d;
+  float* rho;
+  float* sigma;
+  float* bc;
+  uint32_t* order;               // light vertices, level segments
+  uint32_t* hv;                  // heavy entries: vertex
+  uint32_t* hb;                  // first chunk, relative to its level
+  double* hacc;                  // FP64 partial sums of heavy entries
+  uint32_t* hleft;               // chunks still to finish per heavy entry
+  uint32_t* lev_l;               // light segment start per level
+  uint32_t* lev_h;               // heavy entry start per level
+  uint32_t* lev_hc;              // heavy chunks per level
+  uint32_t* lcnt;                // [3] light pushes of the next level
+  unsigned long long* hcnt;      // [3] (entries << 32) | chunks
+  uint32_t* cursor;              // [3]
+  uint32_t* hcursor;             // [3]
+  const uint32_t* sources;
+  uint32_t nsrc;
+  uint32_t max_levels;
+  int* overflow;
+  unsigned long long* stats;     // [0] arcs, [1] supersteps, [2] reached arcs (work units)
+};
+
+// Visit one level segment: light groups over order[lb, lb+nl) (begin/edge/
+// end hooks) and heavy chunks over entries [hbase, hbase+ne).
+template <class Begin, class Edge, class End, class Heavy>
+__device__ __forceinline__ void visit_level(const GraphView& G, const BcWs& ws, uint32_t lb,
+                                            uint32_t nl, uint32_t hbase, uint32_t ne, uint32_t nch,
+                                            uint32_t* cursor, uint32_t* hcursor, Begin&& begin,
+                                            Edge&& edge, End&& end, Heavy&& heavy) {
+  const int lane = lane_id();
+  for (;;) {
+    const uint32_t g = warp_grab(cursor);
+    if ((uint64_t)g * 32 >= nl) break;
+    const uint32_t i = g * 32 + lane;
+    const bool act = i < nl;
+    const uint32_t v = act ? ld_cg(&ws.order[lb + i]) : 0u;
+    begin(v, act);
+    __syncwarp();
+    group_arcs(G, act, v, edge);
+    __syncwarp();
+    end(v, act);
+  }
+  for (;;) {
+    const uint32_t c = warp_grab(hcursor);
+    if (c >= nch) break;
+    uint32_t e = 0;
+    if (lane == 0) e = upper_index(ws.hb + hbase, ne, c);
+    e = __shfl_sync(kFull, e, 0);
+    const uint32_t slot = hbase + e;
+    const uint32_t v = ld_cg(&ws.hv[slot]);
+    const uint32_t j = c - ld_cg(&ws.hb[slot]);
+    const uint32_t rb = __ldg(&G.row[v]), re = __ldg(&G.row[v + 1]);
+    const uint32_t b = rb + j * kChunk, en = min(re, b + kChunk);
+    heavy(v, slot, b, en);
+  }
+}
+
+// Heavy-vertex completion: add this chunk's partial sum; the last chunk
+// returns true (with the vertex total in *total) and re-arms the counter.
+__device__ __forceinline__ bool heavy_done(const BcWs& ws, uint32_t slot, double part,
+                                           uint32_t nchunks, double* total) {
+  bool last = false;
+  if (lane_id() == 0) {
+    atomicAdd(&ws.hacc[slot], part);
+    __threadfence();
+    last = atomicSub(&ws.hleft[slot], 1u) == 1u;
+    if (last) {
+      __threadfence();
+      *total = __ldcg(&ws.hacc[slot]);
+      ws.hacc[slot] = 0.0;
+      ws.hleft[slot] = nchunks;
+    }
+  }
+  return __shfl_sync(kFull, last, 0);
+}
+
+template <class Sync>
+__device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs& ws, double* sacc) {
+  const Warps W = warps_of(s.id(), s.P());
+  const bool leader = s.id() == 0 && threadIdx.x == 0;
+  const int lane = lane_id();
+  double* my = sacc + (threadIdx.x & ~31u);
+  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+    ws.d[v] = -1;
+    ws.rho[v] = 0.f;
+    ws.sigma[v] = 0.f;
+    ws.bc[v] = 0.f;
+  }
+  if (leader) {
+    for (int i = 0; i < 3; ++i) {
+      ws.lcnt[i] = 0;
+      ws.hcnt[i] = 0;
+      ws.cursor[i] = 0;
+      ws.hcursor[i] = 0;
+    }
+    *ws.overflow = 0;
+    ws.stats[0] = ws.stats[1] = ws.stats[2] = 0;
+  }
+  if (!s.sync()) return;
+  unsigned long long arcs = 0, reached_arcs = 0;
+  uint32_t t = 0;  // superstep counter for the rotating slots
+  auto reset_slot = [&](uint32_t tt) {
+    if (leader) {
+      const int old = (tt + 2) % 3;
+      ws.lcnt[old] = 0;
+      ws.hcnt[old] = 0;
+      ws.cursor[old] = 0;
+      ws.hcursor[old] = 0;
+    }
+  };
+  for (uint32_t si = 0; si < ws.nsrc; ++si) {
+    const uint32_t src = ws.sources[si];
+    // -- superstep: seed the source into slot (t+1)
+    reset_slot(t);
+    if (leader) {
+      ws.d[src] = 0;
+      ws.rho[src] = 1.f;
+      const int nx = (t + 1) % 3;
+      const uint32_t deg = G.row[src + 1] - G.row[src];
+      if (is_heavy(G, src)) {
+        const uint32_t nch = chunks_of(deg);
+        ws.hv[0] = src;
+        ws.hb[0] = 0;
+        ws.hacc[0] = 0.0;
+        ws.hleft[0] = nch;
+        ws.hcnt[nx] = (1ull << 32) | nch;
+      } else {
+        ws.order[0] = src;
+        ws.lcnt[nx] = 1;
+      }
+    }
+    if (!s.sync()) return;
+    ++t;
+    // -- forward levels
+    uint32_t lbase = 0, hbase = 0, L = 0;
+    for (;; ++L, ++t) {
+      const int cur = t % 3, nx = (t + 1) % 3;
+      const uint32_t nl = ld_cg(&ws.lcnt[cur]);
+      const unsigned long long hp = __ldcg(&ws.hcnt[cur]);
+      const uint32_t ne = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
+      if (leader && L < ws.max_levels) {
+        ws.lev_l[L] = lbase;
+        ws.lev_h[L] = hbase;
+        ws.lev_hc[L] = nch;
+      }
+      // the slot two supersteps back is free even in the final superstep
+      reset_slot(t);
+      if (nl == 0 && ne == 0) break;
+      if (L + 1 >= ws.max_levels) {
+        if (leader) *ws.overflow = 1;
+        break;
+      }
+      const uint32_t nlbase = lbase + nl, nhbase = hbase + ne;
+      Frontier out{ws.order + nlbase, ws.hv + nhbase, ws.hb + nhbase, &ws.lcnt[nx], &ws.hcnt[nx],
+                   G.V - nlbase, G.nheavy - nhbase, ws.overflow, ws.hleft + nhbase,
+                   ws.hacc + nhbase};
+      const int32_t Li = (int32_t)L;
+      // one arc of a level-L vertex: claim level L+1 or pull a parent's count
+      auto fwd_arc = [&](bool valid, uint32_t arc, double& acc) {
+        uint32_t u = 0;
+        bool want = false;
+        if (valid) {
+          ++arcs;
+          u = __ldg(&G.col[arc]);
+          const int32_t du = ld_cg(&ws.d[u]);
+          if (du == Li - 1) {
+            acc += (double)ld_cg(&ws.rho[u]);
+          } else if (du == -1 && atomicCAS(&ws.d[u], -1, Li + 1) == -1) {
+            want = true;
+          }
+        }
+        // a claimed heavy vertex gets its chunk countdown armed by the push
+        frontier_push(G, out, want, u);
+      };
+      visit_level(
+          G, ws, lbase, nl, hbase, ne, nch, &ws.cursor[cur], &ws.hcursor[cur],
+          [&](uint32_t v, bool act) {
+            my[lane] = 0.0;
+            if (act) reached_arcs += __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
+          },
+          [&](bool valid, int owner, uint32_t arc) {
+            double a = 0.0;
+            fwd_arc(valid, arc, a);
+            if (a != 0.0) atomicAdd(&my[owner], a);
+          },
+          [&](uint32_t v, bool act) {
+            if (act && L > 0) ws.rho[v] = (float)my[lane];
+          },
+          [&](uint32_t v, uint32_t slot, uint32_t b, uint32_t e) {
+            double part = 0.0;
+            for (uint32_t a0 = b; a0 < e; a0 += 32) fwd_arc(a0 + lane < e, a0 + lane, part);
+            part = warp_sum_f64(part);
+            if (lane == 0 && b == __ldg(&G.row[v])) reached_arcs += __ldg(&G.row[v + 1]) - b;
+            double tot = 0.0;
+            const uint32_t deg = __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
+            if (heavy_done(ws, slot, part, chunks_of(deg), &tot) && lane == 0 && L > 0)
+              ws.rho[v] = (float)tot;
+          });
+      if (!s.sync()) return;
+      lbase = nlbase;
+      hbase = nhbase;
+    }
+    ++t;
+    const uint32_t levels = L;  // levels 0 .. L-1 are non-empty
+    const uint32_t total_l = lbase, total_h = hbase;
+    if (!s.sync()) return;
+    // -- backward levels, deepest first
+    for (int32_t Lb = (int32_t)levels - 1; Lb >= 0; --Lb, ++t) {
+      const int cur = t % 3;
+      reset_slot(t);
+      const uint32_t lb = ld_cg(&ws.lev_l[Lb]), le = ld_cg(&ws.lev_l[Lb + 1]);
+      const uint32_t hb0 = ld_cg(&ws.lev_h[Lb]), he = ld_cg(&ws.lev_h[Lb + 1]);
+      const uint32_t nch = ld_cg(&ws.lev_hc[Lb]);
+      auto bwd_arc = [&](bool valid, uint32_t arc, float rv, double& acc) {
+        if (valid) {
+          ++arcs;
+          const uint32_t u = __ldg(&G.col[arc]);
+          if (ld_cg(&ws.d[u]) == Lb + 1) {
+            acc += (double)rv / (double)ld_cg(&ws.rho[u]) * (1.0 + (double)ld_cg(&ws.sigma[u]));
+          }
+        }
+      };
+      float rv_lane = 0.f;
+      visit_level(
+          G, ws, lb, le - lb, hb0, he - hb0, nch, &ws.cursor[cur], &ws.hcursor[cur],
+          [&](uint32_t v, bool act) {
+            my[lane] = 0.0;
+            rv_lane = act ? ld_cg(&ws.rho[v]) : 0.f;
+          },
+          [&](bool valid, int owner, uint32_t arc) {
+            double a = 0.0;
+            bwd_arc(valid, arc, __shfl_sync(kFull, rv_lane, owner), a);
+            if (a != 0.0) atomicAdd(&my[owner], a);
+          },
+          [&](uint32_t v, bool act) {
+            if (act) {
+              const float sg = (float)my[lane];
+              ws.sigma[v] = sg;
+              if (v != src) ws.bc[v] += sg;
+            }
+          },
+          [&](uint32_t v, uint32_t slot, uint32_t b, uint32_t e) {
+            const float rv = ld_cg(&ws.rho[v]);
+            double part = 0.0;
+            for (uint32_t a0 = b; a0 < e; a0 += 32) bwd_arc(a0 + lane < e, a0 + lane, rv, part);
+            part = warp_sum_f64(part);
+            double tot = 0.0;
+            const uint32_t deg = __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
+            if (heavy_done(ws, slot, part, chunks_of(deg), &tot) && lane == 0) {
+              const float sg = (float)tot;
+              ws.sigma[v] = sg;
+              if (v != src) ws.bc[v] += sg;
+            }
+          });
+      if (!s.sync()) return;
+    }
+    // -- reset the reached vertices for the next source
+    for (uint32_t k = W.gthread; k < total_l; k += W.nthreads) {
+      const uint32_t v = ws.order[k];
+      ws.d[v] = -1;
+      ws.rho[v] = 0.f;
+      ws.sigma[v] = 0.f;
+    }
+    for (uint32_t k = W.gthread; k < total_h; k += W.nthreads) {
+      const uint32_t v = ws.hv[k];
+      ws.d[v] = -1;
+      ws.rho[v] = 0.f;
+      ws.sigma[v] = 0.f;
+    }
+    reset_slot(t);
+    if (!s.sync()) return;
+    ++t;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    arcs += __shfl_xor_sync(kFull, arcs, o);
+    reached_arcs += __shfl_xor_sync(kFull, reached_arcs, o);
+  }
+  if (lane == 0) {
+    if (arcs) atomicAdd(&ws.stats[0], arcs);
+    if (reached_arcs) atomicAdd(&ws.stats[2], reached_arcs);
+  }
+  if (leader) ws.stats[1] = t;
+}
+
+__global__ void __launch_bounds__(1024, 1) k_bc_xf(DiscoveryArgs a, GraphView G, BcWs ws) {
+  __shared__ LocalCtx l;
+  __shared__ double sacc[1024];
+  if (!discover(a, &l)) return;
+  XfSync s{&a, &l};
+  bc_body(s, G, ws, sacc);
+}
+
+}  // namespace
+
+using namespace gdbi;
+
+static int bc_run(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc, float* d_bc) {
+  if (!graph_ok(c, g) || !d_bc || (nsrc && !d_sources)) return GDB_ERR_INVALID;
+  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED)
+    return set_error(c, GDB_ERR_UNSUPPORTED, "BC runs on the XF barrier");
+  const uint32_t V = g->V;
+  const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
+  const uint32_t maxlev = V + 2;
+  Bump b;
+  const size_t o_d = b.take((size_t)V * 4), o_rho = b.take((size_t)V * 4), o_sg = b.take((size_t)V * 4);
+  const size_t o_ord = b.take((size_t)V * 4);
+  const size_t o_hv = b.take(hcap * 4), o_hb = b.take(hcap * 4), o_hacc = b.take(hcap * 8),
+               o_hleft = b.take(hcap * 4);
+  const size_t o_ll = b.take((size_t)maxlev * 4), o_lh = b.take((size_t)maxlev * 4),
+               o_lhc = b.take((size_t)maxlev * 4);
+  const size_t o_cnt = b.take(512);
+  char* base = (char*)workspace(c, b.off);
+  if (!base) return GDB_ERR_OOM;
+  BcWs ws;
+  ws.d = (int32_t*)(base + o_d);
+  ws.rho = (float*)(base + o_rho);
+  ws.sigma = (float*)(base + o_sg);
+  ws.bc = d_bc;
+  ws.order = (uint32_t*)(base + o_ord);
+  ws.hv = (uint32_t*)(base + o_hv);
+  ws.hb = (uint32_t*)(base + o_hb);
+  ws.hacc = (double*)(base + o_hacc);
+  ws.hleft = (uint32_t*)(base + o_hleft);
+  ws.lev_l = (uint32_t*)(base + o_ll);
+  ws.lev_h = (uint32_t*)(base + o_lh);
+  ws.lev_hc = (uint32_t*)(base + o_lhc);
+  char* cnt = base + o_cnt;
+  ws.stats = (unsigned long long*)cnt;
+  ws.hcnt = (unsigned long long*)(cnt + 64);
+  ws.lcnt = (uint32_t*)(cnt + 96);
+  ws.cursor = (uint32_t*)(cnt + 112);
+  ws.hcursor = (uint32_t*)(cnt + 128);
+  ws.overflow = (int*)(cnt + 160);
+  ws.sources = d_sources;
+  ws.nsrc = nsrc;
+  ws.max_levels = maxlev - 1;
+  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
+  const int block = c->opt.block_size;
+  Shape s;
+  int rc = persistent_shape(c, (const void*)k_bc_xf, block, 0, &s, c->opt.barrier == GDB_BARRIER_XF);
+  if (rc) return rc;
+  DiscoveryArgs a = discovery_args(c, s);
+  c->last = gdb_run_stats{};
+  GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  k_bc_xf<<<s.grid, block, 0, c->stream>>>(a, g->view(), ws);
+  GDB_CUDA(c, cudaGetLastError());
+  GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  rc = finish_run(c);
+  if (rc) return rc;
+  unsigned long long* hs = (unsigned long long*)pinned(c, 512);
+  if (!hs) return GDB_ERR_OOM;
+  GDB_CUDA(c, cudaMemcpyAsync(hs, cnt, 512, cudaMemcpyDeviceToHost, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (*(int*)((char*)hs + 160)) return set_error(c, GDB_ERR_CAPACITY, "BC list overflow");
+  float ms = 0;
+  GDB_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  int n = 0;
+  read_participating(c, &n);
+  c->last.participating = n;
+  c->last.launched = s.grid;
+  c->last.launches = 1;
+  c->last.kernel_ms = ms;
+  c->last.edges_processed = hs[0];
+  c->last.supersteps = (uint32_t)hs[1];
+  c->last.work_units = hs[2];
+  return GDB_OK;
+}
+
+extern "C" {
+
+int gdb_bc_device(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc, float* d_bc) {
+  return bc_run(c, g, d_sources, nsrc, d_bc);
+}
+
+int gdb_bc(gdb_ctx* c, gdb_graph* g, const uint32_t* sources, uint32_t nsrc, float* bc) {
+  if (!graph_ok(c, g) || !bc || (nsrc && !sources)) return GDB_ERR_INVALID;
+  for (uint32_t i = 0; i < nsrc; ++i)
+    if (sources[i] >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  const size_t nb = (size_t)g->V * 4, sb = std::max<size_t>(nsrc, 1) * 4;
+  char* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, nb + sb, c->stream));
+  cudaError_t e = nsrc ? cudaMemcpyAsync(d + nb, sources, nsrc * 4, cudaMemcpyHostToDevice, c->stream)
+                       : cudaSuccess;
+  int rc = e == cudaSuccess ? bc_run(c, g, (const uint32_t*)(d + nb), nsrc, (float*)d)
+                            : set_cuda_error(c, e, "sources upload");
+  if (rc == GDB_OK) {
+    e = cudaMemcpyAsync(bc, d, nb, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "bc read-back");
+  }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,373 @@
+// Breadth-first search: persistent level-synchronous kernel behind the
+// discovery protocol and the XF barrier.
+//
+// Semantics of LonestarGPU drelax2 (lonestar/apps/bfs/kernel/bfs_port_kernel.cl:146-192,
+// processedge2 bfs_common.cl:73-90): dist[src] = 0, a vertex first reached
+// in superstep L gets L, unreached vertices keep 1e9.  The reference's
+// worklist pushes a vertex once per discovering arc (a benign race,
+// bfs_common.cl:85-88) and needs two barriers per level (bfs_port_kernel.cl:177,188);
+// here a CAS on dist[v] makes every vertex enter the queue exactly once,
+// and three rotating counter sets let one barrier separate levels.
+//
+// Schedules:
+//  * plain: top-down push from a queue every level;
+//  * adaptive: direction-optimising -- a level switches to bottom-up pull
+//    (every unvisited vertex scans its arcs for a parent at L-1, stopping at
+//    the first) when the frontier's arcs exceed the unvisited arcs / 14, and
+//    back when the frontier shrinks below V/24.  Levels are identical.
+#include <algorithm>
+
+#include "gdb_internal.h"
+
+namespace {
+
+using namespace gdb;
+
+struct BfsWs {
+  uint32_t* dist;
+  uint32_t* q[2];
+  uint32_t* hv[2];
+  uint32_t* hb[2];
+  uint32_t* qcount;            // [3]
+  unsigned long long* hcount;  // [3]
+  uint32_t* cursor;            // [3]
+  uint32_t* hcursor;           // [3]
+  int* overflow;
+  unsigned long long* stats;   // [0] arcs inspected, [1] levels, [2] unvisited arcs, [3] frontier arcs
+  uint32_t* mode;              // [3] 0 = top-down, 1 = bottom-up, per level slot
+  uint32_t qcap, hcap;
+  int adaptive;
+};
+
+__device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long* p) {
+  return __ldcg(p);
+}
+
+// Top-down expansion of level L into L+1.
+__device__ __forceinline__ void bfs_top_down(const GraphView& G, const BfsWs& ws, uint32_t L,
+                                             unsigned long long& arcs, unsigned long long& farcs) {
+  const int cur = L % 3, nxt = (L + 1) % 3;
+  const uint32_t n = ld_cg(&ws.qcount[cur]);
+  const unsigned long long hp = ld_cg_u64(&ws.hcount[cur]);
+  Frontier out{pick(ws.q, L + 1), pick(ws.hv, L + 1), pick(ws.hb, L + 1), &ws.qcount[nxt],
+               &ws.hcount[nxt], ws.qcap, ws.hcap, ws.overflow};
+  auto edge = [&](bool valid, uint32_t arc) {
+    uint32_t u = 0;
+    bool want = false;
+    if (valid) {
+      u = __ldg(&G.col[arc]);
+      ++arcs;
+      if (ld_cg(&ws.dist[u]) == kInf && atomicCAS(&ws.dist[u], kInf, L + 1) == kInf) {
+        want = true;
+        if (ws.adaptive) farcs += __ldg(&G.row[u + 1]) - __ldg(&G.row[u]);
+      }
+    }
+    frontier_push(G, out, want, u);
+  };
+  visit_frontier(
+      G, pick(ws.q, L), n, pick(ws.hv, L), pick(ws.hb, L), hp, &ws.cursor[cur], &ws.hcursor[cur],
+      [&](bool valid, int, uint32_t, uint32_t arc) { edge(valid, arc); },
+      [&](bool valid, uint32_t, uint32_t arc) { edge(valid, arc); });
+}
+
+// Bottom-up step for level L+1: every unvisited vertex looks for a parent
+// at level L among its arcs, stopping at the first.  Warp per 32 vertices,
+// each lane scanning its own vertex (degree-limited early exit).
+__device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& ws, uint32_t L,
+                                              const Warps& W, unsigned long long& arcs,
+                                              unsigned long long& farcs) {
+  const int nxt = (L + 1) % 3;
+  Frontier out{pick(ws.q, L + 1), pick(ws.hv, L + 1), pick(ws.hb, L + 1), &ws.qcount[nxt],
+               &ws.hcount[nxt], ws.qcap, ws.hcap, ws.overflow};
+  const int lane = lane_id();
+  const uint32_t ngroups = (G.V + 31) / 32;
+  for (uint32_t g = W.gwarp; g < ngroups; g += W.nwarps) {
+    const uint32_t v = g * 32 + lane;
+    bool want = false;
+    if (v < G.V && ws.dist[v] == kInf) {
+      const uint32_t b = __ldg(&G.row[v]), e = __ldg(&G.row[v + 1]);
+      for (uint32_t a = b; a < e; ++a) {
+        ++arcs;
+        if (ld_cg(&ws.dist[__ldg(&G.col[a])]) == L) {
+          want = true;
+          break;
+        }
+      }
+      if (want) {
+        ws.dist[v] = L + 1;  // only this lane writes v
+        farcs += e - b;
+      }
+    }
+    frontier_push(G, out, want, v);
+  }
+}
+
+template <class Sync>
+__device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsWs& ws, uint32_t src) {
+  const Warps W = warps_of(s.id(), s.P());
+  const bool leader = s.id() == 0 && threadIdx.x == 0;
+  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) ws.dist[v] = kInf;
+  if (leader) {
+    for (int i = 0; i < 3; ++i) {
+      ws.qcount[i] = 0;
+      ws.hcount[i] = 0;
+      ws.cursor[i] = 0;
+      ws.hcursor[i] = 0;
+      ws.mode[i] = 0;
+    }
+    *ws.overflow = 0;
+    for (int i = 0; i < 8; ++i) ws.stats[i] = 0;
+  }
+  if (!s.sync()) return;
+  if (leader) {
+    ws.dist[src] = 0;
+    const uint32_t deg = G.row[src + 1] - G.row[src];
+    if (is_heavy(G, src)) {
+      ws.hv[0][0] = src;
+      ws.hb[0][0] = 0;
+      ws.hcount[0] = (1ull << 32) | chunks_of(deg);
+    } else {
+      ws.q[0][0] = src;
+      ws.qcount[0] = 1;
+    }
+  }
+  if (!s.sync()) return;
+  unsigned long long arcs = 0;
+  uint32_t L = 0;
+  bool bottom_up = false;
+  // direction-choice inputs, identical in every CTA: arcs of the frontier
+  // (mf) and of the still-unvisited vertices (mu).  acc[k % 3] (stats[4..6])
+  // collects the arcs of level k while level k-1 runs.
+  unsigned long long mf = G.row[src + 1] - G.row[src];
+  unsigned long long mu = G.E - mf;
+  for (;; ++L) {
+    const int cur = L % 3, old = (L + 2) % 3;
+    const uint32_t n = ld_cg(&ws.qcount[cur]);
+    const unsigned long long hp = ld_cg_u64(&ws.hcount[cur]);
+    if (n == 0 && hp == 0) break;
+    if (ws.adaptive) {
+      if (L > 0) {
+        mf = ld_cg_u64(&ws.stats[4 + cur]);
+        mu = mu > mf ? mu - mf : 0;
+      }
+      const uint32_t nf = n + (uint32_t)(hp >> 32);
+      if (!bottom_up && mf > mu / 14) bottom_up = true;
+      else if (bottom_up && nf < G.V / 24) bottom_up = false;
+    }
+    if (leader) {
+      ws.qcount[old] = 0;
+      ws.hcount[old] = 0;
+      ws.cursor[old] = 0;
+      ws.hcursor[old] = 0;
+      ws.stats[4 + old] = 0;
+    }
+    unsigned long long farcs = 0;
+    if (bottom_up) bfs_bottom_up(G, ws, L, W, arcs, farcs);
+    else bfs_top_down(G, ws, L, arcs, farcs);
+    if (ws.adaptive) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) farcs += __shfl_xor_sync(kFull, farcs, o);
+      if (lane_id() == 0 && farcs) atomicAdd(&ws.stats[4 + (L + 1) % 3], farcs);
+    }
+    if (!s.sync()) return;
+  }
+  unsigned long long r = arcs;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(kFull, r, o);
+  if (lane_id() == 0 && r) atomicAdd(&ws.stats[0], r);
+  if (leader) ws.stats[1] = L;
+}
+
+__global__ void __launch_bounds__(1024, 1) k_bfs_xf(DiscoveryArgs a, GraphView G, BfsWs ws, uint32_t src) {
+  __shared__ LocalCtx l;
+  if (!discover(a, &l)) return;
+  XfSync s{&a, &l};
+  bfs_body(s, G, ws, src);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_bfs_grid(GraphView G, BfsWs ws, uint32_t src) {
+  GridSync s;
+  bfs_body(s, G, ws, src);
+}
+
+// Relaunch mode: init kernel, then one launch per level (no in-kernel barrier).
+__global__ void k_bfs_init(GraphView G, BfsWs ws, uint32_t src) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
+  for (uint32_t v = t; v < G.V; v += n) ws.dist[v] = (v == src) ? 0u : kInf;
+  if (t == 0) {
+    for (int i = 0; i < 3; ++i) {
+      ws.qcount[i] = 0;
+      ws.hcount[i] = 0;
+      ws.cursor[i] = 0;
+      ws.hcursor[i] = 0;
+    }
+    *ws.overflow = 0;
+    ws.stats[0] = ws.stats[1] = 0;
+    const uint32_t deg = G.row[src + 1] - G.row[src];
+    if (is_heavy(G, src)) {
+      ws.hv[0][0] = src;
+      ws.hb[0][0] = 0;
+      ws.hcount[0] = (1ull << 32) | chunks_of(deg);
+    } else {
+      ws.q[0][0] = src;
+      ws.qcount[0] = 1;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(1024, 1) k_bfs_level(GraphView G, BfsWs ws, uint32_t L) {
+  const int old = (L + 2) % 3;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ws.qcount[old] = 0;
+    ws.hcount[old] = 0;
+    ws.cursor[old] = 0;
+    ws.hcursor[old] = 0;
+    ws.stats[1] = L + 1;
+  }
+  unsigned long long arcs = 0, farcs = 0;
+  bfs_top_down(G, ws, L, arcs, farcs);
+  unsigned long long r = arcs;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(kFull, r, o);
+  if (lane_id() == 0 && r) atomicAdd(&ws.stats[0], r);
+}
+
+}  // namespace
+
+using namespace gdbi;
+
+static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
+  if (!graph_ok(c, g) || !d_dist) return GDB_ERR_INVALID;
+  if (src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  const uint32_t V = g->V;
+  const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
+  Bump b;
+  const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
+  const size_t o_hv0 = b.take(hcap * 4), o_hv1 = b.take(hcap * 4);
+  const size_t o_hb0 = b.take(hcap * 4), o_hb1 = b.take(hcap * 4);
+  const size_t o_cnt = b.take(512);
+  char* base = (char*)workspace(c, b.off);
+  if (!base) return GDB_ERR_OOM;
+  BfsWs ws;
+  ws.dist = d_dist;
+  ws.q[0] = (uint32_t*)(base + o_q0);
+  ws.q[1] = (uint32_t*)(base + o_q1);
+  ws.hv[0] = (uint32_t*)(base + o_hv0);
+  ws.hv[1] = (uint32_t*)(base + o_hv1);
+  ws.hb[0] = (uint32_t*)(base + o_hb0);
+  ws.hb[1] = (uint32_t*)(base + o_hb1);
+  char* cnt = base + o_cnt;
+  ws.stats = (unsigned long long*)cnt;                // 8 x u64
+  ws.hcount = (unsigned long long*)(cnt + 64);        // 3 x u64
+  ws.qcount = (uint32_t*)(cnt + 96);                  // 3
+  ws.cursor = (uint32_t*)(cnt + 112);                 // 3
+  ws.hcursor = (uint32_t*)(cnt + 128);                // 3
+  ws.mode = (uint32_t*)(cnt + 144);                   // 3
+  ws.overflow = (int*)(cnt + 160);
+  ws.qcap = V;
+  ws.hcap = hcap;
+  ws.adaptive = c->opt.schedule == GDB_SCHED_ADAPTIVE;
+  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
+  const GraphView G = g->view();
+  const int block = c->opt.block_size;
+  const int kind = c->opt.barrier;
+  c->last = gdb_run_stats{};
+  int rc = GDB_OK;
+  if (kind == GDB_BARRIER_XF || kind == GDB_BARRIER_XF_FIXED) {
+    Shape s;
+    rc = persistent_shape(c, (const void*)k_bfs_xf, block, 0, &s, kind == GDB_BARRIER_XF);
+    if (rc) return rc;
+    DiscoveryArgs a = discovery_args(c, s);
+    GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    k_bfs_xf<<<s.grid, block, 0, c->stream>>>(a, G, ws, src);
+    GDB_CUDA(c, cudaGetLastError());
+    GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    rc = finish_run(c);
+    if (rc) return rc;
+    int n = 0;
+    read_participating(c, &n);
+    c->last.participating = n;
+    c->last.launched = s.grid;
+    c->last.launches = 1;
+  } else if (kind == GDB_BARRIER_GRID_SYNC) {
+    int occ = 0;
+    GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs_grid, block, 0));
+    int grid = occ * c->sm_count;
+    if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
+    GraphView Gc = G;
+    BfsWs wsc = ws;
+    uint32_t srcc = src;
+    void* args[] = {(void*)&Gc, (void*)&wsc, (void*)&srcc};
+    GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    GDB_CUDA(c, cudaLaunchCooperativeKernel((const void*)k_bfs_grid, grid, block, args, 0, c->stream));
+    GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->last.participating = grid;
+    c->last.launched = grid;
+    c->last.launches = 1;
+  } else if (kind == GDB_BARRIER_RELAUNCH) {
+    if (ws.adaptive) return set_error(c, GDB_ERR_UNSUPPORTED, "adaptive schedule needs a persistent barrier");
+    int occ = 0;
+    GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs_level, block, 0));
+    int grid = occ * c->sm_count;
+    if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
+    uint32_t* h = (uint32_t*)pinned(c, 64);
+    if (!h) return GDB_ERR_OOM;
+    GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    k_bfs_init<<<grid, block, 0, c->stream>>>(G, ws, src);
+    uint32_t launches = 1;
+    for (uint32_t L = 0;; ++L) {
+      k_bfs_level<<<grid, block, 0, c->stream>>>(G, ws, L);
+      ++launches;
+      // the stop flag of the reference's relaunch loop: next frontier size
+      const int nxt = (L + 1) % 3;
+      GDB_CUDA(c, cudaMemcpyAsync(h, &ws.qcount[nxt], 4, cudaMemcpyDeviceToHost, c->stream));
+      GDB_CUDA(c, cudaMemcpyAsync(h + 2, &ws.hcount[nxt], 8, cudaMemcpyDeviceToHost, c->stream));
+      GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (h[0] == 0 && h[2] == 0 && h[3] == 0) break;
+    }
+    GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->last.participating = grid;
+    c->last.launched = grid;
+    c->last.launches = launches;
+  } else {
+    return set_error(c, GDB_ERR_UNSUPPORTED, "barrier kind not available for BFS");
+  }
+  unsigned long long* hs = (unsigned long long*)pinned(c, 512);
+  if (!hs) return GDB_ERR_OOM;
+  GDB_CUDA(c, cudaMemcpyAsync(hs, cnt, 512, cudaMemcpyDeviceToHost, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (*(int*)((char*)hs + 160)) return set_error(c, GDB_ERR_CAPACITY, "BFS queue overflow");
+  float ms = 0;
+  GDB_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->last.kernel_ms = ms;
+  c->last.edges_processed = hs[0];
+  c->last.supersteps = (uint32_t)hs[1];
+  return GDB_OK;
+}
+
+extern "C" {
+
+int gdb_bfs_device(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
+  return bfs_run(c, g, src, d_dist);
+}
+
+int gdb_bfs(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* dist) {
+  if (!graph_ok(c, g) || !dist) return GDB_ERR_INVALID;
+  Bump b;
+  // the output lives after the kernel workspace, which bfs_run sizes itself
+  uint32_t* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, (size_t)g->V * 4, c->stream));
+  int rc = bfs_run(c, g, src, d);
+  if (rc == GDB_OK) {
+    cudaError_t e = cudaMemcpyAsync(dist, d, (size_t)g->V * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "dist read-back");
+  }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
+}  // extern "C"

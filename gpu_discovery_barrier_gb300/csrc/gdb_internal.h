@@ -1,0 +1,104 @@
+// Host-side internals of libgdb: context, graph and launch helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gdb.h"
+#include "gdb_discovery.cuh"
+#include "gdb_sweep.cuh"
+
+struct gdb_ctx {
+  gdb_options opt{};
+  int device = 0;
+  int sm_count = 0;
+  int cc_major = 0, cc_minor = 0;
+  size_t total_mem = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  gdb::DeviceCtx* dctx = nullptr;
+  int* flags = nullptr;
+  int flag_cap = 0;
+  int stall_after = -1;
+  // grow-only device workspace
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  // pinned host staging for small read-backs
+  void* pinned = nullptr;
+  size_t pinned_bytes = 0;
+  gdb_run_stats last{};
+  std::string err;
+};
+
+struct gdb_graph {
+  gdb_ctx* ctx = nullptr;
+  uint32_t V = 0;
+  uint64_t E = 0;
+  uint32_t* row = nullptr;
+  uint32_t* col = nullptr;
+  uint32_t* w = nullptr;
+  bool owns = true;
+  bool owns_w = true;
+  // heavy-vertex table (degree > kHeavyDeg), ascending vertex ids
+  uint32_t nheavy = 0;
+  uint32_t nheavy_chunks = 0;
+  uint32_t* heavy_v = nullptr;
+  uint32_t* heavy_base = nullptr;  // nheavy + 1 chunk prefix
+  uint32_t* heavy_bits = nullptr;  // V-bit membership bitmap
+  gdb::GraphView view() const;
+};
+
+namespace gdbi {
+
+int set_cuda_error(gdb_ctx* c, cudaError_t e, const char* what);
+int set_error(gdb_ctx* c, int status, const std::string& msg);
+
+#define GDB_CUDA(c, expr)                                      \
+  do {                                                         \
+    cudaError_t _e = (expr);                                   \
+    if (_e != cudaSuccess) return gdbi::set_cuda_error(c, _e, #expr); \
+  } while (0)
+
+// Grow-only workspace; returns nullptr on failure (error recorded).
+void* workspace(gdb_ctx* c, size_t bytes);
+void* pinned(gdb_ctx* c, size_t bytes);
+
+// Bump allocator over the workspace (256-byte aligned slices).
+struct Bump {
+  size_t off = 0;
+  size_t take(size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~size_t(255);
+    return o;
+  }
+};
+
+// Launch shape for a persistent kernel: CTAs launched, the occupancy the
+// CUDA API reports, and the discovery arguments.
+struct Shape {
+  int grid = 0;
+  int block = 0;
+  int occ_per_sm = 0;
+  int fit = 0;  // occ_per_sm * sm_count
+};
+
+int persistent_shape(gdb_ctx* c, const void* kernel, int block, size_t smem, Shape* s,
+                     bool allow_oversubscribe = true);
+gdb::DiscoveryArgs discovery_args(gdb_ctx* c, const Shape& s);
+
+// After a persistent run: read the device status; on error re-arm the
+// discovery context and return the status.
+int finish_run(gdb_ctx* c);
+int reset_device_ctx(gdb_ctx* c, int skip);
+int read_participating(gdb_ctx* c, int* n);
+
+// Heavy table construction from a host copy of row_ptr.
+int build_heavy_table(gdb_graph* g, const uint32_t* host_row);
+
+bool graph_ok(gdb_ctx* c, gdb_graph* g);
+
+}  // namespace gdbi

@@ -1,0 +1,405 @@
+// Maximal independent set and greedy colouring with Pannotia semantics.
+//
+// MIS (mega_kernel, pannotia/graph_app/mis/kernel/mis_kernel.cl:220-337):
+// per round every undecided vertex takes the minimum priority over its
+// undecided neighbours (mis1, :245-270); undecided strict local minima join
+// the set, s = 2, and mark their undecided neighbours decided (mis2,
+// :277-312).  The reference stages neighbour marks in cu[] and commits them
+// in a third barrier interval (mis3, :322-330); here the marks go straight
+// into the state array -- two winners are never adjacent, so no winner test
+// can see a mark of the same round -- and a round needs two barriers.
+//
+// Colouring (mega_kernel, pannotia/graph_app/color/kernel/color_kernel.cl:159-252):
+// per round every uncoloured vertex takes the maximum priority over its
+// uncoloured neighbours -- a degree-1 vertex ignores its only neighbour
+// (start != end - 1, :204) -- then the uncoloured vertices above it take
+// the round's colour; stop after a round in which no vertex saw an
+// uncoloured neighbour.  Colours start at 1.
+//
+// Priorities are compared as floats through an order-preserving uint32
+// key, so shared-memory atomicMin/atomicMax give the per-vertex extremum.
+#include <algorithm>
+
+#include "gdb_internal.h"
+
+namespace {
+
+using namespace gdb;
+
+constexpr float kMisBig = 99999999.0f;  // BIGNUM, mis_kernel.cl:68
+
+struct MisWs {
+  int32_t* state;       // -1 undecided, -2 decided
+  int32_t* s;           // output: 2 in the set, 0 otherwise
+  uint32_t* mn;         // light vertices: key of the min undecided neighbour priority
+  uint32_t* hmn[2];     // heavy vertices, by heavy index, double-buffered by round
+  const float* prio;
+  uint32_t* cursor;     // [3]
+  uint32_t* hcursor;    // [3]
+  uint32_t* flag;       // [3] some vertex undecided
+  unsigned long long* stats;  // [0] arcs, [1] rounds
+};
+
+template <class Sync>
+__device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisWs& ws, uint32_t* smem) {
+  const Warps W = warps_of(s.id(), s.P());
+  const bool leader = s.id() == 0 && threadIdx.x == 0;
+  const int lane = lane_id();
+  uint32_t* my = smem + (threadIdx.x & ~31u);
+  const uint32_t big = fkey(kMisBig);
+  // init kernel (mis_kernel.cl:78-93)
+  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+    ws.state[v] = -1;
+    ws.s[v] = 0;
+  }
+  for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) ws.hmn[0][h] = ws.hmn[1][h] = big;
+  if (leader) {
+    for (int i = 0; i < 3; ++i) ws.cursor[i] = ws.hcursor[i] = ws.flag[i] = 0;
+    ws.stats[0] = ws.stats[1] = 0;
+  }
+  if (!s.sync()) return;
+  unsigned long long arcs = 0;
+  uint32_t r = 0;
+  uint32_t t = 0;  // cursor slot counter: two sweeps per round
+  for (;; ++r) {
+    // ---- mis1: min over undecided neighbours
+    {
+      const int cur = t % 3, old = (t + 2) % 3;
+      if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
+      bool undecided_seen = false;
+      sweep_light(
+          G, &ws.cursor[cur],
+          [&](uint32_t v, bool in_range) {
+            const bool und = in_range && ld_cg(&ws.state[v]) == -1;
+            my[lane] = big;
+            undecided_seen |= und;
+            return und;
+          },
+          [&](bool valid, int owner, uint32_t arc) {
+            if (valid) {
+              ++arcs;
+              const uint32_t u = __ldg(&G.col[arc]);
+              if (ld_cg(&ws.state[u]) == -1) {
+                const uint32_t k = fkey(__ldg(&ws.prio[u]));
+                if (k < my[owner]) atomicMin(&my[owner], k);
+              }
+            }
+          },
+          [&](uint32_t v, bool act) {
+            if (act) ws.mn[v] = my[lane];
+          });
+      uint32_t* hmn = pick(ws.hmn, r);
+      sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
+        // a heavy winner's own state is settled here (see mis2)
+        if (ld_cg(&ws.s[v]) == 2) {
+          if (lane == 0) ws.state[v] = -2;
+          return;
+        }
+        if (ld_cg(&ws.state[v]) != -1) return;
+        undecided_seen = true;
+        uint32_t m = big;
+        for (uint32_t a0 = b; a0 < e; a0 += 32) {
+          const uint32_t a = a0 + lane;
+          if (a < e) {
+            ++arcs;
+            const uint32_t u = __ldg(&G.col[a]);
+            if (ld_cg(&ws.state[u]) == -1) m = min(m, fkey(__ldg(&ws.prio[u])));
+          }
+        }
+        m = warp_min_u32(m);
+        if (lane == 0 && m < big) atomicMin(&hmn[h], m);
+      });
+      if (__any_sync(kFull, undecided_seen) && lane == 0) atomicOr(&ws.flag[cur], 1u);
+      if (!s.sync()) return;
+      ++t;
+      if (ld_cg(&ws.flag[cur]) == 0) break;
+    }
+    // ---- mis2: strict local minima join the set and decide their neighbours
+    {
+      const int cur = t % 3, old = (t + 2) % 3;
+      if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
+      // next round's heavy minima start from BIGNUM
+      for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) pick(ws.hmn, r + 1)[h] = big;
+      sweep_light(
+          G, &ws.cursor[cur],
+          [&](uint32_t v, bool in_range) {
+            bool win = false;
+            if (in_range && ld_cg(&ws.state[v]) == -1 && fkey(__ldg(&ws.prio[v])) < ws.mn[v]) {
+              win = true;
+              ws.s[v] = 2;
+              ws.state[v] = -2;
+            }
+            return win;
+          },
+          [&](bool valid, int, uint32_t arc) {
+            if (valid) {
+              ++arcs;
+              const uint32_t u = __ldg(&G.col[arc]);
+              if (ld_cg(&ws.state[u]) == -1) ws.state[u] = -2;
+            }
+          },
+          [](uint32_t, bool) {});
+      const uint32_t* hmn = pick(ws.hmn, r);
+      // A heavy winner is split over chunks: its own state stays -1 here so
+      // every chunk sees the same test; s = 2 marks it and mis1 of the next
+      // round settles its state (all its neighbours are decided by then, so
+      // nobody reads it in between).
+      sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
+        if (ld_cg(&ws.state[v]) != -1) return;
+        if (!(fkey(__ldg(&ws.prio[v])) < ld_cg(&hmn[h]))) return;
+        if (lane == 0) ws.s[v] = 2;
+        for (uint32_t a0 = b; a0 < e; a0 += 32) {
+          const uint32_t a = a0 + lane;
+          if (a < e) {
+            ++arcs;
+            const uint32_t u = __ldg(&G.col[a]);
+            if (ld_cg(&ws.state[u]) == -1) ws.state[u] = -2;
+          }
+        }
+      });
+      if (!s.sync()) return;
+      ++t;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
+  if (lane == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  if (leader) ws.stats[1] = r + 1;
+}
+
+__global__ void __launch_bounds__(1024, 1) k_mis_xf(DiscoveryArgs a, GraphView G, MisWs ws) {
+  __shared__ LocalCtx l;
+  __shared__ uint32_t smem[1024];
+  if (!discover(a, &l)) return;
+  XfSync s{&a, &l};
+  mis_body(s, G, ws, smem);
+}
+
+// ------------------------------------------------------------- colouring
+
+struct ColorWs {
+  int32_t* color;
+  uint32_t* mx;        // light vertices: key of the max uncoloured neighbour priority
+  uint32_t* hmx[2];    // heavy vertices, double-buffered by round
+  const float* prio;
+  uint32_t* cursor;    // [3]
+  uint32_t* hcursor;   // [3]
+  uint32_t* flag;      // [3] some vertex saw an uncoloured neighbour (stop)
+  unsigned long long* stats;  // [0] arcs, [1] rounds
+};
+
+template <class Sync>
+__device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const ColorWs& ws, uint32_t* smem) {
+  const Warps W = warps_of(s.id(), s.P());
+  const bool leader = s.id() == 0 && threadIdx.x == 0;
+  const int lane = lane_id();
+  uint32_t* my = smem + (threadIdx.x & ~31u);
+  const uint32_t none = fkey(-1.0f);  // `maximum = -1` (color_kernel.cl:198)
+  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) ws.color[v] = -1;
+  for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) ws.hmx[0][h] = ws.hmx[1][h] = none;
+  if (leader) {
+    for (int i = 0; i < 3; ++i) ws.cursor[i] = ws.hcursor[i] = ws.flag[i] = 0;
+    ws.stats[0] = ws.stats[1] = 0;
+  }
+  if (!s.sync()) return;
+  unsigned long long arcs = 0;
+  int32_t graph_color = 1;
+  for (uint32_t r = 0;; ++r, ++graph_color) {
+    const int cur = r % 3, old = (r + 2) % 3;
+    if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
+    // ---- color: max over uncoloured neighbours
+    bool saw = false;
+    sweep_light(
+        G, &ws.cursor[cur],
+        [&](uint32_t v, bool in_range) {
+          my[lane] = none;
+          if (!in_range || ld_cg(&ws.color[v]) != -1) return false;
+          // a degree-1 vertex never looks at its neighbour
+          return __ldg(&G.row[v + 1]) - __ldg(&G.row[v]) != 1;
+        },
+        [&](bool valid, int owner, uint32_t arc) {
+          if (valid) {
+            ++arcs;
+            const uint32_t u = __ldg(&G.col[arc]);
+            if (ld_cg(&ws.color[u]) == -1) {
+              saw = true;
+              const uint32_t k = fkey(__ldg(&ws.prio[u]));
+              if (k > my[owner]) atomicMax(&my[owner], k);
+            }
+          }
+        },
+        [&](uint32_t v, bool act) {
+          if (v < G.V && !is_heavy(G, v)) ws.mx[v] = act ? my[lane] : none;
+        });
+    uint32_t* hmx = pick(ws.hmx, r);
+    sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
+      if (ld_cg(&ws.color[v]) != -1) return;
+      uint32_t m = none;
+      bool any = false;
+      for (uint32_t a0 = b; a0 < e; a0 += 32) {
+        const uint32_t a = a0 + lane;
+        if (a < e) {
+          ++arcs;
+          const uint32_t u = __ldg(&G.col[a]);
+          if (ld_cg(&ws.color[u]) == -1) {
+            any = true;
+            m = max(m, fkey(__ldg(&ws.prio[u])));
+          }
+        }
+      }
+      m = warp_max_u32(m);
+      saw |= any;
+      if (lane == 0 && m > none) atomicMax(&hmx[h], m);
+    });
+    if (__any_sync(kFull, saw) && lane == 0) atomicOr(&ws.flag[cur], 1u);
+    if (!s.sync()) return;
+    // ---- color2: uncoloured vertices above the maximum take the colour
+    for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+      if (is_heavy(G, v) || ws.color[v] != -1) continue;
+      if (fkey(__ldg(&ws.prio[v])) > ws.mx[v]) ws.color[v] = graph_color;
+    }
+    for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) {
+      const uint32_t v = __ldg(&G.heavy_v[h]);
+      if (ws.color[v] == -1 && fkey(__ldg(&ws.prio[v])) > hmx[h]) ws.color[v] = graph_color;
+      pick(ws.hmx, r + 1)[h] = none;
+    }
+    if (ld_cg(&ws.flag[cur]) == 0) {
+      if (leader) ws.stats[1] = r + 1;
+      break;
+    }
+    if (!s.sync()) return;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
+  if (lane == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_color_xf(DiscoveryArgs a, GraphView G, ColorWs ws) {
+  __shared__ LocalCtx l;
+  __shared__ uint32_t smem[1024];
+  if (!discover(a, &l)) return;
+  XfSync s{&a, &l};
+  color_body(s, G, ws, smem);
+}
+
+}  // namespace
+
+using namespace gdbi;
+
+template <class K, class Ws>
+static int launch_xf(gdb_ctx* c, K kernel, const GraphView& G, const Ws& ws, unsigned long long* d_stats) {
+  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED)
+    return set_error(c, GDB_ERR_UNSUPPORTED, "this kernel runs on the XF barrier");
+  const int block = c->opt.block_size;
+  Shape s;
+  int rc = persistent_shape(c, (const void*)kernel, block, 0, &s, c->opt.barrier == GDB_BARRIER_XF);
+  if (rc) return rc;
+  DiscoveryArgs a = discovery_args(c, s);
+  c->last = gdb_run_stats{};
+  GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  kernel<<<s.grid, block, 0, c->stream>>>(a, G, ws);
+  GDB_CUDA(c, cudaGetLastError());
+  GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  rc = finish_run(c);
+  if (rc) return rc;
+  unsigned long long* hs = (unsigned long long*)pinned(c, 64);
+  if (!hs) return GDB_ERR_OOM;
+  GDB_CUDA(c, cudaMemcpyAsync(hs, d_stats, 16, cudaMemcpyDeviceToHost, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  float ms = 0;
+  GDB_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  int n = 0;
+  read_participating(c, &n);
+  c->last.participating = n;
+  c->last.launched = s.grid;
+  c->last.launches = 1;
+  c->last.kernel_ms = ms;
+  c->last.edges_processed = hs[0];
+  c->last.supersteps = (uint32_t)hs[1];
+  return GDB_OK;
+}
+
+static int mis_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_s) {
+  if (!graph_ok(c, g) || !d_prio || !d_s) return GDB_ERR_INVALID;
+  const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
+  Bump b;
+  const size_t o_state = b.take((size_t)g->V * 4), o_mn = b.take((size_t)g->V * 4);
+  const size_t o_h0 = b.take(hcap * 4), o_h1 = b.take(hcap * 4), o_cnt = b.take(256);
+  char* base = (char*)workspace(c, b.off);
+  if (!base) return GDB_ERR_OOM;
+  MisWs ws;
+  ws.state = (int32_t*)(base + o_state);
+  ws.s = d_s;
+  ws.mn = (uint32_t*)(base + o_mn);
+  ws.hmn[0] = (uint32_t*)(base + o_h0);
+  ws.hmn[1] = (uint32_t*)(base + o_h1);
+  ws.prio = d_prio;
+  char* cnt = base + o_cnt;
+  ws.stats = (unsigned long long*)cnt;
+  ws.cursor = (uint32_t*)(cnt + 64);
+  ws.hcursor = (uint32_t*)(cnt + 80);
+  ws.flag = (uint32_t*)(cnt + 96);
+  return launch_xf(c, k_mis_xf, g->view(), ws, ws.stats);
+}
+
+static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_color) {
+  if (!graph_ok(c, g) || !d_prio || !d_color) return GDB_ERR_INVALID;
+  const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
+  Bump b;
+  const size_t o_mx = b.take((size_t)g->V * 4);
+  const size_t o_h0 = b.take(hcap * 4), o_h1 = b.take(hcap * 4), o_cnt = b.take(256);
+  char* base = (char*)workspace(c, b.off);
+  if (!base) return GDB_ERR_OOM;
+  ColorWs ws;
+  ws.color = d_color;
+  ws.mx = (uint32_t*)(base + o_mx);
+  ws.hmx[0] = (uint32_t*)(base + o_h0);
+  ws.hmx[1] = (uint32_t*)(base + o_h1);
+  ws.prio = d_prio;
+  char* cnt = base + o_cnt;
+  ws.stats = (unsigned long long*)cnt;
+  ws.cursor = (uint32_t*)(cnt + 64);
+  ws.hcursor = (uint32_t*)(cnt + 80);
+  ws.flag = (uint32_t*)(cnt + 96);
+  return launch_xf(c, k_color_xf, g->view(), ws, ws.stats);
+}
+
+// Host-buffer wrapper: copy the priorities in, run, copy the answer out.
+template <class Run>
+static int with_host_prio(gdb_ctx* c, gdb_graph* g, const float* prio, int32_t* out, Run run) {
+  if (!graph_ok(c, g) || !prio || !out) return GDB_ERR_INVALID;
+  const size_t n = (size_t)g->V * 4;
+  char* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, 2 * n, c->stream));
+  cudaError_t e = cudaMemcpyAsync(d, prio, n, cudaMemcpyHostToDevice, c->stream);
+  int rc = e == cudaSuccess ? run((const float*)d, (int32_t*)(d + n)) : set_cuda_error(c, e, "priorities upload");
+  if (rc == GDB_OK) {
+    e = cudaMemcpyAsync(out, d + n, n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "result read-back");
+  }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
+extern "C" {
+
+int gdb_mis_device(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_s) {
+  return mis_run(c, g, d_prio, d_s);
+}
+
+int gdb_mis(gdb_ctx* c, gdb_graph* g, const float* prio, int32_t* s) {
+  return with_host_prio(c, g, prio, s, [&](const float* dp, int32_t* ds) { return mis_run(c, g, dp, ds); });
+}
+
+int gdb_color_device(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_color) {
+  return color_run(c, g, d_prio, d_color);
+}
+
+int gdb_color(gdb_ctx* c, gdb_graph* g, const float* prio, int32_t* color) {
+  return with_host_prio(c, g, prio, color,
+                        [&](const float* dp, int32_t* dc) { return color_run(c, g, dp, dc); });
+}
+
+}  // extern "C"

@@ -1,0 +1,262 @@
+// Minimum spanning forest by Boruvka rounds in one persistent kernel.
+//
+// Replaces the LonestarGPU MST (host loop lonestar/apps/mst/mst_port.cpp:202-312
+// over dinit/dfindelemin/dfindelemin2/verify_min_elem, mst_common.cl:41-194,
+// and the persistent dfindcompmintwo, mst_port_kernel.cl:35-82).  The
+// reference leaves the device after every kernel and after every `repeat`
+// of dfindcompmintwo to read two words; here the whole round loop stays on
+// the device behind the XF barrier.  A round:
+//   A. every vertex finds its lightest arc to another component and
+//      atomicMin's the key (weight << 32 | arc) into its component's slot
+//      (dfindelemin + dfindelemin2 in one step: the arc index breaks ties);
+//   B1. every component root records the root its lightest arc reaches;
+//   B2. roots hook onto that root, except the smaller id of a mutual pair,
+//      which stays a root (cs_unify breaks cycles by id too,
+//      component_cl.h:58-64); each hook adds its arc's weight once;
+//   C. pointer jumping flattens every vertex onto its root.
+// With unique weights the forest is unique, so weight, edge count and edge
+// set equal the reference's.  The weight is kept exactly (uint64) and also
+// as the reference's wrapping uint32 sum (mst_port_kernel.cl:69); arcs of
+// weight >= 1e9 are never chosen (mst_common.cl:84-88).
+#include <algorithm>
+
+#include "gdb_internal.h"
+
+namespace {
+
+using namespace gdb;
+
+constexpr unsigned long long kNoArc = ~0ull;
+
+struct MstWs {
+  uint32_t* comp;
+  unsigned long long* best;
+  uint32_t* partner;
+  uint8_t* arc_flag;             // nullable
+  uint32_t* cursor;              // [3]
+  uint32_t* hcursor;             // [3]
+  uint32_t* hooks;               // [3]
+  unsigned long long* acc;       // [0] weight, [1] edges, [2] rounds, [3] arcs inspected
+};
+
+template <class Sync>
+__device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstWs& ws,
+                                         unsigned long long* smem) {
+  const Warps W = warps_of(s.id(), s.P());
+  const bool leader = s.id() == 0 && threadIdx.x == 0;
+  const int lane = lane_id();
+  unsigned long long* my = smem + (threadIdx.x & ~31u);
+  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+    ws.comp[v] = v;
+    ws.best[v] = kNoArc;
+  }
+  if (ws.arc_flag)
+    for (uint32_t a = W.gthread; a < G.E; a += W.nthreads) ws.arc_flag[a] = 0;
+  if (leader) {
+    for (int i = 0; i < 3; ++i) ws.cursor[i] = ws.hcursor[i] = ws.hooks[i] = 0;
+    for (int i = 0; i < 4; ++i) ws.acc[i] = 0;
+  }
+  if (!s.sync()) return;
+  unsigned long long arcs = 0, wsum = 0, nedges = 0;
+  uint32_t t = 0, round = 0;
+  for (;; ++round) {
+    // ---- A: lightest arc leaving each vertex's component
+    {
+      const int cur = t % 3, old = (t + 2) % 3;
+      if (leader) ws.cursor[old] = ws.hcursor[old] = ws.hooks[old] = 0;
+      uint32_t cv = 0;
+      sweep_light(
+          G, &ws.cursor[cur],
+          [&](uint32_t v, bool in_range) {
+            my[lane] = kNoArc;
+            cv = in_range ? ld_cg(&ws.comp[v]) : 0u;
+            return true;
+          },
+          [&](bool valid, int owner, uint32_t arc) {
+            const uint32_t co = __shfl_sync(kFull, cv, owner);
+            if (valid) {
+              ++arcs;
+              const uint32_t wt = __ldg(&G.w[arc]);
+              if (wt < kInf && ld_cg(&ws.comp[__ldg(&G.col[arc])]) != co) {
+                const unsigned long long key = ((unsigned long long)wt << 32) | arc;
+                if (key < my[owner]) atomicMin(&my[owner], key);
+              }
+            }
+          },
+          [&](uint32_t, bool act) {
+            if (act && my[lane] != kNoArc) {
+              if (my[lane] < ld_cg(&ws.best[cv])) atomicMin(&ws.best[cv], my[lane]);
+            }
+          });
+      sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
+        const uint32_t c = ld_cg(&ws.comp[v]);
+        unsigned long long m = kNoArc;
+        for (uint32_t a0 = b; a0 < e; a0 += 32) {
+          const uint32_t a = a0 + lane;
+          if (a < e) {
+            ++arcs;
+            const uint32_t wt = __ldg(&G.w[a]);
+            if (wt < kInf && ld_cg(&ws.comp[__ldg(&G.col[a])]) != c) {
+              const unsigned long long key = ((unsigned long long)wt << 32) | a;
+              m = key < m ? key : m;
+            }
+          }
+        }
+        m = warp_min_u64(m);
+        if (lane == 0 && m != kNoArc) atomicMin(&ws.best[c], m);
+      });
+      if (!s.sync()) return;
+      ++t;
+    }
+    // ---- B1: the root each component's lightest arc reaches
+    for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+      if (ws.comp[v] != v) continue;
+      const unsigned long long key = ws.best[v];
+      if (key == kNoArc) continue;
+      ws.partner[v] = ws.comp[__ldg(&G.col[(uint32_t)key])];
+    }
+    if (!s.sync()) return;
+    ++t;
+    // ---- B2: hook; the smaller root of a mutual pair stays a root
+    {
+      const int cur = t % 3, old = (t + 2) % 3;
+      if (leader) ws.cursor[old] = ws.hcursor[old] = ws.hooks[old] = 0;
+      uint32_t hooked = 0;
+      for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+        if (ws.comp[v] != v) continue;
+        const unsigned long long key = ws.best[v];
+        if (key == kNoArc) continue;
+        const uint32_t d = ws.partner[v];
+        ws.best[v] = kNoArc;  // next round starts empty
+        const bool mutual = ws.partner[d] == v;  // partner[] is settled since B1
+        if (mutual && v < d) continue;
+        ws.comp[v] = d;
+        wsum += key >> 32;
+        ++nedges;
+        ++hooked;
+        if (ws.arc_flag) ws.arc_flag[(uint32_t)key] = 1;
+      }
+      hooked = __reduce_add_sync(kFull, hooked);
+      if (lane == 0 && hooked) atomicAdd(&ws.hooks[cur], hooked);
+      if (!s.sync()) return;
+      ++t;
+      if (ld_cg(&ws.hooks[cur]) == 0) break;
+    }
+    // ---- C: pointer jumping onto the roots
+    for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+      uint32_t r = ld_cg(&ws.comp[v]);
+      for (uint32_t p = ld_cg(&ws.comp[r]); p != r; p = ld_cg(&ws.comp[r])) r = p;
+      ws.comp[v] = r;
+    }
+    if (!s.sync()) return;
+    ++t;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    arcs += __shfl_xor_sync(kFull, arcs, o);
+    wsum += __shfl_xor_sync(kFull, wsum, o);
+    nedges += __shfl_xor_sync(kFull, nedges, o);
+  }
+  if (lane == 0) {
+    if (wsum) atomicAdd(&ws.acc[0], wsum);
+    if (nedges) atomicAdd(&ws.acc[1], nedges);
+    if (arcs) atomicAdd(&ws.acc[3], arcs);
+  }
+  if (leader) ws.acc[2] = round + 1;
+}
+
+__global__ void __launch_bounds__(1024, 1) k_mst_xf(DiscoveryArgs a, GraphView G, MstWs ws) {
+  __shared__ LocalCtx l;
+  __shared__ unsigned long long smem[1024];
+  if (!discover(a, &l)) return;
+  XfSync s{&a, &l};
+  mst_body(s, G, ws, smem);
+}
+
+}  // namespace
+
+using namespace gdbi;
+
+static int mst_run(gdb_ctx* c, gdb_graph* g, gdb_mst_result* h_res, gdb_mst_result* d_res,
+                   uint8_t* d_flags) {
+  if (!graph_ok(c, g)) return GDB_ERR_INVALID;
+  if (!g->w) return set_error(c, GDB_ERR_INVALID, "MST needs weights");
+  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED)
+    return set_error(c, GDB_ERR_UNSUPPORTED, "MST runs on the XF barrier");
+  const uint32_t V = g->V;
+  Bump b;
+  const size_t o_comp = b.take((size_t)V * 4), o_best = b.take((size_t)V * 8),
+               o_part = b.take((size_t)V * 4), o_cnt = b.take(256);
+  char* base = (char*)workspace(c, b.off);
+  if (!base) return GDB_ERR_OOM;
+  MstWs ws;
+  ws.comp = (uint32_t*)(base + o_comp);
+  ws.best = (unsigned long long*)(base + o_best);
+  ws.partner = (uint32_t*)(base + o_part);
+  ws.arc_flag = d_flags;
+  char* cnt = base + o_cnt;
+  ws.acc = (unsigned long long*)cnt;
+  ws.cursor = (uint32_t*)(cnt + 64);
+  ws.hcursor = (uint32_t*)(cnt + 80);
+  ws.hooks = (uint32_t*)(cnt + 96);
+  const int block = c->opt.block_size;
+  Shape s;
+  int rc = persistent_shape(c, (const void*)k_mst_xf, block, 0, &s, c->opt.barrier == GDB_BARRIER_XF);
+  if (rc) return rc;
+  DiscoveryArgs a = discovery_args(c, s);
+  c->last = gdb_run_stats{};
+  GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  k_mst_xf<<<s.grid, block, 0, c->stream>>>(a, g->view(), ws);
+  GDB_CUDA(c, cudaGetLastError());
+  GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  rc = finish_run(c);
+  if (rc) return rc;
+  unsigned long long* hs = (unsigned long long*)pinned(c, 256);
+  if (!hs) return GDB_ERR_OOM;
+  GDB_CUDA(c, cudaMemcpyAsync(hs, cnt, 32, cudaMemcpyDeviceToHost, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  gdb_mst_result r;
+  r.weight64 = hs[0];
+  r.weight32 = (uint32_t)hs[0];
+  r.edges = (uint32_t)hs[1];
+  r.components = V - r.edges;
+  r.rounds = (uint32_t)hs[2];
+  if (h_res) *h_res = r;
+  if (d_res) GDB_CUDA(c, cudaMemcpyAsync(d_res, &r, sizeof r, cudaMemcpyHostToDevice, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  float ms = 0;
+  GDB_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  int n = 0;
+  read_participating(c, &n);
+  c->last.participating = n;
+  c->last.launched = s.grid;
+  c->last.launches = 1;
+  c->last.kernel_ms = ms;
+  c->last.edges_processed = hs[3];
+  c->last.supersteps = r.rounds;
+  c->last.work_units = g->E;
+  return GDB_OK;
+}
+
+extern "C" {
+
+int gdb_mst_device(gdb_ctx* c, gdb_graph* g, gdb_mst_result* d_result, uint8_t* d_arc_in_mst) {
+  return mst_run(c, g, nullptr, d_result, d_arc_in_mst);
+}
+
+int gdb_mst(gdb_ctx* c, gdb_graph* g, gdb_mst_result* result, uint8_t* arc_in_mst) {
+  if (!graph_ok(c, g) || !result) return GDB_ERR_INVALID;
+  uint8_t* d = nullptr;
+  if (arc_in_mst) GDB_CUDA(c, cudaMallocAsync((void**)&d, std::max<uint64_t>(g->E, 1), c->stream));
+  int rc = mst_run(c, g, result, nullptr, d);
+  if (rc == GDB_OK && arc_in_mst && g->E) {
+    cudaError_t e = cudaMemcpyAsync(arc_in_mst, d, g->E, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "arc flags read-back");
+  }
+  if (d) cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,435 @@
+// libgdb host runtime: contexts, graphs, workspace, launch shapes, errors.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+
+#include "gdb_internal.h"
+
+namespace gdbi {
+
+int set_cuda_error(gdb_ctx* c, cudaError_t e, const char* what) {
+  if (c) {
+    c->err = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  }
+  cudaGetLastError();  // clear the sticky-free error so the context stays usable
+  return e == cudaErrorMemoryAllocation ? GDB_ERR_OOM : GDB_ERR_CUDA;
+}
+
+int set_error(gdb_ctx* c, int status, const std::string& msg) {
+  if (c) c->err = msg;
+  return status;
+}
+
+void* workspace(gdb_ctx* c, size_t bytes) {
+  if (bytes <= c->ws_bytes) return c->ws;
+  if (c->ws) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->ws);
+    c->ws = nullptr;
+    c->ws_bytes = 0;
+  }
+  size_t want = std::max(bytes, (size_t)1 << 20);
+  cudaError_t e = cudaMalloc(&c->ws, want);
+  if (e != cudaSuccess) {
+    set_cuda_error(c, e, "cudaMalloc(workspace)");
+    c->ws = nullptr;
+    return nullptr;
+  }
+  c->ws_bytes = want;
+  return c->ws;
+}
+
+void* pinned(gdb_ctx* c, size_t bytes) {
+  if (bytes <= c->pinned_bytes) return c->pinned;
+  if (c->pinned) cudaFreeHost(c->pinned);
+  c->pinned = nullptr;
+  c->pinned_bytes = 0;
+  size_t want = std::max(bytes, (size_t)4096);
+  if (cudaMallocHost(&c->pinned, want) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  c->pinned_bytes = want;
+  return c->pinned;
+}
+
+int persistent_shape(gdb_ctx* c, const void* kernel, int block, size_t smem, Shape* s,
+                     bool allow_oversubscribe) {
+  int occ = 0;
+  GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, block, smem));
+  if (occ <= 0) return set_error(c, GDB_ERR_INVALID, "kernel does not fit on an SM at this block size");
+  s->block = block;
+  s->occ_per_sm = occ;
+  s->fit = occ * c->sm_count;
+  int grid = s->fit;
+  if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
+  if (allow_oversubscribe && c->opt.oversubscribe > 0) grid = c->opt.oversubscribe;
+  // the XF master retires at most 32 peers per thread; flags bound P
+  const int cap = std::min(c->flag_cap, 32 * block + 1);
+  if (!(allow_oversubscribe && c->opt.oversubscribe > 0)) grid = std::min(grid, cap);
+  s->grid = std::max(grid, 1);
+  return GDB_OK;
+}
+
+gdb::DiscoveryArgs discovery_args(gdb_ctx* c, const Shape& s) {
+  gdb::DiscoveryArgs a;
+  a.ctx = c->dctx;
+  a.flags = c->flags;
+  a.flag_capacity = c->flag_cap;
+  a.lock_kind = c->opt.lock;
+  a.expected = std::min(s.grid, s.fit);
+  a.timeout_ns = c->opt.timeout_ns ? c->opt.timeout_ns : 2000000000ull;
+  a.close_wait_ns = 50000ull;
+  return a;
+}
+
+int reset_device_ctx(gdb_ctx* c, int skip) {
+  gdb::DeviceCtx h;
+  std::memset(&h, 0, sizeof(h));
+  h.poll_open = 1;
+  h.skip = skip;
+  h.stall_after = c->stall_after;
+  GDB_CUDA(c, cudaMemcpyAsync(c->dctx, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+  GDB_CUDA(c, cudaMemsetAsync(c->flags, 0, (size_t)c->flag_cap * gdb::kLineInts * sizeof(int),
+                              c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GDB_OK;
+}
+
+int finish_run(gdb_ctx* c) {
+  int* h = (int*)pinned(c, 4096);
+  if (!h) return set_error(c, GDB_ERR_OOM, "pinned staging");
+  // status, abort, err_where of the device context
+  GDB_CUDA(c, cudaMemcpyAsync(h, &c->dctx->status, 4 * sizeof(int), cudaMemcpyDeviceToHost,
+                              c->stream));
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return set_cuda_error(c, e, "kernel execution");
+  const int status = h[0], where = h[2];
+  if (status != 0) {
+    int skip = 0;
+    cudaMemcpy(&skip, &c->dctx->skip, sizeof(int), cudaMemcpyDeviceToHost);
+    reset_device_ctx(c, skip);
+    char buf[160];
+    snprintf(buf, sizeof buf, "device reported %s at site %d", gdb_status_string(status), where);
+    c->err = buf;
+    return status;
+  }
+  return GDB_OK;
+}
+
+int read_participating(gdb_ctx* c, int* n) {
+  int* h = (int*)pinned(c, 4096);
+  if (!h) return set_error(c, GDB_ERR_OOM, "pinned staging");
+  GDB_CUDA(c, cudaMemcpyAsync(h, &c->dctx->num_participating, sizeof(int), cudaMemcpyDeviceToHost,
+                              c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  *n = h[0];
+  return GDB_OK;
+}
+
+int build_heavy_table(gdb_graph* g, const uint32_t* hrow) {
+  gdb_ctx* c = g->ctx;
+  std::vector<uint32_t> hv, hb;
+  std::vector<uint32_t> bits((g->V + 31) / 32 + 1, 0);
+  uint64_t chunks = 0;
+  for (uint32_t v = 0; v < g->V; ++v) {
+    uint32_t d = hrow[v + 1] - hrow[v];
+    if (d > gdb::kHeavyDeg) {
+      hv.push_back(v);
+      hb.push_back((uint32_t)chunks);
+      chunks += gdb::chunks_of(d);
+      bits[v >> 5] |= 1u << (v & 31);
+    }
+  }
+  hb.push_back((uint32_t)chunks);
+  g->nheavy = (uint32_t)hv.size();
+  g->nheavy_chunks = (uint32_t)chunks;
+  const size_t nb = bits.size() * 4, nv = std::max<size_t>(hv.size(), 1) * 4, nbase = hb.size() * 4;
+  GDB_CUDA(c, cudaMalloc(&g->heavy_bits, nb));
+  GDB_CUDA(c, cudaMalloc(&g->heavy_v, nv));
+  GDB_CUDA(c, cudaMalloc(&g->heavy_base, nbase));
+  GDB_CUDA(c, cudaMemcpy(g->heavy_bits, bits.data(), nb, cudaMemcpyHostToDevice));
+  if (!hv.empty()) GDB_CUDA(c, cudaMemcpy(g->heavy_v, hv.data(), hv.size() * 4, cudaMemcpyHostToDevice));
+  GDB_CUDA(c, cudaMemcpy(g->heavy_base, hb.data(), nbase, cudaMemcpyHostToDevice));
+  return GDB_OK;
+}
+
+bool graph_ok(gdb_ctx* c, gdb_graph* g) { return c && g && g->ctx == c; }
+
+}  // namespace gdbi
+
+gdb::GraphView gdb_graph::view() const {
+  gdb::GraphView v;
+  v.V = V;
+  v.E = (uint32_t)E;
+  v.row = row;
+  v.col = col;
+  v.w = w;
+  v.nheavy = nheavy;
+  v.nheavy_chunks = nheavy_chunks;
+  v.heavy_v = heavy_v;
+  v.heavy_base = heavy_base;
+  v.heavy_bits = heavy_bits;
+  return v;
+}
+
+using namespace gdbi;
+
+extern "C" {
+
+int gdb_abi_version(void) { return GDB_ABI_VERSION; }
+
+void gdb_options_default(gdb_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->device = -1;
+  o->block_size = 512;
+  o->max_ctas = 0;
+  o->oversubscribe = 0;
+  o->lock = GDB_LOCK_FREE;
+  o->barrier = GDB_BARRIER_XF;
+  o->schedule = GDB_SCHED_PLAIN;
+  o->timeout_ns = 2000000000ull;
+}
+
+const char* gdb_status_string(int s) {
+  switch (s) {
+    case GDB_OK: return "GDB_OK";
+    case GDB_ERR_INVALID: return "GDB_ERR_INVALID";
+    case GDB_ERR_CUDA: return "GDB_ERR_CUDA";
+    case GDB_ERR_OOM: return "GDB_ERR_OOM";
+    case GDB_ERR_TIMEOUT: return "GDB_ERR_TIMEOUT";
+    case GDB_ERR_CAPACITY: return "GDB_ERR_CAPACITY";
+    case GDB_ERR_NOT_CORESIDENT: return "GDB_ERR_NOT_CORESIDENT";
+    case GDB_ERR_UNSUPPORTED: return "GDB_ERR_UNSUPPORTED";
+    default: return "GDB_ERR_UNKNOWN";
+  }
+}
+
+static int check_options(const gdb_options* o) {
+  if (o->block_size != 0 && (o->block_size < 64 || o->block_size > 1024 || (o->block_size & 31)))
+    return GDB_ERR_INVALID;
+  if (o->lock < GDB_LOCK_TICKET || o->lock > GDB_LOCK_FREE) return GDB_ERR_INVALID;
+  if (o->barrier < GDB_BARRIER_XF || o->barrier > GDB_BARRIER_XF_FIXED) return GDB_ERR_INVALID;
+  if (o->schedule < GDB_SCHED_PLAIN || o->schedule > GDB_SCHED_ADAPTIVE) return GDB_ERR_INVALID;
+  if (o->max_ctas < 0 || o->oversubscribe < 0) return GDB_ERR_INVALID;
+  return GDB_OK;
+}
+
+int gdb_ctx_create(const gdb_options* opt, gdb_ctx** out) {
+  if (!out) return GDB_ERR_INVALID;
+  *out = nullptr;
+  gdb_options o;
+  gdb_options_default(&o);
+  if (opt) o = *opt;
+  if (o.block_size == 0) o.block_size = 512;
+  if (o.timeout_ns == 0) o.timeout_ns = 2000000000ull;
+  if (check_options(&o) != GDB_OK) return GDB_ERR_INVALID;
+  gdb_ctx* c = new gdb_ctx();
+  c->opt = o;
+  int dev = o.device;
+  if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return GDB_ERR_CUDA;
+  }
+  c->device = dev;
+  cudaDeviceProp prop;
+  if (cudaSetDevice(dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return GDB_ERR_CUDA;
+  }
+  c->sm_count = prop.multiProcessorCount;
+  c->cc_major = prop.major;
+  c->cc_minor = prop.minor;
+  c->total_mem = prop.totalGlobalMem;
+  // at most 32 resident CTAs per SM on this architecture family
+  c->flag_cap = std::max(64, c->sm_count * 32);
+  bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreate(&c->ev0) == cudaSuccess && cudaEventCreate(&c->ev1) == cudaSuccess &&
+            cudaMalloc(&c->dctx, sizeof(gdb::DeviceCtx)) == cudaSuccess &&
+            cudaMalloc(&c->flags, (size_t)c->flag_cap * gdb::kLineInts * sizeof(int)) == cudaSuccess;
+  if (!ok || reset_device_ctx(c, 0) != GDB_OK) {
+    cudaGetLastError();
+    gdb_ctx_destroy(c);
+    return GDB_ERR_CUDA;
+  }
+  *out = c;
+  return GDB_OK;
+}
+
+int gdb_ctx_destroy(gdb_ctx* c) {
+  if (!c) return GDB_ERR_INVALID;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->ws) cudaFree(c->ws);
+  if (c->pinned) cudaFreeHost(c->pinned);
+  if (c->dctx) cudaFree(c->dctx);
+  if (c->flags) cudaFree(c->flags);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  cudaGetLastError();
+  delete c;
+  return GDB_OK;
+}
+
+int gdb_ctx_set_options(gdb_ctx* c, const gdb_options* opt) {
+  if (!c || !opt) return GDB_ERR_INVALID;
+  gdb_options o = *opt;
+  if (o.block_size == 0) o.block_size = 512;
+  if (o.timeout_ns == 0) o.timeout_ns = 2000000000ull;
+  if (check_options(&o) != GDB_OK) return GDB_ERR_INVALID;
+  o.device = c->device;
+  c->opt = o;
+  return GDB_OK;
+}
+
+int gdb_ctx_get_options(gdb_ctx* c, gdb_options* opt) {
+  if (!c || !opt) return GDB_ERR_INVALID;
+  *opt = c->opt;
+  return GDB_OK;
+}
+
+int gdb_ctx_stream(gdb_ctx* c, void** s) {
+  if (!c || !s) return GDB_ERR_INVALID;
+  *s = (void*)c->stream;
+  return GDB_OK;
+}
+
+const char* gdb_last_error(gdb_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int gdb_last_run_stats(gdb_ctx* c, gdb_run_stats* s) {
+  if (!c || !s) return GDB_ERR_INVALID;
+  *s = c->last;
+  return GDB_OK;
+}
+
+int gdb_debug_stall_master(gdb_ctx* c, int after) {
+  if (!c) return GDB_ERR_INVALID;
+  c->stall_after = after < 0 ? -1 : after;
+  GDB_CUDA(c, cudaMemcpyAsync(&c->dctx->stall_after, &c->stall_after, sizeof(int),
+                              cudaMemcpyHostToDevice, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GDB_OK;
+}
+
+static int graph_common(gdb_ctx* c, uint32_t V, uint64_t E) {
+  if (!c) return GDB_ERR_INVALID;
+  if (V == 0 || V >= 0x7fffffffu || E >= 0xffffffffull) {
+    return set_error(c, GDB_ERR_INVALID, "graph needs 0 < V < 2^31 and E < 2^32");
+  }
+  return GDB_OK;
+}
+
+int gdb_graph_create(gdb_ctx* c, uint32_t V, uint64_t E, const uint32_t* row, const uint32_t* col,
+                     const uint32_t* w, gdb_graph** out) {
+  if (!out || !row || (E && !col)) return GDB_ERR_INVALID;
+  *out = nullptr;
+  int rc = graph_common(c, V, E);
+  if (rc) return rc;
+  if (row[0] != 0 || row[V] != E) return set_error(c, GDB_ERR_INVALID, "row_ptr[0] != 0 or row_ptr[V] != E");
+  gdb_graph* g = new gdb_graph();
+  g->ctx = c;
+  g->V = V;
+  g->E = E;
+  const size_t eb = std::max<uint64_t>(E, 1) * 4;
+  cudaError_t e = cudaMalloc(&g->row, (size_t)(V + 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&g->col, eb);
+  if (e == cudaSuccess && w) e = cudaMalloc(&g->w, eb);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(g->row, row, (size_t)(V + 1) * 4, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess && E) e = cudaMemcpyAsync(g->col, col, E * 4, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess && w && E) e = cudaMemcpyAsync(g->w, w, E * 4, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    rc = set_cuda_error(c, e, "graph upload");
+    gdb_graph_destroy(g);
+    return rc;
+  }
+  rc = build_heavy_table(g, row);
+  if (rc) {
+    gdb_graph_destroy(g);
+    return rc;
+  }
+  *out = g;
+  return GDB_OK;
+}
+
+int gdb_graph_create_device(gdb_ctx* c, uint32_t V, uint64_t E, const uint32_t* d_row,
+                            const uint32_t* d_col, const uint32_t* d_w, gdb_graph** out) {
+  if (!out || !d_row || (E && !d_col)) return GDB_ERR_INVALID;
+  *out = nullptr;
+  int rc = graph_common(c, V, E);
+  if (rc) return rc;
+  std::vector<uint32_t> hrow((size_t)V + 1);
+  cudaError_t e = cudaMemcpy(hrow.data(), d_row, (size_t)(V + 1) * 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return set_cuda_error(c, e, "row_ptr read-back");
+  if (hrow[0] != 0 || hrow[V] != E) return set_error(c, GDB_ERR_INVALID, "row_ptr[0] != 0 or row_ptr[V] != E");
+  gdb_graph* g = new gdb_graph();
+  g->ctx = c;
+  g->V = V;
+  g->E = E;
+  g->row = const_cast<uint32_t*>(d_row);
+  g->col = const_cast<uint32_t*>(d_col);
+  g->w = const_cast<uint32_t*>(d_w);
+  g->owns = false;
+  g->owns_w = false;
+  rc = build_heavy_table(g, hrow.data());
+  if (rc) {
+    gdb_graph_destroy(g);
+    return rc;
+  }
+  *out = g;
+  return GDB_OK;
+}
+
+int gdb_graph_set_weights(gdb_graph* g, const uint32_t* w) {
+  if (!g || !w) return GDB_ERR_INVALID;
+  gdb_ctx* c = g->ctx;
+  if (!g->w || !g->owns_w) {
+    g->w = nullptr;
+    GDB_CUDA(c, cudaMalloc(&g->w, std::max<uint64_t>(g->E, 1) * 4));
+    g->owns_w = true;
+  }
+  if (g->E) GDB_CUDA(c, cudaMemcpyAsync(g->w, w, g->E * 4, cudaMemcpyHostToDevice, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GDB_OK;
+}
+
+int gdb_graph_destroy(gdb_graph* g) {
+  if (!g) return GDB_ERR_INVALID;
+  if (g->ctx && g->ctx->stream) cudaStreamSynchronize(g->ctx->stream);
+  if (g->owns) {
+    cudaFree(g->row);
+    cudaFree(g->col);
+  }
+  if (g->owns_w && g->w) cudaFree(g->w);
+  cudaFree(g->heavy_v);
+  cudaFree(g->heavy_base);
+  cudaFree(g->heavy_bits);
+  cudaGetLastError();
+  delete g;
+  return GDB_OK;
+}
+
+int gdb_graph_info(gdb_graph* g, uint32_t* V, uint64_t* E, uint32_t* heavy) {
+  if (!g) return GDB_ERR_INVALID;
+  if (V) *V = g->V;
+  if (E) *E = g->E;
+  if (heavy) *heavy = g->nheavy;
+  return GDB_OK;
+}
+
+int gdb_device_info_get(gdb_ctx* c, gdb_device_info* info) {
+  if (!c || !info) return GDB_ERR_INVALID;
+  info->device = c->device;
+  info->sm_count = c->sm_count;
+  info->cc_major = c->cc_major;
+  info->cc_minor = c->cc_minor;
+  info->total_mem = c->total_mem;
+  info->flag_capacity = c->flag_cap;
+  info->occupancy_per_sm = 0;
+  return GDB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,458 @@
+// Single-source shortest paths, two reference entry points.
+//
+// 1. Worklist SSSP with LonestarGPU semantics (drelax2,
+//    lonestar/apps/sssp/kernel/sssp_port_kernel.cl:152-197; processedge2
+//    sssp_common.cl:58-81): label-correcting relaxation, atomicMin on the
+//    target, push on improvement; arcs of weight >= 1e9 are skipped.  Its
+//    fixed point is the exact shortest-distance vector, so the result does
+//    not depend on the order of relaxations.  Each superstep pushes a vertex
+//    at most once (a stamp array), the queue is the same light/heavy
+//    frontier as BFS, and one XF barrier separates supersteps.
+//
+// 2. Pannotia Jacobi SSSP (mega_kernel, pannotia/graph_app/sssp/kernel/sssp_kernel.cl:170-244):
+//    y[v] = min(x[v], min_j data[j] + x[col[j]]) over the CSR given (the
+//    reference pulls over the transpose) until nothing changes.  The copy
+//    x = y and the separate diff pass of the reference are folded: the two
+//    vectors swap roles each iteration and the sweep itself raises the
+//    change flag, so an iteration costs one barrier instead of three.
+#include <algorithm>
+
+#include "gdb_internal.h"
+
+namespace {
+
+using namespace gdb;
+
+struct SsspWs {
+  uint32_t* dist;
+  uint32_t* stamp;             // superstep + 1 in which the vertex was pushed
+  uint32_t* q[2];
+  uint32_t* hv[2];
+  uint32_t* hb[2];
+  uint32_t* qcount;            // [3]
+  unsigned long long* hcount;  // [3]
+  uint32_t* cursor;            // [3]
+  uint32_t* hcursor;           // [3]
+  int* overflow;
+  unsigned long long* stats;   // [0] arcs, [1] supersteps
+  uint32_t qcap, hcap;
+};
+
+__device__ __forceinline__ void sssp_step(const GraphView& G, const SsspWs& ws, uint32_t L,
+                                          unsigned long long& arcs) {
+  const int cur = L % 3, nxt = (L + 1) % 3;
+  const uint32_t n = ld_cg(&ws.qcount[cur]);
+  const unsigned long long hp = __ldcg(&ws.hcount[cur]);
+  Frontier out{pick(ws.q, L + 1), pick(ws.hv, L + 1), pick(ws.hb, L + 1), &ws.qcount[nxt],
+               &ws.hcount[nxt], ws.qcap, ws.hcap, ws.overflow};
+  auto relax = [&](bool valid, uint32_t du, uint32_t arc) {
+    uint32_t v = 0;
+    bool want = false;
+    if (valid) {
+      ++arcs;
+      v = __ldg(&G.col[arc]);
+      const uint32_t wt = __ldg(&G.w[arc]);
+      if (wt < kInf) {
+        const uint32_t nd = du + wt;
+        if (nd < ld_cg(&ws.dist[v])) {
+          const uint32_t old = atomicMin(&ws.dist[v], nd);
+          if (nd < old && ld_cg(&ws.stamp[v]) != L + 1 && atomicExch(&ws.stamp[v], L + 1) != L + 1)
+            want = true;
+        }
+      }
+    }
+    frontier_push(G, out, want, v);
+  };
+  // light groups: each lane reads its own vertex's distance once
+  const int lane = lane_id();
+  for (;;) {
+    const uint32_t g = warp_grab(&ws.cursor[cur]);
+    if ((uint64_t)g * 32 >= n) break;
+    const uint32_t i = g * 32 + lane;
+    const bool act = i < n;
+    const uint32_t u = act ? ld_cg(&pick(ws.q, L)[i]) : 0u;
+    const uint32_t du = act ? ld_cg(&ws.dist[u]) : 0u;
+    group_arcs(G, act, u, [&](bool valid, int owner, uint32_t arc) {
+      relax(valid, __shfl_sync(kFull, du, owner), arc);
+    });
+  }
+  const uint32_t ne = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
+  const uint32_t* hv = pick(ws.hv, L);
+  const uint32_t* hb = pick(ws.hb, L);
+  for (;;) {
+    const uint32_t c = warp_grab(&ws.hcursor[cur]);
+    if (c >= nch) break;
+    uint32_t e = 0;
+    if (lane == 0) e = upper_index(hb, ne, c);
+    e = __shfl_sync(kFull, e, 0);
+    const uint32_t u = ld_cg(&hv[e]);
+    const uint32_t j = c - ld_cg(&hb[e]);
+    const uint32_t du = ld_cg(&ws.dist[u]);
+    const uint32_t rb = __ldg(&G.row[u]), re = __ldg(&G.row[u + 1]);
+    const uint32_t b = rb + j * kChunk, en = min(re, b + kChunk);
+    range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, du, arc); });
+  }
+}
+
+template <class Sync>
+__device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const SsspWs& ws, uint32_t src) {
+  const Warps W = warps_of(s.id(), s.P());
+  const bool leader = s.id() == 0 && threadIdx.x == 0;
+  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+    ws.dist[v] = kInf;
+    ws.stamp[v] = 0;
+  }
+  if (leader) {
+    for (int i = 0; i < 3; ++i) {
+      ws.qcount[i] = 0;
+      ws.hcount[i] = 0;
+      ws.cursor[i] = 0;
+      ws.hcursor[i] = 0;
+    }
+    *ws.overflow = 0;
+    ws.stats[0] = ws.stats[1] = 0;
+  }
+  if (!s.sync()) return;
+  if (leader) {
+    ws.dist[src] = 0;
+    ws.stamp[src] = 0;
+    const uint32_t deg = G.row[src + 1] - G.row[src];
+    if (is_heavy(G, src)) {
+      ws.hv[0][0] = src;
+      ws.hb[0][0] = 0;
+      ws.hcount[0] = (1ull << 32) | chunks_of(deg);
+    } else {
+      ws.q[0][0] = src;
+      ws.qcount[0] = 1;
+    }
+  }
+  if (!s.sync()) return;
+  unsigned long long arcs = 0;
+  uint32_t L = 0;
+  for (;; ++L) {
+    const int cur = L % 3, old = (L + 2) % 3;
+    if (ld_cg(&ws.qcount[cur]) == 0 && __ldcg(&ws.hcount[cur]) == 0) break;
+    if (leader) {
+      ws.qcount[old] = 0;
+      ws.hcount[old] = 0;
+      ws.cursor[old] = 0;
+      ws.hcursor[old] = 0;
+    }
+    sssp_step(G, ws, L, arcs);
+    if (!s.sync()) return;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
+  if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  if (leader) ws.stats[1] = L;
+}
+
+__global__ void __launch_bounds__(1024, 1) k_sssp_xf(DiscoveryArgs a, GraphView G, SsspWs ws, uint32_t src) {
+  __shared__ LocalCtx l;
+  if (!discover(a, &l)) return;
+  XfSync s{&a, &l};
+  sssp_body(s, G, ws, src);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_sssp_grid(GraphView G, SsspWs ws, uint32_t src) {
+  GridSync s;
+  sssp_body(s, G, ws, src);
+}
+
+// ------------------------------------------------------------- Jacobi
+
+struct JacobiWs {
+  int32_t* x[2];
+  uint32_t* cursor;    // [3]
+  uint32_t* hcursor;   // [3]
+  uint32_t* changed;   // [3]
+  unsigned long long* stats;  // [0] arcs, [1] iterations
+};
+
+// One Jacobi iteration reading x[k&1] and writing x[(k+1)&1].  Light
+// vertices: per-owner minimum in a shared-memory slot; heavy vertices:
+// chunk minima combined with atomicMin -- valid without re-initialising the
+// target because costs only decrease (its stale content is an older,
+// larger cost of the same vertex).  Arithmetic is the reference's int32
+// (data[j] + x[col[j]], sssp_kernel.cl:219-220).
+__device__ __forceinline__ bool jacobi_iter(const GraphView& G, const JacobiWs& ws, uint32_t k,
+                                            int* smin, unsigned long long& arcs) {
+  const int cur = k % 3;
+  const int32_t* xo = pick(ws.x, k);
+  int32_t* xn = pick(ws.x, k + 1);
+  const int lane = lane_id();
+  int* my = smin + (threadIdx.x & ~31u);
+  bool changed = false;
+  int32_t xv = 0;
+  sweep_light(
+      G, &ws.cursor[cur],
+      [&](uint32_t v, bool in_range) {
+        xv = in_range ? ld_cg(&xo[v]) : 0;
+        my[lane] = xv;
+        return true;
+      },
+      [&](bool valid, int owner, uint32_t arc) {
+        if (valid) {
+          ++arcs;
+          const int32_t c = (int32_t)__ldg(&G.w[arc]) + ld_cg(&xo[__ldg(&G.col[arc])]);
+          if (c < my[owner]) atomicMin(&my[owner], c);
+        }
+      },
+      [&](uint32_t v, bool act) {
+        if (act) {
+          const int32_t m = my[lane];
+          xn[v] = m;
+          if (m != xv) changed = true;
+        }
+      });
+  sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
+    const int32_t xov = ld_cg(&xo[v]);
+    int32_t m = xov;
+    for (uint32_t a0 = b; a0 < e; a0 += 32) {
+      const uint32_t a = a0 + lane;
+      if (a < e) {
+        ++arcs;
+        const int32_t c = (int32_t)__ldg(&G.w[a]) + ld_cg(&xo[__ldg(&G.col[a])]);
+        m = min(m, c);
+      }
+    }
+    m = __reduce_min_sync(kFull, m);
+    if (lane == 0) {
+      atomicMin(&xn[v], m);
+      if (m < xov) changed = true;
+    }
+  });
+  return changed;
+}
+
+template <class Sync>
+__device__ __forceinline__ void jacobi_body(Sync& s, const GraphView& G, const JacobiWs& ws,
+                                            uint32_t src, int* smin) {
+  const Warps W = warps_of(s.id(), s.P());
+  const bool leader = s.id() == 0 && threadIdx.x == 0;
+  // vector_init (sssp_kernel.cl:111-132) into both buffers
+  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+    const int32_t init = v == src ? 0 : GDB_PANNOTIA_BIG;
+    ws.x[0][v] = init;
+    ws.x[1][v] = init;
+  }
+  if (leader) {
+    for (int i = 0; i < 3; ++i) ws.cursor[i] = ws.hcursor[i] = ws.changed[i] = 0;
+    ws.stats[0] = ws.stats[1] = 0;
+  }
+  if (!s.sync()) return;
+  unsigned long long arcs = 0;
+  uint32_t k = 0;
+  // the reference iterates k = 1 .. num_rows-1 (sssp_kernel.cl:185)
+  for (; k + 1 < G.V; ++k) {
+    const int cur = k % 3, old = (k + 2) % 3;
+    if (leader) ws.cursor[old] = ws.hcursor[old] = ws.changed[old] = 0;
+    const bool ch = jacobi_iter(G, ws, k, smin, arcs);
+    if (__any_sync(kFull, ch) && lane_id() == 0) atomicOr(&ws.changed[cur], 1u);
+    if (!s.sync()) return;
+    if (ld_cg(&ws.changed[cur]) == 0) {
+      ++k;
+      break;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
+  if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  // iterations run; the answer is in x[k & 1]
+  if (leader) ws.stats[1] = k;
+}
+
+__global__ void __launch_bounds__(1024, 1) k_jacobi_xf(DiscoveryArgs a, GraphView G, JacobiWs ws, uint32_t src) {
+  __shared__ LocalCtx l;
+  __shared__ int smin[1024];
+  if (!discover(a, &l)) return;
+  XfSync s{&a, &l};
+  jacobi_body(s, G, ws, src, smin);
+}
+
+}  // namespace
+
+using namespace gdbi;
+
+static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
+  if (!graph_ok(c, g) || !d_dist) return GDB_ERR_INVALID;
+  if (src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
+  const uint32_t V = g->V;
+  const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
+  Bump b;
+  const size_t o_st = b.take((size_t)V * 4);
+  const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
+  const size_t o_hv0 = b.take(hcap * 4), o_hv1 = b.take(hcap * 4);
+  const size_t o_hb0 = b.take(hcap * 4), o_hb1 = b.take(hcap * 4);
+  const size_t o_cnt = b.take(512);
+  char* base = (char*)workspace(c, b.off);
+  if (!base) return GDB_ERR_OOM;
+  SsspWs ws;
+  ws.dist = d_dist;
+  ws.stamp = (uint32_t*)(base + o_st);
+  ws.q[0] = (uint32_t*)(base + o_q0);
+  ws.q[1] = (uint32_t*)(base + o_q1);
+  ws.hv[0] = (uint32_t*)(base + o_hv0);
+  ws.hv[1] = (uint32_t*)(base + o_hv1);
+  ws.hb[0] = (uint32_t*)(base + o_hb0);
+  ws.hb[1] = (uint32_t*)(base + o_hb1);
+  char* cnt = base + o_cnt;
+  ws.stats = (unsigned long long*)cnt;
+  ws.hcount = (unsigned long long*)(cnt + 64);
+  ws.qcount = (uint32_t*)(cnt + 96);
+  ws.cursor = (uint32_t*)(cnt + 112);
+  ws.hcursor = (uint32_t*)(cnt + 128);
+  ws.overflow = (int*)(cnt + 160);
+  ws.qcap = V;
+  ws.hcap = hcap;
+  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
+  const GraphView G = g->view();
+  const int block = c->opt.block_size;
+  const int kind = c->opt.barrier;
+  c->last = gdb_run_stats{};
+  int rc = GDB_OK;
+  if (kind == GDB_BARRIER_XF || kind == GDB_BARRIER_XF_FIXED) {
+    Shape s;
+    rc = persistent_shape(c, (const void*)k_sssp_xf, block, 0, &s, kind == GDB_BARRIER_XF);
+    if (rc) return rc;
+    DiscoveryArgs a = discovery_args(c, s);
+    GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    k_sssp_xf<<<s.grid, block, 0, c->stream>>>(a, G, ws, src);
+    GDB_CUDA(c, cudaGetLastError());
+    GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    rc = finish_run(c);
+    if (rc) return rc;
+    int n = 0;
+    read_participating(c, &n);
+    c->last.participating = n;
+    c->last.launched = s.grid;
+  } else if (kind == GDB_BARRIER_GRID_SYNC) {
+    int occ = 0;
+    GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sssp_grid, block, 0));
+    int grid = occ * c->sm_count;
+    if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
+    GraphView Gc = G;
+    SsspWs wsc = ws;
+    uint32_t srcc = src;
+    void* args[] = {(void*)&Gc, (void*)&wsc, (void*)&srcc};
+    GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    GDB_CUDA(c, cudaLaunchCooperativeKernel((const void*)k_sssp_grid, grid, block, args, 0, c->stream));
+    GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->last.participating = grid;
+    c->last.launched = grid;
+  } else {
+    return set_error(c, GDB_ERR_UNSUPPORTED, "barrier kind not available for SSSP");
+  }
+  c->last.launches = 1;
+  unsigned long long* hs = (unsigned long long*)pinned(c, 512);
+  if (!hs) return GDB_ERR_OOM;
+  GDB_CUDA(c, cudaMemcpyAsync(hs, cnt, 512, cudaMemcpyDeviceToHost, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (*(int*)((char*)hs + 160)) return set_error(c, GDB_ERR_CAPACITY, "SSSP queue overflow");
+  float ms = 0;
+  GDB_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->last.kernel_ms = ms;
+  c->last.edges_processed = hs[0];
+  c->last.supersteps = (uint32_t)hs[1];
+  return GDB_OK;
+}
+
+static int jacobi_run(gdb_ctx* c, gdb_graph* g, uint32_t src, int32_t* d_cost) {
+  if (!graph_ok(c, g) || !d_cost) return GDB_ERR_INVALID;
+  if (src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
+  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED)
+    return set_error(c, GDB_ERR_UNSUPPORTED, "Jacobi SSSP runs on the XF barrier");
+  Bump b;
+  const size_t o_x = b.take((size_t)g->V * 4);
+  const size_t o_cnt = b.take(256);
+  char* base = (char*)workspace(c, b.off);
+  if (!base) return GDB_ERR_OOM;
+  JacobiWs ws;
+  ws.x[0] = d_cost;
+  ws.x[1] = (int32_t*)(base + o_x);
+  char* cnt = base + o_cnt;
+  ws.stats = (unsigned long long*)cnt;
+  ws.cursor = (uint32_t*)(cnt + 64);
+  ws.hcursor = (uint32_t*)(cnt + 80);
+  ws.changed = (uint32_t*)(cnt + 96);
+  const GraphView G = g->view();
+  const int block = c->opt.block_size;
+  c->last = gdb_run_stats{};
+  Shape s;
+  int rc = persistent_shape(c, (const void*)k_jacobi_xf, block, 0, &s,
+                            c->opt.barrier == GDB_BARRIER_XF);
+  if (rc) return rc;
+  DiscoveryArgs a = discovery_args(c, s);
+  GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  k_jacobi_xf<<<s.grid, block, 0, c->stream>>>(a, G, ws, src);
+  GDB_CUDA(c, cudaGetLastError());
+  GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  rc = finish_run(c);
+  if (rc) return rc;
+  unsigned long long* hs = (unsigned long long*)pinned(c, 256);
+  if (!hs) return GDB_ERR_OOM;
+  GDB_CUDA(c, cudaMemcpyAsync(hs, cnt, 64, cudaMemcpyDeviceToHost, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  const uint32_t k = (uint32_t)hs[1];
+  if (k & 1) {
+    GDB_CUDA(c, cudaMemcpyAsync(d_cost, ws.x[1], (size_t)g->V * 4, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  float ms = 0;
+  GDB_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  int n = 0;
+  read_participating(c, &n);
+  c->last.participating = n;
+  c->last.launched = s.grid;
+  c->last.launches = 1;
+  c->last.kernel_ms = ms;
+  c->last.edges_processed = hs[0];
+  c->last.supersteps = k;
+  return GDB_OK;
+}
+
+extern "C" {
+
+int gdb_sssp_jacobi_device(gdb_ctx* c, gdb_graph* g, uint32_t src, int32_t* d_cost) {
+  return jacobi_run(c, g, src, d_cost);
+}
+
+int gdb_sssp_jacobi(gdb_ctx* c, gdb_graph* g, uint32_t src, int32_t* cost) {
+  if (!graph_ok(c, g) || !cost) return GDB_ERR_INVALID;
+  int32_t* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, (size_t)g->V * 4, c->stream));
+  int rc = jacobi_run(c, g, src, d);
+  if (rc == GDB_OK) {
+    cudaError_t e = cudaMemcpyAsync(cost, d, (size_t)g->V * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "cost read-back");
+  }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
+int gdb_sssp_device(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
+  return sssp_run(c, g, src, d_dist);
+}
+
+int gdb_sssp(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* dist) {
+  if (!graph_ok(c, g) || !dist) return GDB_ERR_INVALID;
+  uint32_t* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, (size_t)g->V * 4, c->stream));
+  int rc = sssp_run(c, g, src, d);
+  if (rc == GDB_OK) {
+    cudaError_t e = cudaMemcpyAsync(dist, d, (size_t)g->V * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "dist read-back");
+  }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,318 @@
+// Device building blocks shared by the persistent graph kernels.
+//
+// Work distribution over a CSR in HBM:
+//  * light vertices (degree <= kHeavyDeg) are taken 32 at a time by one warp;
+//    the warp scans their degrees and walks their concatenated arc lists 32
+//    arcs per step, each lane finding the vertex that owns its arc with a
+//    5-step shuffle binary search -- consecutive lanes read consecutive
+//    column ids, so col[] streams in full 128-byte lines;
+//  * heavy vertices are cut into chunks of kChunk arcs handed out one per
+//    warp, so a hub never serialises a superstep;
+//  * frontier pushes are warp-aggregated: one atomicAdd per warp and queue.
+#pragma once
+
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gdb_discovery.cuh"
+
+namespace gdb {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr uint32_t kHeavyDeg = 1024;
+constexpr uint32_t kChunk = 1024;
+constexpr uint32_t kInf = GDB_LONESTAR_INF;
+
+struct GraphView {
+  uint32_t V;
+  uint32_t E;
+  const uint32_t* __restrict__ row;
+  const uint32_t* __restrict__ col;
+  const uint32_t* __restrict__ w;
+  uint32_t nheavy;
+  uint32_t nheavy_chunks;
+  const uint32_t* __restrict__ heavy_v;     // ascending ids
+  const uint32_t* __restrict__ heavy_base;  // chunk prefix, nheavy + 1
+  const uint32_t* __restrict__ heavy_bits;  // membership bitmap
+};
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+__device__ __forceinline__ bool is_heavy(const GraphView& G, uint32_t v) {
+  return (__ldg(&G.heavy_bits[v >> 5]) >> (v & 31)) & 1u;
+}
+__host__ __device__ __forceinline__ uint32_t chunks_of(uint32_t deg) { return (deg + kChunk - 1) / kChunk; }
+
+// Loads that bypass L1 for arrays other CTAs update during the kernel.
+__device__ __forceinline__ uint32_t ld_cg(const uint32_t* p) { return __ldcg(p); }
+__device__ __forceinline__ int32_t ld_cg(const int32_t* p) { return __ldcg(p); }
+__device__ __forceinline__ float ld_cg(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ unsigned long long ld_cg(const unsigned long long* p) { return __ldcg(p); }
+__device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
+
+// a[i & 1] without dynamic indexing (which would copy the kernel-parameter
+// array to local memory).
+template <class T>
+__device__ __forceinline__ T pick(const T (&a)[2], uint32_t i) {
+  return (i & 1) ? a[1] : a[0];
+}
+
+// Order-preserving float <-> uint32 map (so atomicMin/Max on uint32 order
+// floats; -0 is folded onto +0 first).
+__device__ __forceinline__ uint32_t fkey(float f) {
+  uint32_t b = __float_as_uint(f == 0.0f ? 0.0f : f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(uint32_t k) {
+  uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+  return __uint_as_float(b);
+}
+
+// Warp identity among the participating CTAs.
+struct Warps {
+  uint32_t gwarp;   // global warp index
+  uint32_t nwarps;  // warps in the participating grid
+  uint32_t gthread;
+  uint32_t nthreads;
+};
+__device__ __forceinline__ Warps warps_of(int id, int P) {
+  Warps w;
+  const uint32_t wpb = blockDim.x >> 5;
+  w.gwarp = (uint32_t)id * wpb + (threadIdx.x >> 5);
+  w.nwarps = (uint32_t)P * wpb;
+  w.gthread = (uint32_t)id * blockDim.x + threadIdx.x;
+  w.nthreads = (uint32_t)P * blockDim.x;
+  return w;
+}
+
+// Lane 0 takes the next ticket from a global cursor; broadcast to the warp.
+__device__ __forceinline__ uint32_t warp_grab(uint32_t* cursor) {
+  uint32_t t = 0;
+  if (lane_id() == 0) t = atomicAdd(cursor, 1u);
+  return __shfl_sync(kFull, t, 0);
+}
+
+// Walk the arcs of the (active, light) vertices held by the 32 lanes.
+// Calls fn(valid, owner_lane, arc) once per 32-arc step with every lane
+// present, so fn may use warp collectives; `valid` marks lanes with an arc.
+template <class Fn>
+__device__ __forceinline__ void group_arcs(const GraphView& G, bool active, uint32_t v, Fn&& fn) {
+  const int lane = lane_id();
+  uint32_t beg = 0, deg = 0;
+  if (active) {
+    beg = __ldg(&G.row[v]);
+    deg = __ldg(&G.row[v + 1]) - beg;
+  }
+  uint32_t pre = deg;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(kFull, pre, o);
+    if (lane >= o) pre += t;
+  }
+  const uint32_t total = __shfl_sync(kFull, pre, 31);
+  pre -= deg;
+  for (uint32_t base = 0; base < total; base += 32) {
+    const uint32_t k = base + lane;
+    int lo = 0;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+      uint32_t p = __shfl_sync(kFull, pre, lo + s);
+      if (p <= k) lo += s;
+    }
+    const uint32_t obeg = __shfl_sync(kFull, beg, lo);
+    const uint32_t opre = __shfl_sync(kFull, pre, lo);
+    fn(k < total, lo, obeg + (k - opre));
+  }
+}
+
+// Walk arcs [b, e) of one vertex, 32 per step, every lane present.
+template <class Fn>
+__device__ __forceinline__ void range_arcs(uint32_t b, uint32_t e, Fn&& fn) {
+  const int lane = lane_id();
+  for (uint32_t a0 = b; a0 < e; a0 += 32) {
+    const uint32_t a = a0 + lane;
+    fn(a < e, a);
+  }
+}
+
+// Largest index i in [0, n) with base[i] <= c (base ascending, base[0] = 0).
+__device__ __forceinline__ uint32_t upper_index(const uint32_t* base, uint32_t n, uint32_t c) {
+  uint32_t lo = 0, hi = n;  // invariant: base[lo] <= c, answer in [lo, hi)
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (ld_cg(&base[mid]) <= c) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// A frontier: light vertex queue plus heavy entries (vertex, first chunk)
+// whose chunk bases ascend with the slot (one packed 64-bit atomicAdd
+// hands out both), so chunk c belongs to the last entry with base <= c.
+struct Frontier {
+  uint32_t* q;        // light vertices
+  uint32_t* hv;       // heavy vertices
+  uint32_t* hb;       // first chunk of each heavy entry
+  uint32_t* qcount;   // light count
+  unsigned long long* hcount;  // (entries << 32) | chunks
+  uint32_t qcap, hcap;
+  int* overflow;      // set when a push would exceed a capacity
+  uint32_t* hleft = nullptr;  // optional: chunk countdown armed at push
+  double* hacc = nullptr;     // optional: FP64 accumulator cleared at push
+};
+
+// Warp-aggregated push of the lanes' `want` vertices.
+__device__ __forceinline__ void frontier_push(const GraphView& G, const Frontier& F, bool want,
+                                              uint32_t v) {
+  const int lane = lane_id();
+  const bool heavy = want && is_heavy(G, v);
+  const bool light = want && !heavy;
+  const unsigned m = __ballot_sync(kFull, light);
+  if (m) {
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(F.qcount, (uint32_t)__popc(m));
+    base = __shfl_sync(kFull, base, leader);
+    if (light) {
+      const uint32_t slot = base + __popc(m & lanemask_lt());
+      if (slot < F.qcap) F.q[slot] = v;
+      else atomicExch(F.overflow, 1);
+    }
+  }
+  if (heavy) {
+    const uint32_t deg = __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
+    const unsigned long long old =
+        atomicAdd(F.hcount, (1ull << 32) | (unsigned long long)chunks_of(deg));
+    const uint32_t slot = (uint32_t)(old >> 32);
+    if (slot < F.hcap) {
+      F.hv[slot] = v;
+      F.hb[slot] = (uint32_t)old;
+      if (F.hleft) {
+        F.hleft[slot] = chunks_of(deg);
+        F.hacc[slot] = 0.0;
+      }
+    } else {
+      atomicExch(F.overflow, 1);
+    }
+  }
+}
+
+// Visit a frontier: light vertices in warp groups of 32, then heavy chunks.
+// light(valid, owner_lane, owner_vertex_in_lane, arc) is called through
+// group_arcs; heavy(valid, v, arc) per 32-arc step of a chunk.
+template <class Light, class Heavy>
+__device__ __forceinline__ void visit_frontier(const GraphView& G, const uint32_t* q, uint32_t n,
+                                               const uint32_t* hv, const uint32_t* hb,
+                                               unsigned long long hpacked, uint32_t* cursor,
+                                               uint32_t* hcursor, Light&& light, Heavy&& heavy) {
+  const int lane = lane_id();
+  for (;;) {
+    const uint32_t g = warp_grab(cursor);
+    if ((uint64_t)g * 32 >= n) break;
+    const uint32_t i = g * 32 + lane;
+    const bool act = i < n;
+    const uint32_t v = act ? ld_cg(&q[i]) : 0u;
+    group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) { light(valid, owner, v, arc); });
+  }
+  const uint32_t ne = (uint32_t)(hpacked >> 32);
+  const uint32_t nch = (uint32_t)hpacked;
+  for (;;) {
+    const uint32_t c = warp_grab(hcursor);
+    if (c >= nch) break;
+    uint32_t e = 0;
+    if (lane == 0) e = upper_index(hb, ne, c);
+    e = __shfl_sync(kFull, e, 0);
+    const uint32_t v = ld_cg(&hv[e]);
+    const uint32_t j = c - ld_cg(&hb[e]);
+    const uint32_t rb = __ldg(&G.row[v]), re = __ldg(&G.row[v + 1]);
+    const uint32_t b = rb + j * kChunk;
+    const uint32_t en = min(re, b + kChunk);
+    range_arcs(b, en, [&](bool valid, uint32_t arc) { heavy(valid, v, arc); });
+  }
+}
+
+// Sweep the light vertices of [0, V) in warp groups of 32 consecutive ids.
+// begin(v, in_range) -> bool active: per-lane setup (v is light and < V
+// when in_range); edge(valid, owner_lane, arc) per 32-arc step;
+// end(v, active) after the group's arcs.  Groups come from `cursor`.
+template <class Begin, class Edge, class End>
+__device__ __forceinline__ void sweep_light(const GraphView& G, uint32_t* cursor, Begin&& begin,
+                                            Edge&& edge, End&& end) {
+  const int lane = lane_id();
+  const uint32_t ngroups = (G.V + 31) / 32;
+  for (;;) {
+    const uint32_t g = warp_grab(cursor);
+    if (g >= ngroups) break;
+    const uint32_t v = g * 32 + lane;
+    const bool in_range = v < G.V && !is_heavy(G, v);
+    const bool act = begin(v, in_range) && in_range;
+    __syncwarp();
+    group_arcs(G, act, v, edge);
+    __syncwarp();
+    end(v, act);
+  }
+}
+
+// Sweep the heavy vertices through the static chunk table, one chunk per
+// warp: fn(v, heavy_index, chunk_in_vertex, arc_begin, arc_end).
+template <class Fn>
+__device__ __forceinline__ void sweep_heavy(const GraphView& G, uint32_t* hcursor, Fn&& fn) {
+  const int lane = lane_id();
+  for (;;) {
+    const uint32_t c = warp_grab(hcursor);
+    if (c >= G.nheavy_chunks) break;
+    uint32_t e = 0;
+    if (lane == 0) e = upper_index(G.heavy_base, G.nheavy, c);
+    e = __shfl_sync(kFull, e, 0);
+    const uint32_t v = __ldg(&G.heavy_v[e]);
+    const uint32_t j = c - __ldg(&G.heavy_base[e]);
+    const uint32_t rb = __ldg(&G.row[v]), re = __ldg(&G.row[v + 1]);
+    const uint32_t b = rb + j * kChunk;
+    const uint32_t en = min(re, b + kChunk);
+    fn(v, e, j, b, en);
+  }
+}
+
+// Warp reductions.
+__device__ __forceinline__ uint32_t warp_min_u32(uint32_t x) { return __reduce_min_sync(kFull, x); }
+__device__ __forceinline__ uint32_t warp_max_u32(uint32_t x) { return __reduce_max_sync(kFull, x); }
+__device__ __forceinline__ uint32_t warp_or_u32(uint32_t x) { return __reduce_or_sync(kFull, x); }
+__device__ __forceinline__ uint32_t warp_add_u32(uint32_t x) { return __reduce_add_sync(kFull, x); }
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long y = __shfl_xor_sync(kFull, x, o);
+    x = y < x ? y : x;
+  }
+  return x;
+}
+__device__ __forceinline__ double warp_sum_f64(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
+  return x;
+}
+
+// Barrier abstraction for the persistent kernels: XF over discovered CTAs
+// or cooperative_groups grid sync over a cooperative launch.
+struct XfSync {
+  const DiscoveryArgs* a;
+  LocalCtx* l;
+  __device__ __forceinline__ bool sync() { return xf_barrier(*a, l); }
+  __device__ __forceinline__ int id() const { return l->id; }
+  __device__ __forceinline__ int P() const { return l->P; }
+};
+struct GridSync {
+  __device__ __forceinline__ bool sync() {
+    cooperative_groups::this_grid().sync();
+    return true;
+  }
+  __device__ __forceinline__ int id() const { return blockIdx.x; }
+  __device__ __forceinline__ int P() const { return gridDim.x; }
+};
+
+}  // namespace gdb

@@ -1,0 +1,362 @@
+"""ctypes mirror of the C ABI in include/gdb.h.
+
+The names follow the reference's host API and kernels:
+
+* discovery (code/discovery_protocol/api/discovery.h): ``init_discovery_kernel_ctx``,
+  ``init_discovery_kernel_ctx_skip``, ``number_of_participating_groups``,
+  ``time_protocol``; occupancy tests (occupancy_tests/src/occupancy_test.c);
+* one call per reference app: ``bfs`` (LonestarGPU bfs drelax2), ``sssp``
+  (LonestarGPU sssp drelax2), ``sssp_jacobi`` (Pannotia sssp mega_kernel),
+  ``mis``, ``color``, ``bc`` (Pannotia mega-kernels), ``mst`` (LonestarGPU mst).
+
+There is no CPU fallback: if ``lib/libgdb.so`` is missing or a call fails, a
+``GdbError`` is raised.  Every call runs on the context's own CUDA stream and
+returns when its result is ready.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libgdb.so"
+
+LONESTAR_INF = 1_000_000_000
+PANNOTIA_BIG = 99_999_999
+
+LOCK_TICKET, LOCK_SPIN, LOCK_FREE = 0, 1, 2
+BARRIER_XF, BARRIER_GRID_SYNC, BARRIER_RELAUNCH, BARRIER_XF_FIXED, BARRIER_RELAUNCH_GRAPH = range(5)
+SCHED_PLAIN, SCHED_ADAPTIVE = 0, 1
+
+STATUS = {0: "GDB_OK", -1: "GDB_ERR_INVALID", -2: "GDB_ERR_CUDA", -3: "GDB_ERR_OOM",
+          -4: "GDB_ERR_TIMEOUT", -5: "GDB_ERR_CAPACITY", -6: "GDB_ERR_NOT_CORESIDENT",
+          -7: "GDB_ERR_UNSUPPORTED"}
+
+
+class GdbError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        super().__init__(f"{where}: {STATUS.get(status, status)}" + (f" ({detail})" if detail else ""))
+
+
+class Options(C.Structure):
+    _fields_ = [("device", C.c_int), ("block_size", C.c_int), ("max_ctas", C.c_int),
+                ("oversubscribe", C.c_int), ("lock", C.c_int), ("barrier", C.c_int),
+                ("schedule", C.c_int), ("reserved0", C.c_int), ("timeout_ns", C.c_uint64)]
+
+
+class RunStats(C.Structure):
+    _fields_ = [("supersteps", C.c_uint32), ("participating", C.c_uint32),
+                ("launched", C.c_uint32), ("launches", C.c_uint32),
+                ("edges_processed", C.c_uint64), ("work_units", C.c_uint64),
+                ("kernel_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class MstResult(C.Structure):
+    _fields_ = [("weight64", C.c_uint64), ("weight32", C.c_uint32), ("components", C.c_uint32),
+                ("edges", C.c_uint32), ("rounds", C.c_uint32)]
+
+
+class DeviceInfo(C.Structure):
+    _fields_ = [("device", C.c_int), ("sm_count", C.c_int), ("cc_major", C.c_int),
+                ("cc_minor", C.c_int), ("total_mem", C.c_size_t), ("occupancy_per_sm", C.c_int),
+                ("flag_capacity", C.c_int)]
+
+
+_LIB = None
+_P = C.c_void_p
+_u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+
+# (name, restype, argtypes) for every symbol of include/gdb.h
+SIGNATURES = [
+    ("gdb_options_default", None, [C.POINTER(Options)]),
+    ("gdb_ctx_create", C.c_int, [C.POINTER(Options), C.POINTER(_P)]),
+    ("gdb_ctx_destroy", C.c_int, [_P]),
+    ("gdb_ctx_set_options", C.c_int, [_P, C.POINTER(Options)]),
+    ("gdb_ctx_get_options", C.c_int, [_P, C.POINTER(Options)]),
+    ("gdb_ctx_stream", C.c_int, [_P, C.POINTER(_P)]),
+    ("gdb_device_info_get", C.c_int, [_P, C.POINTER(DeviceInfo)]),
+    ("gdb_status_string", C.c_char_p, [C.c_int]),
+    ("gdb_last_error", C.c_char_p, [_P]),
+    ("gdb_last_run_stats", C.c_int, [_P, C.POINTER(RunStats)]),
+    ("gdb_abi_version", C.c_int, []),
+    ("gdb_init_discovery_kernel_ctx", C.c_int, [_P]),
+    ("gdb_init_discovery_kernel_ctx_skip", C.c_int, [_P, C.c_int]),
+    ("gdb_number_of_participating_groups", C.c_int, [_P]),
+    ("gdb_time_protocol", C.c_int, [_P, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    ("gdb_occupancy_test", C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    ("gdb_api_occupancy", C.c_int, [_P, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    ("gdb_barrier_bench", C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                    C.POINTER(C.c_int)]),
+    ("gdb_debug_stall_master", C.c_int, [_P, C.c_int]),
+    ("gdb_graph_create", C.c_int, [_P, C.c_uint32, C.c_uint64, _P, _P, _P, C.POINTER(_P)]),
+    ("gdb_graph_create_device", C.c_int, [_P, C.c_uint32, C.c_uint64, _P, _P, _P, C.POINTER(_P)]),
+    ("gdb_graph_set_weights", C.c_int, [_P, _P]),
+    ("gdb_graph_destroy", C.c_int, [_P]),
+    ("gdb_graph_info", C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64),
+                                 C.POINTER(C.c_uint32)]),
+    ("gdb_bfs", C.c_int, [_P, _P, C.c_uint32, _P]),
+    ("gdb_bfs_device", C.c_int, [_P, _P, C.c_uint32, _P]),
+    ("gdb_sssp", C.c_int, [_P, _P, C.c_uint32, _P]),
+    ("gdb_sssp_device", C.c_int, [_P, _P, C.c_uint32, _P]),
+    ("gdb_sssp_jacobi", C.c_int, [_P, _P, C.c_uint32, _P]),
+    ("gdb_sssp_jacobi_device", C.c_int, [_P, _P, C.c_uint32, _P]),
+    ("gdb_mis", C.c_int, [_P, _P, _P, _P]),
+    ("gdb_mis_device", C.c_int, [_P, _P, _P, _P]),
+    ("gdb_color", C.c_int, [_P, _P, _P, _P]),
+    ("gdb_color_device", C.c_int, [_P, _P, _P, _P]),
+    ("gdb_bc", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_bc_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_mst", C.c_int, [_P, _P, C.POINTER(MstResult), _P]),
+    ("gdb_mst_device", C.c_int, [_P, _P, _P, _P]),
+]
+
+
+def lib() -> C.CDLL:
+    """Load lib/libgdb.so; raises when it has not been built."""
+    global _LIB
+    if _LIB is None:
+        if not LIB_PATH.exists():
+            raise GdbError(-2, "libgdb", f"{LIB_PATH} missing -- run __graft_entry__.build()")
+        L = C.CDLL(str(LIB_PATH))
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    lib().gdb_options_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Ctx:
+    """A gdb_ctx: one CUDA stream, the discovery context, a workspace."""
+
+    def __init__(self, **options):
+        self._lib = lib()
+        self.opt = default_options(**options)
+        h = _P()
+        rc = self._lib.gdb_ctx_create(C.byref(self.opt), C.byref(h))
+        if rc != 0:
+            raise GdbError(rc, "gdb_ctx_create")
+        self.h = h
+
+    # -- plumbing
+    def check(self, rc: int, where: str) -> int:
+        if rc < 0:
+            raise GdbError(rc, where, self._lib.gdb_last_error(self.h).decode())
+        return rc
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self._lib.gdb_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_options(self, **kw) -> None:
+        o = Options()
+        self.check(self._lib.gdb_ctx_get_options(self.h, C.byref(o)), "gdb_ctx_get_options")
+        for k, v in kw.items():
+            setattr(o, k, v)
+        self.check(self._lib.gdb_ctx_set_options(self.h, C.byref(o)), "gdb_ctx_set_options")
+        self.opt = o
+
+    def stream(self) -> int:
+        s = _P()
+        self.check(self._lib.gdb_ctx_stream(self.h, C.byref(s)), "gdb_ctx_stream")
+        return s.value or 0
+
+    def device_info(self) -> dict:
+        d = DeviceInfo()
+        self.check(self._lib.gdb_device_info_get(self.h, C.byref(d)), "gdb_device_info_get")
+        return {k: getattr(d, k) for k, _ in d._fields_}
+
+    def last_stats(self) -> dict:
+        s = RunStats()
+        self.check(self._lib.gdb_last_run_stats(self.h, C.byref(s)), "gdb_last_run_stats")
+        return s.as_dict()
+
+    # -- discovery protocol / barrier (discovery.h)
+    def init_discovery_kernel_ctx(self, skip: int | None = None) -> None:
+        if skip is None:
+            self.check(self._lib.gdb_init_discovery_kernel_ctx(self.h), "init_discovery_kernel_ctx")
+        else:
+            self.check(self._lib.gdb_init_discovery_kernel_ctx_skip(self.h, int(skip)),
+                       "init_discovery_kernel_ctx_skip")
+
+    def number_of_participating_groups(self) -> int:
+        return self.check(self._lib.gdb_number_of_participating_groups(self.h),
+                          "number_of_participating_groups")
+
+    def time_protocol(self, upper_bound: int, wgs: int) -> float:
+        ns = C.c_double()
+        self.check(self._lib.gdb_time_protocol(self.h, upper_bound, wgs, C.byref(ns)), "time_protocol")
+        return ns.value
+
+    def occupancy_test(self, wgc: int, wgs: int, lms: int = 0) -> int:
+        n = C.c_int()
+        self.check(self._lib.gdb_occupancy_test(self.h, wgc, wgs, lms, C.byref(n)), "occupancy_test")
+        return n.value
+
+    def api_occupancy(self, wgs: int, lms: int = 0) -> int:
+        n = C.c_int()
+        self.check(self._lib.gdb_api_occupancy(self.h, wgs, lms, C.byref(n)), "api_occupancy")
+        return n.value
+
+    def barrier_bench(self, kind: int, wgs: int = 0, iters: int = 1000) -> tuple[float, int]:
+        ns, groups = C.c_double(), C.c_int()
+        self.check(self._lib.gdb_barrier_bench(self.h, kind, wgs, iters, C.byref(ns), C.byref(groups)),
+                   "barrier_bench")
+        return ns.value, groups.value
+
+    def debug_stall_master(self, after_barriers: int) -> None:
+        self.check(self._lib.gdb_debug_stall_master(self.h, after_barriers), "debug_stall_master")
+
+    # -- graphs
+    def graph(self, row_ptr: np.ndarray, col: np.ndarray, w: np.ndarray | None = None) -> "Graph":
+        return Graph(self, row_ptr, col, w)
+
+    # -- applications (host buffers)
+    def bfs(self, g: "Graph", src: int) -> np.ndarray:
+        out = np.empty(g.V, dtype=np.uint32)
+        self.check(self._lib.gdb_bfs(self.h, g.h, src, _ptr(out)), "gdb_bfs")
+        return out
+
+    def sssp(self, g: "Graph", src: int) -> np.ndarray:
+        out = np.empty(g.V, dtype=np.uint32)
+        self.check(self._lib.gdb_sssp(self.h, g.h, src, _ptr(out)), "gdb_sssp")
+        return out
+
+    def sssp_jacobi(self, g: "Graph", src: int) -> np.ndarray:
+        out = np.empty(g.V, dtype=np.int32)
+        self.check(self._lib.gdb_sssp_jacobi(self.h, g.h, src, _ptr(out)), "gdb_sssp_jacobi")
+        return out
+
+    def mis(self, g: "Graph", node_value: np.ndarray) -> np.ndarray:
+        nv = np.ascontiguousarray(node_value, dtype=np.float32)
+        out = np.empty(g.V, dtype=np.int32)
+        self.check(self._lib.gdb_mis(self.h, g.h, _ptr(nv), _ptr(out)), "gdb_mis")
+        return out
+
+    def color(self, g: "Graph", node_value: np.ndarray) -> np.ndarray:
+        nv = np.ascontiguousarray(node_value, dtype=np.float32)
+        out = np.empty(g.V, dtype=np.int32)
+        self.check(self._lib.gdb_color(self.h, g.h, _ptr(nv), _ptr(out)), "gdb_color")
+        return out
+
+    def bc(self, g: "Graph", sources) -> np.ndarray:
+        s = np.ascontiguousarray(sources, dtype=np.uint32)
+        out = np.empty(g.V, dtype=np.float32)
+        self.check(self._lib.gdb_bc(self.h, g.h, _ptr(s), len(s), _ptr(out)), "gdb_bc")
+        return out
+
+    def mst(self, g: "Graph", with_arcs: bool = False) -> dict:
+        r = MstResult()
+        flags = np.zeros(max(g.E, 1), dtype=np.uint8) if with_arcs else None
+        self.check(self._lib.gdb_mst(self.h, g.h, C.byref(r), _ptr(flags)), "gdb_mst")
+        out = {k: getattr(r, k) for k, _ in r._fields_}
+        if with_arcs:
+            out["arc_in_mst"] = flags[: g.E]
+        return out
+
+    # -- applications on device buffers (integer device pointers)
+    def bfs_device(self, g: "Graph", src: int, d_dist: int) -> None:
+        self.check(self._lib.gdb_bfs_device(self.h, g.h, src, d_dist), "gdb_bfs_device")
+
+    def sssp_device(self, g: "Graph", src: int, d_dist: int) -> None:
+        self.check(self._lib.gdb_sssp_device(self.h, g.h, src, d_dist), "gdb_sssp_device")
+
+    def sssp_jacobi_device(self, g: "Graph", src: int, d_cost: int) -> None:
+        self.check(self._lib.gdb_sssp_jacobi_device(self.h, g.h, src, d_cost), "gdb_sssp_jacobi_device")
+
+    def mis_device(self, g: "Graph", d_prio: int, d_s: int) -> None:
+        self.check(self._lib.gdb_mis_device(self.h, g.h, d_prio, d_s), "gdb_mis_device")
+
+    def color_device(self, g: "Graph", d_prio: int, d_color: int) -> None:
+        self.check(self._lib.gdb_color_device(self.h, g.h, d_prio, d_color), "gdb_color_device")
+
+    def bc_device(self, g: "Graph", d_sources: int, nsrc: int, d_bc: int) -> None:
+        self.check(self._lib.gdb_bc_device(self.h, g.h, d_sources, nsrc, d_bc), "gdb_bc_device")
+
+    def mst_device(self, g: "Graph", d_result: int, d_flags: int | None = None) -> None:
+        self.check(self._lib.gdb_mst_device(self.h, g.h, d_result, d_flags), "gdb_mst_device")
+
+
+class Graph:
+    """A gdb_graph: CSR copied from host arrays (or borrowed device arrays)."""
+
+    def __init__(self, ctx: Ctx, row_ptr, col, w=None, device: bool = False):
+        self.ctx = ctx
+        h = _P()
+        if device:
+            # row_ptr/col/w are (pointer, length) device buffers
+            (rp, V1), (cp, E) = row_ptr, col
+            wp = w[0] if w is not None else None
+            self.V, self.E = V1 - 1, E
+            ctx.check(ctx._lib.gdb_graph_create_device(ctx.h, self.V, self.E, rp, cp, wp, C.byref(h)),
+                      "gdb_graph_create_device")
+        else:
+            self._rp = np.ascontiguousarray(row_ptr, dtype=np.uint32)
+            self._col = np.ascontiguousarray(col, dtype=np.uint32)
+            if self._col.size == 0:
+                self._col = np.zeros(1, dtype=np.uint32)
+            self._w = None if w is None else np.ascontiguousarray(w, dtype=np.uint32)
+            if self._w is not None and self._w.size == 0:
+                self._w = np.zeros(1, dtype=np.uint32)
+            self.V = int(self._rp.shape[0] - 1)
+            self.E = int(np.asarray(col).shape[0])
+            ctx.check(ctx._lib.gdb_graph_create(ctx.h, self.V, self.E, _ptr(self._rp), _ptr(self._col),
+                                                _ptr(self._w), C.byref(h)), "gdb_graph_create")
+        self.h = h
+
+    def set_weights(self, w: np.ndarray) -> None:
+        self._w = np.ascontiguousarray(w, dtype=np.uint32)
+        self.ctx.check(self.ctx._lib.gdb_graph_set_weights(self.h, _ptr(self._w)), "gdb_graph_set_weights")
+
+    def info(self) -> dict:
+        V, E, hv = C.c_uint32(), C.c_uint64(), C.c_uint32()
+        self.ctx.check(self.ctx._lib.gdb_graph_info(self.h, C.byref(V), C.byref(E), C.byref(hv)),
+                       "gdb_graph_info")
+        return {"V": V.value, "E": E.value, "heavy": hv.value}
+
+    def close(self) -> None:
+        if getattr(self, "h", None) and self.ctx.h:
+            self.ctx._lib.gdb_graph_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

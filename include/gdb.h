@@ -1,0 +1,225 @@
+/* gdb.h -- C ABI of the GB300 occupancy-discovery / XF-barrier graph library.
+ *
+ * One process, one GPU.  A gdb_ctx owns a CUDA stream, the device-side
+ * discovery context (protocol state plus XF barrier flags padded to 128-byte
+ * lines) and a grow-only workspace; a gdb_graph owns (or borrows) a CSR in
+ * HBM.  Plain pointers and sizes only -- no CUDA or C++ types cross this
+ * boundary.  Every call is synchronous unless its name ends in _device, in
+ * which case it is enqueued on the context's stream and all pointers are
+ * device pointers.  Errors are negative gdb_status values; no exception
+ * crosses the ABI.  A context is not thread-safe; distinct contexts are
+ * independent.
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   code/discovery_protocol/api/discovery.h          host discovery API
+ *   code/discovery_protocol/api/discovery.cl         device protocol + XF barrier
+ *   code/experiments/occupancy_tests/src/*.c         occupancy / protocol timing
+ *   code/experiments/pannotia/graph_app/{sssp,mis,color,bc}/   mega-kernels
+ *   code/experiments/lonestar_gpu_opencl/apps/{bfs,sssp,mst}/  port kernels
+ */
+#ifndef GDB_H
+#define GDB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GDB_ABI_VERSION 1
+
+/* Sentinels of the reference kernels. */
+#define GDB_LONESTAR_INF 1000000000u /* lonestar/apps/bfs/kernel/bfs_common.cl:35 */
+#define GDB_PANNOTIA_BIG 99999999    /* pannotia/graph_app/sssp/kernel/sssp_kernel.cl:68 */
+
+typedef enum {
+  GDB_OK = 0,
+  GDB_ERR_INVALID = -1,        /* bad argument */
+  GDB_ERR_CUDA = -2,           /* CUDA runtime error (see gdb_last_error) */
+  GDB_ERR_OOM = -3,            /* device allocation failed */
+  GDB_ERR_TIMEOUT = -4,        /* a device wait exceeded options.timeout_ns */
+  GDB_ERR_CAPACITY = -5,       /* a device queue or table overflowed */
+  GDB_ERR_NOT_CORESIDENT = -6, /* a fixed-occupancy launch above what fits */
+  GDB_ERR_UNSUPPORTED = -7     /* option not available for this call */
+} gdb_status;
+
+/* Mutex of the discovery protocol (reference: locks.cl). */
+typedef enum {
+  GDB_LOCK_TICKET = 0, /* fair ticket lock, locks.cl:25-34 (reference default) */
+  GDB_LOCK_SPIN = 1,   /* unfair exchange spin lock, locks.cl:11-20 */
+  GDB_LOCK_FREE = 2    /* one atomic poll word: fetch_add to poll, fetch_or to close */
+} gdb_lock_kind;
+
+/* Inter-CTA barrier between supersteps. */
+typedef enum {
+  GDB_BARRIER_XF = 0,        /* discovery + XF master/slave flags (discovery.cl:177-238) */
+  GDB_BARRIER_GRID_SYNC = 1, /* cooperative launch + cooperative_groups grid.sync() */
+  GDB_BARRIER_RELAUNCH = 2,  /* one launch per superstep, host reads the stop flag */
+  GDB_BARRIER_XF_FIXED = 3,  /* XF over all launched CTAs, no discovery (gbar_cl.h:15-74);
+                                the grid is capped at the occupancy the API reports */
+  GDB_BARRIER_RELAUNCH_GRAPH = 4 /* gdb_barrier_bench only: the relaunches captured
+                                    once in a CUDA graph and replayed */
+} gdb_barrier_kind;
+
+/* Schedule of the traversal options per superstep. */
+typedef enum {
+  GDB_SCHED_PLAIN = 0,    /* fixed: push, queue frontier, persistent */
+  GDB_SCHED_ADAPTIVE = 1  /* per-superstep choice of push/pull (direction-optimising) */
+} gdb_schedule;
+
+typedef struct {
+  int device;          /* CUDA ordinal; -1 = current device */
+  int block_size;      /* threads per CTA of the persistent kernels (0 = 512) */
+  int max_ctas;        /* cap on launched CTAs (0 = occupancy x SMs) */
+  int oversubscribe;   /* >0: launch this many CTAs and let discovery pick
+                          the co-resident ones (the reference launches 1000) */
+  int lock;            /* gdb_lock_kind */
+  int barrier;         /* gdb_barrier_kind */
+  int schedule;        /* gdb_schedule */
+  int reserved0;
+  uint64_t timeout_ns; /* limit for every device spin (0 = 2e9) */
+} gdb_options;
+
+typedef struct {
+  uint32_t supersteps;       /* barrier intervals executed by the last run */
+  uint32_t participating;    /* CTAs that took part (discovered or launched) */
+  uint32_t launched;         /* CTAs launched */
+  uint32_t launches;         /* kernel launches by the last run */
+  uint64_t edges_processed;  /* arcs inspected (all passes) */
+  uint64_t work_units;       /* edges/s work unit of the last run */
+  double kernel_ms;          /* device time of the last run (CUDA events) */
+} gdb_run_stats;
+
+typedef struct {
+  uint64_t weight64;   /* exact forest weight */
+  uint32_t weight32;   /* uint32 sum as the reference accumulates it (wraps) */
+  uint32_t components; /* connected components (V - edges) */
+  uint32_t edges;      /* forest edges */
+  uint32_t rounds;     /* Boruvka rounds */
+} gdb_mst_result;
+
+typedef struct {
+  int device;
+  int sm_count;
+  int cc_major, cc_minor;
+  size_t total_mem;
+  int occupancy_per_sm; /* resident CTAs per SM of the persistent kernels at
+                           options.block_size */
+  int flag_capacity;    /* barrier flags allocated (max participating CTAs) */
+} gdb_device_info;
+
+typedef struct gdb_ctx gdb_ctx;
+typedef struct gdb_graph gdb_graph;
+
+/* ------------------------------------------------------------ context */
+void gdb_options_default(gdb_options* opt);
+int gdb_ctx_create(const gdb_options* opt, gdb_ctx** out);
+int gdb_ctx_destroy(gdb_ctx* ctx);
+int gdb_ctx_set_options(gdb_ctx* ctx, const gdb_options* opt);
+int gdb_ctx_get_options(gdb_ctx* ctx, gdb_options* opt);
+int gdb_ctx_stream(gdb_ctx* ctx, void** cuda_stream); /* cudaStream_t */
+int gdb_device_info_get(gdb_ctx* ctx, gdb_device_info* info);
+const char* gdb_status_string(int status);
+const char* gdb_last_error(gdb_ctx* ctx);
+int gdb_last_run_stats(gdb_ctx* ctx, gdb_run_stats* stats);
+int gdb_abi_version(void);
+
+/* ------------------------------------------- discovery protocol / barrier */
+/* Reset the device discovery context; replaces init_discovery_kernel_ctx
+ * (code/discovery_protocol/api/discovery.h:10, kernel discovery.cl:242-250). */
+int gdb_init_discovery_kernel_ctx(gdb_ctx* ctx);
+/* Same with the skip flag (discovery.h:36): skip = 1 makes every launched CTA
+ * participate without the protocol.  Only kernels capped at the occupancy
+ * the CUDA API reports honour it; over-subscribed launches are refused. */
+int gdb_init_discovery_kernel_ctx_skip(gdb_ctx* ctx, int skip);
+/* Participating CTAs of the last discovery run (discovery.h:63); >= 0 count
+ * or a negative status. */
+int gdb_number_of_participating_groups(gdb_ctx* ctx);
+/* Time one launch of the protocol-only kernel run_prot with upper_bound
+ * CTAs of wgs threads (discovery.h:71, occupancy_tests/src/time_prot.c:20-85),
+ * using options.lock.  *ns = device time of that launch. */
+int gdb_time_protocol(gdb_ctx* ctx, int upper_bound, int wgs, double* ns);
+/* run_test (occupancy_tests/src/kernels/occupancy_test.cl:8-12): protocol
+ * then one XF barrier, with wgc CTAs of wgs threads and lms bytes of dynamic
+ * shared memory each; *participating = CTAs discovered
+ * (occupancy_tests/src/occupancy_test.c:21-89). */
+int gdb_occupancy_test(gdb_ctx* ctx, int wgc, int wgs, int lms, int* participating);
+/* Co-resident CTAs per the CUDA occupancy API for the run_test kernel
+ * (replaces the reference's deadlock search, run_occupancy_tests.py:53-69). */
+int gdb_api_occupancy(gdb_ctx* ctx, int wgs, int lms, int* ctas);
+/* Barrier latency: `iters` empty supersteps with the given gdb_barrier_kind
+ * on CTAs of wgs threads (0 = options.block_size) and options.max_ctas;
+ * *ns_per_barrier = device time / iters, *groups = CTAs synchronised. */
+int gdb_barrier_bench(gdb_ctx* ctx, int barrier_kind, int wgs, int iters,
+                      double* ns_per_barrier, int* groups);
+/* Fault-injection hook for tests: the XF master of the next run stops
+ * releasing after `after_barriers` barriers, so every wait must end by the
+ * timeout with GDB_ERR_TIMEOUT.  Negative = off. */
+int gdb_debug_stall_master(gdb_ctx* ctx, int after_barriers);
+
+/* ---------------------------------------------------------------- graphs */
+/* Symmetric or directed CSR: row_ptr[V+1], col[E], optional w[E] (uint32).
+ * Host arrays are copied to HBM.  Requires E < 2^32 and V < 2^31. */
+int gdb_graph_create(gdb_ctx* ctx, uint32_t V, uint64_t E, const uint32_t* row_ptr,
+                     const uint32_t* col, const uint32_t* w, gdb_graph** out);
+/* Same with device arrays, borrowed (not freed by gdb_graph_destroy). */
+int gdb_graph_create_device(gdb_ctx* ctx, uint32_t V, uint64_t E, const uint32_t* d_row_ptr,
+                            const uint32_t* d_col, const uint32_t* d_w, gdb_graph** out);
+/* Replace the weight array (host array copied). */
+int gdb_graph_set_weights(gdb_graph* g, const uint32_t* w);
+int gdb_graph_destroy(gdb_graph* g);
+int gdb_graph_info(gdb_graph* g, uint32_t* V, uint64_t* E, uint32_t* heavy_vertices);
+
+/* ---------------------------------------------------------- applications */
+/* BFS levels from src; unreached = GDB_LONESTAR_INF.  Replaces LonestarGPU
+ * drelax2 + host bfs() (lonestar/apps/bfs/kernel/bfs_port_kernel.cl:146-192,
+ * lonestar/apps/bfs/bfs_port.cpp:62-194), which fixes src = 0. */
+int gdb_bfs(gdb_ctx* ctx, gdb_graph* g, uint32_t src, uint32_t* dist);
+int gdb_bfs_device(gdb_ctx* ctx, gdb_graph* g, uint32_t src, uint32_t* d_dist);
+
+/* SSSP distances (uint32 weights); unreached = GDB_LONESTAR_INF.  Replaces
+ * LonestarGPU worklist drelax2 (lonestar/apps/sssp/kernel/sssp_port_kernel.cl:152-197,
+ * lonestar/apps/sssp/sssp_port.cpp). */
+int gdb_sssp(gdb_ctx* ctx, gdb_graph* g, uint32_t src, uint32_t* dist);
+int gdb_sssp_device(gdb_ctx* ctx, gdb_graph* g, uint32_t src, uint32_t* d_dist);
+
+/* Pannotia Jacobi SSSP costs (int32); unreached = GDB_PANNOTIA_BIG.  The
+ * graph is the CSR pulled over (the reference passes the transpose).
+ * Replaces mega_kernel (pannotia/graph_app/sssp/kernel/sssp_kernel.cl:170-244,
+ * host pannotia/graph_app/sssp/sssp_gb.cpp:92-343). */
+int gdb_sssp_jacobi(gdb_ctx* ctx, gdb_graph* g, uint32_t src, int32_t* cost);
+int gdb_sssp_jacobi_device(gdb_ctx* ctx, gdb_graph* g, uint32_t src, int32_t* d_cost);
+
+/* Maximal independent set: s_array[v] = 2 in the set, 0 otherwise, for
+ * float priorities node_value (equal priorities on adjacent vertices never
+ * terminate in the reference; this call returns GDB_ERR_TIMEOUT).  Replaces
+ * mega_kernel (pannotia/graph_app/mis/kernel/mis_kernel.cl:220-337). */
+int gdb_mis(gdb_ctx* ctx, gdb_graph* g, const float* node_value, int32_t* s_array);
+int gdb_mis_device(gdb_ctx* ctx, gdb_graph* g, const float* d_node_value, int32_t* d_s_array);
+
+/* Greedy colouring: color[v] = round in which v beat every uncoloured
+ * neighbour (1-based).  Replaces mega_kernel
+ * (pannotia/graph_app/color/kernel/color_kernel.cl:159-252). */
+int gdb_color(gdb_ctx* ctx, gdb_graph* g, const float* node_value, int32_t* color);
+int gdb_color_device(gdb_ctx* ctx, gdb_graph* g, const float* d_node_value, int32_t* d_color);
+
+/* Betweenness centrality (float32) summed over the given sources, no halving
+ * for undirected graphs.  Replaces mega_bc_kernel
+ * (pannotia/graph_app/bc/kernel/bc_kernel.cl:431-513) restricted to a source
+ * list; bc is overwritten. */
+int gdb_bc(gdb_ctx* ctx, gdb_graph* g, const uint32_t* sources, uint32_t nsrc, float* bc);
+int gdb_bc_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc,
+                  float* d_bc);
+
+/* Minimum spanning forest (Boruvka) over the graph's weights; arc_in_mst
+ * (nullable, E bytes) marks one arc of every forest edge.  Replaces the
+ * LonestarGPU MST host loop and kernels (lonestar/apps/mst/mst_port.cpp:202-312,
+ * mst_common.cl:41-194, mst_port_kernel.cl:35-82). */
+int gdb_mst(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* result, uint8_t* arc_in_mst);
+int gdb_mst_device(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* d_result, uint8_t* d_arc_in_mst);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GDB_H */

@@ -1,0 +1,342 @@
+// gdb_discovery.cuh -- device API of the occupancy discovery protocol and
+// the XF inter-CTA barrier for sm_103a.
+//
+// Replaces, for CUDA kernels, the reference's OpenCL device API
+// (code/discovery_protocol/api/discovery.cl): DISCOVERY_PROTOCOL
+// (:261-274) becomes `if (!gdb::discover(...)) return;`, discovery_barrier
+// (:257, XF_barrier :177-238) becomes gdb::xf_barrier, p_get_* (:160-174)
+// keep their names.  The shared state of discovery_kernel_ctx
+// (code/discovery_protocol/api/common.h:33-48) is gdb::DeviceCtx, with every
+// contended word and every barrier flag on its own 128-byte line.
+//
+// Every spin carries a %globaltimer deadline: on expiry the waiter records
+// GDB_ERR_TIMEOUT in the context, raises the abort word, and all CTAs leave
+// their waits -- a kernel using this header never hangs the GPU.  Memory
+// ordering uses cuda::atomic_ref at device (gpu) scope: a slave's arrival is
+// a release, the master's observation an acquire, and the master's release
+// store publishes everything the whole grid wrote before the barrier.
+#pragma once
+
+#include <cuda/atomic>
+#include <stdint.h>
+
+#include "gdb.h"
+
+namespace gdb {
+
+constexpr int kLineInts = 32;                 // one 128-byte line of ints
+constexpr int kPollClosed = 0x40000000;       // lock-free poll: closed bit
+constexpr int kPollCountMask = kPollClosed - 1;
+
+// discovery_kernel_ctx (common.h:33-48), one contended word per line.
+struct __align__(128) DeviceCtx {
+  int lock_counter;   int _p0[31];  // ticket dispenser / spin-lock word
+  int lock_serving;   int _p1[31];  // now_serving
+  int poll_word;      int _p2[31];  // lock-free poll: count | closed bit
+  int kernel_counter; int _p3[31];  // CTAs through the closing phase
+  int published;      int _p4[31];  // lock-free: participant count, 0 = not yet
+  // protocol state touched under the lock (reference fields)
+  int poll_open;      // prot_poll_open
+  int prot_counter;   // prot_counter
+  int num_participating;
+  int skip;
+  int _p5[28];
+  // error reporting
+  int status;         // first gdb_status recorded by the device (0 = OK)
+  int abort;          // raised with any error: every spin gives up
+  int err_where;      // code location of the first error
+  int err_aux;
+  int stall_after;    // test hook: master stops releasing after this many barriers (-1 off)
+  int _p6[27];
+};
+
+// discovery_local_ctx (discovery.cl:67-71), in shared memory.
+struct LocalCtx {
+  int id;             // participating_group_id
+  int P;              // participating_group_size
+  int participating;  // is_participating
+  int ok;             // 0 once this CTA saw an error / abort
+  unsigned long long timeout_ns;  // limit of every single wait
+  int barriers;       // barriers passed (master: for the stall test hook)
+};
+
+// Launch parameters every discovery kernel receives.
+struct DiscoveryArgs {
+  DeviceCtx* ctx;
+  int* flags;              // flag_capacity lines of 32 ints
+  int flag_capacity;
+  int lock_kind;           // gdb_lock_kind
+  int expected;            // CTAs the occupancy API says fit (0 = unknown)
+  unsigned long long timeout_ns;
+  unsigned long long close_wait_ns;  // lock-free: wait for `expected` pollers
+};
+
+using aref = cuda::atomic_ref<int, cuda::thread_scope_device>;
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ int ld_acquire(int* p) {
+  return aref(*p).load(cuda::memory_order_acquire);
+}
+__device__ __forceinline__ int ld_relaxed(int* p) {
+  return aref(*p).load(cuda::memory_order_relaxed);
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  aref(*p).store(v, cuda::memory_order_release);
+}
+__device__ __forceinline__ void st_relaxed(int* p, int v) {
+  aref(*p).store(v, cuda::memory_order_relaxed);
+}
+
+// Record the first error and make every spinning CTA give up.
+__device__ __forceinline__ void raise_error(DeviceCtx* c, int code, int where) {
+  int expect = 0;
+  if (aref(c->status).compare_exchange_strong(expect, code, cuda::memory_order_relaxed))
+    st_relaxed(&c->err_where, where);
+  aref(c->abort).store(1, cuda::memory_order_release);
+}
+
+// Bounded spin: returns false on abort, or when this wait has lasted
+// longer than timeout_ns (then GDB_ERR_TIMEOUT is recorded with `where`).
+// The clock is read only once a wait is not over after a few polls.
+template <class Done>
+__device__ __forceinline__ bool spin_until(DeviceCtx* c, unsigned long long timeout_ns,
+                                           int where, Done done) {
+  unsigned ns = 0;
+  unsigned long long deadline = 0;
+  for (unsigned k = 1;; ++k) {
+    if (done()) return true;
+    if ((k & 15) == 0) {
+      if (ld_relaxed(&c->abort)) return false;
+      const unsigned long long now = globaltimer();
+      if (deadline == 0) {
+        deadline = now + timeout_ns;
+      } else if (now > deadline) {
+        raise_error(c, GDB_ERR_TIMEOUT, where);
+        return false;
+      }
+    }
+    if (k > 32) {
+      __nanosleep(ns);
+      ns = ns < 128 ? ns + 16 : 128;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ locks
+// Ticket lock (locks.cl:25-34) and exchange spin lock (locks.cl:11-20).
+__device__ __forceinline__ bool lock_acquire(DeviceCtx* c, int kind,
+                                             unsigned long long timeout_ns) {
+  if (kind == GDB_LOCK_SPIN) {
+    return spin_until(c, timeout_ns, 1, [&] {
+      return aref(c->lock_counter).exchange(1, cuda::memory_order_acq_rel) == 0;
+    });
+  }
+  const int ticket = aref(c->lock_counter).fetch_add(1, cuda::memory_order_acq_rel);
+  return spin_until(c, timeout_ns, 2, [&] { return ld_acquire(&c->lock_serving) == ticket; });
+}
+__device__ __forceinline__ void lock_release(DeviceCtx* c, int kind) {
+  if (kind == GDB_LOCK_SPIN) {
+    st_release(&c->lock_counter, 0);
+  } else {
+    const int s = ld_relaxed(&c->lock_serving);
+    st_release(&c->lock_serving, s + 1);
+  }
+}
+
+// reset_kernel_context (discovery.cl:79-85): re-arm for the next launch.
+// Called by the last CTA through while it holds the lock; the final release
+// of the lock words is the implicit unlock.
+__device__ __forceinline__ void reset_kernel_context(DeviceCtx* c) {
+  st_relaxed(&c->poll_open, 1);
+  st_relaxed(&c->prot_counter, 0);
+  st_relaxed(&c->kernel_counter, 0);
+  st_release(&c->lock_counter, 0);
+  st_release(&c->lock_serving, 0);
+}
+
+// discovery_protocol_master (discovery.cl:90-136) with a mutex, executed by
+// one thread per CTA.
+__device__ inline void protocol_master_locked(const DiscoveryArgs& a, LocalCtx* l) {
+  DeviceCtx* c = a.ctx;
+  const int kind = a.lock_kind;
+  // polling phase
+  if (!lock_acquire(c, kind, l->timeout_ns)) { l->ok = 0; l->participating = 0; return; }
+  if (ld_relaxed(&c->poll_open)) {
+    const int id = ld_relaxed(&c->prot_counter);
+    l->participating = 1;
+    l->id = id;
+    st_relaxed(&c->prot_counter, id + 1);
+  } else {
+    l->participating = 0;
+  }
+  lock_release(c, kind);
+  // closing phase
+  if (!lock_acquire(c, kind, l->timeout_ns)) { l->ok = 0; l->participating = 0; return; }
+  const int kc = ld_relaxed(&c->kernel_counter) + 1;
+  st_relaxed(&c->kernel_counter, kc);
+  const bool reset = kc == (int)gridDim.x;
+  if (ld_relaxed(&c->poll_open)) {
+    st_relaxed(&c->poll_open, 0);
+    st_relaxed(&c->num_participating, ld_relaxed(&c->prot_counter));
+  }
+  l->P = ld_relaxed(&c->prot_counter);
+  if (reset) reset_kernel_context(c);
+  else lock_release(c, kind);
+}
+
+// Lock-free protocol: one fetch_add polls (the returned count is the id
+// unless the closed bit is set), the first participant through the closing
+// step sets the closed bit with fetch_or and publishes the count it saw.
+// When the occupancy API's figure `expected` is known, participants keep
+// the poll open until that many CTAs have polled or close_wait_ns passed,
+// so CTAs that start a little later are still discovered.
+__device__ inline void protocol_master_lockfree(const DiscoveryArgs& a, LocalCtx* l) {
+  DeviceCtx* c = a.ctx;
+  const int old = aref(c->poll_word).fetch_add(1, cuda::memory_order_acq_rel);
+  if (old & kPollClosed) {
+    l->participating = 0;
+  } else {
+    l->participating = 1;
+    l->id = old & kPollCountMask;
+    if (a.expected > 0) {
+      const unsigned long long until = globaltimer() + a.close_wait_ns;
+      unsigned ns = 0;
+      for (;;) {
+        const int w = ld_relaxed(&c->poll_word);
+        if ((w & kPollClosed) || (w & kPollCountMask) >= a.expected) break;
+        if (globaltimer() > until || ld_relaxed(&c->abort)) break;
+        __nanosleep(ns);
+        ns = ns < 256 ? ns + 32 : 256;
+      }
+    }
+    const int prev = aref(c->poll_word).fetch_or(kPollClosed, cuda::memory_order_acq_rel);
+    if (!(prev & kPollClosed)) {
+      const int P = prev & kPollCountMask;
+      st_relaxed(&c->num_participating, P);
+      st_release(&c->published, P);
+      l->P = P;
+    } else {
+      int P = 0;
+      if (!spin_until(c, l->timeout_ns, 3, [&] { return (P = ld_acquire(&c->published)) != 0; })) {
+        l->ok = 0;
+        l->participating = 0;
+      }
+      l->P = P;
+    }
+  }
+  // the last CTA through re-arms the context for the next launch
+  const int k = aref(c->kernel_counter).fetch_add(1, cuda::memory_order_acq_rel);
+  if (k == (int)gridDim.x - 1) {
+    st_relaxed(&c->published, 0);
+    st_relaxed(&c->poll_word, 0);
+    st_release(&c->kernel_counter, 0);
+  }
+}
+
+// DISCOVERY_PROTOCOL (discovery.cl:261-274).  All threads of the CTA call
+// it; returns true for participating CTAs (the others must return).
+__device__ inline bool discover(const DiscoveryArgs& a, LocalCtx* l) {
+  if (threadIdx.x == 0) {
+    l->ok = 1;
+    l->barriers = 0;
+    l->timeout_ns = a.timeout_ns;
+    DeviceCtx* c = a.ctx;
+    if (ld_relaxed(&c->skip)) {
+      l->P = gridDim.x;
+      l->participating = 1;
+      l->id = blockIdx.x;
+      if (blockIdx.x == 0) st_relaxed(&c->num_participating, gridDim.x);
+    } else if (a.lock_kind == GDB_LOCK_FREE) {
+      protocol_master_lockfree(a, l);
+    } else {
+      protocol_master_locked(a, l);
+    }
+    if (l->participating &&
+        (l->P > a.flag_capacity || l->P - 1 > 32 * (int)blockDim.x)) {
+      raise_error(c, GDB_ERR_CAPACITY, 4);
+      l->ok = 0;
+    }
+    if (!l->ok) l->participating = 0;
+  }
+  __syncthreads();
+  return l->participating != 0;
+}
+
+// p_get_* (discovery.cl:160-174)
+__device__ __forceinline__ int p_get_group_id(const LocalCtx* l) { return l->id; }
+__device__ __forceinline__ int p_get_num_groups(const LocalCtx* l) { return l->P; }
+__device__ __forceinline__ int p_get_global_id(const LocalCtx* l) {
+  return threadIdx.x + blockDim.x * l->id;
+}
+__device__ __forceinline__ int p_get_global_size(const LocalCtx* l) {
+  return l->P * blockDim.x;
+}
+
+// XF barrier (discovery.cl:177-238) over the participating CTAs.  Slave: one
+// elected thread release-stores 1 to its padded flag and spins until the
+// master stores 0.  Master: each thread issues loads for all of its peers'
+// flags at once and retires the ones that arrived, so the wait costs one
+// L2 round trip after the last arrival; then a CTA barrier and release
+// stores of 0.  Returns false (uniformly across the CTA) after an error or
+// a timeout anywhere in the grid.
+__device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l) {
+  DeviceCtx* c = a.ctx;
+  const int P = l->P;
+  int ok = 1;
+  if (l->id == 0) {
+    __syncthreads();
+    // up to 32 peers per thread (P <= 32 * blockDim.x + 1 is checked by the host)
+    unsigned pending = 0;
+    int k = 0;
+    for (int peer = threadIdx.x + 1; peer < P; peer += blockDim.x, ++k) pending |= 1u << k;
+    if (pending) {
+      ok = spin_until(c, l->timeout_ns, 5, [&] {
+        int kk = 0;
+        for (int peer = threadIdx.x + 1; peer < P; peer += blockDim.x, ++kk) {
+          if ((pending >> kk) & 1u) {
+            if (ld_relaxed(&a.flags[(size_t)peer * kLineInts]) != 0) pending &= ~(1u << kk);
+          }
+        }
+        return pending == 0;
+      });
+      __threadfence();  // acquire: order the slaves' writes before ours
+    }
+    ok = __syncthreads_and(ok);
+    if (ok && c->stall_after >= 0 && l->barriers >= c->stall_after) {
+      // test hook: never release; wait on a word nobody sets until the
+      // deadline, which must end every CTA's wait with GDB_ERR_TIMEOUT
+      if (threadIdx.x == 0) {
+        spin_until(c, l->timeout_ns, 6, [&] { return false; });
+      }
+      ok = 0;
+    }
+    if (ok) {
+      __threadfence();  // release: publish the grid's writes with the flags
+      for (int peer = threadIdx.x + 1; peer < P; peer += blockDim.x)
+        st_relaxed(&a.flags[(size_t)peer * kLineInts], 0);
+    }
+    if (threadIdx.x == 0) l->barriers++;
+  } else {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int* f = &a.flags[(size_t)l->id * kLineInts];
+      __threadfence();
+      st_relaxed(f, 1);
+      ok = spin_until(c, l->timeout_ns, 7, [&] { return ld_relaxed(f) == 0; });
+      __threadfence();
+      l->ok = ok;
+    }
+    __syncthreads();
+    ok = l->ok;
+  }
+  // every CTA leaves together on error
+  if (threadIdx.x == 0 && !ok) l->ok = 0;
+  __syncthreads();
+  return l->ok != 0;
+}
+
+}  // namespace gdb

@@ -1,0 +1,133 @@
+"""GPU parity of every application entry point against the CPU oracle.
+
+Integer results (BFS levels, SSSP distances, MIS set, colours, MST weight /
+edge count / edge set) must be bit-exact; BC float32 scores must be within
+1e-4 relative of the oracle's float32 restatement and of the FP64 Brandes
+oracle (RTOL below).  Calls go through the C ABI (gdb.Ctx -> libgdb.so).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from gpu_discovery_barrier_gb300 import gdb, graphgen as gg
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-4  # BC tolerance stated by the parity contract
+
+
+def graphs():
+    out = [
+        ("grid16", gg.grid(16, 16)),
+        ("grid256x256", gg.grid(256, 256)),
+        ("rmat12", gg.rmat(1 << 12, 16, seed=5)),
+        ("rmat14_hubs", gg.rmat(1 << 14, 32, seed=6)),
+        ("grid3x1000", gg.grid(3, 1000)),
+    ]
+    # star: one hub of degree 3000 (heavy chunks) plus isolated vertices
+    V = 5000
+    pairs = [(0, i) for i in range(1, 3001)] + [(3001, 3002), (3002, 3003)]
+    out.append(("star_isolated", gg.from_edges(V, pairs)))
+    out.append(("path", gg.from_edges(400, [(i, i + 1) for i in range(399)])))
+    out.append(("single", gg.from_edges(1, [])))
+    out.append(("pair", gg.from_edges(2, [(0, 1)])))
+    return out
+
+
+GRAPHS = graphs()
+IDS = [n for n, _ in GRAPHS]
+
+
+def bc_close(got, want):
+    scale = np.maximum(np.abs(want), 1e-6 * max(1.0, float(np.max(np.abs(want))) if want.size else 1.0))
+    return np.all(np.abs(got.astype(np.float64) - want) <= RTOL * scale + 1e-6)
+
+
+@pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
+def test_bfs(ctx, name, g):
+    G = ctx.graph(g.row_ptr, g.col)
+    for src in sorted(set([0, g.V - 1] + list(gg.sources(g, 3, seed=7)))):
+        got = ctx.bfs(G, int(src))
+        assert np.array_equal(got, oracle.bfs(g, int(src))), (name, src)
+
+
+@pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC, gdb.BARRIER_RELAUNCH])
+@pytest.mark.parametrize("schedule", [gdb.SCHED_PLAIN, gdb.SCHED_ADAPTIVE])
+def test_bfs_barrier_kinds(barrier, schedule):
+    if barrier == gdb.BARRIER_RELAUNCH and schedule == gdb.SCHED_ADAPTIVE:
+        pytest.skip("adaptive needs a persistent barrier")
+    g = gg.rmat(1 << 13, 16, seed=9)
+    with gdb.Ctx(barrier=barrier, schedule=schedule) as c:
+        G = c.graph(g.row_ptr, g.col)
+        for src in gg.sources(g, 3, seed=1):
+            assert np.array_equal(c.bfs(G, int(src)), oracle.bfs(g, int(src)))
+
+
+@pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
+def test_sssp_worklist(ctx, name, g):
+    w = gg.uniform_weights(g, 1, 255, seed=1)
+    gw = g.with_weights(w)
+    G = ctx.graph(g.row_ptr, g.col, w)
+    for src in sorted(set([0] + list(gg.sources(g, 2, seed=3)))):
+        got = ctx.sssp(G, int(src))
+        assert np.array_equal(got, oracle.sssp_worklist(gw, int(src))), (name, src)
+
+
+@pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC])
+def test_sssp_barrier_kinds(barrier):
+    g = gg.grid(64, 64)
+    w = gg.uniform_weights(g, 1, 1000, seed=1)
+    with gdb.Ctx(barrier=barrier) as c:
+        G = c.graph(g.row_ptr, g.col, w)
+        assert np.array_equal(c.sssp(G, 0), oracle.sssp_worklist(g.with_weights(w), 0))
+
+
+@pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
+def test_sssp_jacobi(ctx, name, g):
+    w = gg.uniform_weights(g, 1, 100, seed=2)
+    gw = g.with_weights(w)
+    G = ctx.graph(g.row_ptr, g.col, w)
+    got = ctx.sssp_jacobi(G, 0)
+    assert np.array_equal(got, oracle.sssp_jacobi(gw, 0)), name
+
+
+@pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
+def test_mis(ctx, name, g):
+    prio = gg.priorities(g.V, seed=4)
+    G = ctx.graph(g.row_ptr, g.col)
+    got = ctx.mis(G, prio)
+    want, _ = oracle.mis(g, prio)
+    assert np.array_equal(got, want), name
+
+
+@pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
+def test_color(ctx, name, g):
+    prio = gg.priorities(g.V, seed=5)
+    G = ctx.graph(g.row_ptr, g.col)
+    got = ctx.color(G, prio)
+    want, _ = oracle.color(g, prio)
+    assert np.array_equal(got, want), name
+
+
+@pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
+def test_bc(ctx, name, g):
+    srcs = gg.sources(g, 4, seed=8) if g.E else np.array([0], dtype=np.uint32)
+    G = ctx.graph(g.row_ptr, g.col)
+    got = ctx.bc(G, srcs)
+    want32 = oracle.bc_f32(g, g, srcs)
+    want64 = oracle.bc_f64(g, srcs)
+    assert bc_close(got, want64), name
+    assert bc_close(got, want32.astype(np.float64)), name
+
+
+@pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
+def test_mst(ctx, name, g):
+    uw = gg.unique_weights(g, seed=9)
+    gu = g.with_weights(uw)
+    G = ctx.graph(g.row_ptr, g.col, uw)
+    got = ctx.mst(G, with_arcs=True)
+    want = oracle.mst(gu)
+    assert got["weight64"] == want["weight64"], name
+    assert got["weight32"] == want["weight32"], name
+    assert got["edges"] == want["edges"] and got["components"] == want["components"], name
+    assert oracle.mst_edge_set(g, got["arc_in_mst"]) == oracle.mst_edge_set(g, want["arc_in_mst"])

@@ -1,0 +1,69 @@
+"""GPU tests of the discovery protocol and the barriers.
+
+Every wait in the device code has a deadline; the timeout test stalls the
+XF master through the library's test hook (a flag nothing releases) and
+checks that the kernel ends with GDB_ERR_TIMEOUT and the context stays
+usable -- no trap, no fault, no hang.
+"""
+import pytest
+
+from gpu_discovery_barrier_gb300 import gdb
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("lock", [gdb.LOCK_TICKET, gdb.LOCK_SPIN, gdb.LOCK_FREE])
+def test_occupancy_test_discovers_coresident(lock):
+    with gdb.Ctx(lock=lock) as c:
+        fit = c.api_occupancy(256)
+        assert fit > 0
+        # exactly the API occupancy: every CTA can be co-resident
+        n = c.occupancy_test(fit, 256)
+        assert 1 <= n <= fit
+        # over-subscribed like the reference (1000 + fit CTAs): only
+        # co-resident CTAs take part and the barrier still completes
+        n2 = c.occupancy_test(fit + 1000, 256)
+        assert 1 <= n2 <= fit
+        assert c.number_of_participating_groups() == n2
+
+
+@pytest.mark.parametrize("lock", [gdb.LOCK_TICKET, gdb.LOCK_FREE])
+def test_protocol_self_resets(lock):
+    """The last CTA re-arms the context, so launches need no re-init
+    (discovery.cl:80-84 / reset_kernel_context)."""
+    with gdb.Ctx(lock=lock) as c:
+        fit = c.api_occupancy(128)
+        for _ in range(3):
+            ns = c.time_protocol(fit, 128)
+            assert ns > 0
+            assert 1 <= c.number_of_participating_groups() <= fit
+
+
+def test_skip_refuses_oversubscription():
+    with gdb.Ctx() as c:
+        fit = c.api_occupancy(256)
+        c.init_discovery_kernel_ctx(skip=1)
+        with pytest.raises(gdb.GdbError) as e:
+            c.occupancy_test(fit + 1, 256)
+        assert e.value.status == -6
+        assert c.occupancy_test(fit, 256) == fit
+        c.init_discovery_kernel_ctx()
+
+
+@pytest.mark.parametrize("kind", [gdb.BARRIER_XF, gdb.BARRIER_XF_FIXED, gdb.BARRIER_GRID_SYNC,
+                                  gdb.BARRIER_RELAUNCH, gdb.BARRIER_RELAUNCH_GRAPH])
+def test_barrier_bench(kind):
+    with gdb.Ctx() as c:
+        ns, groups = c.barrier_bench(kind, 256, 200)
+        assert ns > 0 and groups >= 1
+
+
+def test_timeout_reports_and_recovers():
+    with gdb.Ctx(timeout_ns=50_000_000) as c:
+        c.debug_stall_master(3)
+        with pytest.raises(gdb.GdbError) as e:
+            c.barrier_bench(gdb.BARRIER_XF, 256, 20)
+        assert e.value.status == -4
+        c.debug_stall_master(-1)
+        ns, groups = c.barrier_bench(gdb.BARRIER_XF, 256, 20)
+        assert ns > 0 and groups >= 1
