@@ -64,7 +64,9 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
   for (;; ++r) {
     // ---- mis1: min over undecided neighbours
     {
-      const int cur = t % 3, old = (t + 2) % 3;
+      // flag[t % 3] is read after this superstep's barrier: clear the slot
+      // of superstep t - 2
+      const int cur = t % 3, old = (t + 1) % 3;
       if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
       bool undecided_seen = false;
       sweep_light(
@@ -116,7 +118,9 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
     }
     // ---- mis2: strict local minima join the set and decide their neighbours
     {
-      const int cur = t % 3, old = (t + 2) % 3;
+      // flag[t % 3] is read after this superstep's barrier: clear the slot
+      // of superstep t - 2
+      const int cur = t % 3, old = (t + 1) % 3;
       if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
       // next round's heavy minima start from BIGNUM
       for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) pick(ws.hmn, r + 1)[h] = big;

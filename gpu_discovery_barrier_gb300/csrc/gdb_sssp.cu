@@ -245,7 +245,9 @@ __device__ __forceinline__ void jacobi_body(Sync& s, const GraphView& G, const J
   uint32_t k = 0;
   // the reference iterates k = 1 .. num_rows-1 (sssp_kernel.cl:185)
   for (; k + 1 < G.V; ++k) {
-    const int cur = k % 3, old = (k + 2) % 3;
+    // changed[k % 3] is written in iteration k and read after its barrier,
+    // so the slot cleared now is the one of iteration k - 2
+    const int cur = k % 3, old = (k + 1) % 3;
     if (leader) ws.cursor[old] = ws.hcursor[old] = ws.changed[old] = 0;
     const bool ch = jacobi_iter(G, ws, k, smin, arcs);
     if (__any_sync(kFull, ch) && lane_id() == 0) atomicOr(&ws.changed[cur], 1u);
@@ -258,7 +260,9 @@ __device__ __forceinline__ void jacobi_body(Sync& s, const GraphView& G, const J
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
   if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
-  // iterations run; the answer is in x[k & 1]
+  // k iterations ran; the answer is the vector the last one read,
+  // x[(k - 1) & 1] -- the reference's host reads x (sssp_gb.cpp:310), which
+  // lags y by one iteration when the num_rows - 1 cap ends the loop
   if (leader) ws.stats[1] = k;
 }
 
@@ -397,7 +401,7 @@ static int jacobi_run(gdb_ctx* c, gdb_graph* g, uint32_t src, int32_t* d_cost) {
   GDB_CUDA(c, cudaMemcpyAsync(hs, cnt, 64, cudaMemcpyDeviceToHost, c->stream));
   GDB_CUDA(c, cudaStreamSynchronize(c->stream));
   const uint32_t k = (uint32_t)hs[1];
-  if (k & 1) {
+  if (k >= 1 && ((k - 1) & 1)) {
     GDB_CUDA(c, cudaMemcpyAsync(d_cost, ws.x[1], (size_t)g->V * 4, cudaMemcpyDeviceToDevice, c->stream));
   }
   GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));

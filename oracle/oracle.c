@@ -141,9 +141,9 @@ int orc_sssp_jacobi(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
                     const uint32_t* w, uint32_t src, int32_t* cost,
                     uint32_t* iterations) {
   if (src >= V) return -1;
-  int32_t* x = (int32_t*)malloc(sizeof(int32_t) * V);
-  int32_t* y = cost;
-  if (!x) return -2;
+  int32_t* x = cost;
+  int32_t* y = (int32_t*)malloc(sizeof(int32_t) * V);
+  if (!y) return -2;
   for (uint32_t i = 0; i < V; ++i) x[i] = y[i] = (i == src) ? 0 : ORC_PANNOTIA_BIG;
   uint32_t it = 0;
   for (uint32_t k = 1; k < V; ++k) {
@@ -162,15 +162,18 @@ int orc_sssp_jacobi(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
       if (y[v] != x[v]) stop = 1;
     if (!stop) break;
   }
-  /* mega_kernel leaves the answer in both vectors; the host reads x
-   * (vector_d1, sssp_gb.cpp:310), equal to y once converged. */
-  free(x);
+  /* The host reads x (vector_d1, sssp_gb.cpp:310): equal to y once
+   * converged, but one iteration behind when the k < num_rows cap ends the
+   * loop first (a path of V vertices then leaves its far end at BIG_NUM). */
+  free(y);
   if (iterations) *iterations = it;
   return 0;
 }
 
 /* Same fixed point as orc_sssp_jacobi (cost = min(BIG_NUM, distance)),
- * computed with Dijkstra so it finishes on large graphs. */
+ * computed with Dijkstra so it finishes on large graphs.  Equal to the
+ * Jacobi result whenever the iteration converges before the num_rows - 1
+ * cap, i.e. when no shortest path needs V - 1 arcs. */
 int orc_sssp_dijkstra_int(uint32_t V, const uint32_t* row_ptr,
                           const uint32_t* col, const uint32_t* w, uint32_t src,
                           int32_t* cost) {
