@@ -1,0 +1,497 @@
+#!/usr/bin/env python
+"""Benchmark: the plain persistent suite on an R-MAT scale-22 graph.
+
+One step = the full suite over one seeded R-MAT graph (scale 22, edge factor
+16, a,b,c = 0.57,0.19,0.19, symmetrised, deduplicated): BFS and worklist
+SSSP (weights U[1,255]) from 16 seeded sources, MIS and greedy colouring
+with seeded priorities, BC from the same 16 sources, Boruvka MST with
+unique weights.  The metric is edges/s: the arcs out of reached vertices
+for every BFS / SSSP / BC source plus all arcs for MIS, colouring and MST,
+divided by the device time of the step.
+
+* value: graphs resident in HBM, outputs in device buffers, CUDA events on
+  the library's stream around K steps (inputs > L2, so no flush is needed);
+* e2e: the same step through the host-buffer C-ABI calls a user makes
+  (graph upload from pinned host memory and result read-back included);
+* roofline: algorithmic bytes / measured launch time of the kernel with the
+  largest time share, against MEASURED_PEAKS.json's HBM bandwidth;
+* cpu_baseline: the CPU oracle on a bounded sample of the same workload.
+
+``--impl reference`` times the CPU implementation of the path on the host's
+cores instead (see the design doc for why it is the oracle port).
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NSRC = 16
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gdb", "reference"], default="gdb")
+    p.add_argument("--scale", type=int, default=22)
+    p.add_argument("--edge-factor", type=float, default=16)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--apps", default="bfs,sssp,mis,color,bc,mst")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------- workload
+
+
+def make_workload(scale: int, ef: float):
+    from gpu_discovery_barrier_gb300 import graphgen as gg
+
+    g = gg.rmat_scale(scale, ef, seed=1)
+    return {
+        "g": g,
+        "w": gg.uniform_weights(g, 1, 255, seed=1),
+        "uw": gg.unique_weights(g, seed=3),
+        "prio": gg.priorities(g.V, seed=4),
+        "src": gg.sources(g, NSRC, seed=2),
+    }
+
+
+def reach(g, dist):
+    """(reached vertices, arcs out of them) from a BFS level vector."""
+    m = dist != 1_000_000_000
+    deg = g.degrees()
+    return int(m.sum()), int(deg[m].sum())
+
+
+# -------------------------------------------------------------- roofline
+
+def alg_bytes(app: str, g, reached, rounds: int) -> float:
+    """Algorithmic bytes of one launch (uint32 = 4 B), schedule-independent:
+    BFS 8E_r + 12V_r + 4V; SSSP 12E_r + 12V_r + 4V; BC 20E_r + 24V_r + 12V
+    per source; MST (12E + 16V) per round; MIS/colour (12E + 8V) per round
+    bound from above by the full graph."""
+    V, E = g.V, g.E
+    if app == "bfs":
+        return sum(8 * er + 12 * vr + 4 * V for vr, er in reached)
+    if app == "sssp":
+        return sum(12 * er + 12 * vr + 4 * V for vr, er in reached)
+    if app == "bc":
+        return sum(20 * er + 24 * vr + 12 * V for vr, er in reached)
+    if app == "mst":
+        return rounds * (12 * E + 16 * V)
+    return rounds * (12 * E + 8 * V)
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- clocks
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"gdb_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        self.path.unlink(missing_ok=True)
+        busy = [x for x in sm if smax and x > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": smax,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------- GPU suite
+
+
+class GpuSuite:
+    def __init__(self, wl, apps, device):
+        import torch
+
+        from gpu_discovery_barrier_gb300 import gdb
+
+        self.torch = torch
+        self.gdb = gdb
+        self.wl = wl
+        self.apps = apps
+        g = wl["g"]
+        self.ctx = gdb.Ctx(device=device)
+        self.G = self.ctx.graph(g.row_ptr, g.col, wl["w"])
+        self.Gu = self.ctx.graph(g.row_ptr, g.col, wl["uw"])
+        dev = torch.device("cuda", device)
+        V = g.V
+        self.d_dist = torch.empty(V, dtype=torch.int32, device=dev)
+        self.d_out = torch.empty(V, dtype=torch.int32, device=dev)
+        self.d_bc = torch.empty(V, dtype=torch.float32, device=dev)
+        self.d_prio = torch.from_numpy(wl["prio"]).to(dev)
+        self.d_src = torch.from_numpy(wl["src"].astype(np.int32)).to(dev)
+        self.d_mst = torch.zeros(4, dtype=torch.int64, device=dev)
+        self.stream = torch.cuda.ExternalStream(self.ctx.stream(), device=dev)
+
+    def step_device(self, record: dict):
+        """One suite pass on resident inputs; per-app kernel time and launches."""
+        c, src = self.ctx, self.wl["src"]
+
+        def note(app):
+            st = c.last_stats()
+            r = record.setdefault(app, {"ms": 0.0, "launches": 0, "calls": 0, "supersteps": 0})
+            r["ms"] += st["kernel_ms"]
+            r["launches"] += st["launches"]
+            r["calls"] += 1
+            r["supersteps"] += st["supersteps"]
+
+        if "bfs" in self.apps:
+            for s in src:
+                c.bfs_device(self.G, int(s), self.d_dist.data_ptr())
+                note("bfs")
+        if "sssp" in self.apps:
+            for s in src:
+                c.sssp_device(self.G, int(s), self.d_dist.data_ptr())
+                note("sssp")
+        if "mis" in self.apps:
+            c.mis_device(self.G, self.d_prio.data_ptr(), self.d_out.data_ptr())
+            note("mis")
+        if "color" in self.apps:
+            c.color_device(self.G, self.d_prio.data_ptr(), self.d_out.data_ptr())
+            note("color")
+        if "bc" in self.apps:
+            c.bc_device(self.G, self.d_src.data_ptr(), len(src), self.d_bc.data_ptr())
+            note("bc")
+        if "mst" in self.apps:
+            c.mst_device(self.Gu, self.d_mst.data_ptr(), None)
+            note("mst")
+
+    def step_e2e(self, host):
+        """The same suite through the host-buffer API, graph upload included."""
+        gdb = self.gdb
+        c, g, src = self.ctx, self.wl["g"], self.wl["src"]
+        G = gdb.Graph(c, host["row"], host["col"], host["w"])
+        outs = 0
+        if "bfs" in self.apps:
+            for s in src:
+                outs += c.bfs(G, int(s)).nbytes
+        if "sssp" in self.apps:
+            for s in src:
+                outs += c.sssp(G, int(s)).nbytes
+        if "mis" in self.apps:
+            outs += c.mis(G, host["prio"]).nbytes
+        if "color" in self.apps:
+            outs += c.color(G, host["prio"]).nbytes
+        if "bc" in self.apps:
+            outs += c.bc(G, src).nbytes
+        if "mst" in self.apps:
+            G.set_weights(host["uw"])
+            c.mst(G)
+            outs += 24
+        G.close()
+        return outs
+
+
+def pinned_copy(torch, a: np.ndarray) -> np.ndarray:
+    t = torch.empty(a.shape, dtype={np.dtype(np.uint32): torch.int32,
+                                    np.dtype(np.float32): torch.float32}[a.dtype], pin_memory=True)
+    out = t.numpy().view(a.dtype)
+    out[...] = a
+    out._keep = t  # type: ignore[attr-defined]
+    return out
+
+
+# ----------------------------------------------------------- CPU sample
+
+
+def cpu_sample(wl, threads: int, full: bool):
+    """Bounded sample of the suite on the CPU oracle.  `full`: every app,
+    all 16 sources, spread over `threads` host threads (ctypes releases the
+    GIL); otherwise one source of BFS/SSSP/BC plus MIS on one thread."""
+    import oracle as O
+
+    g, src = wl["g"], wl["src"]
+    gw = g.with_weights(wl["w"])
+    gu = g.with_weights(wl["uw"])
+    srcs = [int(s) for s in src] if full else [int(src[0])]
+    tasks = []
+    for s in srcs:
+        tasks.append(("bfs", lambda s=s: O.bfs(g, s)))
+        tasks.append(("sssp", lambda s=s: O.sssp_worklist(gw, s)))
+        tasks.append(("bc", lambda s=s: O.bc_f64(g, [s])))
+    tasks.append(("mis", lambda: O.mis(g, wl["prio"])))
+    if full:
+        tasks.append(("color", lambda: O.color_fast(g, wl["prio"])))
+        tasks.append(("mst", lambda: O.mst(gu)))
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda t: t[1](), tasks))
+    return time.perf_counter() - t0, [t[0] for t in tasks], srcs
+
+
+def units_of(names, srcs, er_by_src, E):
+    u = 0
+    per = {"bfs": [], "sssp": [], "bc": []}
+    for n in names:
+        if n in per:
+            per[n].append(1)
+    for n in ("bfs", "sssp", "bc"):
+        u += sum(er_by_src[s] for s in srcs) if per[n] else 0
+    u += E * sum(1 for n in names if n in ("mis", "color", "mst"))
+    return u
+
+
+# ------------------------------------------------------------------ main
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if os.environ.get("GDB_BENCH_BACKEND") != "gloo" else "gloo")
+    return rank, world, local
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def base_line(args, world, metric_value, ms_per_step, cfg):
+    return {
+        "metric": "edges/sec (plain persistent suite: BFS+SSSP+BC x16 sources, MIS, colour, MST)",
+        "value": metric_value,
+        "unit": "edges/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32",
+        "data": "synthetic (seeded R-MAT generator; the reference's datasets are external)",
+        "config": cfg,
+    }
+
+
+def run_reference(args, rank, world):
+    import oracle as O
+
+    if rank != 0:
+        return
+    wl = make_workload(args.scale, args.edge_factor)
+    g = wl["g"]
+    er = {int(s): reach(g, O.par_bfs(g, int(s)))[1] for s in wl["src"]}
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(wl, threads, full=False)
+    times, units = [], 0
+    for _ in range(args.steps):
+        dt, names, srcs = cpu_sample(wl, threads, full=True)
+        times.append(dt)
+        units += units_of(names, srcs, er, g.E)
+    total = sum(times)
+    value = units / total
+    cfg = {"workload": f"rmat scale {args.scale} ef {args.edge_factor:g} suite", "V": g.V, "E": g.E,
+           "sources": NSRC, "global_batch": 1, "parallelism": "host threads", "l2": "inputs > L2"}
+    line = base_line(args, 1, value, 1e3 * total / args.steps, cfg)
+    line["impl"] = "reference"
+    line["cpu_baseline"] = {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
+                            "sample": "full suite per step (16 sources of BFS/SSSP/BC, MIS, "
+                                      "colour, MST) on the CPU oracle over all host threads; "
+                                      "warm-up steps use the one-source sample"}
+    line["e2e"] = {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    print(json.dumps(line), flush=True)
+
+
+def run_gdb(args, rank, world, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    apps = args.apps.split(",")
+    wl = make_workload(args.scale, args.edge_factor)
+    g = wl["g"]
+    suite = GpuSuite(wl, apps, local)
+    er_by_src, reached = {}, []
+    for s in wl["src"]:
+        vr, erv = reach(g, suite.ctx.bfs(suite.G, int(s)))
+        er_by_src[int(s)] = erv
+        reached.append((vr, erv))
+    sum_er = sum(er_by_src.values())
+    units_per_step = 0
+    for a in apps:
+        units_per_step += sum_er if a in ("bfs", "sssp", "bc") else g.E
+
+    for _ in range(args.warmup):
+        suite.step_device({})
+    rec: dict = {}
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(suite.stream):
+            start.record(suite.stream)
+            for _ in range(args.steps):
+                suite.step_device(rec)
+            end.record(suite.stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = start.elapsed_time(end)
+    ms = reduce_max(ms, world)
+    value = world * units_per_step * args.steps / (ms / 1e3)
+    clocks = clk.summary()
+
+    # roofline of the kernel with the largest time share
+    dom = max(rec, key=lambda a: rec[a]["ms"])
+    r = rec[dom]
+    launch_ms = r["ms"] / r["calls"]
+    rounds = max(1, r["supersteps"] // max(1, r["calls"]))
+    if dom in ("bfs", "sssp"):
+        # one source per launch: the mean over the 16 sources
+        mean = (sum(v for v, _ in reached) / len(reached), sum(e for _, e in reached) / len(reached))
+        nbytes = alg_bytes(dom, g, [mean], 0)
+    elif dom == "bc":
+        nbytes = alg_bytes("bc", g, reached, 0)
+    else:
+        nbytes = alg_bytes(dom, g, [], rounds)
+    peak, peak_kind = peaks()
+    achieved = nbytes / (launch_ms / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(dom)
+    roof = {"bound": "hbm", "kernel": f"k_{dom}_xf", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "alg_bytes_per_launch": nbytes, "launch_ms": launch_ms, "traffic": traffic}
+
+    # end to end through the host-buffer API
+    e2e = None
+    if not args.no_e2e:
+        host = {"row": pinned_copy(torch, g.row_ptr), "col": pinned_copy(torch, g.col),
+                "w": pinned_copy(torch, wl["w"]), "uw": pinned_copy(torch, wl["uw"]),
+                "prio": pinned_copy(torch, wl["prio"])}
+        h2d = sum(host[k].nbytes for k in host) + 4 * NSRC
+        suite.step_e2e(host)
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d2h = 0
+        for _ in range(args.steps):
+            d2h = suite.step_e2e(host)
+        torch.cuda.synchronize()
+        dt = reduce_max(time.perf_counter() - t0, world)
+        e2e = {"value": world * units_per_step * args.steps / dt, "unit": "edges/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        dt, names, srcs = cpu_sample(wl, 1, full=False)
+        cpu = {"value": units_of(names, srcs, er_by_src, g.E) / dt, "unit": "edges/s", "cores": 1,
+               "kind": "port", "sample": "BFS, worklist SSSP and BC from one source plus MIS on the "
+                                         f"same graph, serial CPU oracle ({dt:.1f} s)"}
+
+    if rank == 0:
+        cfg = {"workload": f"rmat scale {args.scale} ef {args.edge_factor:g} suite", "V": g.V,
+               "E": g.E, "sources": NSRC, "apps": apps, "global_batch": world,
+               "parallelism": f"replicas x{world}", "l2": "inputs > L2 (no flush)",
+               "block": suite.ctx.opt.block_size, "barrier": "xf", "lock": "lock-free poll"}
+        line = base_line(args, world, value, ms / args.steps, cfg)
+        line["clocks"] = clocks
+        line["e2e"] = e2e
+        line["roofline"] = roof
+        line["cpu_baseline"] = cpu
+        line["gpu_launches"] = sum(r["launches"] for r in rec.values())
+        line["per_app_ms"] = {a: rec[a]["ms"] / args.steps for a in rec}
+        line["per_app_supersteps"] = {a: rec[a]["supersteps"] // args.steps for a in rec}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gdb(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -53,6 +53,7 @@ def lib() -> C.CDLL:
         L.orc_sssp_dijkstra_int.argtypes = [U32, _u32p, _u32p, _u32p, U32, _i32p]
         L.orc_mis.argtypes = [U32, _u32p, _u32p, _f32p, _i32p, C.POINTER(U32)]
         L.orc_color.argtypes = [U32, _u32p, _u32p, _f32p, _i32p, C.POINTER(U32)]
+        L.orc_color_fast.argtypes = [U32, _u32p, _u32p, _f32p, _i32p, C.POINTER(U32)]
         L.orc_bc_f32.argtypes = [U32, _u32p, _u32p, _u32p, _u32p, _u32p, U32, _f32p]
         L.orc_bc_f64.argtypes = [U32, _u32p, _u32p, _u32p, U32, _f64p]
         L.orc_mst.argtypes = [U32, _u32p, _u32p, _u32p, C.POINTER(C.c_uint64), C.POINTER(U32),
@@ -121,6 +122,15 @@ def color(g, prio: np.ndarray) -> tuple[np.ndarray, int]:
     r = C.c_uint32()
     _check(lib().orc_color(g.V, g.row_ptr, _nz(g.col), np.ascontiguousarray(prio, np.float32),
                            c, C.byref(r)), "color")
+    return c, r.value
+
+
+def color_fast(g, prio: np.ndarray) -> tuple[np.ndarray, int]:
+    """Same colouring from its closed form (fast on large graphs)."""
+    c = np.empty(g.V, dtype=np.int32)
+    r = C.c_uint32()
+    _check(lib().orc_color_fast(g.V, g.row_ptr, _nz(g.col), np.ascontiguousarray(prio, np.float32),
+                                c, C.byref(r)), "color_fast")
     return c, r.value
 
 

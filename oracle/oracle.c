@@ -273,6 +273,47 @@ int orc_color(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
   return 0;
 }
 
+/* Closed form of the same colouring, for graphs where the round-by-round
+ * restatement is too slow (thousands of rounds on R-MAT): a vertex takes
+ * colour 1 + the largest colour among its higher-priority neighbours (0 if
+ * none) -- in the kernel it becomes colourable in the first round after all
+ * of those are coloured, and no neighbour of lower priority can be coloured
+ * before it -- and a degree-1 vertex takes colour 1 (it never looks at its
+ * neighbour).  Vertices are visited in decreasing priority (priorities
+ * distinct on adjacent vertices, as the kernel needs to terminate). */
+static const float* g_prio_sort;
+static int cmp_prio_desc(const void* a, const void* b) {
+  float x = g_prio_sort[*(const uint32_t*)a], y = g_prio_sort[*(const uint32_t*)b];
+  if (x > y) return -1;
+  if (x < y) return 1;
+  return (*(const uint32_t*)a < *(const uint32_t*)b) ? -1 : 1;
+}
+
+int orc_color_fast(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
+                   const float* nv, int32_t* color, uint32_t* rounds) {
+  uint32_t* ord = (uint32_t*)malloc(sizeof(uint32_t) * (V ? V : 1));
+  if (!ord) return -2;
+  for (uint32_t i = 0; i < V; ++i) { ord[i] = i; color[i] = 0; }
+  g_prio_sort = nv;
+  qsort(ord, V, sizeof(uint32_t), cmp_prio_desc);
+  int32_t mx = 0;
+  for (uint32_t k = 0; k < V; ++k) {
+    uint32_t v = ord[k];
+    int32_t c = 1;
+    if (row_ptr[v + 1] - row_ptr[v] != 1) {
+      for (uint32_t e = row_ptr[v]; e < row_ptr[v + 1]; ++e) {
+        uint32_t u = col[e];
+        if (nv[u] > nv[v] && color[u] + 1 > c) c = color[u] + 1;
+      }
+    }
+    color[v] = c;
+    if (c > mx) mx = c;
+  }
+  if (rounds) *rounds = (uint32_t)mx;
+  free(ord);
+  return 0;
+}
+
 /* ------------------------------------------------------------------- BC */
 
 /* Pannotia BC per source, float32, in the order one work-item executes
@@ -380,11 +421,6 @@ static uint32_t uf_find(uint32_t* p, uint32_t x) {
   return x;
 }
 
-static int cmp_u64(const void* a, const void* b) {
-  uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
-  return x < y ? -1 : x > y;
-}
-
 /* Minimum spanning forest by Kruskal.  With unique weights the forest is
  * unique, so it equals what the reference's Boruvka computes
  * (lonestar/apps/mst/mst_port.cpp:202-312, mst_common.cl:41-194,
@@ -412,7 +448,26 @@ int orc_mst(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
       if (u < col[e] && w[e] < ORC_LONESTAR_INF)
         key[n++] = ((uint64_t)w[e] << 32) | e;
     }
-  qsort(key, n, sizeof(uint64_t), cmp_u64);
+  /* LSD radix sort of the 64-bit keys, 16 bits per pass, skipping passes
+   * whose digit is constant */
+  {
+    uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * (n ? n : 1));
+    size_t* cnt = (size_t*)malloc(sizeof(size_t) * 65537);
+    if (!tmp || !cnt) { free(tmp); free(cnt); free(key); free(src); free(p); return -2; }
+    for (int pass = 0; pass < 4; ++pass) {
+      const int sh = 16 * pass;
+      memset(cnt, 0, sizeof(size_t) * 65537);
+      for (uint64_t i = 0; i < n; ++i) cnt[((key[i] >> sh) & 0xFFFF) + 1]++;
+      int nonzero = 0;
+      for (int d = 1; d <= 65536; ++d) nonzero += cnt[d] != 0;
+      if (nonzero <= 1) continue;
+      for (int d = 1; d <= 65536; ++d) cnt[d] += cnt[d - 1];
+      for (uint64_t i = 0; i < n; ++i) tmp[cnt[(key[i] >> sh) & 0xFFFF]++] = key[i];
+      uint64_t* t = key; key = tmp; tmp = t;
+    }
+    free(tmp);
+    free(cnt);
+  }
   for (uint32_t i = 0; i < V; ++i) p[i] = i;
   if (arc_in_mst) memset(arc_in_mst, 0, E);
   uint64_t total = 0;

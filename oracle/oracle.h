@@ -42,6 +42,8 @@ int orc_mis(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
             const float* node_value, int32_t* s_array, uint32_t* rounds);
 int orc_color(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
               const float* node_value, int32_t* color, uint32_t* rounds);
+int orc_color_fast(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
+                   const float* node_value, int32_t* color, uint32_t* rounds);
 int orc_bc_f32(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
                const uint32_t* trow, const uint32_t* tcol,
                const uint32_t* sources, uint32_t nsrc, float* bc);
