@@ -246,12 +246,16 @@ class GpuSuite:
         return outs
 
 
+_PINNED_KEEP: list = []
+
+
 def pinned_copy(torch, a: np.ndarray) -> np.ndarray:
+    """Copy into page-locked host memory (kept alive for the process)."""
     t = torch.empty(a.shape, dtype={np.dtype(np.uint32): torch.int32,
                                     np.dtype(np.float32): torch.float32}[a.dtype], pin_memory=True)
+    _PINNED_KEEP.append(t)
     out = t.numpy().view(a.dtype)
     out[...] = a
-    out._keep = t  # type: ignore[attr-defined]
     return out
 
 

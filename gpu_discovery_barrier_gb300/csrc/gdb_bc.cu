@@ -199,10 +199,11 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
           ++arcs;
           u = __ldg(&G.col[arc]);
           const int32_t du = ld_cg(&ws.d[u]);
-          if (du == Li - 1) {
+          if (du == -1) {
+            // unvisited (-1 is also L - 1 at level 0: test it first)
+            want = atomicCAS(&ws.d[u], -1, Li + 1) == -1;
+          } else if (Li > 0 && du == Li - 1) {
             acc += (double)ld_cg(&ws.rho[u]);
-          } else if (du == -1 && atomicCAS(&ws.d[u], -1, Li + 1) == -1) {
-            want = true;
           }
         }
         // a claimed heavy vertex gets its chunk countdown armed by the push

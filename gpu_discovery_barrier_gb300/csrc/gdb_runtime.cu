@@ -96,9 +96,12 @@ int reset_device_ctx(gdb_ctx* c, int skip) {
   return GDB_OK;
 }
 
+// Pinned staging layout: [0, 3072) run statistics of the callers,
+// [3072, 3584) participating count, [3584, 4096) device status.
 int finish_run(gdb_ctx* c) {
-  int* h = (int*)pinned(c, 4096);
-  if (!h) return set_error(c, GDB_ERR_OOM, "pinned staging");
+  char* base = (char*)pinned(c, 4096);
+  if (!base) return set_error(c, GDB_ERR_OOM, "pinned staging");
+  int* h = (int*)(base + 3584);
   // status, abort, err_where of the device context
   GDB_CUDA(c, cudaMemcpyAsync(h, &c->dctx->status, 4 * sizeof(int), cudaMemcpyDeviceToHost,
                               c->stream));
@@ -118,8 +121,9 @@ int finish_run(gdb_ctx* c) {
 }
 
 int read_participating(gdb_ctx* c, int* n) {
-  int* h = (int*)pinned(c, 4096);
-  if (!h) return set_error(c, GDB_ERR_OOM, "pinned staging");
+  char* base = (char*)pinned(c, 4096);
+  if (!base) return set_error(c, GDB_ERR_OOM, "pinned staging");
+  int* h = (int*)(base + 3072);
   GDB_CUDA(c, cudaMemcpyAsync(h, &c->dctx->num_participating, sizeof(int), cudaMemcpyDeviceToHost,
                               c->stream));
   GDB_CUDA(c, cudaStreamSynchronize(c->stream));
