@@ -64,17 +64,20 @@ __device__ __forceinline__ void visit_level(const GraphView& G, const BcWs& ws, 
                                             uint32_t* cursor, uint32_t* hcursor, Begin&& begin,
                                             Edge&& edge, End&& end, Heavy&& heavy) {
   const int lane = lane_id();
+  const uint32_t ngroups = (nl + 31) / 32;
   for (;;) {
-    const uint32_t g = warp_grab(cursor);
-    if ((uint64_t)g * 32 >= nl) break;
-    const uint32_t i = g * 32 + lane;
-    const bool act = i < nl;
-    const uint32_t v = act ? ld_cg(&ws.order[lb + i]) : 0u;
-    begin(v, act);
-    __syncwarp();
-    group_arcs(G, act, v, edge);
-    __syncwarp();
-    end(v, act);
+    const uint32_t g0 = warp_grab(cursor) * kGrab;
+    if (g0 >= ngroups) break;
+    for (uint32_t g = g0; g < min(g0 + kGrab, ngroups); ++g) {
+      const uint32_t i = g * 32 + lane;
+      const bool act = i < nl;
+      const uint32_t v = act ? ld_cg(&ws.order[lb + i]) : 0u;
+      begin(v, act);
+      __syncwarp();
+      group_arcs(G, act, v, edge);
+      __syncwarp();
+      end(v, act);
+    }
   }
   for (;;) {
     const uint32_t c = warp_grab(hcursor);

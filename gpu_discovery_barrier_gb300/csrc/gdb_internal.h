@@ -24,6 +24,7 @@ struct gdb_ctx {
   int* flags = nullptr;
   int flag_cap = 0;
   int stall_after = -1;
+  unsigned long long launches = 0;  // launch ids for the XF epochs
   // grow-only device workspace
   void* ws = nullptr;
   size_t ws_bytes = 0;

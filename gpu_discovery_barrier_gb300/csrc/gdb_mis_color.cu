@@ -185,13 +185,20 @@ struct ColorWs {
   int32_t* color;
   uint32_t* mx;        // light vertices: key of the max uncoloured neighbour priority
   uint32_t* hmx[2];    // heavy vertices, double-buffered by round
+  uint32_t* list[2];   // uncoloured light vertices of the round / of the next round
   const float* prio;
+  uint32_t* lcount;    // [3] survivors pushed in a phase-B superstep
   uint32_t* cursor;    // [3]
   uint32_t* hcursor;   // [3]
   uint32_t* flag;      // [3] some vertex saw an uncoloured neighbour (stop)
+  int* overflow;
   unsigned long long* stats;  // [0] arcs, [1] rounds
 };
 
+// Rounds keep the still-uncoloured light vertices in a compacted list, so a
+// round costs work proportional to the vertices left (R-MAT needs
+// thousands of rounds, most of them over a handful of vertices); heavy
+// vertices are few and are checked through the static chunk table.
 template <class Sync>
 __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const ColorWs& ws, uint32_t* smem) {
   const Warps W = warps_of(s.id(), s.P());
@@ -199,79 +206,111 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   const int lane = lane_id();
   uint32_t* my = smem + (threadIdx.x & ~31u);
   const uint32_t none = fkey(-1.0f);  // `maximum = -1` (color_kernel.cl:198)
-  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) ws.color[v] = -1;
-  for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) ws.hmx[0][h] = ws.hmx[1][h] = none;
-  if (leader) {
-    for (int i = 0; i < 3; ++i) ws.cursor[i] = ws.hcursor[i] = ws.flag[i] = 0;
-    ws.stats[0] = ws.stats[1] = 0;
+  // color[] = -1 (host init, color_gb.cpp:149); the first list holds every
+  // light vertex
+  for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
+    const uint32_t v = g * 32 + lane;
+    if (v < G.V) ws.color[v] = -1;
+    warp_append(ws.list[0], &ws.lcount[2], G.V, ws.overflow, v < G.V && !is_heavy(G, v), v);
   }
+  for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) ws.hmx[0][h] = ws.hmx[1][h] = none;
   if (!s.sync()) return;
   unsigned long long arcs = 0;
   int32_t graph_color = 1;
+  // superstep t: 2r = phase A of round r, 2r+1 = phase B; the init pushed
+  // into lcount[2], read like a phase-B count at the top of round 0
+  uint32_t t = 0;
+  uint32_t n_prev_slot = 2;
   for (uint32_t r = 0;; ++r, ++graph_color) {
-    const int cur = r % 3, old = (r + 2) % 3;
-    if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
-    // ---- color: max over uncoloured neighbours
-    bool saw = false;
-    sweep_light(
-        G, &ws.cursor[cur],
-        [&](uint32_t v, bool in_range) {
-          my[lane] = none;
-          if (!in_range || ld_cg(&ws.color[v]) != -1) return false;
+    const uint32_t* list = pick(ws.list, r);
+    uint32_t* next = pick(ws.list, r + 1);
+    const uint32_t n = ld_cg(&ws.lcount[n_prev_slot]);
+    // ---- color: max over uncoloured neighbours (superstep t = 2r)
+    {
+      const int cur = t % 3, old = (t + 1) % 3;
+      if (leader) ws.lcount[old] = ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
+      bool saw = false;
+      const uint32_t ngroups = (n + 31) / 32;
+      for (;;) {
+        const uint32_t g0 = warp_grab(&ws.cursor[cur]) * kGrab;
+        if (g0 >= ngroups) break;
+        for (uint32_t g = g0; g < min(g0 + kGrab, ngroups); ++g) {
+          const uint32_t i = g * 32 + lane;
+          const uint32_t v = i < n ? ld_cg(&list[i]) : 0u;
           // a degree-1 vertex never looks at its neighbour
-          return __ldg(&G.row[v + 1]) - __ldg(&G.row[v]) != 1;
-        },
-        [&](bool valid, int owner, uint32_t arc) {
-          if (valid) {
-            ++arcs;
-            const uint32_t u = __ldg(&G.col[arc]);
-            if (ld_cg(&ws.color[u]) == -1) {
-              saw = true;
-              const uint32_t k = fkey(__ldg(&ws.prio[u]));
-              if (k > my[owner]) atomicMax(&my[owner], k);
+          const bool act = i < n && __ldg(&G.row[v + 1]) - __ldg(&G.row[v]) != 1;
+          my[lane] = none;
+          __syncwarp();
+          group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) {
+            if (valid) {
+              ++arcs;
+              const uint32_t u = __ldg(&G.col[arc]);
+              if (ld_cg(&ws.color[u]) == -1) {
+                saw = true;
+                const uint32_t k = fkey(__ldg(&ws.prio[u]));
+                if (k > my[owner]) atomicMax(&my[owner], k);
+              }
             }
-          }
-        },
-        [&](uint32_t v, bool act) {
-          if (v < G.V && !is_heavy(G, v)) ws.mx[v] = act ? my[lane] : none;
-        });
-    uint32_t* hmx = pick(ws.hmx, r);
-    sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
-      if (ld_cg(&ws.color[v]) != -1) return;
-      uint32_t m = none;
-      bool any = false;
-      for (uint32_t a0 = b; a0 < e; a0 += 32) {
-        const uint32_t a = a0 + lane;
-        if (a < e) {
-          ++arcs;
-          const uint32_t u = __ldg(&G.col[a]);
-          if (ld_cg(&ws.color[u]) == -1) {
-            any = true;
-            m = max(m, fkey(__ldg(&ws.prio[u])));
-          }
+          });
+          __syncwarp();
+          if (i < n) ws.mx[v] = my[lane];
         }
       }
-      m = warp_max_u32(m);
-      saw |= any;
-      if (lane == 0 && m > none) atomicMax(&hmx[h], m);
-    });
-    if (__any_sync(kFull, saw) && lane == 0) atomicOr(&ws.flag[cur], 1u);
-    if (!s.sync()) return;
-    // ---- color2: uncoloured vertices above the maximum take the colour
-    for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
-      if (is_heavy(G, v) || ws.color[v] != -1) continue;
-      if (fkey(__ldg(&ws.prio[v])) > ws.mx[v]) ws.color[v] = graph_color;
+      uint32_t* hmx = pick(ws.hmx, r);
+      sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
+        if (ld_cg(&ws.color[v]) != -1) return;
+        uint32_t m = none;
+        bool any = false;
+        for (uint32_t a0 = b; a0 < e; a0 += 32) {
+          const uint32_t a = a0 + lane;
+          if (a < e) {
+            ++arcs;
+            const uint32_t u = __ldg(&G.col[a]);
+            if (ld_cg(&ws.color[u]) == -1) {
+              any = true;
+              m = max(m, fkey(__ldg(&ws.prio[u])));
+            }
+          }
+        }
+        m = warp_max_u32(m);
+        saw |= any;
+        if (lane == 0 && m > none) atomicMax(&hmx[h], m);
+      });
+      if (__any_sync(kFull, saw) && lane == 0) atomicOr(&ws.flag[cur], 1u);
+      if (!s.sync()) return;
+      ++t;
     }
-    for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) {
-      const uint32_t v = __ldg(&G.heavy_v[h]);
-      if (ws.color[v] == -1 && fkey(__ldg(&ws.prio[v])) > hmx[h]) ws.color[v] = graph_color;
-      pick(ws.hmx, r + 1)[h] = none;
+    // ---- color2: uncoloured vertices above the maximum take the colour;
+    // the others go to the next round's list (superstep t = 2r+1)
+    {
+      const int cur = t % 3, old = (t + 1) % 3;
+      const bool stop = ld_cg(&ws.flag[(t - 1) % 3]) == 0;
+      if (leader) ws.lcount[old] = ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
+      for (uint32_t g = W.gwarp; g * 32 < n; g += W.nwarps) {
+        const uint32_t i = g * 32 + lane;
+        bool keep = false;
+        uint32_t v = 0;
+        if (i < n) {
+          v = ld_cg(&list[i]);
+          if (fkey(__ldg(&ws.prio[v])) > ws.mx[v]) ws.color[v] = graph_color;
+          else keep = true;
+        }
+        warp_append(next, &ws.lcount[cur], G.V, ws.overflow, keep, v);
+      }
+      const uint32_t* hmx = pick(ws.hmx, r);
+      for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) {
+        const uint32_t v = __ldg(&G.heavy_v[h]);
+        if (ws.color[v] == -1 && fkey(__ldg(&ws.prio[v])) > hmx[h]) ws.color[v] = graph_color;
+        pick(ws.hmx, r + 1)[h] = none;
+      }
+      if (stop) {
+        if (leader) ws.stats[1] = r + 1;
+        break;
+      }
+      if (!s.sync()) return;
+      n_prev_slot = cur;
+      ++t;
     }
-    if (ld_cg(&ws.flag[cur]) == 0) {
-      if (leader) ws.stats[1] = r + 1;
-      break;
-    }
-    if (!s.sync()) return;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
@@ -351,12 +390,15 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
   Bump b;
   const size_t o_mx = b.take((size_t)g->V * 4);
+  const size_t o_l0 = b.take((size_t)g->V * 4), o_l1 = b.take((size_t)g->V * 4);
   const size_t o_h0 = b.take(hcap * 4), o_h1 = b.take(hcap * 4), o_cnt = b.take(256);
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
   ColorWs ws;
   ws.color = d_color;
   ws.mx = (uint32_t*)(base + o_mx);
+  ws.list[0] = (uint32_t*)(base + o_l0);
+  ws.list[1] = (uint32_t*)(base + o_l1);
   ws.hmx[0] = (uint32_t*)(base + o_h0);
   ws.hmx[1] = (uint32_t*)(base + o_h1);
   ws.prio = d_prio;
@@ -365,7 +407,15 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   ws.cursor = (uint32_t*)(cnt + 64);
   ws.hcursor = (uint32_t*)(cnt + 80);
   ws.flag = (uint32_t*)(cnt + 96);
-  return launch_xf(c, k_color_xf, g->view(), ws, ws.stats);
+  ws.lcount = (uint32_t*)(cnt + 112);
+  ws.overflow = (int*)(cnt + 128);
+  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 256, c->stream));
+  int rc = launch_xf(c, k_color_xf, g->view(), ws, ws.stats);
+  if (rc) return rc;
+  int* h = (int*)pinned(c, 4096);
+  GDB_CUDA(c, cudaMemcpy(h, ws.overflow, 4, cudaMemcpyDeviceToHost));
+  if (h[0]) return set_error(c, GDB_ERR_CAPACITY, "colour list overflow");
+  return GDB_OK;
 }
 
 // Host-buffer wrapper: copy the priorities in, run, copy the answer out.

@@ -80,6 +80,8 @@ gdb::DiscoveryArgs discovery_args(gdb_ctx* c, const Shape& s) {
   a.expected = std::min(s.grid, s.fit);
   a.timeout_ns = c->opt.timeout_ns ? c->opt.timeout_ns : 2000000000ull;
   a.close_wait_ns = 50000ull;
+  a.launch_id = ++c->launches;
+  a.xf_release = c->opt.xf_release;
   return a;
 }
 
@@ -217,6 +219,7 @@ static int check_options(const gdb_options* o) {
   if (o->barrier < GDB_BARRIER_XF || o->barrier > GDB_BARRIER_XF_FIXED) return GDB_ERR_INVALID;
   if (o->schedule < GDB_SCHED_PLAIN || o->schedule > GDB_SCHED_ADAPTIVE) return GDB_ERR_INVALID;
   if (o->max_ctas < 0 || o->oversubscribe < 0) return GDB_ERR_INVALID;
+  if (o->xf_release < 0 || o->xf_release > 1) return GDB_ERR_INVALID;
   return GDB_OK;
 }
 
@@ -285,7 +288,11 @@ int gdb_ctx_set_options(gdb_ctx* c, const gdb_options* opt) {
   if (o.timeout_ns == 0) o.timeout_ns = 2000000000ull;
   if (check_options(&o) != GDB_OK) return GDB_ERR_INVALID;
   o.device = c->device;
+  const bool mode_change = o.xf_release != c->opt.xf_release;
   c->opt = o;
+  // per-slave flags read "arrived" as != 0: clear the epochs the broadcast
+  // form leaves in them
+  if (mode_change) return reset_device_ctx(c, 0);
   return GDB_OK;
 }
 

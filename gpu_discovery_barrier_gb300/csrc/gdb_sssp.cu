@@ -65,16 +65,19 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const SsspWs& ws, 
   };
   // light groups: each lane reads its own vertex's distance once
   const int lane = lane_id();
+  const uint32_t ngroups = (n + 31) / 32;
   for (;;) {
-    const uint32_t g = warp_grab(&ws.cursor[cur]);
-    if ((uint64_t)g * 32 >= n) break;
-    const uint32_t i = g * 32 + lane;
-    const bool act = i < n;
-    const uint32_t u = act ? ld_cg(&pick(ws.q, L)[i]) : 0u;
-    const uint32_t du = act ? ld_cg(&ws.dist[u]) : 0u;
-    group_arcs(G, act, u, [&](bool valid, int owner, uint32_t arc) {
-      relax(valid, __shfl_sync(kFull, du, owner), arc);
-    });
+    const uint32_t g0 = warp_grab(&ws.cursor[cur]) * kGrab;
+    if (g0 >= ngroups) break;
+    for (uint32_t g = g0; g < min(g0 + kGrab, ngroups); ++g) {
+      const uint32_t i = g * 32 + lane;
+      const bool act = i < n;
+      const uint32_t u = act ? ld_cg(&pick(ws.q, L)[i]) : 0u;
+      const uint32_t du = act ? ld_cg(&ws.dist[u]) : 0u;
+      group_arcs(G, act, u, [&](bool valid, int owner, uint32_t arc) {
+        relax(valid, __shfl_sync(kFull, du, owner), arc);
+      });
+    }
   }
   const uint32_t ne = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
   const uint32_t* hv = pick(ws.hv, L);

@@ -23,6 +23,9 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr uint32_t kHeavyDeg = 1024;
 constexpr uint32_t kChunk = 1024;
 constexpr uint32_t kInf = GDB_LONESTAR_INF;
+// groups of 32 vertices a warp takes per atomic on a work cursor (one
+// cursor word is shared by every warp of the grid, so grabs are batched)
+constexpr uint32_t kGrab = 4;
 
 struct GraphView {
   uint32_t V;
@@ -202,6 +205,22 @@ __device__ __forceinline__ void frontier_push(const GraphView& G, const Frontier
   }
 }
 
+// Warp-aggregated append of the lanes' `want` values to a list.
+__device__ __forceinline__ void warp_append(uint32_t* list, uint32_t* count, uint32_t cap,
+                                            int* overflow, bool want, uint32_t v) {
+  const unsigned m = __ballot_sync(kFull, want);
+  if (!m) return;
+  const int lane = lane_id(), leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+  base = __shfl_sync(kFull, base, leader);
+  if (want) {
+    const uint32_t slot = base + __popc(m & lanemask_lt());
+    if (slot < cap) list[slot] = v;
+    else atomicExch(overflow, 1);
+  }
+}
+
 // Visit a frontier: light vertices in warp groups of 32, then heavy chunks.
 // light(valid, owner_lane, owner_vertex_in_lane, arc) is called through
 // group_arcs; heavy(valid, v, arc) per 32-arc step of a chunk.
@@ -211,13 +230,16 @@ __device__ __forceinline__ void visit_frontier(const GraphView& G, const uint32_
                                                unsigned long long hpacked, uint32_t* cursor,
                                                uint32_t* hcursor, Light&& light, Heavy&& heavy) {
   const int lane = lane_id();
+  const uint32_t ngroups = (n + 31) / 32;
   for (;;) {
-    const uint32_t g = warp_grab(cursor);
-    if ((uint64_t)g * 32 >= n) break;
-    const uint32_t i = g * 32 + lane;
-    const bool act = i < n;
-    const uint32_t v = act ? ld_cg(&q[i]) : 0u;
-    group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) { light(valid, owner, v, arc); });
+    const uint32_t g0 = warp_grab(cursor) * kGrab;
+    if (g0 >= ngroups) break;
+    for (uint32_t g = g0; g < min(g0 + kGrab, ngroups); ++g) {
+      const uint32_t i = g * 32 + lane;
+      const bool act = i < n;
+      const uint32_t v = act ? ld_cg(&q[i]) : 0u;
+      group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) { light(valid, owner, v, arc); });
+    }
   }
   const uint32_t ne = (uint32_t)(hpacked >> 32);
   const uint32_t nch = (uint32_t)hpacked;
@@ -246,15 +268,17 @@ __device__ __forceinline__ void sweep_light(const GraphView& G, uint32_t* cursor
   const int lane = lane_id();
   const uint32_t ngroups = (G.V + 31) / 32;
   for (;;) {
-    const uint32_t g = warp_grab(cursor);
-    if (g >= ngroups) break;
-    const uint32_t v = g * 32 + lane;
-    const bool in_range = v < G.V && !is_heavy(G, v);
-    const bool act = begin(v, in_range) && in_range;
-    __syncwarp();
-    group_arcs(G, act, v, edge);
-    __syncwarp();
-    end(v, act);
+    const uint32_t g0 = warp_grab(cursor) * kGrab;
+    if (g0 >= ngroups) break;
+    for (uint32_t g = g0; g < min(g0 + kGrab, ngroups); ++g) {
+      const uint32_t v = g * 32 + lane;
+      const bool in_range = v < G.V && !is_heavy(G, v);
+      const bool act = begin(v, in_range) && in_range;
+      __syncwarp();
+      group_arcs(G, act, v, edge);
+      __syncwarp();
+      end(v, act);
+    }
   }
 }
 

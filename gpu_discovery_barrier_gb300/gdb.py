@@ -44,7 +44,7 @@ class GdbError(RuntimeError):
 class Options(C.Structure):
     _fields_ = [("device", C.c_int), ("block_size", C.c_int), ("max_ctas", C.c_int),
                 ("oversubscribe", C.c_int), ("lock", C.c_int), ("barrier", C.c_int),
-                ("schedule", C.c_int), ("reserved0", C.c_int), ("timeout_ns", C.c_uint64)]
+                ("schedule", C.c_int), ("xf_release", C.c_int), ("timeout_ns", C.c_uint64)]
 
 
 class RunStats(C.Structure):

@@ -77,7 +77,8 @@ typedef struct {
   int lock;            /* gdb_lock_kind */
   int barrier;         /* gdb_barrier_kind */
   int schedule;        /* gdb_schedule */
-  int reserved0;
+  int xf_release;      /* XF release form: 0 = master clears every slave's
+                          flag (the reference's), 1 = one broadcast epoch word */
   uint64_t timeout_ns; /* limit for every device spin (0 = 2e9) */
 } gdb_options;
 

@@ -48,6 +48,9 @@ struct __align__(128) DeviceCtx {
   int err_aux;
   int stall_after;    // test hook: master stops releasing after this many barriers (-1 off)
   int _p6[27];
+  // broadcast release word of the epoch form of the XF barrier
+  unsigned long long release;
+  unsigned long long _p7[15];
 };
 
 // discovery_local_ctx (discovery.cl:67-71), in shared memory.
@@ -60,6 +63,12 @@ struct LocalCtx {
   int barriers;       // barriers passed (master: for the stall test hook)
 };
 
+// XF release forms.
+enum XfRelease {
+  kXfPerSlave = 0,  // the master stores 0 into every slave's flag (discovery.cl:203-209)
+  kXfBroadcast = 1  // slaves store a launch-unique epoch; one broadcast release word
+};
+
 // Launch parameters every discovery kernel receives.
 struct DiscoveryArgs {
   DeviceCtx* ctx;
@@ -69,6 +78,8 @@ struct DiscoveryArgs {
   int expected;            // CTAs the occupancy API says fit (0 = unknown)
   unsigned long long timeout_ns;
   unsigned long long close_wait_ns;  // lock-free: wait for `expected` pollers
+  unsigned long long launch_id;      // > every earlier launch's: epochs never repeat
+  int xf_release;                    // XfRelease
 };
 
 using aref = cuda::atomic_ref<int, cuda::thread_scope_device>;
@@ -89,6 +100,13 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 }
 __device__ __forceinline__ void st_relaxed(int* p, int v) {
   aref(*p).store(v, cuda::memory_order_relaxed);
+}
+using aref64 = cuda::atomic_ref<unsigned long long, cuda::thread_scope_device>;
+__device__ __forceinline__ unsigned long long ld_relaxed64(unsigned long long* p) {
+  return aref64(*p).load(cuda::memory_order_relaxed);
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() {
+  cuda::atomic_thread_fence(cuda::memory_order_acq_rel, cuda::thread_scope_device);
 }
 
 // Record the first error and make every spinning CTA give up.
@@ -277,15 +295,25 @@ __device__ __forceinline__ int p_get_global_size(const LocalCtx* l) {
 }
 
 // XF barrier (discovery.cl:177-238) over the participating CTAs.  Slave: one
-// elected thread release-stores 1 to its padded flag and spins until the
-// master stores 0.  Master: each thread issues loads for all of its peers'
+// elected thread publishes its arrival in its own padded flag and spins
+// until released.  Master: each thread issues loads for all of its peers'
 // flags at once and retires the ones that arrived, so the wait costs one
-// L2 round trip after the last arrival; then a CTA barrier and release
-// stores of 0.  Returns false (uniformly across the CTA) after an error or
+// L2 round trip after the last arrival; then a CTA barrier and the
+// release.  Two release forms (DiscoveryArgs::xf_release):
+//  * per-slave: arrival stores 1, the master stores 0 into every flag
+//    (the reference's form);
+//  * broadcast: arrival stores the barrier's epoch (launch id << 32 |
+//    barrier count, never repeated), the master stores the epoch once into
+//    a broadcast word every slave polls -- no per-slave stores, no resets.
+// Ordering: fence.acq_rel.gpu + relaxed store on the releasing side,
+// relaxed polls + fence.acq_rel.gpu on the acquiring side, CTA barriers
+// in between.  Returns false (uniformly across the CTA) after an error or
 // a timeout anywhere in the grid.
 __device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l) {
   DeviceCtx* c = a.ctx;
   const int P = l->P;
+  const bool bcast = a.xf_release == kXfBroadcast;
+  const unsigned long long tag = (a.launch_id << 32) | (unsigned)(l->barriers + 1);
   int ok = 1;
   if (l->id == 0) {
     __syncthreads();
@@ -298,12 +326,15 @@ __device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l) {
         int kk = 0;
         for (int peer = threadIdx.x + 1; peer < P; peer += blockDim.x, ++kk) {
           if ((pending >> kk) & 1u) {
-            if (ld_relaxed(&a.flags[(size_t)peer * kLineInts]) != 0) pending &= ~(1u << kk);
+            int* f = &a.flags[(size_t)peer * kLineInts];
+            const bool arrived = bcast ? ld_relaxed64((unsigned long long*)f) >= tag
+                                       : ld_relaxed(f) != 0;
+            if (arrived) pending &= ~(1u << kk);
           }
         }
         return pending == 0;
       });
-      __threadfence();  // acquire: order the slaves' writes before ours
+      fence_acq_rel_gpu();  // acquire: the slaves' writes before ours
     }
     ok = __syncthreads_and(ok);
     if (ok && c->stall_after >= 0 && l->barriers >= c->stall_after) {
@@ -315,26 +346,40 @@ __device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l) {
       ok = 0;
     }
     if (ok) {
-      __threadfence();  // release: publish the grid's writes with the flags
-      for (int peer = threadIdx.x + 1; peer < P; peer += blockDim.x)
-        st_relaxed(&a.flags[(size_t)peer * kLineInts], 0);
+      if (bcast) {
+        if (threadIdx.x == 0) {
+          fence_acq_rel_gpu();  // release: the grid's writes before the word
+          aref64(c->release).store(tag, cuda::memory_order_relaxed);
+        }
+      } else {
+        fence_acq_rel_gpu();  // release: publish the grid's writes with the flags
+        for (int peer = threadIdx.x + 1; peer < P; peer += blockDim.x)
+          st_relaxed(&a.flags[(size_t)peer * kLineInts], 0);
+      }
     }
-    if (threadIdx.x == 0) l->barriers++;
   } else {
     __syncthreads();
     if (threadIdx.x == 0) {
       int* f = &a.flags[(size_t)l->id * kLineInts];
-      __threadfence();
-      st_relaxed(f, 1);
-      ok = spin_until(c, l->timeout_ns, 7, [&] { return ld_relaxed(f) == 0; });
-      __threadfence();
+      fence_acq_rel_gpu();
+      if (bcast) {
+        aref64(*(unsigned long long*)f).store(tag, cuda::memory_order_relaxed);
+        ok = spin_until(c, l->timeout_ns, 7, [&] { return ld_relaxed64(&c->release) >= tag; });
+      } else {
+        st_relaxed(f, 1);
+        ok = spin_until(c, l->timeout_ns, 7, [&] { return ld_relaxed(f) == 0; });
+      }
+      fence_acq_rel_gpu();
       l->ok = ok;
     }
     __syncthreads();
     ok = l->ok;
   }
   // every CTA leaves together on error
-  if (threadIdx.x == 0 && !ok) l->ok = 0;
+  if (threadIdx.x == 0) {
+    if (!ok) l->ok = 0;
+    l->barriers++;
+  }
   __syncthreads();
   return l->ok != 0;
 }

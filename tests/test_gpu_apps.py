@@ -111,13 +111,20 @@ def test_color(ctx, name, g):
 
 @pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
 def test_bc(ctx, name, g):
+    """Path counts are float32 as in the reference (bc_kernel.cl rho); on
+    long grids they overflow (C(510,255) ~ 1e152 on 256x256), making the
+    reference's own scores inf/NaN.  Where the float32 oracle is finite the
+    GPU must be within RTOL of it and of the FP64 oracle; where it is not,
+    the GPU result must not be finite either."""
     srcs = gg.sources(g, 4, seed=8) if g.E else np.array([0], dtype=np.uint32)
     G = ctx.graph(g.row_ptr, g.col)
     got = ctx.bc(G, srcs)
-    want32 = oracle.bc_f32(g, g, srcs)
+    want32 = oracle.bc_f32(g, g, srcs).astype(np.float64)
     want64 = oracle.bc_f64(g, srcs)
-    assert bc_close(got, want64), name
-    assert bc_close(got, want32.astype(np.float64)), name
+    fin = np.isfinite(want32)
+    assert bc_close(got[fin], want64[fin]), name
+    assert bc_close(got[fin], want32[fin]), name
+    assert not np.any(np.isfinite(got[~fin])), name
 
 
 @pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
