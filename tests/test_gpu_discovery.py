@@ -50,16 +50,35 @@ def test_skip_refuses_oversubscription():
         c.init_discovery_kernel_ctx()
 
 
+@pytest.mark.parametrize("xf_release", [0, 1])
 @pytest.mark.parametrize("kind", [gdb.BARRIER_XF, gdb.BARRIER_XF_FIXED, gdb.BARRIER_GRID_SYNC,
                                   gdb.BARRIER_RELAUNCH, gdb.BARRIER_RELAUNCH_GRAPH])
-def test_barrier_bench(kind):
-    with gdb.Ctx() as c:
+def test_barrier_bench(kind, xf_release):
+    with gdb.Ctx(xf_release=xf_release) as c:
         ns, groups = c.barrier_bench(kind, 256, 200)
         assert ns > 0 and groups >= 1
 
 
-def test_timeout_reports_and_recovers():
-    with gdb.Ctx(timeout_ns=50_000_000) as c:
+def test_release_modes_switch_in_one_context():
+    """Switching the XF release form must not leave stale arrivals."""
+    import numpy as np
+
+    import oracle
+    from gpu_discovery_barrier_gb300 import graphgen as gg
+
+    g = gg.rmat(1 << 12, 8, seed=3)
+    with gdb.Ctx() as c:
+        G = c.graph(g.row_ptr, g.col)
+        want = oracle.bfs(g, 1)
+        for rel in (1, 0, 1, 0):
+            c.set_options(xf_release=rel)
+            assert np.array_equal(c.bfs(G, 1), want)
+            c.barrier_bench(gdb.BARRIER_XF, 256, 50)
+
+
+@pytest.mark.parametrize("xf_release", [0, 1])
+def test_timeout_reports_and_recovers(xf_release):
+    with gdb.Ctx(timeout_ns=50_000_000, xf_release=xf_release) as c:
         c.debug_stall_master(3)
         with pytest.raises(gdb.GdbError) as e:
             c.barrier_bench(gdb.BARRIER_XF, 256, 20)
