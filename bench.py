@@ -82,8 +82,9 @@ def reach(g, dist):
 def alg_bytes(app: str, g, reached, rounds: int) -> float:
     """Algorithmic bytes of one launch (uint32 = 4 B), schedule-independent:
     BFS 8E_r + 12V_r + 4V; SSSP 12E_r + 12V_r + 4V; BC 20E_r + 24V_r + 12V
-    per source; MST (12E + 16V) per round; MIS/colour (12E + 8V) per round
-    bound from above by the full graph."""
+    per source; MST (12E + 16V) per round; colouring 24E + 16V (one count
+    pass and one countdown pass over the arcs); MIS (12E + 8V) per round,
+    bounded from above by the full graph."""
     V, E = g.V, g.E
     if app == "bfs":
         return sum(8 * er + 12 * vr + 4 * V for vr, er in reached)
@@ -93,6 +94,10 @@ def alg_bytes(app: str, g, reached, rounds: int) -> float:
         return sum(20 * er + 24 * vr + 12 * V for vr, er in reached)
     if app == "mst":
         return rounds * (12 * E + 16 * V)
+    if app == "color":
+        # count pass (col + neighbour priority per arc) and one countdown
+        # pass (col, neighbour degree and priority, counter) per arc
+        return 8 * E + 8 * V + 16 * E + 8 * V
     return rounds * (12 * E + 8 * V)
 
 

@@ -66,9 +66,9 @@ __device__ __forceinline__ void visit_level(const GraphView& G, const BcWs& ws, 
   const int lane = lane_id();
   const uint32_t ngroups = (nl + 31) / 32;
   for (;;) {
-    const uint32_t g0 = warp_grab(cursor) * kGrab;
+    const uint32_t g0 = warp_grab(cursor);
     if (g0 >= ngroups) break;
-    for (uint32_t g = g0; g < min(g0 + kGrab, ngroups); ++g) {
+    for (uint32_t g = g0; g < min(g0 + 1, ngroups); ++g) {
       const uint32_t i = g * 32 + lane;
       const bool act = i < nl;
       const uint32_t v = act ? ld_cg(&ws.order[lb + i]) : 0u;

@@ -180,141 +180,174 @@ __global__ void __launch_bounds__(1024, 1) k_mis_xf(DiscoveryArgs a, GraphView G
 }
 
 // ------------------------------------------------------------- colouring
+//
+// The round structure of the reference colours v in the first round after
+// all of its higher-priority neighbours are coloured: colour(v) = 1 + the
+// largest colour among them (0 if none), and a degree-1 vertex takes 1.
+// Re-scanning every uncoloured vertex's arcs each round (the reference's
+// O(E x rounds), thousands of rounds on R-MAT) is replaced by peeling that
+// priority DAG: every vertex counts the neighbours it waits for; the
+// vertices coloured in round r walk their arcs once and count down their
+// lower-priority neighbours, and a counter reaching zero puts that vertex
+// in round r+1.  One barrier per round, every arc touched twice in total,
+// the same colours.  Neighbours of equal priority wait for each other, so
+// -- as in the reference, which never terminates then -- they stay
+// uncoloured; the host reports that as an error.
 
 struct ColorWs {
   int32_t* color;
-  uint32_t* mx;        // light vertices: key of the max uncoloured neighbour priority
-  uint32_t* hmx[2];    // heavy vertices, double-buffered by round
-  uint32_t* list[2];   // uncoloured light vertices of the round / of the next round
+  uint32_t* cnt;       // neighbours still to be coloured before this vertex
   const float* prio;
-  uint32_t* lcount;    // [3] survivors pushed in a phase-B superstep
-  uint32_t* cursor;    // [3]
-  uint32_t* hcursor;   // [3]
-  uint32_t* flag;      // [3] some vertex saw an uncoloured neighbour (stop)
+  uint32_t* q[2];
+  uint32_t* hv[2];
+  uint32_t* hb[2];
+  uint32_t* qcount;            // [3]
+  unsigned long long* hcount;  // [3]
+  uint32_t* cursor;            // [3]
+  uint32_t* hcursor;           // [3]
   int* overflow;
-  unsigned long long* stats;  // [0] arcs, [1] rounds
+  unsigned long long* stats;   // [0] arcs, [1] rounds, [2] coloured vertices
+  uint32_t qcap, hcap;
 };
 
-// Rounds keep the still-uncoloured light vertices in a compacted list, so a
-// round costs work proportional to the vertices left (R-MAT needs
-// thousands of rounds, most of them over a handful of vertices); heavy
-// vertices are few and are checked through the static chunk table.
+// u waits for v: u looks at its neighbours (degree != 1) and v's priority
+// is not below u's.
+__device__ __forceinline__ bool waits_for(const GraphView& G, const float* prio, uint32_t u,
+                                          float pv) {
+  return __ldg(&G.row[u + 1]) - __ldg(&G.row[u]) != 1 && pv >= __ldg(&prio[u]);
+}
+
 template <class Sync>
 __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const ColorWs& ws, uint32_t* smem) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
   const int lane = lane_id();
   uint32_t* my = smem + (threadIdx.x & ~31u);
-  const uint32_t none = fkey(-1.0f);  // `maximum = -1` (color_kernel.cl:198)
-  // color[] = -1 (host init, color_gb.cpp:149); the first list holds every
-  // light vertex
-  for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
-    const uint32_t v = g * 32 + lane;
-    if (v < G.V) ws.color[v] = -1;
-    warp_append(ws.list[0], &ws.lcount[2], G.V, ws.overflow, v < G.V && !is_heavy(G, v), v);
-  }
-  for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) ws.hmx[0][h] = ws.hmx[1][h] = none;
-  if (!s.sync()) return;
   unsigned long long arcs = 0;
-  int32_t graph_color = 1;
-  // superstep t: 2r = phase A of round r, 2r+1 = phase B; the init pushed
-  // into lcount[2], read like a phase-B count at the top of round 0
-  uint32_t t = 0;
-  uint32_t n_prev_slot = 2;
-  for (uint32_t r = 0;; ++r, ++graph_color) {
-    const uint32_t* list = pick(ws.list, r);
-    uint32_t* next = pick(ws.list, r + 1);
-    const uint32_t n = ld_cg(&ws.lcount[n_prev_slot]);
-    // ---- color: max over uncoloured neighbours (superstep t = 2r)
-    {
-      const int cur = t % 3, old = (t + 1) % 3;
-      if (leader) ws.lcount[old] = ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
-      bool saw = false;
-      const uint32_t ngroups = (n + 31) / 32;
-      for (;;) {
-        const uint32_t g0 = warp_grab(&ws.cursor[cur]) * kGrab;
-        if (g0 >= ngroups) break;
-        for (uint32_t g = g0; g < min(g0 + kGrab, ngroups); ++g) {
-          const uint32_t i = g * 32 + lane;
-          const uint32_t v = i < n ? ld_cg(&list[i]) : 0u;
+  // -- superstep 0: color = -1; count the neighbours each vertex waits for
+  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+    ws.color[v] = -1;
+    if (is_heavy(G, v)) ws.cnt[v] = 0;
+  }
+  if (!s.sync()) return;
+  {
+    float pv_lane = 0.f;
+    sweep_light(
+        G, &ws.cursor[0],
+        [&](uint32_t v, bool in_range) {
+          my[lane] = 0;
+          pv_lane = in_range ? __ldg(&ws.prio[v]) : 0.f;
           // a degree-1 vertex never looks at its neighbour
-          const bool act = i < n && __ldg(&G.row[v + 1]) - __ldg(&G.row[v]) != 1;
-          my[lane] = none;
-          __syncwarp();
-          group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) {
-            if (valid) {
-              ++arcs;
-              const uint32_t u = __ldg(&G.col[arc]);
-              if (ld_cg(&ws.color[u]) == -1) {
-                saw = true;
-                const uint32_t k = fkey(__ldg(&ws.prio[u]));
-                if (k > my[owner]) atomicMax(&my[owner], k);
-              }
-            }
-          });
-          __syncwarp();
-          if (i < n) ws.mx[v] = my[lane];
-        }
-      }
-      uint32_t* hmx = pick(ws.hmx, r);
-      sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
-        if (ld_cg(&ws.color[v]) != -1) return;
-        uint32_t m = none;
-        bool any = false;
-        for (uint32_t a0 = b; a0 < e; a0 += 32) {
-          const uint32_t a = a0 + lane;
-          if (a < e) {
+          return in_range && __ldg(&G.row[v + 1]) - __ldg(&G.row[v]) != 1;
+        },
+        [&](bool valid, int owner, uint32_t arc) {
+          const float pv = __shfl_sync(kFull, pv_lane, owner);
+          if (valid) {
             ++arcs;
-            const uint32_t u = __ldg(&G.col[a]);
-            if (ld_cg(&ws.color[u]) == -1) {
-              any = true;
-              m = max(m, fkey(__ldg(&ws.prio[u])));
-            }
+            if (__ldg(&ws.prio[__ldg(&G.col[arc])]) >= pv) atomicAdd(&my[owner], 1u);
           }
+        },
+        [&](uint32_t v, bool) {
+          if (v < G.V && !is_heavy(G, v)) ws.cnt[v] = my[lane];
+        });
+    sweep_heavy(G, &ws.hcursor[0], [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
+      const float pv = __ldg(&ws.prio[v]);
+      uint32_t n = 0;
+      for (uint32_t a0 = b; a0 < e; a0 += 32) {
+        const uint32_t a = a0 + lane;
+        if (a < e) {
+          ++arcs;
+          n += __ldg(&ws.prio[__ldg(&G.col[a])]) >= pv;
         }
-        m = warp_max_u32(m);
-        saw |= any;
-        if (lane == 0 && m > none) atomicMax(&hmx[h], m);
+      }
+      n = warp_add_u32(n);
+      if (lane == 0 && n) atomicAdd(&ws.cnt[v], n);
+    });
+  }
+  if (!s.sync()) return;
+  // -- superstep 1: vertices that wait for nobody take colour 1
+  {
+    Frontier out{pick(ws.q, 1), pick(ws.hv, 1), pick(ws.hb, 1), &ws.qcount[1], &ws.hcount[1],
+                 ws.qcap, ws.hcap, ws.overflow};
+    for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
+      const uint32_t v = g * 32 + lane;
+      const bool first = v < G.V && ld_cg(&ws.cnt[v]) == 0;
+      if (first) ws.color[v] = 1;
+      frontier_push(G, out, first, v);
+    }
+    if (leader) ws.cursor[2] = ws.hcursor[2] = 0;
+  }
+  if (!s.sync()) return;
+  // -- rounds: the vertices coloured in round r (queue slot r % 3) count
+  // down the neighbours waiting for them
+  uint32_t r = 1;
+  unsigned long long coloured = 0;
+  for (;; ++r) {
+    const int cur = r % 3, nxt = (r + 1) % 3, old = (r + 2) % 3;
+    const uint32_t n = ld_cg(&ws.qcount[cur]);
+    const unsigned long long hp = __ldcg(&ws.hcount[cur]);
+    if (n == 0 && hp == 0) break;
+    if (leader) {
+      ws.qcount[old] = 0;
+      ws.hcount[old] = 0;
+      ws.cursor[old] = 0;
+      ws.hcursor[old] = 0;
+    }
+    coloured += (leader ? n + (uint32_t)(hp >> 32) : 0);
+    Frontier out{pick(ws.q, r + 1), pick(ws.hv, r + 1), pick(ws.hb, r + 1), &ws.qcount[nxt],
+                 &ws.hcount[nxt], ws.qcap, ws.hcap, ws.overflow};
+    const int32_t next_color = (int32_t)r + 1;
+    float pv_lane = 0.f;
+    auto relax = [&](bool valid, float pv, uint32_t arc) {
+      uint32_t u = 0;
+      bool ready = false;
+      if (valid) {
+        ++arcs;
+        u = __ldg(&G.col[arc]);
+        if (waits_for(G, ws.prio, u, pv) && atomicSub(&ws.cnt[u], 1u) == 1u) {
+          ws.color[u] = next_color;
+          ready = true;
+        }
+      }
+      frontier_push(G, out, ready, u);
+    };
+    const uint32_t* q = pick(ws.q, r);
+    for (;;) {
+      const uint32_t g = warp_grab(&ws.cursor[cur]);
+      if ((uint64_t)g * 32 >= n) break;
+      const uint32_t i = g * 32 + lane;
+      const bool act = i < n;
+      const uint32_t v = act ? ld_cg(&q[i]) : 0u;
+      pv_lane = act ? __ldg(&ws.prio[v]) : 0.f;
+      group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) {
+        relax(valid, __shfl_sync(kFull, pv_lane, owner), arc);
       });
-      if (__any_sync(kFull, saw) && lane == 0) atomicOr(&ws.flag[cur], 1u);
-      if (!s.sync()) return;
-      ++t;
     }
-    // ---- color2: uncoloured vertices above the maximum take the colour;
-    // the others go to the next round's list (superstep t = 2r+1)
-    {
-      const int cur = t % 3, old = (t + 1) % 3;
-      const bool stop = ld_cg(&ws.flag[(t - 1) % 3]) == 0;
-      if (leader) ws.lcount[old] = ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
-      for (uint32_t g = W.gwarp; g * 32 < n; g += W.nwarps) {
-        const uint32_t i = g * 32 + lane;
-        bool keep = false;
-        uint32_t v = 0;
-        if (i < n) {
-          v = ld_cg(&list[i]);
-          if (fkey(__ldg(&ws.prio[v])) > ws.mx[v]) ws.color[v] = graph_color;
-          else keep = true;
-        }
-        warp_append(next, &ws.lcount[cur], G.V, ws.overflow, keep, v);
-      }
-      const uint32_t* hmx = pick(ws.hmx, r);
-      for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) {
-        const uint32_t v = __ldg(&G.heavy_v[h]);
-        if (ws.color[v] == -1 && fkey(__ldg(&ws.prio[v])) > hmx[h]) ws.color[v] = graph_color;
-        pick(ws.hmx, r + 1)[h] = none;
-      }
-      if (stop) {
-        if (leader) ws.stats[1] = r + 1;
-        break;
-      }
-      if (!s.sync()) return;
-      n_prev_slot = cur;
-      ++t;
+    const uint32_t ne = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
+    const uint32_t* hv = pick(ws.hv, r);
+    const uint32_t* hb = pick(ws.hb, r);
+    for (;;) {
+      const uint32_t c = warp_grab(&ws.hcursor[cur]);
+      if (c >= nch) break;
+      uint32_t e = 0;
+      if (lane == 0) e = upper_index(hb, ne, c);
+      e = __shfl_sync(kFull, e, 0);
+      const uint32_t v = ld_cg(&hv[e]);
+      const uint32_t j = c - ld_cg(&hb[e]);
+      const float pv = __ldg(&ws.prio[v]);
+      const uint32_t rb = __ldg(&G.row[v]), re = __ldg(&G.row[v + 1]);
+      const uint32_t b = rb + j * kChunk, en = min(re, b + kChunk);
+      range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, pv, arc); });
     }
+    if (!s.sync()) return;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
   if (lane == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  if (leader) {
+    ws.stats[1] = r - 1;
+    ws.stats[2] = coloured;
+  }
 }
 
 __global__ void __launch_bounds__(1024, 1) k_color_xf(DiscoveryArgs a, GraphView G, ColorWs ws) {
@@ -387,34 +420,45 @@ static int mis_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_s) 
 
 static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_color) {
   if (!graph_ok(c, g) || !d_prio || !d_color) return GDB_ERR_INVALID;
+  const uint32_t V = g->V;
   const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
   Bump b;
-  const size_t o_mx = b.take((size_t)g->V * 4);
-  const size_t o_l0 = b.take((size_t)g->V * 4), o_l1 = b.take((size_t)g->V * 4);
-  const size_t o_h0 = b.take(hcap * 4), o_h1 = b.take(hcap * 4), o_cnt = b.take(256);
+  const size_t o_cnt_v = b.take((size_t)V * 4);
+  const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
+  const size_t o_hv0 = b.take(hcap * 4), o_hv1 = b.take(hcap * 4);
+  const size_t o_hb0 = b.take(hcap * 4), o_hb1 = b.take(hcap * 4);
+  const size_t o_cnt = b.take(512);
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
   ColorWs ws;
   ws.color = d_color;
-  ws.mx = (uint32_t*)(base + o_mx);
-  ws.list[0] = (uint32_t*)(base + o_l0);
-  ws.list[1] = (uint32_t*)(base + o_l1);
-  ws.hmx[0] = (uint32_t*)(base + o_h0);
-  ws.hmx[1] = (uint32_t*)(base + o_h1);
+  ws.cnt = (uint32_t*)(base + o_cnt_v);
   ws.prio = d_prio;
+  ws.q[0] = (uint32_t*)(base + o_q0);
+  ws.q[1] = (uint32_t*)(base + o_q1);
+  ws.hv[0] = (uint32_t*)(base + o_hv0);
+  ws.hv[1] = (uint32_t*)(base + o_hv1);
+  ws.hb[0] = (uint32_t*)(base + o_hb0);
+  ws.hb[1] = (uint32_t*)(base + o_hb1);
   char* cnt = base + o_cnt;
-  ws.stats = (unsigned long long*)cnt;
-  ws.cursor = (uint32_t*)(cnt + 64);
-  ws.hcursor = (uint32_t*)(cnt + 80);
-  ws.flag = (uint32_t*)(cnt + 96);
-  ws.lcount = (uint32_t*)(cnt + 112);
-  ws.overflow = (int*)(cnt + 128);
-  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 256, c->stream));
+  ws.stats = (unsigned long long*)cnt;             // 4 x u64
+  ws.hcount = (unsigned long long*)(cnt + 64);     // 3 x u64
+  ws.qcount = (uint32_t*)(cnt + 96);
+  ws.cursor = (uint32_t*)(cnt + 112);
+  ws.hcursor = (uint32_t*)(cnt + 128);
+  ws.overflow = (int*)(cnt + 160);
+  ws.qcap = V;
+  ws.hcap = hcap;
+  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
   int rc = launch_xf(c, k_color_xf, g->view(), ws, ws.stats);
   if (rc) return rc;
-  int* h = (int*)pinned(c, 4096);
-  GDB_CUDA(c, cudaMemcpy(h, ws.overflow, 4, cudaMemcpyDeviceToHost));
-  if (h[0]) return set_error(c, GDB_ERR_CAPACITY, "colour list overflow");
+  unsigned long long* h = (unsigned long long*)pinned(c, 4096);
+  GDB_CUDA(c, cudaMemcpy(h, cnt, 192, cudaMemcpyDeviceToHost));
+  if (*(int*)((char*)h + 160)) return set_error(c, GDB_ERR_CAPACITY, "colour queue overflow");
+  if (h[2] != V)
+    return set_error(c, GDB_ERR_INVALID,
+                     "adjacent vertices of equal priority never take a colour (the reference "
+                     "kernel does not terminate on such input)");
   return GDB_OK;
 }
 

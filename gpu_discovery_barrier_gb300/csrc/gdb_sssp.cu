@@ -67,9 +67,9 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const SsspWs& ws, 
   const int lane = lane_id();
   const uint32_t ngroups = (n + 31) / 32;
   for (;;) {
-    const uint32_t g0 = warp_grab(&ws.cursor[cur]) * kGrab;
+    const uint32_t g0 = warp_grab(&ws.cursor[cur]);
     if (g0 >= ngroups) break;
-    for (uint32_t g = g0; g < min(g0 + kGrab, ngroups); ++g) {
+    for (uint32_t g = g0; g < min(g0 + 1, ngroups); ++g) {
       const uint32_t i = g * 32 + lane;
       const bool act = i < n;
       const uint32_t u = act ? ld_cg(&pick(ws.q, L)[i]) : 0u;

@@ -230,16 +230,13 @@ __device__ __forceinline__ void visit_frontier(const GraphView& G, const uint32_
                                                unsigned long long hpacked, uint32_t* cursor,
                                                uint32_t* hcursor, Light&& light, Heavy&& heavy) {
   const int lane = lane_id();
-  const uint32_t ngroups = (n + 31) / 32;
   for (;;) {
-    const uint32_t g0 = warp_grab(cursor) * kGrab;
-    if (g0 >= ngroups) break;
-    for (uint32_t g = g0; g < min(g0 + kGrab, ngroups); ++g) {
-      const uint32_t i = g * 32 + lane;
-      const bool act = i < n;
-      const uint32_t v = act ? ld_cg(&q[i]) : 0u;
-      group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) { light(valid, owner, v, arc); });
-    }
+    const uint32_t g = warp_grab(cursor);
+    if ((uint64_t)g * 32 >= n) break;
+    const uint32_t i = g * 32 + lane;
+    const bool act = i < n;
+    const uint32_t v = act ? ld_cg(&q[i]) : 0u;
+    group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) { light(valid, owner, v, arc); });
   }
   const uint32_t ne = (uint32_t)(hpacked >> 32);
   const uint32_t nch = (uint32_t)hpacked;
@@ -288,17 +285,19 @@ template <class Fn>
 __device__ __forceinline__ void sweep_heavy(const GraphView& G, uint32_t* hcursor, Fn&& fn) {
   const int lane = lane_id();
   for (;;) {
-    const uint32_t c = warp_grab(hcursor);
-    if (c >= G.nheavy_chunks) break;
-    uint32_t e = 0;
-    if (lane == 0) e = upper_index(G.heavy_base, G.nheavy, c);
-    e = __shfl_sync(kFull, e, 0);
-    const uint32_t v = __ldg(&G.heavy_v[e]);
-    const uint32_t j = c - __ldg(&G.heavy_base[e]);
-    const uint32_t rb = __ldg(&G.row[v]), re = __ldg(&G.row[v + 1]);
-    const uint32_t b = rb + j * kChunk;
-    const uint32_t en = min(re, b + kChunk);
-    fn(v, e, j, b, en);
+    const uint32_t c0 = warp_grab(hcursor) * kGrab;
+    if (c0 >= G.nheavy_chunks) break;
+    for (uint32_t c = c0; c < min(c0 + kGrab, G.nheavy_chunks); ++c) {
+      uint32_t e = 0;
+      if (lane == 0) e = upper_index(G.heavy_base, G.nheavy, c);
+      e = __shfl_sync(kFull, e, 0);
+      const uint32_t v = __ldg(&G.heavy_v[e]);
+      const uint32_t j = c - __ldg(&G.heavy_base[e]);
+      const uint32_t rb = __ldg(&G.row[v]), re = __ldg(&G.row[v + 1]);
+      const uint32_t b = rb + j * kChunk;
+      const uint32_t en = min(re, b + kChunk);
+      fn(v, e, j, b, en);
+    }
   }
 }
 
