@@ -59,29 +59,25 @@ struct BcWs {
 // Visit one level segment: light groups over order[lb, lb+nl) (begin/edge/
 // end hooks) and heavy chunks over entries [hbase, hbase+ne).
 template <class Begin, class Edge, class End, class Heavy>
-__device__ __forceinline__ void visit_level(const GraphView& G, const BcWs& ws, uint32_t lb,
+__device__ __forceinline__ void visit_level(const GraphView& G, const Warps& W, const BcWs& ws,
+                                            uint32_t lb,
                                             uint32_t nl, uint32_t hbase, uint32_t ne, uint32_t nch,
                                             uint32_t* cursor, uint32_t* hcursor, Begin&& begin,
                                             Edge&& edge, End&& end, Heavy&& heavy) {
   const int lane = lane_id();
-  const uint32_t ngroups = (nl + 31) / 32;
-  for (;;) {
-    const uint32_t g0 = warp_grab(cursor);
-    if (g0 >= ngroups) break;
-    for (uint32_t g = g0; g < min(g0 + 1, ngroups); ++g) {
-      const uint32_t i = g * 32 + lane;
-      const bool act = i < nl;
-      const uint32_t v = act ? ld_cg(&ws.order[lb + i]) : 0u;
-      begin(v, act);
-      __syncwarp();
-      group_arcs(G, act, v, edge);
-      __syncwarp();
-      end(v, act);
-    }
+  WorkTaker lt((nl + 31) / 32, W, cursor);
+  for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
+    const uint32_t i = g * 32 + lane;
+    const bool act = i < nl;
+    const uint32_t v = act ? ld_cg(&ws.order[lb + i]) : 0u;
+    begin(v, act);
+    __syncwarp();
+    group_arcs(G, act, v, edge);
+    __syncwarp();
+    end(v, act);
   }
-  for (;;) {
-    const uint32_t c = warp_grab(hcursor);
-    if (c >= nch) break;
+  WorkTaker ht(nch, W, hcursor);
+  for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
     uint32_t e = 0;
     if (lane == 0) e = upper_index(ws.hb + hbase, ne, c);
     e = __shfl_sync(kFull, e, 0);
@@ -213,7 +209,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
         frontier_push(G, out, want, u);
       };
       visit_level(
-          G, ws, lbase, nl, hbase, ne, nch, &ws.cursor[cur], &ws.hcursor[cur],
+          G, W, ws, lbase, nl, hbase, ne, nch, &ws.cursor[cur], &ws.hcursor[cur],
           [&](uint32_t v, bool act) {
             my[lane] = 0.0;
             if (act) reached_arcs += __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
@@ -262,7 +258,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       };
       float rv_lane = 0.f;
       visit_level(
-          G, ws, lb, le - lb, hb0, he - hb0, nch, &ws.cursor[cur], &ws.hcursor[cur],
+          G, W, ws, lb, le - lb, hb0, he - hb0, nch, &ws.cursor[cur], &ws.hcursor[cur],
           [&](uint32_t v, bool act) {
             my[lane] = 0.0;
             rv_lane = act ? ld_cg(&ws.rho[v]) : 0.f;

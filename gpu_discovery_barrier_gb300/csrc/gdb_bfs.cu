@@ -44,8 +44,9 @@ __device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long
 }
 
 // Top-down expansion of level L into L+1.
-__device__ __forceinline__ void bfs_top_down(const GraphView& G, const BfsWs& ws, uint32_t L,
-                                             unsigned long long& arcs, unsigned long long& farcs) {
+__device__ __forceinline__ void bfs_top_down(const GraphView& G, const Warps& W, const BfsWs& ws,
+                                             uint32_t L, unsigned long long& arcs,
+                                             unsigned long long& farcs) {
   const int cur = L % 3, nxt = (L + 1) % 3;
   const uint32_t n = ld_cg(&ws.qcount[cur]);
   const unsigned long long hp = ld_cg_u64(&ws.hcount[cur]);
@@ -65,7 +66,7 @@ __device__ __forceinline__ void bfs_top_down(const GraphView& G, const BfsWs& ws
     frontier_push(G, out, want, u);
   };
   visit_frontier(
-      G, pick(ws.q, L), n, pick(ws.hv, L), pick(ws.hb, L), hp, &ws.cursor[cur], &ws.hcursor[cur],
+      G, W, pick(ws.q, L), n, pick(ws.hv, L), pick(ws.hb, L), hp, &ws.cursor[cur], &ws.hcursor[cur],
       [&](bool valid, int, uint32_t, uint32_t arc) { edge(valid, arc); },
       [&](bool valid, uint32_t, uint32_t arc) { edge(valid, arc); });
 }
@@ -163,7 +164,7 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
     }
     unsigned long long farcs = 0;
     if (bottom_up) bfs_bottom_up(G, ws, L, W, arcs, farcs);
-    else bfs_top_down(G, ws, L, arcs, farcs);
+    else bfs_top_down(G, W, ws, L, arcs, farcs);
     if (ws.adaptive) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) farcs += __shfl_xor_sync(kFull, farcs, o);
@@ -225,7 +226,12 @@ __global__ void __launch_bounds__(1024, 1) k_bfs_level(GraphView G, BfsWs ws, ui
     ws.stats[1] = L + 1;
   }
   unsigned long long arcs = 0, farcs = 0;
-  bfs_top_down(G, ws, L, arcs, farcs);
+  Warps W;
+  W.gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  W.nwarps = (gridDim.x * blockDim.x) >> 5;
+  W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
+  W.nthreads = gridDim.x * blockDim.x;
+  bfs_top_down(G, W, ws, L, arcs, farcs);
   unsigned long long r = arcs;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(kFull, r, o);

@@ -312,9 +312,8 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
       frontier_push(G, out, ready, u);
     };
     const uint32_t* q = pick(ws.q, r);
-    for (;;) {
-      const uint32_t g = warp_grab(&ws.cursor[cur]);
-      if ((uint64_t)g * 32 >= n) break;
+    WorkTaker lt((n + 31) / 32, W, &ws.cursor[cur]);
+    for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
       const uint32_t i = g * 32 + lane;
       const bool act = i < n;
       const uint32_t v = act ? ld_cg(&q[i]) : 0u;
@@ -326,9 +325,8 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
     const uint32_t ne = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
     const uint32_t* hv = pick(ws.hv, r);
     const uint32_t* hb = pick(ws.hb, r);
-    for (;;) {
-      const uint32_t c = warp_grab(&ws.hcursor[cur]);
-      if (c >= nch) break;
+    WorkTaker ht(nch, W, &ws.hcursor[cur]);
+    for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
       uint32_t e = 0;
       if (lane == 0) e = upper_index(hb, ne, c);
       e = __shfl_sync(kFull, e, 0);

@@ -38,8 +38,8 @@ struct SsspWs {
   uint32_t qcap, hcap;
 };
 
-__device__ __forceinline__ void sssp_step(const GraphView& G, const SsspWs& ws, uint32_t L,
-                                          unsigned long long& arcs) {
+__device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, const SsspWs& ws,
+                                          uint32_t L, unsigned long long& arcs) {
   const int cur = L % 3, nxt = (L + 1) % 3;
   const uint32_t n = ld_cg(&ws.qcount[cur]);
   const unsigned long long hp = __ldcg(&ws.hcount[cur]);
@@ -65,26 +65,21 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const SsspWs& ws, 
   };
   // light groups: each lane reads its own vertex's distance once
   const int lane = lane_id();
-  const uint32_t ngroups = (n + 31) / 32;
-  for (;;) {
-    const uint32_t g0 = warp_grab(&ws.cursor[cur]);
-    if (g0 >= ngroups) break;
-    for (uint32_t g = g0; g < min(g0 + 1, ngroups); ++g) {
-      const uint32_t i = g * 32 + lane;
-      const bool act = i < n;
-      const uint32_t u = act ? ld_cg(&pick(ws.q, L)[i]) : 0u;
-      const uint32_t du = act ? ld_cg(&ws.dist[u]) : 0u;
-      group_arcs(G, act, u, [&](bool valid, int owner, uint32_t arc) {
-        relax(valid, __shfl_sync(kFull, du, owner), arc);
-      });
-    }
+  WorkTaker lt((n + 31) / 32, W, &ws.cursor[cur]);
+  for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
+    const uint32_t i = g * 32 + lane;
+    const bool act = i < n;
+    const uint32_t u = act ? ld_cg(&pick(ws.q, L)[i]) : 0u;
+    const uint32_t du = act ? ld_cg(&ws.dist[u]) : 0u;
+    group_arcs(G, act, u, [&](bool valid, int owner, uint32_t arc) {
+      relax(valid, __shfl_sync(kFull, du, owner), arc);
+    });
   }
   const uint32_t ne = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
   const uint32_t* hv = pick(ws.hv, L);
   const uint32_t* hb = pick(ws.hb, L);
-  for (;;) {
-    const uint32_t c = warp_grab(&ws.hcursor[cur]);
-    if (c >= nch) break;
+  WorkTaker ht(nch, W, &ws.hcursor[cur]);
+  for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
     uint32_t e = 0;
     if (lane == 0) e = upper_index(hb, ne, c);
     e = __shfl_sync(kFull, e, 0);
@@ -141,7 +136,7 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
       ws.cursor[old] = 0;
       ws.hcursor[old] = 0;
     }
-    sssp_step(G, ws, L, arcs);
+    sssp_step(G, W, ws, L, arcs);
     if (!s.sync()) return;
   }
 #pragma unroll

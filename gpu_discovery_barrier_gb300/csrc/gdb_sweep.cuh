@@ -100,6 +100,24 @@ __device__ __forceinline__ uint32_t warp_grab(uint32_t* cursor) {
   return __shfl_sync(kFull, t, 0);
 }
 
+// Work items [0, n) over the warps of the grid: warp w first takes item w
+// without any atomic, then -- only when there are more items than warps --
+// keeps taking tickets nwarps + cursor++.  Small frontiers (thousands of
+// rounds of colouring, the tail levels of traversals) cost no atomics.
+struct WorkTaker {
+  uint32_t n, nwarps, next;
+  uint32_t* cursor;
+  __device__ __forceinline__ WorkTaker(uint32_t n_, const Warps& W, uint32_t* c)
+      : n(n_), nwarps(W.nwarps), next(W.gwarp), cursor(c) {}
+  // next item or n when done
+  __device__ __forceinline__ uint32_t take() {
+    const uint32_t g = next;
+    if (g >= n) return n;
+    next = n <= nwarps ? n : nwarps + warp_grab(cursor);
+    return g;
+  }
+};
+
 // Walk the arcs of the (active, light) vertices held by the 32 lanes.
 // Calls fn(valid, owner_lane, arc) once per 32-arc step with every lane
 // present, so fn may use warp collectives; `valid` marks lanes with an arc.
@@ -225,14 +243,13 @@ __device__ __forceinline__ void warp_append(uint32_t* list, uint32_t* count, uin
 // light(valid, owner_lane, owner_vertex_in_lane, arc) is called through
 // group_arcs; heavy(valid, v, arc) per 32-arc step of a chunk.
 template <class Light, class Heavy>
-__device__ __forceinline__ void visit_frontier(const GraphView& G, const uint32_t* q, uint32_t n,
-                                               const uint32_t* hv, const uint32_t* hb,
+__device__ __forceinline__ void visit_frontier(const GraphView& G, const Warps& W, const uint32_t* q,
+                                               uint32_t n, const uint32_t* hv, const uint32_t* hb,
                                                unsigned long long hpacked, uint32_t* cursor,
                                                uint32_t* hcursor, Light&& light, Heavy&& heavy) {
   const int lane = lane_id();
-  for (;;) {
-    const uint32_t g = warp_grab(cursor);
-    if ((uint64_t)g * 32 >= n) break;
+  WorkTaker lt((n + 31) / 32, W, cursor);
+  for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
     const uint32_t i = g * 32 + lane;
     const bool act = i < n;
     const uint32_t v = act ? ld_cg(&q[i]) : 0u;
@@ -240,9 +257,8 @@ __device__ __forceinline__ void visit_frontier(const GraphView& G, const uint32_
   }
   const uint32_t ne = (uint32_t)(hpacked >> 32);
   const uint32_t nch = (uint32_t)hpacked;
-  for (;;) {
-    const uint32_t c = warp_grab(hcursor);
-    if (c >= nch) break;
+  WorkTaker ht(nch, W, hcursor);
+  for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
     uint32_t e = 0;
     if (lane == 0) e = upper_index(hb, ne, c);
     e = __shfl_sync(kFull, e, 0);
