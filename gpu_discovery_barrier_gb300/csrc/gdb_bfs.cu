@@ -377,3 +377,168 @@ int gdb_bfs(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* dist) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// BFS without any device allocation.
+//
+// Some callers cannot allocate device memory when they run a traversal: a
+// host that has handed all of the GPU's memory to its own pool allocator, a
+// plug-in that must not call cudaMalloc/cudaFree because those calls
+// synchronise the device behind the host's back, or code on a latency path
+// that was budgeted to allocate nothing.  gdb_bfs_noalloc serves them: it
+// runs the same persistent BFS kernel as gdb_bfs_device, but its queues,
+// counters and discovery/barrier state live in one file-scope device array
+// of fixed size, so the call allocates nothing (no context, no graph
+// handle, no workspace).  Limits: V <= GDB_NOALLOC_MAX_VERTICES, at most
+// kNoAllocMaxCtas participating CTAs; every vertex is walked as a light
+// vertex (no heavy-vertex table), which is exact but slower on hubs.
+namespace {
+
+constexpr uint32_t kNoAllocMaxV = GDB_NOALLOC_MAX_VERTICES;
+constexpr int kNoAllocMaxCtas = 1024;
+constexpr int kNoAllocBlock = 512;
+
+// Byte offsets inside the scratch array.
+constexpr size_t kNaCtx = 0;                                        // gdb::DeviceCtx
+constexpr size_t kNaFlags = 4096;                                   // barrier flag lines
+constexpr size_t kNaQ0 = kNaFlags + (size_t)kNoAllocMaxCtas * 128;  // frontier queues
+constexpr size_t kNaQ1 = kNaQ0 + (size_t)kNoAllocMaxV * 4;
+constexpr size_t kNaBits = kNaQ1 + (size_t)kNoAllocMaxV * 4;        // heavy bitmap (all zero)
+constexpr size_t kNaBitsBytes = ((size_t)kNoAllocMaxV / 32 + 64) * 4;
+constexpr size_t kNaSmall = kNaBits + kNaBitsBytes;                 // empty heavy tables
+constexpr size_t kNaCounters = kNaSmall + 256;                      // BFS counters (512 B)
+constexpr size_t kNaTotal = kNaCounters + 512;
+static_assert(sizeof(gdb::DeviceCtx) <= kNaFlags, "discovery context does not fit");
+
+// The scratch every GPU that loads this library keeps until the process
+// exits (about 8.6 MB).  Host code must not use its name as an address:
+// the address comes from cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) unsigned char g_bfs_noalloc_scratch[kNaTotal];
+
+struct NoAllocDevice {
+  bool ready;
+  unsigned char* base;  // device address of g_bfs_noalloc_scratch
+  int sm_count;
+  int occupancy;
+  unsigned long long launches;
+};
+constexpr int kNoAllocMaxDevices = 64;
+static NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+
+// Set-up of the current device: the scratch's address, the launch shape and
+// a re-armed discovery context with cleared barrier flags.
+static int noalloc_arm(int dev, cudaStream_t stream) {
+  NoAllocDevice& d = g_noalloc_dev[dev];
+  if (!d.ready) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_bfs_noalloc_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return GDB_ERR_CUDA;
+    }
+    int sms = 0, occ = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs_xf, kNoAllocBlock, 0) != cudaSuccess ||
+        occ <= 0) {
+      cudaGetLastError();
+      return GDB_ERR_CUDA;
+    }
+    d.base = (unsigned char*)p;
+    d.sm_count = sms;
+    d.occupancy = occ;
+  }
+  gdb::DeviceCtx h;
+  std::memset(&h, 0, sizeof(h));
+  h.poll_open = 1;
+  h.stall_after = -1;
+  if (cudaMemcpyAsync(d.base + kNaCtx, &h, sizeof(h), cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+      cudaMemsetAsync(d.base + kNaFlags, 0, (size_t)kNoAllocMaxCtas * 128, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess) {
+    cudaGetLastError();
+    return GDB_ERR_CUDA;
+  }
+  d.ready = true;
+  return GDB_OK;
+}
+
+}  // namespace
+
+extern "C" int gdb_bfs_noalloc(const uint32_t* d_row_ptr, const uint32_t* d_col, uint32_t V,
+                               uint64_t E, uint32_t src, uint32_t* d_dist, void* cuda_stream) {
+  if (!d_row_ptr || (E && !d_col) || !d_dist || V == 0 || V > kNoAllocMaxV || src >= V ||
+      E >= 0xffffffffull)
+    return GDB_ERR_INVALID;
+  cudaStream_t stream = (cudaStream_t)cuda_stream;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    cudaGetLastError();
+    return GDB_ERR_CUDA;
+  }
+  NoAllocDevice& d = g_noalloc_dev[dev];
+  if (!d.ready) {
+    const int rc = noalloc_arm(dev, stream);
+    if (rc) return rc;
+  }
+  unsigned char* base = d.base;
+  // what must start at zero: the counters, the heavy bitmap and tables
+  if (cudaMemsetAsync(base + kNaCounters, 0, 512, stream) != cudaSuccess ||
+      cudaMemsetAsync(base + kNaSmall, 0, 256, stream) != cudaSuccess ||
+      cudaMemsetAsync(base + kNaBits, 0, ((size_t)V / 32 + 2) * 4, stream) != cudaSuccess) {
+    cudaGetLastError();
+    return GDB_ERR_CUDA;
+  }
+  GraphView G;
+  G.V = V;
+  G.E = (uint32_t)E;
+  G.row = d_row_ptr;
+  G.col = d_col;
+  G.w = nullptr;
+  G.nheavy = 0;
+  G.nheavy_chunks = 0;
+  G.heavy_v = (const uint32_t*)(base + kNaSmall);
+  G.heavy_base = (const uint32_t*)(base + kNaSmall + 64);
+  G.heavy_bits = (const uint32_t*)(base + kNaBits);
+  BfsWs ws;
+  ws.dist = d_dist;
+  ws.q[0] = (uint32_t*)(base + kNaQ0);
+  ws.q[1] = (uint32_t*)(base + kNaQ1);
+  ws.hv[0] = ws.hv[1] = (uint32_t*)(base + kNaSmall + 128);
+  ws.hb[0] = ws.hb[1] = (uint32_t*)(base + kNaSmall + 192);
+  unsigned char* cnt = base + kNaCounters;
+  ws.stats = (unsigned long long*)cnt;
+  ws.hcount = (unsigned long long*)(cnt + 64);
+  ws.qcount = (uint32_t*)(cnt + 96);
+  ws.cursor = (uint32_t*)(cnt + 112);
+  ws.hcursor = (uint32_t*)(cnt + 128);
+  ws.mode = (uint32_t*)(cnt + 144);
+  ws.overflow = (int*)(cnt + 160);
+  ws.qcap = V;
+  ws.hcap = 1;
+  ws.adaptive = 0;
+  DiscoveryArgs a;
+  a.ctx = (gdb::DeviceCtx*)(base + kNaCtx);
+  a.flags = (int*)(base + kNaFlags);
+  a.flag_capacity = kNoAllocMaxCtas;
+  a.lock_kind = GDB_LOCK_FREE;
+  const int grid = std::min(std::min(d.occupancy * d.sm_count, kNoAllocMaxCtas), 32 * kNoAllocBlock + 1);
+  a.expected = grid;
+  a.timeout_ns = 2000000000ull;
+  a.close_wait_ns = 50000ull;
+  a.launch_id = ++d.launches;
+  a.xf_release = gdb::kXfPerSlave;
+  k_bfs_xf<<<grid, kNoAllocBlock, 0, stream>>>(a, G, ws, src);
+  if (cudaGetLastError() != cudaSuccess) return GDB_ERR_CUDA;
+  int h[4] = {0, 0, 0, 0};
+  int overflow = 0;
+  if (cudaMemcpyAsync(h, &a.ctx->status, sizeof(h), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaMemcpyAsync(&overflow, ws.overflow, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess) {
+    cudaGetLastError();
+    return GDB_ERR_CUDA;
+  }
+  if (h[0] != 0) {
+    // re-arm the discovery context and flags after an error
+    noalloc_arm(dev, stream);
+    return h[0];
+  }
+  return overflow ? GDB_ERR_CAPACITY : GDB_OK;
+}

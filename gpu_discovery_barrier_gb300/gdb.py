@@ -117,7 +117,19 @@ SIGNATURES = [
     ("gdb_bc_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
     ("gdb_mst", C.c_int, [_P, _P, C.POINTER(MstResult), _P]),
     ("gdb_mst_device", C.c_int, [_P, _P, _P, _P]),
+    ("gdb_bfs_noalloc", C.c_int, [_P, _P, C.c_uint32, C.c_uint64, C.c_uint32, _P, _P]),
 ]
+
+NOALLOC_MAX_VERTICES = 1 << 20
+
+
+def bfs_noalloc(d_row_ptr: int, d_col: int, V: int, E: int, src: int, d_dist: int,
+                stream: int = 0) -> None:
+    """gdb_bfs_noalloc: BFS from device pointers without any device
+    allocation (see include/gdb.h); raises GdbError on failure."""
+    rc = lib().gdb_bfs_noalloc(d_row_ptr, d_col, V, E, src, d_dist, stream)
+    if rc != 0:
+        raise GdbError(rc, "gdb_bfs_noalloc")
 
 
 def lib() -> C.CDLL:

@@ -220,6 +220,24 @@ int gdb_bc_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_
 int gdb_mst(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* result, uint8_t* arc_in_mst);
 int gdb_mst_device(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* d_result, uint8_t* d_arc_in_mst);
 
+/* -------------------------------------------- allocation-free BFS variant */
+/* No counterpart in the reference: an extra entry point for callers that
+ * cannot allocate device memory (a host whose own pool owns the GPU's
+ * memory, a plug-in that must not trigger the device synchronisation of
+ * cudaMalloc/cudaFree).  Same levels as gdb_bfs_device, from plain device
+ * pointers, on the caller's stream (0 = default stream), without a
+ * context, graph handle or workspace: queues, counters and the discovery
+ * and barrier state live in one fixed device array inside the library
+ * (about 8.6 MB, kept by every GPU that loads the library until the process
+ * exits).  V above GDB_NOALLOC_MAX_VERTICES returns GDB_ERR_INVALID.
+ * The first call on a device looks up that array's address and arms it, so
+ * make that first call before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (other streams, other threads) race
+ * and must be serialised by the caller.  Synchronous. */
+#define GDB_NOALLOC_MAX_VERTICES (1u << 20)
+int gdb_bfs_noalloc(const uint32_t* d_row_ptr, const uint32_t* d_col, uint32_t V, uint64_t E,
+                    uint32_t src, uint32_t* d_dist, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
