@@ -38,13 +38,14 @@ struct BcWs {
   float* sigma;
   float* bc;
   uint32_t* order;               // light vertices, level segments
-  uint32_t* hv;                  // heavy entries: vertex
-  uint32_t* hb;                  // first chunk, relative to its level
-  double* hacc;                  // FP64 partial sums of heavy entries
-  uint32_t* hleft;               // chunks still to finish per heavy entry
+  uint4* hc;                     // heavy chunk entries, level segments
+  double* hacc;                  // FP64 partial sums per heavy vertex slot
+  uint32_t* hleft;               // chunks still to finish per heavy vertex slot
+  uint32_t hc_cap;               // chunk entries available
   uint32_t* lev_l;               // light segment start per level
-  uint32_t* lev_h;               // heavy entry start per level
+  uint32_t* lev_h;               // heavy chunk-entry start per level
   uint32_t* lev_hc;              // heavy chunks per level
+  uint32_t* lev_hv;              // heavy vertex-slot start per level
   uint32_t* lcnt;                // [3] light pushes of the next level
   unsigned long long* hcnt;      // [3] (entries << 32) | chunks
   uint32_t* cursor;              // [3]
@@ -57,13 +58,13 @@ struct BcWs {
 };
 
 // Visit one level segment: light groups over order[lb, lb+nl) (begin/edge/
-// end hooks) and heavy chunks over entries [hbase, hbase+ne).
+// end hooks) and the level's heavy chunk entries hc[hcb, hcb+nch), whose
+// vertex slots start at hvb: heavy(v, slot, chunks_of_v, arc_begin, arc_end).
 template <class Begin, class Edge, class End, class Heavy>
 __device__ __forceinline__ void visit_level(const GraphView& G, const Warps& W, const BcWs& ws,
-                                            uint32_t lb,
-                                            uint32_t nl, uint32_t hbase, uint32_t ne, uint32_t nch,
-                                            uint32_t* cursor, uint32_t* hcursor, Begin&& begin,
-                                            Edge&& edge, End&& end, Heavy&& heavy) {
+                                            uint32_t lb, uint32_t nl, uint32_t hcb, uint32_t hvb,
+                                            uint32_t nch, uint32_t* cursor, uint32_t* hcursor,
+                                            Begin&& begin, Edge&& edge, End&& end, Heavy&& heavy) {
   const int lane = lane_id();
   WorkTaker lt((nl + 31) / 32, W, cursor);
   for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
@@ -78,15 +79,10 @@ __device__ __forceinline__ void visit_level(const GraphView& G, const Warps& W, 
   }
   WorkTaker ht(nch, W, hcursor);
   for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
-    uint32_t e = 0;
-    if (lane == 0) e = upper_index(ws.hb + hbase, ne, c);
-    e = __shfl_sync(kFull, e, 0);
-    const uint32_t slot = hbase + e;
-    const uint32_t v = ld_cg(&ws.hv[slot]);
-    const uint32_t j = c - ld_cg(&ws.hb[slot]);
-    const uint32_t rb = __ldg(&G.row[v]), re = __ldg(&G.row[v + 1]);
-    const uint32_t b = rb + j * kChunk, en = min(re, b + kChunk);
-    heavy(v, slot, b, en);
+    const uint4 ent = ld_cg(&ws.hc[hcb + c]);
+    uint32_t b, en;
+    chunk_range(G, ent, b, en);
+    heavy(ent.x, hvb + ent.z, ent.w, b, en);
   }
 }
 
@@ -151,44 +147,36 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       ws.d[src] = 0;
       ws.rho[src] = 1.f;
       const int nx = (t + 1) % 3;
-      const uint32_t deg = G.row[src + 1] - G.row[src];
-      if (is_heavy(G, src)) {
-        const uint32_t nch = chunks_of(deg);
-        ws.hv[0] = src;
-        ws.hb[0] = 0;
-        ws.hacc[0] = 0.0;
-        ws.hleft[0] = nch;
-        ws.hcnt[nx] = (1ull << 32) | nch;
-      } else {
-        ws.order[0] = src;
-        ws.lcnt[nx] = 1;
-      }
+      frontier_seed(G, Frontier{ws.order, ws.hc, &ws.lcnt[nx], &ws.hcnt[nx], G.V, ws.hc_cap,
+                                ws.overflow, G.nheavy, ws.hleft, ws.hacc},
+                    src);
     }
     if (!s.sync()) return;
     ++t;
     // -- forward levels
-    uint32_t lbase = 0, hbase = 0, L = 0;
+    uint32_t lbase = 0, hcbase = 0, hvbase = 0, L = 0;
     for (;; ++L, ++t) {
       const int cur = t % 3, nx = (t + 1) % 3;
       const uint32_t nl = ld_cg(&ws.lcnt[cur]);
       const unsigned long long hp = __ldcg(&ws.hcnt[cur]);
-      const uint32_t ne = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
+      const uint32_t nhv = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
       if (leader && L < ws.max_levels) {
         ws.lev_l[L] = lbase;
-        ws.lev_h[L] = hbase;
+        ws.lev_h[L] = hcbase;
         ws.lev_hc[L] = nch;
+        ws.lev_hv[L] = hvbase;
       }
       // the slot two supersteps back is free even in the final superstep
       reset_slot(t);
-      if (nl == 0 && ne == 0) break;
+      if (nl == 0 && nhv == 0) break;
       if (L + 1 >= ws.max_levels) {
         if (leader) *ws.overflow = 1;
         break;
       }
-      const uint32_t nlbase = lbase + nl, nhbase = hbase + ne;
-      Frontier out{ws.order + nlbase, ws.hv + nhbase, ws.hb + nhbase, &ws.lcnt[nx], &ws.hcnt[nx],
-                   G.V - nlbase, G.nheavy - nhbase, ws.overflow, ws.hleft + nhbase,
-                   ws.hacc + nhbase};
+      const uint32_t nlbase = lbase + nl, nhcbase = hcbase + nch, nhvbase = hvbase + nhv;
+      Frontier out{ws.order + nlbase, ws.hc + nhcbase, &ws.lcnt[nx], &ws.hcnt[nx], G.V - nlbase,
+                   ws.hc_cap - nhcbase, ws.overflow, G.nheavy - nhvbase, ws.hleft + nhvbase,
+                   ws.hacc + nhvbase};
       const int32_t Li = (int32_t)L;
       // one arc of a level-L vertex: claim level L+1 or pull a parent's count
       auto fwd_arc = [&](bool valid, uint32_t arc, double& acc) {
@@ -209,7 +197,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
         frontier_push(G, out, want, u);
       };
       visit_level(
-          G, W, ws, lbase, nl, hbase, ne, nch, &ws.cursor[cur], &ws.hcursor[cur],
+          G, W, ws, lbase, nl, hcbase, hvbase, nch, &ws.cursor[cur], &ws.hcursor[cur],
           [&](uint32_t v, bool act) {
             my[lane] = 0.0;
             if (act) reached_arcs += __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
@@ -222,30 +210,30 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
           [&](uint32_t v, bool act) {
             if (act && L > 0) ws.rho[v] = (float)my[lane];
           },
-          [&](uint32_t v, uint32_t slot, uint32_t b, uint32_t e) {
+          [&](uint32_t v, uint32_t slot, uint32_t nchunks, uint32_t b, uint32_t e) {
             double part = 0.0;
             for (uint32_t a0 = b; a0 < e; a0 += 32) fwd_arc(a0 + lane < e, a0 + lane, part);
             part = warp_sum_f64(part);
             if (lane == 0 && b == __ldg(&G.row[v])) reached_arcs += __ldg(&G.row[v + 1]) - b;
             double tot = 0.0;
-            const uint32_t deg = __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
-            if (heavy_done(ws, slot, part, chunks_of(deg), &tot) && lane == 0 && L > 0)
+            if (heavy_done(ws, slot, part, nchunks, &tot) && lane == 0 && L > 0)
               ws.rho[v] = (float)tot;
           });
       if (!s.sync()) return;
       lbase = nlbase;
-      hbase = nhbase;
+      hcbase = nhcbase;
+      hvbase = nhvbase;
     }
     ++t;
     const uint32_t levels = L;  // levels 0 .. L-1 are non-empty
-    const uint32_t total_l = lbase, total_h = hbase;
+    const uint32_t total_l = lbase, total_hc = hcbase;
     if (!s.sync()) return;
     // -- backward levels, deepest first
     for (int32_t Lb = (int32_t)levels - 1; Lb >= 0; --Lb, ++t) {
       const int cur = t % 3;
       reset_slot(t);
       const uint32_t lb = ld_cg(&ws.lev_l[Lb]), le = ld_cg(&ws.lev_l[Lb + 1]);
-      const uint32_t hb0 = ld_cg(&ws.lev_h[Lb]), he = ld_cg(&ws.lev_h[Lb + 1]);
+      const uint32_t hcb = ld_cg(&ws.lev_h[Lb]), hvb = ld_cg(&ws.lev_hv[Lb]);
       const uint32_t nch = ld_cg(&ws.lev_hc[Lb]);
       auto bwd_arc = [&](bool valid, uint32_t arc, float rv, double& acc) {
         if (valid) {
@@ -258,7 +246,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       };
       float rv_lane = 0.f;
       visit_level(
-          G, W, ws, lb, le - lb, hb0, he - hb0, nch, &ws.cursor[cur], &ws.hcursor[cur],
+          G, W, ws, lb, le - lb, hcb, hvb, nch, &ws.cursor[cur], &ws.hcursor[cur],
           [&](uint32_t v, bool act) {
             my[lane] = 0.0;
             rv_lane = act ? ld_cg(&ws.rho[v]) : 0.f;
@@ -275,14 +263,13 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
               if (v != src) ws.bc[v] += sg;
             }
           },
-          [&](uint32_t v, uint32_t slot, uint32_t b, uint32_t e) {
+          [&](uint32_t v, uint32_t slot, uint32_t nchunks, uint32_t b, uint32_t e) {
             const float rv = ld_cg(&ws.rho[v]);
             double part = 0.0;
             for (uint32_t a0 = b; a0 < e; a0 += 32) bwd_arc(a0 + lane < e, a0 + lane, rv, part);
             part = warp_sum_f64(part);
             double tot = 0.0;
-            const uint32_t deg = __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
-            if (heavy_done(ws, slot, part, chunks_of(deg), &tot) && lane == 0) {
+            if (heavy_done(ws, slot, part, nchunks, &tot) && lane == 0) {
               const float sg = (float)tot;
               ws.sigma[v] = sg;
               if (v != src) ws.bc[v] += sg;
@@ -297,11 +284,12 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       ws.rho[v] = 0.f;
       ws.sigma[v] = 0.f;
     }
-    for (uint32_t k = W.gthread; k < total_h; k += W.nthreads) {
-      const uint32_t v = ws.hv[k];
-      ws.d[v] = -1;
-      ws.rho[v] = 0.f;
-      ws.sigma[v] = 0.f;
+    for (uint32_t k = W.gthread; k < total_hc; k += W.nthreads) {
+      const uint4 ent = ws.hc[k];
+      if (ent.y != 0) continue;  // one entry per vertex: its first chunk
+      ws.d[ent.x] = -1;
+      ws.rho[ent.x] = 0.f;
+      ws.sigma[ent.x] = 0.f;
     }
     reset_slot(t);
     if (!s.sync()) return;
@@ -337,14 +325,15 @@ static int bc_run(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t 
     return set_error(c, GDB_ERR_UNSUPPORTED, "BC runs on the XF barrier");
   const uint32_t V = g->V;
   const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
+  const uint32_t ccap = std::max<uint32_t>(g->nheavy_chunks, 1);
   const uint32_t maxlev = V + 2;
   Bump b;
   const size_t o_d = b.take((size_t)V * 4), o_rho = b.take((size_t)V * 4), o_sg = b.take((size_t)V * 4);
   const size_t o_ord = b.take((size_t)V * 4);
-  const size_t o_hv = b.take(hcap * 4), o_hb = b.take(hcap * 4), o_hacc = b.take(hcap * 8),
-               o_hleft = b.take(hcap * 4);
+  const size_t o_hc = b.take((size_t)ccap * 16), o_hacc = b.take((size_t)hcap * 8),
+               o_hleft = b.take((size_t)hcap * 4);
   const size_t o_ll = b.take((size_t)maxlev * 4), o_lh = b.take((size_t)maxlev * 4),
-               o_lhc = b.take((size_t)maxlev * 4);
+               o_lhc = b.take((size_t)maxlev * 4), o_lhv = b.take((size_t)maxlev * 4);
   const size_t o_cnt = b.take(512);
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
@@ -354,13 +343,14 @@ static int bc_run(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t 
   ws.sigma = (float*)(base + o_sg);
   ws.bc = d_bc;
   ws.order = (uint32_t*)(base + o_ord);
-  ws.hv = (uint32_t*)(base + o_hv);
-  ws.hb = (uint32_t*)(base + o_hb);
+  ws.hc = (uint4*)(base + o_hc);
+  ws.hc_cap = ccap;
   ws.hacc = (double*)(base + o_hacc);
   ws.hleft = (uint32_t*)(base + o_hleft);
   ws.lev_l = (uint32_t*)(base + o_ll);
   ws.lev_h = (uint32_t*)(base + o_lh);
   ws.lev_hc = (uint32_t*)(base + o_lhc);
+  ws.lev_hv = (uint32_t*)(base + o_lhv);
   char* cnt = base + o_cnt;
   ws.stats = (unsigned long long*)cnt;
   ws.hcnt = (unsigned long long*)(cnt + 64);

@@ -26,10 +26,9 @@ using namespace gdb;
 struct BfsWs {
   uint32_t* dist;
   uint32_t* q[2];
-  uint32_t* hv[2];
-  uint32_t* hb[2];
+  uint4* hc[2];                // heavy chunk entries
   uint32_t* qcount;            // [3]
-  unsigned long long* hcount;  // [3]
+  unsigned long long* hcount;  // [3] (heavy vertices << 32) | chunk entries
   uint32_t* cursor;            // [3]
   uint32_t* hcursor;           // [3]
   int* overflow;
@@ -50,8 +49,8 @@ __device__ __forceinline__ void bfs_top_down(const GraphView& G, const Warps& W,
   const int cur = L % 3, nxt = (L + 1) % 3;
   const uint32_t n = ld_cg(&ws.qcount[cur]);
   const unsigned long long hp = ld_cg_u64(&ws.hcount[cur]);
-  Frontier out{pick(ws.q, L + 1), pick(ws.hv, L + 1), pick(ws.hb, L + 1), &ws.qcount[nxt],
-               &ws.hcount[nxt], ws.qcap, ws.hcap, ws.overflow};
+  Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
+               ws.qcap, ws.hcap, ws.overflow};
   auto edge = [&](bool valid, uint32_t arc) {
     uint32_t u = 0;
     bool want = false;
@@ -66,7 +65,7 @@ __device__ __forceinline__ void bfs_top_down(const GraphView& G, const Warps& W,
     frontier_push(G, out, want, u);
   };
   visit_frontier(
-      G, W, pick(ws.q, L), n, pick(ws.hv, L), pick(ws.hb, L), hp, &ws.cursor[cur], &ws.hcursor[cur],
+      G, W, pick(ws.q, L), n, pick(ws.hc, L), hp, &ws.cursor[cur], &ws.hcursor[cur],
       [&](bool valid, int, uint32_t, uint32_t arc) { edge(valid, arc); },
       [&](bool valid, uint32_t, uint32_t arc) { edge(valid, arc); });
 }
@@ -78,8 +77,8 @@ __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& w
                                               const Warps& W, unsigned long long& arcs,
                                               unsigned long long& farcs) {
   const int nxt = (L + 1) % 3;
-  Frontier out{pick(ws.q, L + 1), pick(ws.hv, L + 1), pick(ws.hb, L + 1), &ws.qcount[nxt],
-               &ws.hcount[nxt], ws.qcap, ws.hcap, ws.overflow};
+  Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
+               ws.qcap, ws.hcap, ws.overflow};
   const int lane = lane_id();
   const uint32_t ngroups = (G.V + 31) / 32;
   for (uint32_t g = W.gwarp; g < ngroups; g += W.nwarps) {
@@ -122,15 +121,9 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
   if (!s.sync()) return;
   if (leader) {
     ws.dist[src] = 0;
-    const uint32_t deg = G.row[src + 1] - G.row[src];
-    if (is_heavy(G, src)) {
-      ws.hv[0][0] = src;
-      ws.hb[0][0] = 0;
-      ws.hcount[0] = (1ull << 32) | chunks_of(deg);
-    } else {
-      ws.q[0][0] = src;
-      ws.qcount[0] = 1;
-    }
+    frontier_seed(G, Frontier{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap,
+                              ws.overflow},
+                  src);
   }
   if (!s.sync()) return;
   unsigned long long arcs = 0;
@@ -204,15 +197,9 @@ __global__ void k_bfs_init(GraphView G, BfsWs ws, uint32_t src) {
     }
     *ws.overflow = 0;
     ws.stats[0] = ws.stats[1] = 0;
-    const uint32_t deg = G.row[src + 1] - G.row[src];
-    if (is_heavy(G, src)) {
-      ws.hv[0][0] = src;
-      ws.hb[0][0] = 0;
-      ws.hcount[0] = (1ull << 32) | chunks_of(deg);
-    } else {
-      ws.q[0][0] = src;
-      ws.qcount[0] = 1;
-    }
+    frontier_seed(G, Frontier{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap,
+                              ws.overflow},
+                  src);
   }
 }
 
@@ -246,11 +233,10 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
   if (!graph_ok(c, g) || !d_dist) return GDB_ERR_INVALID;
   if (src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
   const uint32_t V = g->V;
-  const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
+  const uint32_t hcap = chunk_capacity(g);
   Bump b;
   const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
-  const size_t o_hv0 = b.take(hcap * 4), o_hv1 = b.take(hcap * 4);
-  const size_t o_hb0 = b.take(hcap * 4), o_hb1 = b.take(hcap * 4);
+  const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
   const size_t o_cnt = b.take(512);
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
@@ -258,10 +244,8 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
   ws.dist = d_dist;
   ws.q[0] = (uint32_t*)(base + o_q0);
   ws.q[1] = (uint32_t*)(base + o_q1);
-  ws.hv[0] = (uint32_t*)(base + o_hv0);
-  ws.hv[1] = (uint32_t*)(base + o_hv1);
-  ws.hb[0] = (uint32_t*)(base + o_hb0);
-  ws.hb[1] = (uint32_t*)(base + o_hb1);
+  ws.hc[0] = (uint4*)(base + o_hc0);
+  ws.hc[1] = (uint4*)(base + o_hc1);
   char* cnt = base + o_cnt;
   ws.stats = (unsigned long long*)cnt;                // 8 x u64
   ws.hcount = (unsigned long long*)(cnt + 64);        // 3 x u64
@@ -495,14 +479,13 @@ extern "C" int gdb_bfs_noalloc(const uint32_t* d_row_ptr, const uint32_t* d_col,
   G.nheavy = 0;
   G.nheavy_chunks = 0;
   G.heavy_v = (const uint32_t*)(base + kNaSmall);
-  G.heavy_base = (const uint32_t*)(base + kNaSmall + 64);
+  G.heavy_chunk = (const uint4*)(base + kNaSmall + 64);
   G.heavy_bits = (const uint32_t*)(base + kNaBits);
   BfsWs ws;
   ws.dist = d_dist;
   ws.q[0] = (uint32_t*)(base + kNaQ0);
   ws.q[1] = (uint32_t*)(base + kNaQ1);
-  ws.hv[0] = ws.hv[1] = (uint32_t*)(base + kNaSmall + 128);
-  ws.hb[0] = ws.hb[1] = (uint32_t*)(base + kNaSmall + 192);
+  ws.hc[0] = ws.hc[1] = (uint4*)(base + kNaSmall + 128);
   unsigned char* cnt = base + kNaCounters;
   ws.stats = (unsigned long long*)cnt;
   ws.hcount = (unsigned long long*)(cnt + 64);

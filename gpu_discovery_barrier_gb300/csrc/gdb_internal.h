@@ -48,7 +48,7 @@ struct gdb_graph {
   uint32_t nheavy = 0;
   uint32_t nheavy_chunks = 0;
   uint32_t* heavy_v = nullptr;
-  uint32_t* heavy_base = nullptr;  // nheavy + 1 chunk prefix
+  uint4* heavy_chunk = nullptr;    // one entry per chunk: {v, chunk, heavy index, chunks}
   uint32_t* heavy_bits = nullptr;  // V-bit membership bitmap
   gdb::GraphView view() const;
 };
@@ -99,6 +99,7 @@ int read_participating(gdb_ctx* c, int* n);
 
 // Heavy table construction from a host copy of row_ptr.
 int build_heavy_table(gdb_graph* g, const uint32_t* host_row);
+uint32_t chunk_capacity(const gdb_graph* g);
 
 bool graph_ok(gdb_ctx* c, gdb_graph* g);
 

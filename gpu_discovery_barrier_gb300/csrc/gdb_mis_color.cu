@@ -199,8 +199,7 @@ struct ColorWs {
   uint32_t* cnt;       // neighbours still to be coloured before this vertex
   const float* prio;
   uint32_t* q[2];
-  uint32_t* hv[2];
-  uint32_t* hb[2];
+  uint4* hc[2];                // heavy chunk entries
   uint32_t* qcount;            // [3]
   unsigned long long* hcount;  // [3]
   uint32_t* cursor;            // [3]
@@ -267,8 +266,8 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   if (!s.sync()) return;
   // -- superstep 1: vertices that wait for nobody take colour 1
   {
-    Frontier out{pick(ws.q, 1), pick(ws.hv, 1), pick(ws.hb, 1), &ws.qcount[1], &ws.hcount[1],
-                 ws.qcap, ws.hcap, ws.overflow};
+    Frontier out{pick(ws.q, 1), pick(ws.hc, 1), &ws.qcount[1], &ws.hcount[1], ws.qcap, ws.hcap,
+                 ws.overflow};
     for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
       const uint32_t v = g * 32 + lane;
       const bool first = v < G.V && ld_cg(&ws.cnt[v]) == 0;
@@ -294,8 +293,8 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
       ws.hcursor[old] = 0;
     }
     coloured += (leader ? n + (uint32_t)(hp >> 32) : 0);
-    Frontier out{pick(ws.q, r + 1), pick(ws.hv, r + 1), pick(ws.hb, r + 1), &ws.qcount[nxt],
-                 &ws.hcount[nxt], ws.qcap, ws.hcap, ws.overflow};
+    Frontier out{pick(ws.q, r + 1), pick(ws.hc, r + 1), &ws.qcount[nxt], &ws.hcount[nxt],
+                 ws.qcap, ws.hcap, ws.overflow};
     const int32_t next_color = (int32_t)r + 1;
     float pv_lane = 0.f;
     auto relax = [&](bool valid, float pv, uint32_t arc) {
@@ -322,19 +321,14 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
         relax(valid, __shfl_sync(kFull, pv_lane, owner), arc);
       });
     }
-    const uint32_t ne = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
-    const uint32_t* hv = pick(ws.hv, r);
-    const uint32_t* hb = pick(ws.hb, r);
+    const uint32_t nch = (uint32_t)hp;
+    const uint4* hc = pick(ws.hc, r);
     WorkTaker ht(nch, W, &ws.hcursor[cur]);
     for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
-      uint32_t e = 0;
-      if (lane == 0) e = upper_index(hb, ne, c);
-      e = __shfl_sync(kFull, e, 0);
-      const uint32_t v = ld_cg(&hv[e]);
-      const uint32_t j = c - ld_cg(&hb[e]);
-      const float pv = __ldg(&ws.prio[v]);
-      const uint32_t rb = __ldg(&G.row[v]), re = __ldg(&G.row[v + 1]);
-      const uint32_t b = rb + j * kChunk, en = min(re, b + kChunk);
+      const uint4 ent = ld_cg(&hc[c]);
+      const float pv = __ldg(&ws.prio[ent.x]);
+      uint32_t b, en;
+      chunk_range(G, ent, b, en);
       range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, pv, arc); });
     }
     if (!s.sync()) return;
@@ -419,12 +413,11 @@ static int mis_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_s) 
 static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_color) {
   if (!graph_ok(c, g) || !d_prio || !d_color) return GDB_ERR_INVALID;
   const uint32_t V = g->V;
-  const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
+  const uint32_t hcap = chunk_capacity(g);
   Bump b;
   const size_t o_cnt_v = b.take((size_t)V * 4);
   const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
-  const size_t o_hv0 = b.take(hcap * 4), o_hv1 = b.take(hcap * 4);
-  const size_t o_hb0 = b.take(hcap * 4), o_hb1 = b.take(hcap * 4);
+  const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
   const size_t o_cnt = b.take(512);
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
@@ -434,10 +427,8 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   ws.prio = d_prio;
   ws.q[0] = (uint32_t*)(base + o_q0);
   ws.q[1] = (uint32_t*)(base + o_q1);
-  ws.hv[0] = (uint32_t*)(base + o_hv0);
-  ws.hv[1] = (uint32_t*)(base + o_hv1);
-  ws.hb[0] = (uint32_t*)(base + o_hb0);
-  ws.hb[1] = (uint32_t*)(base + o_hb1);
+  ws.hc[0] = (uint4*)(base + o_hc0);
+  ws.hc[1] = (uint4*)(base + o_hc1);
   char* cnt = base + o_cnt;
   ws.stats = (unsigned long long*)cnt;             // 4 x u64
   ws.hcount = (unsigned long long*)(cnt + 64);     // 3 x u64

@@ -135,29 +135,37 @@ int read_participating(gdb_ctx* c, int* n) {
 
 int build_heavy_table(gdb_graph* g, const uint32_t* hrow) {
   gdb_ctx* c = g->ctx;
-  std::vector<uint32_t> hv, hb;
+  std::vector<uint32_t> hv;
+  std::vector<uint4> chunks;
   std::vector<uint32_t> bits((g->V + 31) / 32 + 1, 0);
-  uint64_t chunks = 0;
   for (uint32_t v = 0; v < g->V; ++v) {
-    uint32_t d = hrow[v + 1] - hrow[v];
+    const uint32_t d = hrow[v + 1] - hrow[v];
     if (d > gdb::kHeavyDeg) {
+      const uint32_t h = (uint32_t)hv.size(), n = gdb::chunks_of(d);
       hv.push_back(v);
-      hb.push_back((uint32_t)chunks);
-      chunks += gdb::chunks_of(d);
+      for (uint32_t j = 0; j < n; ++j) chunks.push_back(make_uint4(v, j, h, n));
       bits[v >> 5] |= 1u << (v & 31);
     }
   }
-  hb.push_back((uint32_t)chunks);
   g->nheavy = (uint32_t)hv.size();
-  g->nheavy_chunks = (uint32_t)chunks;
-  const size_t nb = bits.size() * 4, nv = std::max<size_t>(hv.size(), 1) * 4, nbase = hb.size() * 4;
+  g->nheavy_chunks = (uint32_t)chunks.size();
+  const size_t nb = bits.size() * 4, nv = std::max<size_t>(hv.size(), 1) * 4,
+               nc = std::max<size_t>(chunks.size(), 1) * sizeof(uint4);
   GDB_CUDA(c, cudaMalloc(&g->heavy_bits, nb));
   GDB_CUDA(c, cudaMalloc(&g->heavy_v, nv));
-  GDB_CUDA(c, cudaMalloc(&g->heavy_base, nbase));
+  GDB_CUDA(c, cudaMalloc(&g->heavy_chunk, nc));
   GDB_CUDA(c, cudaMemcpy(g->heavy_bits, bits.data(), nb, cudaMemcpyHostToDevice));
   if (!hv.empty()) GDB_CUDA(c, cudaMemcpy(g->heavy_v, hv.data(), hv.size() * 4, cudaMemcpyHostToDevice));
-  GDB_CUDA(c, cudaMemcpy(g->heavy_base, hb.data(), nbase, cudaMemcpyHostToDevice));
+  if (!chunks.empty())
+    GDB_CUDA(c, cudaMemcpy(g->heavy_chunk, chunks.data(), chunks.size() * sizeof(uint4),
+                           cudaMemcpyHostToDevice));
   return GDB_OK;
+}
+
+// Capacity of a frontier's chunk entries: sum of ceil(d / kChunk) over the
+// heavy vertices, at most E / kChunk + nheavy.
+uint32_t chunk_capacity(const gdb_graph* g) {
+  return (uint32_t)std::max<uint64_t>(g->E / gdb::kChunk + g->nheavy + 1, 1);
 }
 
 bool graph_ok(gdb_ctx* c, gdb_graph* g) { return c && g && g->ctx == c; }
@@ -174,7 +182,7 @@ gdb::GraphView gdb_graph::view() const {
   v.nheavy = nheavy;
   v.nheavy_chunks = nheavy_chunks;
   v.heavy_v = heavy_v;
-  v.heavy_base = heavy_base;
+  v.heavy_chunk = heavy_chunk;
   v.heavy_bits = heavy_bits;
   return v;
 }
@@ -416,7 +424,7 @@ int gdb_graph_destroy(gdb_graph* g) {
   }
   if (g->owns_w && g->w) cudaFree(g->w);
   cudaFree(g->heavy_v);
-  cudaFree(g->heavy_base);
+  cudaFree(g->heavy_chunk);
   cudaFree(g->heavy_bits);
   cudaGetLastError();
   delete g;

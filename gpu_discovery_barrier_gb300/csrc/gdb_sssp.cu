@@ -27,8 +27,7 @@ struct SsspWs {
   uint32_t* dist;
   uint32_t* stamp;             // superstep + 1 in which the vertex was pushed
   uint32_t* q[2];
-  uint32_t* hv[2];
-  uint32_t* hb[2];
+  uint4* hc[2];                // heavy chunk entries
   uint32_t* qcount;            // [3]
   unsigned long long* hcount;  // [3]
   uint32_t* cursor;            // [3]
@@ -43,8 +42,8 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, co
   const int cur = L % 3, nxt = (L + 1) % 3;
   const uint32_t n = ld_cg(&ws.qcount[cur]);
   const unsigned long long hp = __ldcg(&ws.hcount[cur]);
-  Frontier out{pick(ws.q, L + 1), pick(ws.hv, L + 1), pick(ws.hb, L + 1), &ws.qcount[nxt],
-               &ws.hcount[nxt], ws.qcap, ws.hcap, ws.overflow};
+  Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
+               ws.qcap, ws.hcap, ws.overflow};
   auto relax = [&](bool valid, uint32_t du, uint32_t arc) {
     uint32_t v = 0;
     bool want = false;
@@ -75,19 +74,14 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, co
       relax(valid, __shfl_sync(kFull, du, owner), arc);
     });
   }
-  const uint32_t ne = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
-  const uint32_t* hv = pick(ws.hv, L);
-  const uint32_t* hb = pick(ws.hb, L);
+  const uint32_t nch = (uint32_t)hp;
+  const uint4* hc = pick(ws.hc, L);
   WorkTaker ht(nch, W, &ws.hcursor[cur]);
   for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
-    uint32_t e = 0;
-    if (lane == 0) e = upper_index(hb, ne, c);
-    e = __shfl_sync(kFull, e, 0);
-    const uint32_t u = ld_cg(&hv[e]);
-    const uint32_t j = c - ld_cg(&hb[e]);
-    const uint32_t du = ld_cg(&ws.dist[u]);
-    const uint32_t rb = __ldg(&G.row[u]), re = __ldg(&G.row[u + 1]);
-    const uint32_t b = rb + j * kChunk, en = min(re, b + kChunk);
+    const uint4 ent = ld_cg(&hc[c]);
+    const uint32_t du = ld_cg(&ws.dist[ent.x]);
+    uint32_t b, en;
+    chunk_range(G, ent, b, en);
     range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, du, arc); });
   }
 }
@@ -114,15 +108,9 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
   if (leader) {
     ws.dist[src] = 0;
     ws.stamp[src] = 0;
-    const uint32_t deg = G.row[src + 1] - G.row[src];
-    if (is_heavy(G, src)) {
-      ws.hv[0][0] = src;
-      ws.hb[0][0] = 0;
-      ws.hcount[0] = (1ull << 32) | chunks_of(deg);
-    } else {
-      ws.q[0][0] = src;
-      ws.qcount[0] = 1;
-    }
+    frontier_seed(G, Frontier{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap,
+                              ws.overflow},
+                  src);
   }
   if (!s.sync()) return;
   unsigned long long arcs = 0;
@@ -281,12 +269,11 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
   if (src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
   if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
   const uint32_t V = g->V;
-  const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
+  const uint32_t hcap = chunk_capacity(g);
   Bump b;
   const size_t o_st = b.take((size_t)V * 4);
   const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
-  const size_t o_hv0 = b.take(hcap * 4), o_hv1 = b.take(hcap * 4);
-  const size_t o_hb0 = b.take(hcap * 4), o_hb1 = b.take(hcap * 4);
+  const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
   const size_t o_cnt = b.take(512);
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
@@ -295,10 +282,8 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
   ws.stamp = (uint32_t*)(base + o_st);
   ws.q[0] = (uint32_t*)(base + o_q0);
   ws.q[1] = (uint32_t*)(base + o_q1);
-  ws.hv[0] = (uint32_t*)(base + o_hv0);
-  ws.hv[1] = (uint32_t*)(base + o_hv1);
-  ws.hb[0] = (uint32_t*)(base + o_hb0);
-  ws.hb[1] = (uint32_t*)(base + o_hb1);
+  ws.hc[0] = (uint4*)(base + o_hc0);
+  ws.hc[1] = (uint4*)(base + o_hc1);
   char* cnt = base + o_cnt;
   ws.stats = (unsigned long long*)cnt;
   ws.hcount = (unsigned long long*)(cnt + 64);

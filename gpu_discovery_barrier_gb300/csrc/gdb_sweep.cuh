@@ -6,8 +6,10 @@
 //    arcs per step, each lane finding the vertex that owns its arc with a
 //    5-step shuffle binary search -- consecutive lanes read consecutive
 //    column ids, so col[] streams in full 128-byte lines;
-//  * heavy vertices are cut into chunks of kChunk arcs handed out one per
-//    warp, so a hub never serialises a superstep;
+//  * heavy vertices (degree > kHeavyDeg) are cut into chunks of kChunk arcs;
+//    every chunk is its own work entry {vertex, chunk, vertex slot, chunks},
+//    handed out one per warp, so neither a hub nor a sparse superstep's
+//    lone medium-degree vertex serialises a superstep;
 //  * frontier pushes are warp-aggregated: one atomicAdd per warp and queue.
 #pragma once
 
@@ -20,8 +22,8 @@
 namespace gdb {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr uint32_t kHeavyDeg = 1024;
-constexpr uint32_t kChunk = 1024;
+constexpr uint32_t kHeavyDeg = 128;
+constexpr uint32_t kChunk = 128;
 constexpr uint32_t kInf = GDB_LONESTAR_INF;
 // groups of 32 vertices a warp takes per atomic on a work cursor (one
 // cursor word is shared by every warp of the grid, so grabs are batched)
@@ -36,7 +38,7 @@ struct GraphView {
   uint32_t nheavy;
   uint32_t nheavy_chunks;
   const uint32_t* __restrict__ heavy_v;     // ascending ids
-  const uint32_t* __restrict__ heavy_base;  // chunk prefix, nheavy + 1
+  const uint4* __restrict__ heavy_chunk;    // {vertex, chunk, heavy index, chunks}
   const uint32_t* __restrict__ heavy_bits;  // membership bitmap
 };
 
@@ -57,6 +59,7 @@ __device__ __forceinline__ int32_t ld_cg(const int32_t* p) { return __ldcg(p); }
 __device__ __forceinline__ float ld_cg(const float* p) { return __ldcg(p); }
 __device__ __forceinline__ unsigned long long ld_cg(const unsigned long long* p) { return __ldcg(p); }
 __device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ uint4 ld_cg(const uint4* p) { return __ldcg(p); }
 
 // a[i & 1] without dynamic indexing (which would copy the kernel-parameter
 // array to local memory).
@@ -161,33 +164,24 @@ __device__ __forceinline__ void range_arcs(uint32_t b, uint32_t e, Fn&& fn) {
   }
 }
 
-// Largest index i in [0, n) with base[i] <= c (base ascending, base[0] = 0).
-__device__ __forceinline__ uint32_t upper_index(const uint32_t* base, uint32_t n, uint32_t c) {
-  uint32_t lo = 0, hi = n;  // invariant: base[lo] <= c, answer in [lo, hi)
-  while (hi - lo > 1) {
-    uint32_t mid = (lo + hi) >> 1;
-    if (ld_cg(&base[mid]) <= c) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// A frontier: light vertex queue plus heavy entries (vertex, first chunk)
-// whose chunk bases ascend with the slot (one packed 64-bit atomicAdd
-// hands out both), so chunk c belongs to the last entry with base <= c.
+// A frontier: a queue of light vertices plus one work entry per heavy chunk,
+// {vertex, chunk index, vertex slot, chunks of the vertex}.  One packed
+// 64-bit atomicAdd on hcount reserves a vertex slot (high word) and the
+// vertex's run of chunk entries (low word).
 struct Frontier {
   uint32_t* q;        // light vertices
-  uint32_t* hv;       // heavy vertices
-  uint32_t* hb;       // first chunk of each heavy entry
+  uint4* hc;          // heavy chunk entries
   uint32_t* qcount;   // light count
-  unsigned long long* hcount;  // (entries << 32) | chunks
-  uint32_t qcap, hcap;
+  unsigned long long* hcount;  // (vertex slots << 32) | chunk entries
+  uint32_t qcap, hcap;         // capacities: light vertices, chunk entries
   int* overflow;      // set when a push would exceed a capacity
-  uint32_t* hleft = nullptr;  // optional: chunk countdown armed at push
-  double* hacc = nullptr;     // optional: FP64 accumulator cleared at push
+  uint32_t vcap = 0xffffffffu;  // optional: vertex-slot capacity
+  uint32_t* hleft = nullptr;    // optional: chunk countdown per slot, armed at push
+  double* hacc = nullptr;       // optional: FP64 accumulator per slot, cleared at push
 };
 
-// Warp-aggregated push of the lanes' `want` vertices.
+// Warp-aggregated push of the lanes' `want` vertices; the warp writes each
+// heavy vertex's chunk entries together.
 __device__ __forceinline__ void frontier_push(const GraphView& G, const Frontier& F, bool want,
                                               uint32_t v) {
   const int lane = lane_id();
@@ -205,38 +199,52 @@ __device__ __forceinline__ void frontier_push(const GraphView& G, const Frontier
       else atomicExch(F.overflow, 1);
     }
   }
-  if (heavy) {
-    const uint32_t deg = __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
-    const unsigned long long old =
-        atomicAdd(F.hcount, (1ull << 32) | (unsigned long long)chunks_of(deg));
-    const uint32_t slot = (uint32_t)(old >> 32);
-    if (slot < F.hcap) {
-      F.hv[slot] = v;
-      F.hb[slot] = (uint32_t)old;
-      if (F.hleft) {
-        F.hleft[slot] = chunks_of(deg);
-        F.hacc[slot] = 0.0;
-      }
-    } else {
-      atomicExch(F.overflow, 1);
+  for (unsigned hm = __ballot_sync(kFull, heavy); hm; hm &= hm - 1) {
+    const int l = __ffs(hm) - 1;
+    const uint32_t hvx = __shfl_sync(kFull, v, l);
+    unsigned long long old = 0;
+    uint32_t nch = 0;
+    if (lane == l) {
+      nch = chunks_of(__ldg(&G.row[hvx + 1]) - __ldg(&G.row[hvx]));
+      old = atomicAdd(F.hcount, (1ull << 32) | (unsigned long long)nch);
+    }
+    old = __shfl_sync(kFull, old, l);
+    nch = __shfl_sync(kFull, nch, l);
+    const uint32_t vslot = (uint32_t)(old >> 32), cbase = (uint32_t)old;
+    if (cbase + nch > F.hcap || vslot >= F.vcap) {
+      if (lane == l) atomicExch(F.overflow, 1);
+      continue;
+    }
+    for (uint32_t j = lane; j < nch; j += 32) F.hc[cbase + j] = make_uint4(hvx, j, vslot, nch);
+    if (lane == l && F.hleft) {
+      F.hleft[vslot] = nch;
+      F.hacc[vslot] = 0.0;
     }
   }
 }
 
-// Warp-aggregated append of the lanes' `want` values to a list.
-__device__ __forceinline__ void warp_append(uint32_t* list, uint32_t* count, uint32_t cap,
-                                            int* overflow, bool want, uint32_t v) {
-  const unsigned m = __ballot_sync(kFull, want);
-  if (!m) return;
-  const int lane = lane_id(), leader = __ffs(m) - 1;
-  uint32_t base = 0;
-  if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
-  base = __shfl_sync(kFull, base, leader);
-  if (want) {
-    const uint32_t slot = base + __popc(m & lanemask_lt());
-    if (slot < cap) list[slot] = v;
-    else atomicExch(overflow, 1);
+// One thread seeds a frontier with vertex v (the traversal's source).
+__device__ __forceinline__ void frontier_seed(const GraphView& G, const Frontier& F, uint32_t v) {
+  if (is_heavy(G, v)) {
+    const uint32_t nch = chunks_of(G.row[v + 1] - G.row[v]);
+    for (uint32_t j = 0; j < nch; ++j) F.hc[j] = make_uint4(v, j, 0u, nch);
+    if (F.hleft) {
+      F.hleft[0] = nch;
+      F.hacc[0] = 0.0;
+    }
+    *F.hcount = (1ull << 32) | nch;
+  } else {
+    F.q[0] = v;
+    *F.qcount = 1;
   }
+}
+
+// Arc range [b, e) of heavy chunk entry `ent`.
+__device__ __forceinline__ void chunk_range(const GraphView& G, const uint4& ent, uint32_t& b,
+                                            uint32_t& e) {
+  const uint32_t rb = __ldg(&G.row[ent.x]), re = __ldg(&G.row[ent.x + 1]);
+  b = rb + ent.y * kChunk;
+  e = min(re, b + kChunk);
 }
 
 // Visit a frontier: light vertices in warp groups of 32, then heavy chunks.
@@ -244,7 +252,7 @@ __device__ __forceinline__ void warp_append(uint32_t* list, uint32_t* count, uin
 // group_arcs; heavy(valid, v, arc) per 32-arc step of a chunk.
 template <class Light, class Heavy>
 __device__ __forceinline__ void visit_frontier(const GraphView& G, const Warps& W, const uint32_t* q,
-                                               uint32_t n, const uint32_t* hv, const uint32_t* hb,
+                                               uint32_t n, const uint4* hc,
                                                unsigned long long hpacked, uint32_t* cursor,
                                                uint32_t* hcursor, Light&& light, Heavy&& heavy) {
   const int lane = lane_id();
@@ -255,19 +263,13 @@ __device__ __forceinline__ void visit_frontier(const GraphView& G, const Warps& 
     const uint32_t v = act ? ld_cg(&q[i]) : 0u;
     group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) { light(valid, owner, v, arc); });
   }
-  const uint32_t ne = (uint32_t)(hpacked >> 32);
   const uint32_t nch = (uint32_t)hpacked;
   WorkTaker ht(nch, W, hcursor);
   for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
-    uint32_t e = 0;
-    if (lane == 0) e = upper_index(hb, ne, c);
-    e = __shfl_sync(kFull, e, 0);
-    const uint32_t v = ld_cg(&hv[e]);
-    const uint32_t j = c - ld_cg(&hb[e]);
-    const uint32_t rb = __ldg(&G.row[v]), re = __ldg(&G.row[v + 1]);
-    const uint32_t b = rb + j * kChunk;
-    const uint32_t en = min(re, b + kChunk);
-    range_arcs(b, en, [&](bool valid, uint32_t arc) { heavy(valid, v, arc); });
+    const uint4 ent = ld_cg(&hc[c]);
+    uint32_t b, en;
+    chunk_range(G, ent, b, en);
+    range_arcs(b, en, [&](bool valid, uint32_t arc) { heavy(valid, ent.x, arc); });
   }
 }
 
@@ -295,24 +297,18 @@ __device__ __forceinline__ void sweep_light(const GraphView& G, uint32_t* cursor
   }
 }
 
-// Sweep the heavy vertices through the static chunk table, one chunk per
-// warp: fn(v, heavy_index, chunk_in_vertex, arc_begin, arc_end).
+// Sweep the heavy vertices through the static chunk table, kGrab chunks
+// per grab: fn(v, heavy_index, chunk_in_vertex, arc_begin, arc_end).
 template <class Fn>
 __device__ __forceinline__ void sweep_heavy(const GraphView& G, uint32_t* hcursor, Fn&& fn) {
-  const int lane = lane_id();
   for (;;) {
     const uint32_t c0 = warp_grab(hcursor) * kGrab;
     if (c0 >= G.nheavy_chunks) break;
     for (uint32_t c = c0; c < min(c0 + kGrab, G.nheavy_chunks); ++c) {
-      uint32_t e = 0;
-      if (lane == 0) e = upper_index(G.heavy_base, G.nheavy, c);
-      e = __shfl_sync(kFull, e, 0);
-      const uint32_t v = __ldg(&G.heavy_v[e]);
-      const uint32_t j = c - __ldg(&G.heavy_base[e]);
-      const uint32_t rb = __ldg(&G.row[v]), re = __ldg(&G.row[v + 1]);
-      const uint32_t b = rb + j * kChunk;
-      const uint32_t en = min(re, b + kChunk);
-      fn(v, e, j, b, en);
+      const uint4 ent = __ldg(&G.heavy_chunk[c]);
+      uint32_t b, en;
+      chunk_range(G, ent, b, en);
+      fn(ent.x, ent.z, ent.y, b, en);
     }
   }
 }
