@@ -66,10 +66,11 @@ __device__ __forceinline__ void visit_level(const GraphView& G, const Warps& W, 
                                             uint32_t nch, uint32_t* cursor, uint32_t* hcursor,
                                             Begin&& begin, Edge&& edge, End&& end, Heavy&& heavy) {
   const int lane = lane_id();
-  WorkTaker lt((nl + 31) / 32, W, cursor);
+  const uint32_t k = group_width(nl, W.nwarps);
+  WorkTaker lt((nl + k - 1) / k, W, cursor);
   for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
-    const uint32_t i = g * 32 + lane;
-    const bool act = i < nl;
+    const uint32_t i = g * k + lane;
+    const bool act = (uint32_t)lane < k && i < nl;
     const uint32_t v = act ? ld_cg(&ws.order[lb + i]) : 0u;
     begin(v, act);
     __syncwarp();

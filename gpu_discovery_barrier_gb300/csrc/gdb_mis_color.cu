@@ -311,10 +311,11 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
       frontier_push(G, out, ready, u);
     };
     const uint32_t* q = pick(ws.q, r);
-    WorkTaker lt((n + 31) / 32, W, &ws.cursor[cur]);
+    const uint32_t k = group_width(n, W.nwarps);
+    WorkTaker lt((n + k - 1) / k, W, &ws.cursor[cur]);
     for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
-      const uint32_t i = g * 32 + lane;
-      const bool act = i < n;
+      const uint32_t i = g * k + lane;
+      const bool act = (uint32_t)lane < k && i < n;
       const uint32_t v = act ? ld_cg(&q[i]) : 0u;
       pv_lane = act ? __ldg(&ws.prio[v]) : 0.f;
       group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) {

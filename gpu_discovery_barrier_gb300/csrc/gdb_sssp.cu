@@ -64,10 +64,11 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, co
   };
   // light groups: each lane reads its own vertex's distance once
   const int lane = lane_id();
-  WorkTaker lt((n + 31) / 32, W, &ws.cursor[cur]);
+  const uint32_t k = group_width(n, W.nwarps);
+  WorkTaker lt((n + k - 1) / k, W, &ws.cursor[cur]);
   for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
-    const uint32_t i = g * 32 + lane;
-    const bool act = i < n;
+    const uint32_t i = g * k + lane;
+    const bool act = (uint32_t)lane < k && i < n;
     const uint32_t u = act ? ld_cg(&pick(ws.q, L)[i]) : 0u;
     const uint32_t du = act ? ld_cg(&ws.dist[u]) : 0u;
     group_arcs(G, act, u, [&](bool valid, int owner, uint32_t arc) {

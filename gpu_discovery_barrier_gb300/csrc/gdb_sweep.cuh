@@ -164,6 +164,15 @@ __device__ __forceinline__ void range_arcs(uint32_t b, uint32_t e, Fn&& fn) {
   }
 }
 
+// Vertices per warp group for a frontier of n light vertices: 32 when there
+// is enough work for every warp, fewer (down to one vertex per warp) when
+// the frontier is small, so sparse supersteps spread over all warps.
+__device__ __forceinline__ uint32_t group_width(uint32_t n, uint32_t nwarps) {
+  if (n >= 32u * nwarps) return 32u;
+  const uint32_t k = n / nwarps;
+  return k < 1u ? 1u : k;
+}
+
 // A frontier: a queue of light vertices plus one work entry per heavy chunk,
 // {vertex, chunk index, vertex slot, chunks of the vertex}.  One packed
 // 64-bit atomicAdd on hcount reserves a vertex slot (high word) and the
@@ -256,10 +265,11 @@ __device__ __forceinline__ void visit_frontier(const GraphView& G, const Warps& 
                                                unsigned long long hpacked, uint32_t* cursor,
                                                uint32_t* hcursor, Light&& light, Heavy&& heavy) {
   const int lane = lane_id();
-  WorkTaker lt((n + 31) / 32, W, cursor);
+  const uint32_t k = group_width(n, W.nwarps);
+  WorkTaker lt((n + k - 1) / k, W, cursor);
   for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
-    const uint32_t i = g * 32 + lane;
-    const bool act = i < n;
+    const uint32_t i = g * k + lane;
+    const bool act = (uint32_t)lane < k && i < n;
     const uint32_t v = act ? ld_cg(&q[i]) : 0u;
     group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) { light(valid, owner, v, arc); });
   }
