@@ -172,14 +172,14 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
   if (leader) ws.stats[1] = L;
 }
 
-__global__ void __launch_bounds__(1024, 1) k_bfs_xf(DiscoveryArgs a, GraphView G, BfsWs ws, uint32_t src) {
+__global__ void __launch_bounds__(512, 3) k_bfs_xf(DiscoveryArgs a, GraphView G, BfsWs ws, uint32_t src) {
   __shared__ LocalCtx l;
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
   bfs_body(s, G, ws, src);
 }
 
-__global__ void __launch_bounds__(1024, 1) k_bfs_grid(GraphView G, BfsWs ws, uint32_t src) {
+__global__ void __launch_bounds__(512, 3) k_bfs_grid(GraphView G, BfsWs ws, uint32_t src) {
   GridSync s;
   bfs_body(s, G, ws, src);
 }
@@ -203,7 +203,7 @@ __global__ void k_bfs_init(GraphView G, BfsWs ws, uint32_t src) {
   }
 }
 
-__global__ void __launch_bounds__(1024, 1) k_bfs_level(GraphView G, BfsWs ws, uint32_t L) {
+__global__ void __launch_bounds__(512, 3) k_bfs_level(GraphView G, BfsWs ws, uint32_t L) {
   const int old = (L + 2) % 3;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     ws.qcount[old] = 0;

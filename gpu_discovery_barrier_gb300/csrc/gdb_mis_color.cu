@@ -171,7 +171,7 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
   if (leader) ws.stats[1] = r + 1;
 }
 
-__global__ void __launch_bounds__(1024, 1) k_mis_xf(DiscoveryArgs a, GraphView G, MisWs ws) {
+__global__ void __launch_bounds__(512, 3) k_mis_xf(DiscoveryArgs a, GraphView G, MisWs ws) {
   __shared__ LocalCtx l;
   __shared__ uint32_t smem[1024];
   if (!discover(a, &l)) return;
@@ -343,7 +343,7 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   }
 }
 
-__global__ void __launch_bounds__(1024, 1) k_color_xf(DiscoveryArgs a, GraphView G, ColorWs ws) {
+__global__ void __launch_bounds__(512, 3) k_color_xf(DiscoveryArgs a, GraphView G, ColorWs ws) {
   __shared__ LocalCtx l;
   __shared__ uint32_t smem[1024];
   if (!discover(a, &l)) return;

@@ -165,7 +165,7 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
   if (leader) ws.acc[2] = round + 1;
 }
 
-__global__ void __launch_bounds__(1024, 1) k_mst_xf(DiscoveryArgs a, GraphView G, MstWs ws) {
+__global__ void __launch_bounds__(512, 3) k_mst_xf(DiscoveryArgs a, GraphView G, MstWs ws) {
   __shared__ LocalCtx l;
   __shared__ unsigned long long smem[1024];
   if (!discover(a, &l)) return;

@@ -134,14 +134,14 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
   if (leader) ws.stats[1] = L;
 }
 
-__global__ void __launch_bounds__(1024, 1) k_sssp_xf(DiscoveryArgs a, GraphView G, SsspWs ws, uint32_t src) {
+__global__ void __launch_bounds__(512, 3) k_sssp_xf(DiscoveryArgs a, GraphView G, SsspWs ws, uint32_t src) {
   __shared__ LocalCtx l;
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
   sssp_body(s, G, ws, src);
 }
 
-__global__ void __launch_bounds__(1024, 1) k_sssp_grid(GraphView G, SsspWs ws, uint32_t src) {
+__global__ void __launch_bounds__(512, 3) k_sssp_grid(GraphView G, SsspWs ws, uint32_t src) {
   GridSync s;
   sssp_body(s, G, ws, src);
 }
@@ -253,7 +253,7 @@ __device__ __forceinline__ void jacobi_body(Sync& s, const GraphView& G, const J
   if (leader) ws.stats[1] = k;
 }
 
-__global__ void __launch_bounds__(1024, 1) k_jacobi_xf(DiscoveryArgs a, GraphView G, JacobiWs ws, uint32_t src) {
+__global__ void __launch_bounds__(512, 3) k_jacobi_xf(DiscoveryArgs a, GraphView G, JacobiWs ws, uint32_t src) {
   __shared__ LocalCtx l;
   __shared__ int smin[1024];
   if (!discover(a, &l)) return;

@@ -70,7 +70,8 @@ typedef enum {
 
 typedef struct {
   int device;          /* CUDA ordinal; -1 = current device */
-  int block_size;      /* threads per CTA of the persistent kernels (0 = 512) */
+  int block_size;      /* threads per CTA of the persistent kernels (0 = 512;
+                          the graph kernels take at most 512) */
   int max_ctas;        /* cap on launched CTAs (0 = occupancy x SMs) */
   int oversubscribe;   /* >0: launch this many CTAs and let discovery pick
                           the co-resident ones (the reference launches 1000) */
