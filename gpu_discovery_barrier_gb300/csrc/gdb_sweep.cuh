@@ -22,8 +22,11 @@
 namespace gdb {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr uint32_t kHeavyDeg = 128;
+constexpr uint32_t kHeavyDeg = 64;
 constexpr uint32_t kChunk = 128;
+// light vertices a warp takes at once: bounds a work item to
+// kGroupMax * kHeavyDeg arcs, so the last item of a superstep is short
+constexpr uint32_t kGroupMax = 8;
 constexpr uint32_t kInf = GDB_LONESTAR_INF;
 // groups of 32 vertices a warp takes per atomic on a work cursor (one
 // cursor word is shared by every warp of the grid, so grabs are batched)
@@ -164,11 +167,12 @@ __device__ __forceinline__ void range_arcs(uint32_t b, uint32_t e, Fn&& fn) {
   }
 }
 
-// Vertices per warp group for a frontier of n light vertices: 32 when there
-// is enough work for every warp, fewer (down to one vertex per warp) when
-// the frontier is small, so sparse supersteps spread over all warps.
+// Vertices per warp group for a frontier of n light vertices: kGroupMax
+// when there is enough work for every warp, fewer (down to one vertex per
+// warp) when the frontier is small, so sparse supersteps spread over all
+// warps.
 __device__ __forceinline__ uint32_t group_width(uint32_t n, uint32_t nwarps) {
-  if (n >= 32u * nwarps) return 32u;
+  if (n >= kGroupMax * nwarps) return kGroupMax;
   const uint32_t k = n / nwarps;
   return k < 1u ? 1u : k;
 }
