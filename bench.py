@@ -51,6 +51,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--apps", default="bfs,sssp,mis,color,bc,mst")
+    p.add_argument("--workload", choices=["rmat", "grid4096"], default="rmat",
+                   help="rmat: the R-MAT suite (default); grid4096: the barrier-bound "
+                        "4096x4096 grid, BFS and SSSP from the corner per barrier kind")
     return p.parse_args()
 
 
@@ -489,11 +492,70 @@ def run_gdb(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def run_grid(args, rank, world, local):
+    """Barrier-bound case: 4096x4096 grid (V = 16,777,216, 67,092,480 arcs,
+    weights U[1,1000]), BFS and SSSP from the corner, thousands of
+    supersteps; the same traversals on every barrier kind, plus the barrier
+    latency of each kind at the CTA count the traversal kernels use."""
+    import torch
+
+    from gpu_discovery_barrier_gb300 import gdb, graphgen as gg
+
+    torch.cuda.set_device(local)
+    g = gg.grid(4096, 4096)
+    w = gg.uniform_weights(g, 1, 1000, seed=1)
+    dev = torch.device("cuda", local)
+    d_out = torch.empty(g.V, dtype=torch.int32, device=dev)
+    kinds = {"xf": gdb.BARRIER_XF, "grid_sync": gdb.BARRIER_GRID_SYNC,
+             "relaunch": gdb.BARRIER_RELAUNCH}
+    res = {}
+    with gdb.Ctx() as c:
+        G = c.graph(g.row_ptr, g.col, w)
+        for name, kind in kinds.items():
+            c.set_options(barrier=kind)
+            r = {}
+            for app in ("bfs", "sssp"):
+                if app == "sssp" and kind == gdb.BARRIER_RELAUNCH:
+                    continue
+                fn = c.bfs_device if app == "bfs" else c.sssp_device
+                for _ in range(args.warmup):
+                    fn(G, 0, d_out.data_ptr())
+                ms, steps = [], 0
+                for _ in range(args.steps):
+                    fn(G, 0, d_out.data_ptr())
+                    st = c.last_stats()
+                    ms.append(st["kernel_ms"])
+                    steps = st["supersteps"]
+                t = statistics.median(ms)
+                r[app] = {"ms": t, "supersteps": steps, "edges_per_s": g.E / (t / 1e3),
+                          "us_per_superstep": 1e3 * t / max(steps, 1)}
+            bk = kind if kind != gdb.BARRIER_RELAUNCH else gdb.BARRIER_RELAUNCH
+            ns, groups = c.barrier_bench(bk, 512, 2000)
+            r["barrier_ns"] = ns
+            r["barrier_ctas"] = groups
+            res[name] = r
+        c.set_options(barrier=gdb.BARRIER_XF)
+        ns_g, gr_g = c.barrier_bench(gdb.BARRIER_RELAUNCH_GRAPH, 512, 2000)
+    xf = res["xf"]
+    value = 2 * g.E / ((xf["bfs"]["ms"] + xf["sssp"]["ms"]) / 1e3)
+    cfg = {"workload": "grid 4096x4096, BFS + SSSP from vertex 0", "V": g.V, "E": g.E,
+           "weights": "U[1,1000] seed 1", "global_batch": 1, "parallelism": "replicas x1",
+           "l2": "inputs > L2 (no flush)"}
+    line = base_line(args, world, value, xf["bfs"]["ms"] + xf["sssp"]["ms"], cfg)
+    line["metric"] = "edges/sec (BFS + SSSP on the 4096x4096 grid, XF barrier)"
+    line["barrier_kinds"] = res
+    line["relaunch_graph_barrier_ns"] = ns_g
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "grid4096":
+        run_grid(args, rank, world, local)
     else:
         run_gdb(args, rank, world, local)
     if world > 1:

@@ -1,0 +1,35 @@
+"""Full-size checks that need no oracle run: BFS levels on the 4096x4096
+grid are the Manhattan distance from the corner (8,190 supersteps), and
+the SSSP answer on a 1024x1024 grid passes the reference's own validity
+check (dverifysolution: no arc can still relax it, sssp_common.cl:41-56)
+and equals the oracle's."""
+import numpy as np
+import pytest
+
+import oracle
+from gpu_discovery_barrier_gb300 import gdb, graphgen as gg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC])
+def test_grid4096_bfs_levels(barrier):
+    R = C = 4096
+    g = gg.grid(R, C)
+    with gdb.Ctx(barrier=barrier) as c:
+        G = c.graph(g.row_ptr, g.col)
+        d = c.bfs(G, 0)
+        assert c.last_stats()["supersteps"] == R + C - 1
+    r, col = np.divmod(np.arange(g.V, dtype=np.int64), C)
+    assert np.array_equal(d.astype(np.int64), r + col)
+
+
+def test_grid1024_sssp_valid_and_exact():
+    g = gg.grid(1024, 1024)
+    w = gg.uniform_weights(g, 1, 1000, seed=1)
+    with gdb.Ctx() as c:
+        G = c.graph(g.row_ptr, g.col, w)
+        d = c.sssp(G, 0)
+    gw = g.with_weights(w)
+    assert oracle.verify_dist(gw, d, weighted=True) == 0
+    assert np.array_equal(d, oracle.sssp_worklist(gw, 0))
