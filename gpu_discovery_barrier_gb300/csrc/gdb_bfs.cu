@@ -225,6 +225,48 @@ __global__ void __launch_bounds__(512, 3) k_bfs_level(GraphView G, BfsWs ws, uin
   if (lane_id() == 0 && r) atomicAdd(&ws.stats[0], r);
 }
 
+// Graph-relaunch mode: the body of a CUDA-graph WHILE node.  The level
+// number lives in ctl[0]; the last CTA to finish (ctl[1] counts them)
+// advances it and sets the loop condition to "next frontier not empty".
+__global__ void __launch_bounds__(512, 3) k_bfs_glevel(GraphView G, BfsWs ws, uint32_t* ctl,
+                                                       cudaGraphConditionalHandle cond) {
+  __shared__ uint32_t sL;
+  if (threadIdx.x == 0) sL = ld_cg(&ctl[0]);
+  __syncthreads();
+  const uint32_t L = sL;
+  const int old = (L + 2) % 3;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ws.qcount[old] = 0;
+    ws.hcount[old] = 0;
+    ws.cursor[old] = 0;
+    ws.hcursor[old] = 0;
+  }
+  unsigned long long arcs = 0, farcs = 0;
+  Warps W;
+  W.gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  W.nwarps = (gridDim.x * blockDim.x) >> 5;
+  W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
+  W.nthreads = gridDim.x * blockDim.x;
+  bfs_top_down(G, W, ws, L, arcs, farcs);
+  unsigned long long r = arcs;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(kFull, r, o);
+  if (lane_id() == 0 && r) atomicAdd(&ws.stats[0], r);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ctl[1], 1u) == gridDim.x - 1) {
+      __threadfence();
+      const int nxt = (L + 1) % 3;
+      const bool more = ld_cg(&ws.qcount[nxt]) != 0 || __ldcg(&ws.hcount[nxt]) != 0;
+      ctl[0] = L + 1;
+      ctl[1] = 0;
+      ws.stats[1] = L + 1;
+      cudaGraphSetConditional(cond, more ? 1u : 0u);
+    }
+  }
+}
+
 }  // namespace
 
 using namespace gdbi;
@@ -321,6 +363,18 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
     c->last.participating = grid;
     c->last.launched = grid;
     c->last.launches = launches;
+  } else if (kind == GDB_BARRIER_RELAUNCH_GRAPH) {
+    if (ws.adaptive) return set_error(c, GDB_ERR_UNSUPPORTED, "adaptive schedule needs a persistent barrier");
+    int occ = 0;
+    GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs_glevel, block, 0));
+    int grid = occ * c->sm_count;
+    if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
+    uint32_t* ctl = (uint32_t*)(cnt + 192);  // [0] level, [1] CTAs done
+    rc = graph_while_run(c, (const void*)k_bfs_init, grid, block, G, ws, src,
+                         (const void*)k_bfs_glevel, ctl);
+    if (rc) return rc;
+    c->last.participating = grid;
+    c->last.launched = grid;
   } else {
     return set_error(c, GDB_ERR_UNSUPPORTED, "barrier kind not available for BFS");
   }

@@ -103,4 +103,59 @@ uint32_t chunk_capacity(const gdb_graph* g);
 
 bool graph_ok(gdb_ctx* c, gdb_graph* g);
 
+// Build, run and free a graph: init<<<grid, block>>>(G, ws, src), then a
+// WHILE node whose body is level<<<grid, block>>>(G, ws, ctl, handle).
+// ctl[0..1] must be zero before the launch (the init kernel leaves them).
+template <class Ws>
+inline int graph_while_run(gdb_ctx* c, const void* init, int grid, int block, const gdb::GraphView& G,
+                           const Ws& ws, uint32_t src, const void* level, uint32_t* ctl) {
+  GDB_CUDA(c, cudaMemsetAsync(ctl, 0, 8, c->stream));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaGraphCreate(&graph, 0);
+  cudaGraphConditionalHandle cond = 0;
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault);
+  gdb::GraphView g0 = G;
+  Ws w0 = ws;
+  uint32_t s0 = src;
+  uint32_t* ctl0 = ctl;
+  void* init_args[] = {(void*)&g0, (void*)&w0, (void*)&s0};
+  void* level_args[] = {(void*)&g0, (void*)&w0, (void*)&ctl0, (void*)&cond};
+  cudaGraphNode_t n_init = nullptr, n_cond = nullptr, n_level = nullptr;
+  if (e == cudaSuccess) {
+    cudaKernelNodeParams kp = {};
+    kp.func = (void*)init;
+    kp.gridDim = dim3(grid);
+    kp.blockDim = dim3(block);
+    kp.kernelParams = init_args;
+    e = cudaGraphAddKernelNode(&n_init, graph, nullptr, 0, &kp);
+  }
+  cudaGraphNodeParams cp = {};
+  if (e == cudaSuccess) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    e = cudaGraphAddNode(&n_cond, graph, &n_init, nullptr, 1, &cp);
+  }
+  if (e == cudaSuccess) {
+    cudaKernelNodeParams kp = {};
+    kp.func = (void*)level;
+    kp.gridDim = dim3(grid);
+    kp.blockDim = dim3(block);
+    kp.kernelParams = level_args;
+    e = cudaGraphAddKernelNode(&n_level, cp.conditional.phGraph_out[0], nullptr, 0, &kp);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e == cudaSuccess) e = cudaGraphUpload(exec, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->stream);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return set_cuda_error(c, e, "graph relaunch");
+  return GDB_OK;
+}
+
 }  // namespace gdbi

@@ -224,7 +224,7 @@ static int check_options(const gdb_options* o) {
   if (o->block_size != 0 && (o->block_size < 64 || o->block_size > 1024 || (o->block_size & 31)))
     return GDB_ERR_INVALID;
   if (o->lock < GDB_LOCK_TICKET || o->lock > GDB_LOCK_FREE) return GDB_ERR_INVALID;
-  if (o->barrier < GDB_BARRIER_XF || o->barrier > GDB_BARRIER_XF_FIXED) return GDB_ERR_INVALID;
+  if (o->barrier < GDB_BARRIER_XF || o->barrier > GDB_BARRIER_RELAUNCH_GRAPH) return GDB_ERR_INVALID;
   if (o->schedule < GDB_SCHED_PLAIN || o->schedule > GDB_SCHED_ADAPTIVE) return GDB_ERR_INVALID;
   if (o->max_ctas < 0 || o->oversubscribe < 0) return GDB_ERR_INVALID;
   if (o->xf_release < 0 || o->xf_release > 1) return GDB_ERR_INVALID;

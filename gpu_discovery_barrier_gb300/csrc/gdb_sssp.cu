@@ -146,6 +146,68 @@ __global__ void __launch_bounds__(512, 3) k_sssp_grid(GraphView G, SsspWs ws, ui
   sssp_body(s, G, ws, src);
 }
 
+// Graph-relaunch mode (CUDA-graph WHILE node): an init launch, then one
+// launch per superstep; the last CTA of a superstep advances ctl[0] and
+// sets the loop condition.
+__global__ void k_sssp_init(GraphView G, SsspWs ws, uint32_t src) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
+  for (uint32_t v = t; v < G.V; v += n) {
+    ws.dist[v] = v == src ? 0u : kInf;
+    ws.stamp[v] = 0;
+  }
+  if (t == 0) {
+    for (int i = 0; i < 3; ++i) {
+      ws.qcount[i] = 0;
+      ws.hcount[i] = 0;
+      ws.cursor[i] = 0;
+      ws.hcursor[i] = 0;
+    }
+    *ws.overflow = 0;
+    ws.stats[0] = ws.stats[1] = 0;
+    frontier_seed(G, Frontier{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap,
+                              ws.overflow},
+                  src);
+  }
+}
+
+__global__ void __launch_bounds__(512, 3) k_sssp_glevel(GraphView G, SsspWs ws, uint32_t* ctl,
+                                                        cudaGraphConditionalHandle cond) {
+  __shared__ uint32_t sL;
+  if (threadIdx.x == 0) sL = ld_cg(&ctl[0]);
+  __syncthreads();
+  const uint32_t L = sL;
+  const int old = (L + 2) % 3;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ws.qcount[old] = 0;
+    ws.hcount[old] = 0;
+    ws.cursor[old] = 0;
+    ws.hcursor[old] = 0;
+  }
+  Warps W;
+  W.gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  W.nwarps = (gridDim.x * blockDim.x) >> 5;
+  W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
+  W.nthreads = gridDim.x * blockDim.x;
+  unsigned long long arcs = 0;
+  sssp_step(G, W, ws, L, arcs);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
+  if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ctl[1], 1u) == gridDim.x - 1) {
+      __threadfence();
+      const int nxt = (L + 1) % 3;
+      const bool more = ld_cg(&ws.qcount[nxt]) != 0 || __ldcg(&ws.hcount[nxt]) != 0;
+      ctl[0] = L + 1;
+      ctl[1] = 0;
+      ws.stats[1] = L + 1;
+      cudaGraphSetConditional(cond, more ? 1u : 0u);
+    }
+  }
+}
+
 // ------------------------------------------------------------- Jacobi
 
 struct JacobiWs {
@@ -328,6 +390,17 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
     GDB_CUDA(c, cudaLaunchCooperativeKernel((const void*)k_sssp_grid, grid, block, args, 0, c->stream));
     GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->last.participating = grid;
+    c->last.launched = grid;
+  } else if (kind == GDB_BARRIER_RELAUNCH_GRAPH) {
+    int occ = 0;
+    GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sssp_glevel, block, 0));
+    int grid = occ * c->sm_count;
+    if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
+    uint32_t* ctl = (uint32_t*)(cnt + 192);  // [0] superstep, [1] CTAs done
+    rc = graph_while_run(c, (const void*)k_sssp_init, grid, block, G, ws, src,
+                         (const void*)k_sssp_glevel, ctl);
+    if (rc) return rc;
     c->last.participating = grid;
     c->last.launched = grid;
   } else {

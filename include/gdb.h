@@ -58,8 +58,10 @@ typedef enum {
   GDB_BARRIER_RELAUNCH = 2,  /* one launch per superstep, host reads the stop flag */
   GDB_BARRIER_XF_FIXED = 3,  /* XF over all launched CTAs, no discovery (gbar_cl.h:15-74);
                                 the grid is capped at the occupancy the API reports */
-  GDB_BARRIER_RELAUNCH_GRAPH = 4 /* gdb_barrier_bench only: the relaunches captured
-                                    once in a CUDA graph and replayed */
+  GDB_BARRIER_RELAUNCH_GRAPH = 4 /* one launch per superstep from a CUDA graph: a WHILE
+                                    node whose condition the last CTA of each superstep
+                                    sets -- no host round trip (BFS, SSSP; in
+                                    gdb_barrier_bench: captured relaunches replayed) */
 } gdb_barrier_kind;
 
 /* Schedule of the traversal options per superstep. */

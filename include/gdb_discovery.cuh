@@ -27,6 +27,7 @@ namespace gdb {
 constexpr int kLineInts = 32;                 // one 128-byte line of ints
 constexpr int kPollClosed = 0x40000000;       // lock-free poll: closed bit
 constexpr int kPollCountMask = kPollClosed - 1;
+constexpr unsigned kBarrierSpin = 4096;        // polls before a barrier wait backs off
 
 // discovery_kernel_ctx (common.h:33-48), one contended word per line.
 struct __align__(128) DeviceCtx {
@@ -120,9 +121,11 @@ __device__ __forceinline__ void raise_error(DeviceCtx* c, int code, int where) {
 // Bounded spin: returns false on abort, or when this wait has lasted
 // longer than timeout_ns (then GDB_ERR_TIMEOUT is recorded with `where`).
 // The clock is read only once a wait is not over after a few polls.
+// `pure` polls spin without sleeping (barrier waits are short when every
+// CTA is resident), after which __nanosleep backs the poller off.
 template <class Done>
 __device__ __forceinline__ bool spin_until(DeviceCtx* c, unsigned long long timeout_ns,
-                                           int where, Done done) {
+                                           int where, Done done, unsigned pure = 32) {
   unsigned ns = 0;
   unsigned long long deadline = 0;
   for (unsigned k = 1;; ++k) {
@@ -137,7 +140,7 @@ __device__ __forceinline__ bool spin_until(DeviceCtx* c, unsigned long long time
         return false;
       }
     }
-    if (k > 32) {
+    if (k > pure) {
       __nanosleep(ns);
       ns = ns < 128 ? ns + 16 : 128;
     }
@@ -333,7 +336,7 @@ __device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l) {
           }
         }
         return pending == 0;
-      });
+      }, kBarrierSpin);
       fence_acq_rel_gpu();  // acquire: the slaves' writes before ours
     }
     ok = __syncthreads_and(ok);
@@ -364,10 +367,11 @@ __device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l) {
       fence_acq_rel_gpu();
       if (bcast) {
         aref64(*(unsigned long long*)f).store(tag, cuda::memory_order_relaxed);
-        ok = spin_until(c, l->timeout_ns, 7, [&] { return ld_relaxed64(&c->release) >= tag; });
+        ok = spin_until(c, l->timeout_ns, 7, [&] { return ld_relaxed64(&c->release) >= tag; },
+                        kBarrierSpin);
       } else {
         st_relaxed(f, 1);
-        ok = spin_until(c, l->timeout_ns, 7, [&] { return ld_relaxed(f) == 0; });
+        ok = spin_until(c, l->timeout_ns, 7, [&] { return ld_relaxed(f) == 0; }, kBarrierSpin);
       }
       fence_acq_rel_gpu();
       l->ok = ok;

@@ -51,10 +51,11 @@ def test_bfs(ctx, name, g):
         assert np.array_equal(got, oracle.bfs(g, int(src))), (name, src)
 
 
-@pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC, gdb.BARRIER_RELAUNCH])
+@pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC, gdb.BARRIER_RELAUNCH,
+                                     gdb.BARRIER_RELAUNCH_GRAPH])
 @pytest.mark.parametrize("schedule", [gdb.SCHED_PLAIN, gdb.SCHED_ADAPTIVE])
 def test_bfs_barrier_kinds(barrier, schedule):
-    if barrier == gdb.BARRIER_RELAUNCH and schedule == gdb.SCHED_ADAPTIVE:
+    if barrier in (gdb.BARRIER_RELAUNCH, gdb.BARRIER_RELAUNCH_GRAPH) and schedule == gdb.SCHED_ADAPTIVE:
         pytest.skip("adaptive needs a persistent barrier")
     g = gg.rmat(1 << 13, 16, seed=9)
     with gdb.Ctx(barrier=barrier, schedule=schedule) as c:
@@ -73,7 +74,8 @@ def test_sssp_worklist(ctx, name, g):
         assert np.array_equal(got, oracle.sssp_worklist(gw, int(src))), (name, src)
 
 
-@pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC])
+@pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC,
+                                     gdb.BARRIER_RELAUNCH_GRAPH])
 def test_sssp_barrier_kinds(barrier):
     g = gg.grid(64, 64)
     w = gg.uniform_weights(g, 1, 1000, seed=1)
