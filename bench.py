@@ -51,7 +51,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--apps", default="bfs,sssp,mis,color,bc,mst")
-    p.add_argument("--workload", choices=["rmat", "grid4096"], default="rmat",
+    p.add_argument("--batch-graphs", type=int, default=512)
+    p.add_argument("--no-tune", action="store_true")
+    p.add_argument("--workload", choices=["rmat", "grid4096", "batch"], default="rmat",
                    help="rmat: the R-MAT suite (default); grid4096: the barrier-bound "
                         "4096x4096 grid, BFS and SSSP from the corner per barrier kind")
     return p.parse_args()
@@ -546,6 +548,132 @@ def run_grid(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def run_batch(args, rank, world, local):
+    """Mixed batch: n graphs (V log-uniform in [1e3, 1e6], half R-MAT with
+    edge factor 8..32, half grids with aspect ratio log-uniform in [1, 64]),
+    one BFS and one SSSP from a seeded source each.  The batched form (one
+    union graph, two persistent launches replayed from a captured CUDA
+    graph, autotuned shape and thresholds) against the plain path run graph
+    by graph (2n persistent launches); results compared bit-exact."""
+    import torch
+
+    from gpu_discovery_barrier_gb300 import autotune, gdb, graphgen as gg
+
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    members = gg.mixed_batch(args.batch_graphs, 1000, 1_000_000, seed=1 + rank)
+    gen_s = time.perf_counter() - t0
+    srcs = [m.meta["source"] for m in members]
+    V = sum(m.V for m in members)
+    E = sum(m.E for m in members)
+    with gdb.Ctx() as c:
+        stream = torch.cuda.ExternalStream(c.stream())
+        dev = torch.device("cuda", local)
+        # ---- plain path, graph by graph (device-resident, one pass)
+        Gs = [c.graph(m.row_ptr, m.col, m.w) for m in members]
+        d_b = torch.empty(max(m.V for m in members), dtype=torch.int32, device=dev)
+        d_s = torch.empty_like(d_b)
+        plain_out = []
+        for i in range(min(4, len(members))):                  # warm-up
+            c.bfs_device(Gs[i], srcs[i], d_b.data_ptr())
+            c.sssp_device(Gs[i], srcs[i], d_s.data_ptr())
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        plain_kernel_ms = 0.0
+        ev0.record(stream)
+        for i, m in enumerate(members):
+            c.bfs_device(Gs[i], srcs[i], d_b.data_ptr())
+            plain_kernel_ms += c.last_stats()["kernel_ms"]
+            c.sssp_device(Gs[i], srcs[i], d_s.data_ptr())
+            plain_kernel_ms += c.last_stats()["kernel_ms"]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = ev0.elapsed_time(ev1)
+        # plain results for the comparison (untimed)
+        for i, m in enumerate(members):
+            plain_out.append((c.bfs(Gs[i], srcs[i]), c.sssp(Gs[i], srcs[i])))
+        del Gs
+        # ---- batched form
+        U = c.graph_batch(members)
+        off = U.vertex_offset
+        usrc = [int(off[i]) + s for i, s in enumerate(srcs)]
+        tune = None
+        if not args.no_tune:
+            tune = autotune.tune_batch(c, U, usrc, apps=3, reps=2)
+        with c.batch(U, usrc) as B:
+            for _ in range(args.warmup):
+                B.run()
+            barrier(world)
+            torch.cuda.synchronize()
+            with ClockSampler(local) as clk:
+                ev0.record(stream)
+                for _ in range(args.steps):
+                    B.launch()
+                    B.wait()
+                ev1.record(stream)
+                torch.cuda.synchronize()
+            ms = reduce_max(ev0.elapsed_time(ev1), world)
+            clocks = clk.summary()
+            res = B.results()
+            arcs_bfs, steps_bfs = B.app_stats(gdb.BATCH_BFS)
+            arcs_sssp, steps_sssp = B.app_stats(gdb.BATCH_SSSP)
+            identical = all(
+                np.array_equal(res["bfs"][off[i]:off[i + 1]], plain_out[i][0])
+                and np.array_equal(res["sssp"][off[i]:off[i + 1]], plain_out[i][1])
+                for i in range(len(members)))
+            # work units: arcs of the reached vertices, per query
+            deg = np.concatenate([np.diff(m.row_ptr.astype(np.int64)) for m in members])
+            reached = res["bfs"] != gdb.LONESTAR_INF
+            er = int(deg[reached].sum())
+            vr = int(reached.sum())
+            units = 2 * er
+            value = world * units * args.steps / (ms / 1e3)
+            plain_value = units / (plain_ms / 1e3)
+            # end to end through the host-buffer API: sources in, both
+            # result arrays out, every step
+            e2e = None
+            if not args.no_e2e:
+                B.set_sources(usrc)
+                B.run()
+                B.results()
+                barrier(world)
+                t1 = time.perf_counter()
+                for _ in range(args.steps):
+                    B.set_sources(usrc)
+                    B.run()
+                    B.results()
+                dt = reduce_max(time.perf_counter() - t1, world)
+                e2e = {"value": world * units * args.steps / dt, "unit": "edges/s",
+                       "h2d_bytes_per_step": 4 * len(usrc), "d2h_bytes_per_step": 8 * V}
+    # algorithmic bytes of one replay: BFS + SSSP over the reached part
+    nbytes = (8 * er + 12 * vr + 4 * V) + (12 * er + 12 * vr + 4 * V)
+    peak, peak_kind = peaks()
+    achieved = nbytes / (ms / args.steps / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_bfs_xf + k_sssp_xf (one replay)", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "alg_bytes_per_launch": nbytes, "launch_ms": ms / args.steps, "traffic": None}
+    cfg = {"workload": f"mixed batch: {len(members)} graphs (V log-uniform 1e3..1e6, half R-MAT "
+                       "ef 8..32, half grids aspect 1..64), BFS + SSSP per graph",
+           "V": V, "E": E, "graphs": len(members), "global_batch": world,
+           "parallelism": f"replicas x{world}", "l2": "inputs > L2 (no flush)",
+           "tuned": tune["options"] if tune else None, "generation_s": round(gen_s, 1)}
+    if rank == 0:
+        line = base_line(args, world, value, ms / args.steps, cfg)
+        line["metric"] = "edges/sec (batched BFS + SSSP over the mixed batch)"
+        line["clocks"] = clocks
+        line["e2e"] = e2e
+        line["roofline"] = roof
+        line["cpu_baseline"] = None
+        line["gpu_launches"] = 2 * args.steps
+        line["plain"] = {"value": plain_value, "ms": plain_ms, "kernel_ms_sum": plain_kernel_ms,
+                         "launches": 2 * len(members)}
+        line["speedup_vs_plain"] = value / world / plain_value
+        line["bit_identical"] = bool(identical)
+        line["supersteps"] = {"bfs": steps_bfs, "sssp": steps_sssp}
+        line["arcs_inspected"] = {"bfs": arcs_bfs, "sssp": arcs_sssp}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup(args.gpus)
@@ -553,6 +681,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "grid4096":
         run_grid(args, rank, world, local)
+    elif args.workload == "batch":
+        run_batch(args, rank, world, local)
     else:
         run_gdb(args, rank, world, local)
     if world > 1:

@@ -40,6 +40,7 @@ CUDA_SOURCES = [
     "gdb_mis_color.cu",
     "gdb_bc.cu",
     "gdb_mst.cu",
+    "gdb_batch.cu",
 ]
 
 

@@ -36,6 +36,9 @@ struct BfsWs {
   uint32_t* mode;              // [3] 0 = top-down, 1 = bottom-up, per level slot
   uint32_t qcap, hcap;
   int adaptive;
+  uint32_t alpha, beta;        // direction thresholds of the adaptive schedule
+  const uint32_t* srcs;        // multi-source run when nsrc > 0
+  uint32_t nsrc;
 };
 
 __device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long* p) {
@@ -119,11 +122,12 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
     for (int i = 0; i < 8; ++i) ws.stats[i] = 0;
   }
   if (!s.sync()) return;
-  if (leader) {
+  const Frontier f0{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap, ws.overflow};
+  if (ws.nsrc) {
+    frontier_seed_many(G, f0, W, ws.srcs, ws.nsrc, ws.dist, kInf);
+  } else if (leader) {
     ws.dist[src] = 0;
-    frontier_seed(G, Frontier{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap,
-                              ws.overflow},
-                  src);
+    frontier_seed(G, f0, src);
   }
   if (!s.sync()) return;
   unsigned long long arcs = 0;
@@ -132,7 +136,7 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
   // direction-choice inputs, identical in every CTA: arcs of the frontier
   // (mf) and of the still-unvisited vertices (mu).  acc[k % 3] (stats[4..6])
   // collects the arcs of level k while level k-1 runs.
-  unsigned long long mf = G.row[src + 1] - G.row[src];
+  unsigned long long mf = ws.nsrc ? 0ull : (unsigned long long)(G.row[src + 1] - G.row[src]);
   unsigned long long mu = G.E - mf;
   for (;; ++L) {
     const int cur = L % 3, old = (L + 2) % 3;
@@ -145,8 +149,8 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
         mu = mu > mf ? mu - mf : 0;
       }
       const uint32_t nf = n + (uint32_t)(hp >> 32);
-      if (!bottom_up && mf > mu / 14) bottom_up = true;
-      else if (bottom_up && nf < G.V / 24) bottom_up = false;
+      if (!bottom_up && mf > mu / ws.alpha) bottom_up = true;
+      else if (bottom_up && nf < G.V / ws.beta) bottom_up = false;
     }
     if (leader) {
       ws.qcount[old] = 0;
@@ -271,34 +275,86 @@ __global__ void __launch_bounds__(512, 3) k_bfs_glevel(GraphView G, BfsWs ws, ui
 
 using namespace gdbi;
 
-static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
-  if (!graph_ok(c, g) || !d_dist) return GDB_ERR_INVALID;
-  if (src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+// Workspace of one BFS run: two light queues, two chunk-entry queues, the
+// 512-byte counter block.
+static size_t bfs_layout(const gdb_graph* g, char* base, uint32_t* d_dist, BfsWs* ws, char** cnt_out) {
   const uint32_t V = g->V;
   const uint32_t hcap = chunk_capacity(g);
   Bump b;
   const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
   const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
   const size_t o_cnt = b.take(512);
-  char* base = (char*)workspace(c, b.off);
-  if (!base) return GDB_ERR_OOM;
-  BfsWs ws;
-  ws.dist = d_dist;
-  ws.q[0] = (uint32_t*)(base + o_q0);
-  ws.q[1] = (uint32_t*)(base + o_q1);
-  ws.hc[0] = (uint4*)(base + o_hc0);
-  ws.hc[1] = (uint4*)(base + o_hc1);
+  if (!base) return b.off;
+  ws->dist = d_dist;
+  ws->q[0] = (uint32_t*)(base + o_q0);
+  ws->q[1] = (uint32_t*)(base + o_q1);
+  ws->hc[0] = (uint4*)(base + o_hc0);
+  ws->hc[1] = (uint4*)(base + o_hc1);
   char* cnt = base + o_cnt;
-  ws.stats = (unsigned long long*)cnt;                // 8 x u64
-  ws.hcount = (unsigned long long*)(cnt + 64);        // 3 x u64
-  ws.qcount = (uint32_t*)(cnt + 96);                  // 3
-  ws.cursor = (uint32_t*)(cnt + 112);                 // 3
-  ws.hcursor = (uint32_t*)(cnt + 128);                // 3
-  ws.mode = (uint32_t*)(cnt + 144);                   // 3
-  ws.overflow = (int*)(cnt + 160);
-  ws.qcap = V;
-  ws.hcap = hcap;
+  ws->stats = (unsigned long long*)cnt;                // 8 x u64
+  ws->hcount = (unsigned long long*)(cnt + 64);        // 3 x u64
+  ws->qcount = (uint32_t*)(cnt + 96);                  // 3
+  ws->cursor = (uint32_t*)(cnt + 112);                 // 3
+  ws->hcursor = (uint32_t*)(cnt + 128);                // 3
+  ws->mode = (uint32_t*)(cnt + 144);                   // 3
+  ws->overflow = (int*)(cnt + 160);
+  ws->qcap = V;
+  ws->hcap = hcap;
+  ws->adaptive = 0;
+  ws->alpha = 14;
+  ws->beta = 24;
+  ws->srcs = nullptr;
+  ws->nsrc = 0;
+  *cnt_out = cnt;
+  return b.off;
+}
+
+size_t gdbi::bfs_workspace_bytes(const gdb_graph* g) {
+  return bfs_layout(g, nullptr, nullptr, nullptr, nullptr);
+}
+
+// Enqueue one XF-barrier BFS (counter reset + persistent launch) on
+// `stream` without waiting, so that it can be stream-captured.  `proto`
+// carries the discovery context and flags the launch synchronises through.
+int gdbi::bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
+                      uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto,
+                      int adaptive) {
+  BfsWs ws;
+  char* cnt = nullptr;
+  bfs_layout(g, (char*)wsbase, d_dist, &ws, &cnt);
+  ws.srcs = d_srcs;
+  ws.nsrc = nsrc;
+  ws.adaptive = adaptive;
+  if (c->opt.pull_alpha) ws.alpha = c->opt.pull_alpha;
+  if (c->opt.push_beta) ws.beta = c->opt.push_beta;
+  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, stream));
+  Shape s;
+  int rc = persistent_shape(c, (const void*)k_bfs_xf, c->opt.block_size, 0, &s, false);
+  if (rc) return rc;
+  DiscoveryArgs a = proto;
+  a.expected = std::min(s.grid, s.fit);
+  k_bfs_xf<<<s.grid, c->opt.block_size, 0, stream>>>(a, g->view(), ws, 0u);
+  GDB_CUDA(c, cudaGetLastError());
+  return GDB_OK;
+}
+
+static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_srcs, uint32_t nsrc,
+                   uint32_t* d_dist) {
+  if (!graph_ok(c, g) || !d_dist || (nsrc && !d_srcs)) return GDB_ERR_INVALID;
+  if (!nsrc && src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  BfsWs ws;
+  char* cnt = nullptr;
+  char* base = (char*)workspace(c, bfs_layout(g, nullptr, nullptr, nullptr, nullptr));
+  if (!base) return GDB_ERR_OOM;
+  bfs_layout(g, base, d_dist, &ws, &cnt);
   ws.adaptive = c->opt.schedule == GDB_SCHED_ADAPTIVE;
+  if (c->opt.pull_alpha) ws.alpha = c->opt.pull_alpha;
+  if (c->opt.push_beta) ws.beta = c->opt.push_beta;
+  ws.srcs = d_srcs;
+  ws.nsrc = nsrc;
+  if (nsrc && c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED &&
+      c->opt.barrier != GDB_BARRIER_GRID_SYNC)
+    return set_error(c, GDB_ERR_UNSUPPORTED, "multi-source BFS needs a persistent barrier");
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
   const GraphView G = g->view();
   const int block = c->opt.block_size;
@@ -394,7 +450,33 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
 extern "C" {
 
 int gdb_bfs_device(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
-  return bfs_run(c, g, src, d_dist);
+  return bfs_run(c, g, src, nullptr, 0, d_dist);
+}
+
+int gdb_bfs_multi_device(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc,
+                         uint32_t* d_dist) {
+  if (nsrc == 0) return GDB_ERR_INVALID;
+  return bfs_run(c, g, 0, d_sources, nsrc, d_dist);
+}
+
+int gdb_bfs_multi(gdb_ctx* c, gdb_graph* g, const uint32_t* sources, uint32_t nsrc, uint32_t* dist) {
+  if (!graph_ok(c, g) || !dist || !sources || nsrc == 0) return GDB_ERR_INVALID;
+  for (uint32_t i = 0; i < nsrc; ++i)
+    if (sources[i] >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  const size_t nb = (size_t)g->V * 4;
+  char* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, nb + (size_t)nsrc * 4, c->stream));
+  cudaError_t e = cudaMemcpyAsync(d + nb, sources, (size_t)nsrc * 4, cudaMemcpyHostToDevice, c->stream);
+  int rc = e == cudaSuccess ? bfs_run(c, g, 0, (const uint32_t*)(d + nb), nsrc, (uint32_t*)d)
+                            : set_cuda_error(c, e, "sources upload");
+  if (rc == GDB_OK) {
+    e = cudaMemcpyAsync(dist, d, nb, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "dist read-back");
+  }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
 }
 
 int gdb_bfs(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* dist) {
@@ -403,7 +485,7 @@ int gdb_bfs(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* dist) {
   // the output lives after the kernel workspace, which bfs_run sizes itself
   uint32_t* d = nullptr;
   GDB_CUDA(c, cudaMallocAsync((void**)&d, (size_t)g->V * 4, c->stream));
-  int rc = bfs_run(c, g, src, d);
+  int rc = bfs_run(c, g, src, nullptr, 0, d);
   if (rc == GDB_OK) {
     cudaError_t e = cudaMemcpyAsync(dist, d, (size_t)g->V * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -551,6 +633,10 @@ extern "C" int gdb_bfs_noalloc(const uint32_t* d_row_ptr, const uint32_t* d_col,
   ws.qcap = V;
   ws.hcap = 1;
   ws.adaptive = 0;
+  ws.alpha = 14;
+  ws.beta = 24;
+  ws.srcs = nullptr;
+  ws.nsrc = 0;
   DiscoveryArgs a;
   a.ctx = (gdb::DeviceCtx*)(base + kNaCtx);
   a.flags = (int*)(base + kNaFlags);

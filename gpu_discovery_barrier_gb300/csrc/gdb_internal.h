@@ -103,6 +103,17 @@ uint32_t chunk_capacity(const gdb_graph* g);
 
 bool graph_ok(gdb_ctx* c, gdb_graph* g);
 
+// Stream-capturable XF launches over a caller-owned workspace (the batch
+// form): bytes of one run's workspace, and an enqueue that only issues a
+// counter reset and the persistent launch on `stream`.  `proto` supplies the
+// discovery context, flags, lock, timeout and release form.
+size_t bfs_workspace_bytes(const gdb_graph* g);
+size_t sssp_workspace_bytes(const gdb_graph* g);
+int bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
+                uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto, int adaptive);
+int sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
+                 uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto);
+
 // Build, run and free a graph: init<<<grid, block>>>(G, ws, src), then a
 // WHILE node whose body is level<<<grid, block>>>(G, ws, ctl, handle).
 // ctl[0..1] must be zero before the launch (the init kernel leaves them).

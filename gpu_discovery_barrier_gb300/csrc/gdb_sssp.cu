@@ -35,6 +35,8 @@ struct SsspWs {
   int* overflow;
   unsigned long long* stats;   // [0] arcs, [1] supersteps
   uint32_t qcap, hcap;
+  const uint32_t* srcs;        // multi-source run when nsrc > 0
+  uint32_t nsrc;
 };
 
 __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, const SsspWs& ws,
@@ -106,12 +108,13 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
     ws.stats[0] = ws.stats[1] = 0;
   }
   if (!s.sync()) return;
-  if (leader) {
+  const Frontier f0{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap, ws.overflow};
+  if (ws.nsrc) {
+    frontier_seed_many(G, f0, W, ws.srcs, ws.nsrc, ws.dist, kInf);
+  } else if (leader) {
     ws.dist[src] = 0;
     ws.stamp[src] = 0;
-    frontier_seed(G, Frontier{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap,
-                              ws.overflow},
-                  src);
+    frontier_seed(G, f0, src);
   }
   if (!s.sync()) return;
   unsigned long long arcs = 0;
@@ -327,10 +330,9 @@ __global__ void __launch_bounds__(512, 3) k_jacobi_xf(DiscoveryArgs a, GraphView
 
 using namespace gdbi;
 
-static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
-  if (!graph_ok(c, g) || !d_dist) return GDB_ERR_INVALID;
-  if (src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
-  if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
+// Workspace of one worklist SSSP run: stamps, two light queues, two
+// chunk-entry queues, the 512-byte counter block.
+static size_t sssp_layout(const gdb_graph* g, char* base, uint32_t* d_dist, SsspWs* ws, char** cnt_out) {
   const uint32_t V = g->V;
   const uint32_t hcap = chunk_capacity(g);
   Bump b;
@@ -338,24 +340,65 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
   const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
   const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
   const size_t o_cnt = b.take(512);
-  char* base = (char*)workspace(c, b.off);
+  if (!base) return b.off;
+  ws->dist = d_dist;
+  ws->stamp = (uint32_t*)(base + o_st);
+  ws->q[0] = (uint32_t*)(base + o_q0);
+  ws->q[1] = (uint32_t*)(base + o_q1);
+  ws->hc[0] = (uint4*)(base + o_hc0);
+  ws->hc[1] = (uint4*)(base + o_hc1);
+  char* cnt = base + o_cnt;
+  ws->stats = (unsigned long long*)cnt;
+  ws->hcount = (unsigned long long*)(cnt + 64);
+  ws->qcount = (uint32_t*)(cnt + 96);
+  ws->cursor = (uint32_t*)(cnt + 112);
+  ws->hcursor = (uint32_t*)(cnt + 128);
+  ws->overflow = (int*)(cnt + 160);
+  ws->qcap = V;
+  ws->hcap = hcap;
+  ws->srcs = nullptr;
+  ws->nsrc = 0;
+  *cnt_out = cnt;
+  return b.off;
+}
+
+size_t gdbi::sssp_workspace_bytes(const gdb_graph* g) {
+  return sssp_layout(g, nullptr, nullptr, nullptr, nullptr);
+}
+
+int gdbi::sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
+                       uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto) {
+  if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
+  SsspWs ws;
+  char* cnt = nullptr;
+  sssp_layout(g, (char*)wsbase, d_dist, &ws, &cnt);
+  ws.srcs = d_srcs;
+  ws.nsrc = nsrc;
+  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, stream));
+  Shape s;
+  int rc = persistent_shape(c, (const void*)k_sssp_xf, c->opt.block_size, 0, &s, false);
+  if (rc) return rc;
+  DiscoveryArgs a = proto;
+  a.expected = std::min(s.grid, s.fit);
+  k_sssp_xf<<<s.grid, c->opt.block_size, 0, stream>>>(a, g->view(), ws, 0u);
+  GDB_CUDA(c, cudaGetLastError());
+  return GDB_OK;
+}
+
+static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_srcs, uint32_t nsrc,
+                    uint32_t* d_dist) {
+  if (!graph_ok(c, g) || !d_dist || (nsrc && !d_srcs)) return GDB_ERR_INVALID;
+  if (!nsrc && src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
+  if (nsrc && c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH)
+    return set_error(c, GDB_ERR_UNSUPPORTED, "multi-source SSSP needs a persistent barrier");
+  char* base = (char*)workspace(c, sssp_layout(g, nullptr, nullptr, nullptr, nullptr));
   if (!base) return GDB_ERR_OOM;
   SsspWs ws;
-  ws.dist = d_dist;
-  ws.stamp = (uint32_t*)(base + o_st);
-  ws.q[0] = (uint32_t*)(base + o_q0);
-  ws.q[1] = (uint32_t*)(base + o_q1);
-  ws.hc[0] = (uint4*)(base + o_hc0);
-  ws.hc[1] = (uint4*)(base + o_hc1);
-  char* cnt = base + o_cnt;
-  ws.stats = (unsigned long long*)cnt;
-  ws.hcount = (unsigned long long*)(cnt + 64);
-  ws.qcount = (uint32_t*)(cnt + 96);
-  ws.cursor = (uint32_t*)(cnt + 112);
-  ws.hcursor = (uint32_t*)(cnt + 128);
-  ws.overflow = (int*)(cnt + 160);
-  ws.qcap = V;
-  ws.hcap = hcap;
+  char* cnt = nullptr;
+  sssp_layout(g, base, d_dist, &ws, &cnt);
+  ws.srcs = d_srcs;
+  ws.nsrc = nsrc;
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
   const GraphView G = g->view();
   const int block = c->opt.block_size;
@@ -498,14 +541,40 @@ int gdb_sssp_jacobi(gdb_ctx* c, gdb_graph* g, uint32_t src, int32_t* cost) {
 }
 
 int gdb_sssp_device(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* d_dist) {
-  return sssp_run(c, g, src, d_dist);
+  return sssp_run(c, g, src, nullptr, 0, d_dist);
+}
+
+int gdb_sssp_multi_device(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc,
+                          uint32_t* d_dist) {
+  if (nsrc == 0) return GDB_ERR_INVALID;
+  return sssp_run(c, g, 0, d_sources, nsrc, d_dist);
+}
+
+int gdb_sssp_multi(gdb_ctx* c, gdb_graph* g, const uint32_t* sources, uint32_t nsrc, uint32_t* dist) {
+  if (!graph_ok(c, g) || !dist || !sources || nsrc == 0) return GDB_ERR_INVALID;
+  for (uint32_t i = 0; i < nsrc; ++i)
+    if (sources[i] >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  const size_t nb = (size_t)g->V * 4;
+  char* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, nb + (size_t)nsrc * 4, c->stream));
+  cudaError_t e = cudaMemcpyAsync(d + nb, sources, (size_t)nsrc * 4, cudaMemcpyHostToDevice, c->stream);
+  int rc = e == cudaSuccess ? sssp_run(c, g, 0, (const uint32_t*)(d + nb), nsrc, (uint32_t*)d)
+                            : set_cuda_error(c, e, "sources upload");
+  if (rc == GDB_OK) {
+    e = cudaMemcpyAsync(dist, d, nb, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "dist read-back");
+  }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
 }
 
 int gdb_sssp(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* dist) {
   if (!graph_ok(c, g) || !dist) return GDB_ERR_INVALID;
   uint32_t* d = nullptr;
   GDB_CUDA(c, cudaMallocAsync((void**)&d, (size_t)g->V * 4, c->stream));
-  int rc = sssp_run(c, g, src, d);
+  int rc = sssp_run(c, g, src, nullptr, 0, d);
   if (rc == GDB_OK) {
     cudaError_t e = cudaMemcpyAsync(dist, d, (size_t)g->V * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

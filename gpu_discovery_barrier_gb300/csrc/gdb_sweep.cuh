@@ -252,6 +252,25 @@ __device__ __forceinline__ void frontier_seed(const GraphView& G, const Frontier
   }
 }
 
+// Many sources at once: the grid's warps push every source not seen before
+// (CAS on its distance from `unreached` to 0) into frontier F.  Used for
+// batches: on a disjoint union of graphs with one source per graph, each
+// vertex is reached only from its own graph's source.
+__device__ __forceinline__ void frontier_seed_many(const GraphView& G, const Frontier& F,
+                                                   const Warps& W, const uint32_t* srcs,
+                                                   uint32_t nsrc, uint32_t* dist,
+                                                   uint32_t unreached) {
+  const int lane = lane_id();
+  for (uint32_t base = W.gwarp * 32; base < nsrc; base += W.nwarps * 32) {
+    const uint32_t i = base + lane;
+    bool want = i < nsrc;
+    const uint32_t v = want ? __ldg(&srcs[i]) : 0u;
+    if (v >= G.V) want = false;  // out-of-range sources are ignored
+    if (want) want = atomicCAS(&dist[v], unreached, 0u) == unreached;
+    frontier_push(G, F, want, v);
+  }
+}
+
 // Arc range [b, e) of heavy chunk entry `ent`.
 __device__ __forceinline__ void chunk_range(const GraphView& G, const uint4& ent, uint32_t& b,
                                             uint32_t& e) {

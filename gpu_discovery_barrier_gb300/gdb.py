@@ -23,6 +23,7 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libgdb.so"
 
+ABI_VERSION = 2  # GDB_ABI_VERSION of include/gdb.h
 LONESTAR_INF = 1_000_000_000
 PANNOTIA_BIG = 99_999_999
 
@@ -44,7 +45,8 @@ class GdbError(RuntimeError):
 class Options(C.Structure):
     _fields_ = [("device", C.c_int), ("block_size", C.c_int), ("max_ctas", C.c_int),
                 ("oversubscribe", C.c_int), ("lock", C.c_int), ("barrier", C.c_int),
-                ("schedule", C.c_int), ("xf_release", C.c_int), ("timeout_ns", C.c_uint64)]
+                ("schedule", C.c_int), ("xf_release", C.c_int), ("timeout_ns", C.c_uint64),
+                ("pull_alpha", C.c_uint32), ("push_beta", C.c_uint32)]
 
 
 class RunStats(C.Structure):
@@ -117,8 +119,24 @@ SIGNATURES = [
     ("gdb_bc_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
     ("gdb_mst", C.c_int, [_P, _P, C.POINTER(MstResult), _P]),
     ("gdb_mst_device", C.c_int, [_P, _P, _P, _P]),
+    ("gdb_bfs_multi", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_bfs_multi_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_sssp_multi", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_sssp_multi_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_graph_create_batch", C.c_int, [_P, C.c_uint32, _P, _P, _P, _P, _P, _P, C.POINTER(_P)]),
+    ("gdb_batch_create", C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, C.POINTER(_P)]),
+    ("gdb_batch_set_sources", C.c_int, [_P, _P]),
+    ("gdb_batch_launch", C.c_int, [_P]),
+    ("gdb_batch_wait", C.c_int, [_P, C.POINTER(C.c_double)]),
+    ("gdb_batch_run", C.c_int, [_P, C.POINTER(C.c_double)]),
+    ("gdb_batch_results", C.c_int, [_P, _P, _P]),
+    ("gdb_batch_device_result", _P, [_P, C.c_uint32]),
+    ("gdb_batch_app_stats", C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]),
+    ("gdb_batch_destroy", C.c_int, [_P]),
     ("gdb_bfs_noalloc", C.c_int, [_P, _P, C.c_uint32, C.c_uint64, C.c_uint32, _P, _P]),
 ]
+
+BATCH_BFS, BATCH_SSSP = 1, 2
 
 NOALLOC_MAX_VERTICES = 1 << 20
 
@@ -132,6 +150,15 @@ def bfs_noalloc(d_row_ptr: int, d_col: int, V: int, E: int, src: int, d_dist: in
         raise GdbError(rc, "gdb_bfs_noalloc")
 
 
+class DeviceArray:
+    """A library-owned device array exposed through __cuda_array_interface__
+    (zero copy), e.g. ``torch.as_tensor(DeviceArray(p, n), device="cuda")``."""
+
+    def __init__(self, ptr: int, n: int, typestr: str = "<u4"):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
 def lib() -> C.CDLL:
     """Load lib/libgdb.so; raises when it has not been built."""
     global _LIB
@@ -143,6 +170,8 @@ def lib() -> C.CDLL:
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args
+        if L.gdb_abi_version() != ABI_VERSION:
+            raise GdbError(-1, "libgdb", f"ABI {L.gdb_abi_version()} != {ABI_VERSION}: rebuild")
         _LIB = L
     return _LIB
 
@@ -302,6 +331,27 @@ class Ctx:
             out["arc_in_mst"] = flags[: g.E]
         return out
 
+    # -- multi-source and batched forms (no reference counterpart)
+    def bfs_multi(self, g: "Graph", sources) -> np.ndarray:
+        s = np.ascontiguousarray(sources, dtype=np.uint32)
+        out = np.empty(g.V, dtype=np.uint32)
+        self.check(self._lib.gdb_bfs_multi(self.h, g.h, _ptr(s), len(s), _ptr(out)), "gdb_bfs_multi")
+        return out
+
+    def sssp_multi(self, g: "Graph", sources) -> np.ndarray:
+        s = np.ascontiguousarray(sources, dtype=np.uint32)
+        out = np.empty(g.V, dtype=np.uint32)
+        self.check(self._lib.gdb_sssp_multi(self.h, g.h, _ptr(s), len(s), _ptr(out)), "gdb_sssp_multi")
+        return out
+
+    def graph_batch(self, graphs, weights: bool = True) -> "Graph":
+        """Disjoint union of CSR graphs (objects with row_ptr, col and w);
+        the result's ``vertex_offset`` maps member i to its vertex range."""
+        return Graph.batch(self, graphs, weights)
+
+    def batch(self, g: "Graph", sources, apps: int = 3) -> "Batch":
+        return Batch(self, g, sources, apps)
+
     # -- applications on device buffers (integer device pointers)
     def bfs_device(self, g: "Graph", src: int, d_dist: int) -> None:
         self.check(self._lib.gdb_bfs_device(self.h, g.h, src, d_dist), "gdb_bfs_device")
@@ -323,6 +373,14 @@ class Ctx:
 
     def mst_device(self, g: "Graph", d_result: int, d_flags: int | None = None) -> None:
         self.check(self._lib.gdb_mst_device(self.h, g.h, d_result, d_flags), "gdb_mst_device")
+
+    def bfs_multi_device(self, g: "Graph", d_sources: int, nsrc: int, d_dist: int) -> None:
+        self.check(self._lib.gdb_bfs_multi_device(self.h, g.h, d_sources, nsrc, d_dist),
+                   "gdb_bfs_multi_device")
+
+    def sssp_multi_device(self, g: "Graph", d_sources: int, nsrc: int, d_dist: int) -> None:
+        self.check(self._lib.gdb_sssp_multi_device(self.h, g.h, d_sources, nsrc, d_dist),
+                   "gdb_sssp_multi_device")
 
 
 class Graph:
@@ -352,6 +410,27 @@ class Graph:
                                                 _ptr(self._w), C.byref(h)), "gdb_graph_create")
         self.h = h
 
+    @classmethod
+    def batch(cls, ctx: Ctx, graphs, weights: bool = True) -> "Graph":
+        n = len(graphs)
+        rps = [np.ascontiguousarray(g.row_ptr, dtype=np.uint32) for g in graphs]
+        cols = [np.ascontiguousarray(g.col, dtype=np.uint32) for g in graphs]
+        ws = [np.ascontiguousarray(g.w, dtype=np.uint32) for g in graphs] if weights else None
+        Vs = np.array([r.shape[0] - 1 for r in rps], dtype=np.uint32)
+        Es = np.array([c.shape[0] for c in cols], dtype=np.uint64)
+        arr = lambda xs: (C.c_void_p * n)(*[x.ctypes.data for x in xs])  # noqa: E731
+        rp_a, col_a = arr(rps), arr(cols)
+        w_a = arr(ws) if weights else None
+        off = np.empty(n + 1, dtype=np.uint32)
+        h = _P()
+        ctx.check(ctx._lib.gdb_graph_create_batch(ctx.h, n, _ptr(Vs), _ptr(Es), rp_a, col_a, w_a,
+                                                  _ptr(off), C.byref(h)), "gdb_graph_create_batch")
+        self = cls.__new__(cls)
+        self.ctx, self.h = ctx, h
+        self.V, self.E = int(off[n]), int(Es.sum())
+        self.vertex_offset = off
+        return self
+
     def set_weights(self, w: np.ndarray) -> None:
         self._w = np.ascontiguousarray(w, dtype=np.uint32)
         self.ctx.check(self.ctx._lib.gdb_graph_set_weights(self.h, _ptr(self._w)), "gdb_graph_set_weights")
@@ -366,6 +445,76 @@ class Graph:
         if getattr(self, "h", None) and self.ctx.h:
             self.ctx._lib.gdb_graph_destroy(self.h)
         self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """A gdb_batch: BFS and/or SSSP from one source per member graph of a
+    batch union, captured once into a CUDA graph and replayed by run()."""
+
+    def __init__(self, ctx: Ctx, g: Graph, sources, apps: int = BATCH_BFS | BATCH_SSSP):
+        self.ctx, self.g, self.apps = ctx, g, apps
+        s = np.ascontiguousarray(sources, dtype=np.uint32)
+        self.nsrc = len(s)
+        h = _P()
+        ctx.check(ctx._lib.gdb_batch_create(ctx.h, g.h, apps, _ptr(s), len(s), C.byref(h)),
+                  "gdb_batch_create")
+        self.h = h
+
+    def set_sources(self, sources) -> None:
+        s = np.ascontiguousarray(sources, dtype=np.uint32)
+        if len(s) != self.nsrc:
+            raise GdbError(-1, "gdb_batch_set_sources", "source count differs from the batch's")
+        self.ctx.check(self.ctx._lib.gdb_batch_set_sources(self.h, _ptr(s)), "gdb_batch_set_sources")
+
+    def run(self) -> float:
+        ms = C.c_double()
+        self.ctx.check(self.ctx._lib.gdb_batch_run(self.h, C.byref(ms)), "gdb_batch_run")
+        return ms.value
+
+    def launch(self) -> None:
+        self.ctx.check(self.ctx._lib.gdb_batch_launch(self.h), "gdb_batch_launch")
+
+    def wait(self) -> float:
+        ms = C.c_double()
+        self.ctx.check(self.ctx._lib.gdb_batch_wait(self.h, C.byref(ms)), "gdb_batch_wait")
+        return ms.value
+
+    def results(self) -> dict:
+        out = {}
+        b = np.empty(self.g.V, dtype=np.uint32) if self.apps & BATCH_BFS else None
+        s = np.empty(self.g.V, dtype=np.uint32) if self.apps & BATCH_SSSP else None
+        self.ctx.check(self.ctx._lib.gdb_batch_results(self.h, _ptr(b), _ptr(s)), "gdb_batch_results")
+        if b is not None:
+            out["bfs"] = b
+        if s is not None:
+            out["sssp"] = s
+        return out
+
+    def device_result(self, app: int) -> int:
+        return self.ctx._lib.gdb_batch_device_result(self.h, app) or 0
+
+    def app_stats(self, app: int) -> tuple[int, int]:
+        arcs, steps = C.c_uint64(), C.c_uint32()
+        self.ctx.check(self.ctx._lib.gdb_batch_app_stats(self.h, app, C.byref(arcs), C.byref(steps)),
+                       "gdb_batch_app_stats")
+        return arcs.value, steps.value
+
+    def close(self) -> None:
+        if getattr(self, "h", None) and self.ctx.h:
+            self.ctx._lib.gdb_batch_destroy(self.h)
+        self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def __del__(self):
         try:

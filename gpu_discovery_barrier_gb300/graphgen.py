@@ -178,3 +178,47 @@ def from_edges(V: int, pairs, weights=None, symmetric: bool = True) -> CSR:
     col = np.array([v for (_u, v) in keys], dtype=np.uint32)
     w = np.array([arcs[k] for k in keys], dtype=np.uint32) if weights is not None else None
     return CSR(rp, col, w, f"edges_V{V}")
+
+
+def _splitmix64(x: int) -> int:
+    x = (x + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    z = x
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return z ^ (z >> 31)
+
+
+def _unit(seed: int, i: int, k: int) -> float:
+    """Counter-based uniform in [0, 1) for member i, draw k."""
+    return (_splitmix64((seed << 40) ^ (i << 8) ^ k) >> 11) / float(1 << 53)
+
+
+def mixed_batch(n: int, vmin: int = 1000, vmax: int = 1_000_000, seed: int = 1,
+                max_aspect: float = 64.0) -> list[CSR]:
+    """The mixed batch workload: n graphs with vertex counts log-uniform in
+    [vmin, vmax]; even members are R-MAT (edge factor uniform in 8..32,
+    (a,b,c,d) = (0.57,0.19,0.19,0.05)), odd members 2-D grids whose aspect
+    ratio is log-uniform in [1, max_aspect].  Each member carries weights
+    (R-MAT uniform [1,255], grid uniform [1,1000]) and meta["source"], one
+    seeded non-isolated vertex."""
+    out = []
+    lo, hi = np.log(vmin), np.log(vmax)
+    for i in range(n):
+        V = int(round(np.exp(lo + _unit(seed, i, 0) * (hi - lo))))
+        gseed = (seed << 20) + i
+        if i % 2 == 0:
+            ef = 8 + int(_unit(seed, i, 1) * 25)
+            g = rmat(V, ef, seed=gseed)
+            w = uniform_weights(g, 1, 255, gseed)
+        else:
+            aspect = float(np.exp(_unit(seed, i, 2) * np.log(max_aspect)))
+            rows = max(1, int(round(np.sqrt(V / aspect))))
+            cols = max(1, int(round(V / rows)))
+            g = grid(rows, cols)
+            w = uniform_weights(g, 1, 1000, gseed)
+        g = g.with_weights(w)
+        s = sources(g, 1, gseed)
+        g.meta["source"] = int(s[0]) if len(s) else 0
+        g.meta["kind"] = "rmat" if i % 2 == 0 else "grid"
+        out.append(g)
+    return out

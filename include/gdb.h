@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GDB_ABI_VERSION 1
+#define GDB_ABI_VERSION 2
 
 /* Sentinels of the reference kernels. */
 #define GDB_LONESTAR_INF 1000000000u /* lonestar/apps/bfs/kernel/bfs_common.cl:35 */
@@ -83,6 +83,11 @@ typedef struct {
   int xf_release;      /* XF release form: 0 = master clears every slave's
                           flag (the reference's), 1 = one broadcast epoch word */
   uint64_t timeout_ns; /* limit for every device spin (0 = 2e9) */
+  /* direction-optimising BFS thresholds (GDB_SCHED_ADAPTIVE): switch to
+     pull when frontier arcs > unvisited arcs / pull_alpha, back to push
+     when the frontier has < V / push_beta vertices (0 = 14 / 24) */
+  uint32_t pull_alpha;
+  uint32_t push_beta;
 } gdb_options;
 
 typedef struct {
@@ -222,6 +227,56 @@ int gdb_bc_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_
  * mst_common.cl:41-194, mst_port_kernel.cl:35-82). */
 int gdb_mst(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* result, uint8_t* arc_in_mst);
 int gdb_mst_device(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* d_result, uint8_t* d_arc_in_mst);
+
+/* ------------------------------------------------ multi-source forms */
+/* No reference counterpart (they serve the batched form).  Every vertex
+ * takes its level / distance from the nearest of the nsrc sources, as from
+ * a super-source with zero-weight arcs to each of them; on a disjoint union
+ * of graphs with one source per member graph this is every member's own
+ * single-source answer.  Persistent barriers only (XF, XF_FIXED,
+ * GRID_SYNC); other kinds return GDB_ERR_UNSUPPORTED.  The host forms check
+ * the sources; the device forms ignore sources >= V. */
+int gdb_bfs_multi(gdb_ctx* ctx, gdb_graph* g, const uint32_t* sources, uint32_t nsrc, uint32_t* dist);
+int gdb_bfs_multi_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc,
+                         uint32_t* d_dist);
+int gdb_sssp_multi(gdb_ctx* ctx, gdb_graph* g, const uint32_t* sources, uint32_t nsrc, uint32_t* dist);
+int gdb_sssp_multi_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc,
+                          uint32_t* d_dist);
+
+/* ---------------------------------------------------------- batched form */
+/* No reference counterpart.  n host CSR graphs packed into one disjoint
+ * union: member i's vertex v becomes vertex_offset[i] + v (vertex_offset:
+ * n + 1 entries out, nullable).  w = NULL, or n weight arrays.  The union
+ * must satisfy V < 2^31 and E < 2^32. */
+int gdb_graph_create_batch(gdb_ctx* ctx, uint32_t n, const uint32_t* V, const uint64_t* E,
+                           const uint32_t* const* row_ptr, const uint32_t* const* col,
+                           const uint32_t* const* w, uint32_t* vertex_offset, gdb_graph** out);
+
+#define GDB_BATCH_BFS 1u
+#define GDB_BATCH_SSSP 2u
+typedef struct gdb_batch gdb_batch;
+/* Capture the persistent launches of `apps` (GDB_BATCH_* mask) over graph g
+ * from the nsrc host sources (union vertex ids) into one CUDA graph, with a
+ * workspace, result arrays, discovery context and barrier flags owned by
+ * the batch.  Launch shape (block_size, max_ctas), lock, schedule and
+ * timeout come from ctx's options at this call; the XF barrier uses the
+ * per-slave release form (valid on every replay).  g must outlive b. */
+int gdb_batch_create(gdb_ctx* ctx, gdb_graph* g, uint32_t apps, const uint32_t* sources,
+                     uint32_t nsrc, gdb_batch** out);
+/* Replace the sources (same count) read by the next replay. */
+int gdb_batch_set_sources(gdb_batch* b, const uint32_t* sources);
+/* Replay on ctx's stream without waiting / wait for the replay, check the
+ * device status and counters; *ms = device time of the replay (nullable). */
+int gdb_batch_launch(gdb_batch* b);
+int gdb_batch_wait(gdb_batch* b, double* ms);
+int gdb_batch_run(gdb_batch* b, double* ms); /* launch + wait */
+/* Copy the last replay's results to host arrays of V entries (NULL skips). */
+int gdb_batch_results(gdb_batch* b, uint32_t* bfs_dist, uint32_t* sssp_dist);
+/* Device array (V entries) of one app's results; NULL if not captured. */
+const uint32_t* gdb_batch_device_result(gdb_batch* b, uint32_t app);
+/* Arcs inspected and barrier intervals of one app in the last replay. */
+int gdb_batch_app_stats(gdb_batch* b, uint32_t app, uint64_t* arcs, uint32_t* supersteps);
+int gdb_batch_destroy(gdb_batch* b);
 
 /* -------------------------------------------- allocation-free BFS variant */
 /* No counterpart in the reference: an extra entry point for callers that

@@ -42,5 +42,35 @@ def test_library_exports_every_declared_symbol():
 def test_no_compute_calls_needed_for_abi_version():
     from gpu_discovery_barrier_gb300 import gdb
 
-    assert gdb.lib().gdb_abi_version() == 1
+    assert gdb.lib().gdb_abi_version() == gdb.ABI_VERSION
     assert gdb.lib().gdb_status_string(-4) == b"GDB_ERR_TIMEOUT"
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes structures have the C structs' sizes and field offsets
+    (compiled here with gcc against include/gdb.h)."""
+    import shutil
+    import subprocess
+
+    from gpu_discovery_barrier_gb300 import gdb
+
+    if not shutil.which("gcc"):
+        pytest.skip("no gcc")
+    structs = {"gdb_options": gdb.Options, "gdb_run_stats": gdb.RunStats,
+               "gdb_mst_result": gdb.MstResult, "gdb_device_info": gdb.DeviceInfo}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gdb.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{ROOT / 'include'}", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
