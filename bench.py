@@ -508,13 +508,16 @@ def run_grid(args, rank, world, local):
     w = gg.uniform_weights(g, 1, 1000, seed=1)
     dev = torch.device("cuda", local)
     d_out = torch.empty(g.V, dtype=torch.int32, device=dev)
-    kinds = {"xf": gdb.BARRIER_XF, "grid_sync": gdb.BARRIER_GRID_SYNC,
-             "relaunch": gdb.BARRIER_RELAUNCH, "relaunch_graph": gdb.BARRIER_RELAUNCH_GRAPH}
+    kinds = {"xf": (gdb.BARRIER_XF, gdb.SCHED_PLAIN),
+             "xf_adaptive": (gdb.BARRIER_XF, gdb.SCHED_ADAPTIVE),
+             "grid_sync": (gdb.BARRIER_GRID_SYNC, gdb.SCHED_PLAIN),
+             "relaunch": (gdb.BARRIER_RELAUNCH, gdb.SCHED_PLAIN),
+             "relaunch_graph": (gdb.BARRIER_RELAUNCH_GRAPH, gdb.SCHED_PLAIN)}
     res = {}
     with gdb.Ctx() as c:
         G = c.graph(g.row_ptr, g.col, w)
-        for name, kind in kinds.items():
-            c.set_options(barrier=kind)
+        for name, (kind, sched) in kinds.items():
+            c.set_options(barrier=kind, schedule=sched)
             r = {}
             for app in ("bfs", "sssp"):
                 if app == "sssp" and kind == gdb.BARRIER_RELAUNCH:
@@ -530,12 +533,16 @@ def run_grid(args, rank, world, local):
                     steps = st["supersteps"]
                 t = statistics.median(ms)
                 r[app] = {"ms": t, "supersteps": steps, "edges_per_s": g.E / (t / 1e3),
-                          "us_per_superstep": 1e3 * t / max(steps, 1)}
+                          "us_per_superstep": 1e3 * t / max(steps, 1),
+                          "arcs_inspected": st["edges_processed"]}
+                if app == "sssp":
+                    r[app]["delta"] = st["sssp_delta"]
+                    r[app]["phases"] = st["phases"]
             ns, groups = c.barrier_bench(kind, 512, 2000)
             r["barrier_ns"] = ns
             r["barrier_ctas"] = groups
             res[name] = r
-        c.set_options(barrier=gdb.BARRIER_XF)
+        c.set_options(barrier=gdb.BARRIER_XF, schedule=gdb.SCHED_PLAIN)
     xf = res["xf"]
     value = 2 * g.E / ((xf["bfs"]["ms"] + xf["sssp"]["ms"]) / 1e3)
     cfg = {"workload": "grid 4096x4096, BFS + SSSP from vertex 0", "V": g.V, "E": g.E,

@@ -41,6 +41,7 @@ struct gdb_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint32_t delta = 0;         // near-far bucket width of the SSSP launch
   unsigned long long host_stats[2][8] = {};
 };
 
@@ -144,6 +145,7 @@ int gdb_batch_create(gdb_ctx* c, gdb_graph* g, uint32_t apps, const uint32_t* so
   e = cudaMemcpyAsync(b->d_srcs, sources, (size_t)nsrc * 4, cudaMemcpyHostToDevice, c->stream);
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "batch sources"));
   if ((rc = batch_arm(b))) return fail(rc);
+  if ((apps & GDB_BATCH_SSSP) && (rc = sssp_pick_delta(c, g, &b->delta))) return fail(rc);
 
   gdb::DiscoveryArgs proto;
   proto.ctx = b->dctx;
@@ -165,7 +167,7 @@ int gdb_batch_create(gdb_ctx* c, gdb_graph* g, uint32_t apps, const uint32_t* so
     if (apps & GDB_BATCH_BFS)
       rc = bfs_enqueue(c, g, b->ws_bfs, b->d_srcs, nsrc, b->d_bfs, cs, proto, adaptive);
     if (rc == GDB_OK && (apps & GDB_BATCH_SSSP))
-      rc = sssp_enqueue(c, g, b->ws_sssp, b->d_srcs, nsrc, b->d_sssp, cs, proto);
+      rc = sssp_enqueue(c, g, b->ws_sssp, b->d_srcs, nsrc, b->d_sssp, cs, proto, b->delta);
     cudaError_t e2 = cudaStreamEndCapture(cs, &b->graph);
     if (rc == GDB_OK && e2 != cudaSuccess) rc = set_cuda_error(c, e2, "batch capture");
   } else {

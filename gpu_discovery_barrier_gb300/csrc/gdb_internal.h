@@ -50,6 +50,7 @@ struct gdb_graph {
   uint32_t* heavy_v = nullptr;
   uint4* heavy_chunk = nullptr;    // one entry per chunk: {v, chunk, heavy index, chunks}
   uint32_t* heavy_bits = nullptr;  // V-bit membership bitmap
+  double wmean = -1.0;             // mean usable weight (< 0: not measured yet)
   gdb::GraphView view() const;
 };
 
@@ -112,7 +113,10 @@ size_t sssp_workspace_bytes(const gdb_graph* g);
 int bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
                 uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto, int adaptive);
 int sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
-                 uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto);
+                 uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto,
+                 uint32_t delta);
+// Near-far bucket width for g under c's options (0 = plain schedule).
+int sssp_pick_delta(gdb_ctx* c, gdb_graph* g, uint32_t* delta);
 
 // Build, run and free a graph: init<<<grid, block>>>(G, ws, src), then a
 // WHILE node whose body is level<<<grid, block>>>(G, ws, ctl, handle).

@@ -410,6 +410,7 @@ int gdb_graph_set_weights(gdb_graph* g, const uint32_t* w) {
     GDB_CUDA(c, cudaMalloc(&g->w, std::max<uint64_t>(g->E, 1) * 4));
     g->owns_w = true;
   }
+  g->wmean = -1.0;
   if (g->E) GDB_CUDA(c, cudaMemcpyAsync(g->w, w, g->E * 4, cudaMemcpyHostToDevice, c->stream));
   GDB_CUDA(c, cudaStreamSynchronize(c->stream));
   return GDB_OK;

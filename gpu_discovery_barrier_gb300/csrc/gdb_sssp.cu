@@ -9,6 +9,17 @@
 //    at most once (a stamp array), the queue is the same light/heavy
 //    frontier as BFS, and one XF barrier separates supersteps.
 //
+//    Near-far schedule (delta > 0; Davidson, Baxter, Garland, Owens,
+//    "Work-efficient parallel GPU methods for single-source shortest
+//    paths", IPDPS 2014): only improvements below the current split enter
+//    the next frontier; the others go to a far pile, each vertex at most
+//    once per pile.  When the near frontier runs dry, one superstep filters
+//    the pile: entries below the old split were settled and are dropped,
+//    entries below the new split (pile minimum + delta) form the next near
+//    frontier, the rest move to the next pile.  This bounds label-correcting
+//    rework to one bucket's width; the fixed point, and so every distance,
+//    is the same as the plain schedule's.
+//
 // 2. Pannotia Jacobi SSSP (mega_kernel, pannotia/graph_app/sssp/kernel/sssp_kernel.cl:170-244):
 //    y[v] = min(x[v], min_j data[j] + x[col[j]]) over the CSR given (the
 //    reference pulls over the transpose) until nothing changes.  The copy
@@ -37,32 +48,77 @@ struct SsspWs {
   uint32_t qcap, hcap;
   const uint32_t* srcs;        // multi-source run when nsrc > 0
   uint32_t nsrc;
+  // near-far schedule (delta > 0): far piles ping-pong by phase parity,
+  // their counters and minima rotate over three slots by phase % 3
+  uint32_t delta;
+  uint32_t* far[2];
+  uint32_t* farcount;          // [3]
+  uint32_t* farmin;            // [3]
+  uint32_t* farmark;           // phase + 1 of the pile holding the vertex
 };
 
+// Warp-aggregated append of the lanes' `want` vertices to the far pile of
+// `phase` (each vertex at most once per pile, so V entries suffice).
+__device__ __forceinline__ void far_push(const SsspWs& ws, uint32_t phase, bool want, uint32_t v) {
+  const unsigned m = __ballot_sync(kFull, want);
+  if (!m) return;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane_id() == leader) base = atomicAdd(&ws.farcount[phase % 3], (uint32_t)__popc(m));
+  base = __shfl_sync(kFull, base, leader);
+  if (want) {
+    const uint32_t slot = base + __popc(m & lanemask_lt());
+    if (slot < ws.qcap) pick(ws.far, phase)[slot] = v;
+    else atomicExch(ws.overflow, 1);
+  }
+}
+
+// Lower the minimum distance of the pile of `phase` by the lanes' `has` d.
+__device__ __forceinline__ void pile_min(const SsspWs& ws, uint32_t phase, bool has, uint32_t d) {
+  uint32_t dm = has ? d : 0xFFFFFFFFu;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) dm = min(dm, __shfl_xor_sync(kFull, dm, o));
+  if (lane_id() == 0 && dm != 0xFFFFFFFFu) atomicMin(&ws.farmin[phase % 3], dm);
+}
+
 __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, const SsspWs& ws,
-                                          uint32_t L, unsigned long long& arcs) {
+                                          uint32_t L, uint32_t split, uint32_t phase,
+                                          unsigned long long& arcs) {
   const int cur = L % 3, nxt = (L + 1) % 3;
   const uint32_t n = ld_cg(&ws.qcount[cur]);
   const unsigned long long hp = __ldcg(&ws.hcount[cur]);
   Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
                ws.qcap, ws.hcap, ws.overflow};
+  const uint32_t pile = phase + 1;
   auto relax = [&](bool valid, uint32_t du, uint32_t arc) {
-    uint32_t v = 0;
-    bool want = false;
+    uint32_t v = 0, nd = 0;
+    bool want = false, far = false;
     if (valid) {
       ++arcs;
       v = __ldg(&G.col[arc]);
       const uint32_t wt = __ldg(&G.w[arc]);
       if (wt < kInf) {
-        const uint32_t nd = du + wt;
+        nd = du + wt;
         if (nd < ld_cg(&ws.dist[v])) {
           const uint32_t old = atomicMin(&ws.dist[v], nd);
-          if (nd < old && ld_cg(&ws.stamp[v]) != L + 1 && atomicExch(&ws.stamp[v], L + 1) != L + 1)
-            want = true;
+          if (nd < old) {
+            if (nd < split) {
+              want = ld_cg(&ws.stamp[v]) != L + 1 && atomicExch(&ws.stamp[v], L + 1) != L + 1;
+            } else {
+              // the pile minimum must see every far improvement, queued or not
+              far = true;
+            }
+          }
         }
       }
     }
     frontier_push(G, out, want, v);
+    if (ws.delta && __any_sync(kFull, far)) {
+      const bool add = far && ld_cg(&ws.farmark[v]) != pile && atomicExch(&ws.farmark[v], pile) != pile;
+      far_push(ws, phase, add, v);
+      // improvements of vertices already in the pile lower its minimum too
+      pile_min(ws, phase, far, nd);
+    }
   };
   // light groups: each lane reads its own vertex's distance once
   const int lane = lane_id();
@@ -89,6 +145,31 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, co
   }
 }
 
+// Phase change of the near-far schedule: split the far pile of `phase`
+// into the next near frontier ([lo, split)), dropped settled entries
+// (< lo) and the pile of phase + 1 (>= split).
+__device__ __forceinline__ void far_filter(const GraphView& G, const Warps& W, const SsspWs& ws,
+                                           uint32_t L, uint32_t phase, uint32_t lo, uint32_t split) {
+  const int nxt = (L + 1) % 3;
+  Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
+               ws.qcap, ws.hcap, ws.overflow};
+  const uint32_t fn = ld_cg(&ws.farcount[phase % 3]);
+  const uint32_t* pile = pick(ws.far, phase);
+  const int lane = lane_id();
+  for (uint32_t base = W.gwarp * 32; base < fn; base += W.nwarps * 32) {
+    const uint32_t i = base + lane;
+    const bool act = i < fn;
+    const uint32_t v = act ? ld_cg(&pile[i]) : 0u;
+    const uint32_t d = act ? ld_cg(&ws.dist[v]) : 0u;
+    const bool near = act && d >= lo && d < split;
+    const bool keep = act && d >= split;
+    if (keep) ws.farmark[v] = phase + 2;
+    frontier_push(G, out, near, v);
+    far_push(ws, phase + 1, keep, v);
+    pile_min(ws, phase + 1, keep, d);
+  }
+}
+
 template <class Sync>
 __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const SsspWs& ws, uint32_t src) {
   const Warps W = warps_of(s.id(), s.P());
@@ -96,6 +177,7 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.dist[v] = kInf;
     ws.stamp[v] = 0;
+    if (ws.delta) ws.farmark[v] = 0;
   }
   if (leader) {
     for (int i = 0; i < 3; ++i) {
@@ -103,9 +185,13 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
       ws.hcount[i] = 0;
       ws.cursor[i] = 0;
       ws.hcursor[i] = 0;
+      if (ws.delta) {
+        ws.farcount[i] = 0;
+        ws.farmin[i] = 0xFFFFFFFFu;
+      }
     }
     *ws.overflow = 0;
-    ws.stats[0] = ws.stats[1] = 0;
+    ws.stats[0] = ws.stats[1] = ws.stats[2] = 0;
   }
   if (!s.sync()) return;
   const Frontier f0{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap, ws.overflow};
@@ -119,22 +205,43 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
   if (!s.sync()) return;
   unsigned long long arcs = 0;
   uint32_t L = 0;
+  // every CTA derives split and phase from the same counters after each
+  // barrier, so they stay uniform across the grid
+  uint32_t split = ws.delta ? ws.delta : 0xFFFFFFFFu, phase = 0;
   for (;; ++L) {
     const int cur = L % 3, old = (L + 2) % 3;
-    if (ld_cg(&ws.qcount[cur]) == 0 && __ldcg(&ws.hcount[cur]) == 0) break;
+    const bool dry = ld_cg(&ws.qcount[cur]) == 0 && __ldcg(&ws.hcount[cur]) == 0;
+    if (dry && (!ws.delta || ld_cg(&ws.farcount[phase % 3]) == 0)) break;
     if (leader) {
       ws.qcount[old] = 0;
       ws.hcount[old] = 0;
       ws.cursor[old] = 0;
       ws.hcursor[old] = 0;
     }
-    sssp_step(G, W, ws, L, arcs);
+    if (dry) {
+      const uint32_t lo = split;
+      const unsigned long long nx =
+          (unsigned long long)max(lo, ld_cg(&ws.farmin[phase % 3])) + ws.delta;
+      split = (uint32_t)min(nx, 0xFFFFFFFFull);
+      if (leader) {
+        // slot (phase + 2) % 3 was last read by the previous phase change
+        ws.farcount[(phase + 2) % 3] = 0;
+        ws.farmin[(phase + 2) % 3] = 0xFFFFFFFFu;
+      }
+      far_filter(G, W, ws, L, phase, lo, split);
+      ++phase;
+    } else {
+      sssp_step(G, W, ws, L, split, phase, arcs);
+    }
     if (!s.sync()) return;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
   if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
-  if (leader) ws.stats[1] = L;
+  if (leader) {
+    ws.stats[1] = L;
+    ws.stats[2] = phase;
+  }
 }
 
 __global__ void __launch_bounds__(512, 3) k_sssp_xf(DiscoveryArgs a, GraphView G, SsspWs ws, uint32_t src) {
@@ -192,7 +299,7 @@ __global__ void __launch_bounds__(512, 3) k_sssp_glevel(GraphView G, SsspWs ws, 
   W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
   W.nthreads = gridDim.x * blockDim.x;
   unsigned long long arcs = 0;
-  sssp_step(G, W, ws, L, arcs);
+  sssp_step(G, W, ws, L, 0xFFFFFFFFu, 0, arcs);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
   if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
@@ -326,6 +433,29 @@ __global__ void __launch_bounds__(512, 3) k_jacobi_xf(DiscoveryArgs a, GraphView
   jacobi_body(s, G, ws, src, smin);
 }
 
+// Sum and count of the usable weights (< kInf), for the automatic bucket
+// width of the near-far schedule.
+__global__ void k_weight_sum(const uint32_t* w, unsigned long long E, unsigned long long* out) {
+  unsigned long long sum = 0, cnt = 0;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < E;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint32_t x = __ldg(&w[i]);
+    if (x < kInf) {
+      sum += x;
+      ++cnt;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sum += __shfl_xor_sync(kFull, sum, o);
+    cnt += __shfl_xor_sync(kFull, cnt, o);
+  }
+  if (lane_id() == 0 && cnt) {
+    atomicAdd(&out[0], sum);
+    atomicAdd(&out[1], cnt);
+  }
+}
+
 }  // namespace
 
 using namespace gdbi;
@@ -339,10 +469,14 @@ static size_t sssp_layout(const gdb_graph* g, char* base, uint32_t* d_dist, Sssp
   const size_t o_st = b.take((size_t)V * 4);
   const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
   const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
+  const size_t o_f0 = b.take((size_t)V * 4), o_f1 = b.take((size_t)V * 4), o_fm = b.take((size_t)V * 4);
   const size_t o_cnt = b.take(512);
   if (!base) return b.off;
   ws->dist = d_dist;
   ws->stamp = (uint32_t*)(base + o_st);
+  ws->far[0] = (uint32_t*)(base + o_f0);
+  ws->far[1] = (uint32_t*)(base + o_f1);
+  ws->farmark = (uint32_t*)(base + o_fm);
   ws->q[0] = (uint32_t*)(base + o_q0);
   ws->q[1] = (uint32_t*)(base + o_q1);
   ws->hc[0] = (uint4*)(base + o_hc0);
@@ -354,10 +488,14 @@ static size_t sssp_layout(const gdb_graph* g, char* base, uint32_t* d_dist, Sssp
   ws->cursor = (uint32_t*)(cnt + 112);
   ws->hcursor = (uint32_t*)(cnt + 128);
   ws->overflow = (int*)(cnt + 160);
+  // cnt + 192: graph-relaunch control words
+  ws->farcount = (uint32_t*)(cnt + 224);               // 3
+  ws->farmin = (uint32_t*)(cnt + 240);                 // 3
   ws->qcap = V;
   ws->hcap = hcap;
   ws->srcs = nullptr;
   ws->nsrc = 0;
+  ws->delta = 0;
   *cnt_out = cnt;
   return b.off;
 }
@@ -366,14 +504,48 @@ size_t gdbi::sssp_workspace_bytes(const gdb_graph* g) {
   return sssp_layout(g, nullptr, nullptr, nullptr, nullptr);
 }
 
+// Bucket width of the near-far schedule: options.sssp_delta if set, else
+// 32 x mean weight / mean degree under the adaptive schedule (the
+// heuristic of Davidson et al.), else 0 (plain label-correcting).
+int gdbi::sssp_pick_delta(gdb_ctx* c, gdb_graph* g, uint32_t* delta) {
+  *delta = 0;
+  if (c->opt.sssp_delta) {
+    *delta = c->opt.sssp_delta;
+    return GDB_OK;
+  }
+  if (c->opt.schedule != GDB_SCHED_ADAPTIVE || !g->w || g->E == 0) return GDB_OK;
+  if (g->wmean < 0) {
+    unsigned long long* d = nullptr;
+    unsigned long long* h = (unsigned long long*)pinned(c, 4096);
+    if (!h) return GDB_ERR_OOM;
+    GDB_CUDA(c, cudaMallocAsync((void**)&d, 16, c->stream));
+    cudaError_t e = cudaMemsetAsync(d, 0, 16, c->stream);
+    if (e == cudaSuccess) {
+      k_weight_sum<<<4 * c->sm_count, 256, 0, c->stream>>>(g->w, g->E, d);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, c->stream);
+    cudaFreeAsync(d, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return set_cuda_error(c, e, "weight mean");
+    g->wmean = h[1] ? (double)h[0] / (double)h[1] : 1.0;
+  }
+  const double deg = (double)g->E / std::max<uint32_t>(g->V, 1);
+  const double dl = 32.0 * g->wmean / std::max(deg, 1.0);
+  *delta = (uint32_t)std::min(std::max(dl, 1.0), 1e9);
+  return GDB_OK;
+}
+
 int gdbi::sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
-                       uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto) {
+                       uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto,
+                       uint32_t delta) {
   if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
   SsspWs ws;
   char* cnt = nullptr;
   sssp_layout(g, (char*)wsbase, d_dist, &ws, &cnt);
   ws.srcs = d_srcs;
   ws.nsrc = nsrc;
+  ws.delta = delta;
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, stream));
   Shape s;
   int rc = persistent_shape(c, (const void*)k_sssp_xf, c->opt.block_size, 0, &s, false);
@@ -392,6 +564,9 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
   if (nsrc && c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH)
     return set_error(c, GDB_ERR_UNSUPPORTED, "multi-source SSSP needs a persistent barrier");
+  uint32_t delta = 0;
+  int rc = c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH ? GDB_OK : sssp_pick_delta(c, g, &delta);
+  if (rc) return rc;
   char* base = (char*)workspace(c, sssp_layout(g, nullptr, nullptr, nullptr, nullptr));
   if (!base) return GDB_ERR_OOM;
   SsspWs ws;
@@ -399,12 +574,12 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   sssp_layout(g, base, d_dist, &ws, &cnt);
   ws.srcs = d_srcs;
   ws.nsrc = nsrc;
+  ws.delta = delta;
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
   const GraphView G = g->view();
   const int block = c->opt.block_size;
   const int kind = c->opt.barrier;
   c->last = gdb_run_stats{};
-  int rc = GDB_OK;
   if (kind == GDB_BARRIER_XF || kind == GDB_BARRIER_XF_FIXED) {
     Shape s;
     rc = persistent_shape(c, (const void*)k_sssp_xf, block, 0, &s, kind == GDB_BARRIER_XF);
@@ -460,6 +635,8 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   c->last.kernel_ms = ms;
   c->last.edges_processed = hs[0];
   c->last.supersteps = (uint32_t)hs[1];
+  c->last.phases = (uint32_t)hs[2];
+  c->last.sssp_delta = delta;
   return GDB_OK;
 }
 

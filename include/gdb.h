@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GDB_ABI_VERSION 2
+#define GDB_ABI_VERSION 3
 
 /* Sentinels of the reference kernels. */
 #define GDB_LONESTAR_INF 1000000000u /* lonestar/apps/bfs/kernel/bfs_common.cl:35 */
@@ -88,6 +88,11 @@ typedef struct {
      when the frontier has < V / push_beta vertices (0 = 14 / 24) */
   uint32_t pull_alpha;
   uint32_t push_beta;
+  /* worklist SSSP bucket width: > 0 = near-far schedule with this width;
+     0 = automatic width (32 x mean weight / mean degree) under
+     GDB_SCHED_ADAPTIVE, the reference's label-correcting worklist under
+     GDB_SCHED_PLAIN.  Distances are the same for every width. */
+  uint32_t sssp_delta;
 } gdb_options;
 
 typedef struct {
@@ -98,6 +103,8 @@ typedef struct {
   uint64_t edges_processed;  /* arcs inspected (all passes) */
   uint64_t work_units;       /* edges/s work unit of the last run */
   double kernel_ms;          /* device time of the last run (CUDA events) */
+  uint32_t phases;           /* SSSP near-far phase changes of the last run */
+  uint32_t sssp_delta;       /* SSSP bucket width used (0 = plain worklist) */
 } gdb_run_stats;
 
 typedef struct {

@@ -85,6 +85,50 @@ def test_sssp_barrier_kinds(barrier):
 
 
 @pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
+@pytest.mark.parametrize("delta", [1, 37, 300, 1 << 20])
+def test_sssp_near_far(name, g, delta):
+    """The near-far schedule reaches the same distances for every bucket width."""
+    w = gg.uniform_weights(g, 1, 255, seed=1)
+    gw = g.with_weights(w)
+    with gdb.Ctx(sssp_delta=delta) as c:
+        G = c.graph(g.row_ptr, g.col, w)
+        for src in sorted(set([0] + list(gg.sources(g, 2, seed=3)))):
+            got = c.sssp(G, int(src))
+            assert np.array_equal(got, oracle.sssp_worklist(gw, int(src))), (name, src, delta)
+            st = c.last_stats()
+            assert st["sssp_delta"] == delta
+
+
+@pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC])
+def test_sssp_near_far_auto_width(barrier):
+    g = gg.grid(96, 80)
+    w = gg.uniform_weights(g, 1, 1000, seed=1)
+    with gdb.Ctx(barrier=barrier, schedule=gdb.SCHED_ADAPTIVE) as c:
+        G = c.graph(g.row_ptr, g.col, w)
+        got = c.sssp(G, 0)
+        st = c.last_stats()
+        assert np.array_equal(got, oracle.sssp_worklist(g.with_weights(w), 0))
+        # 32 x mean weight (~500) / mean degree (~4)
+        assert 2000 < st["sssp_delta"] < 6000
+        assert st["phases"] > 1
+        # weights replaced: the width follows the new mean
+        w2 = gg.uniform_weights(g, 1, 10, seed=2)
+        G.set_weights(w2)
+        assert np.array_equal(c.sssp(G, 5), oracle.sssp_worklist(g.with_weights(w2), 5))
+        assert c.last_stats()["sssp_delta"] < 100
+
+
+def test_sssp_near_far_multi_source():
+    g = gg.rmat(1 << 12, 16, seed=8)
+    w = gg.uniform_weights(g, 1, 255, seed=8)
+    srcs = [int(s) for s in gg.sources(g, 4, seed=1)]
+    with gdb.Ctx(sssp_delta=50) as c:
+        G = c.graph(g.row_ptr, g.col, w)
+        want = np.minimum.reduce([oracle.sssp_worklist(g.with_weights(w), s) for s in srcs])
+        assert np.array_equal(c.sssp_multi(G, srcs), want)
+
+
+@pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
 def test_sssp_jacobi(ctx, name, g):
     w = gg.uniform_weights(g, 1, 100, seed=2)
     gw = g.with_weights(w)

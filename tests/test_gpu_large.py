@@ -24,10 +24,11 @@ def test_grid4096_bfs_levels(barrier):
     assert np.array_equal(d.astype(np.int64), r + col)
 
 
-def test_grid1024_sssp_valid_and_exact():
+@pytest.mark.parametrize("schedule", [gdb.SCHED_PLAIN, gdb.SCHED_ADAPTIVE])
+def test_grid1024_sssp_valid_and_exact(schedule):
     g = gg.grid(1024, 1024)
     w = gg.uniform_weights(g, 1, 1000, seed=1)
-    with gdb.Ctx() as c:
+    with gdb.Ctx(schedule=schedule) as c:
         G = c.graph(g.row_ptr, g.col, w)
         d = c.sssp(G, 0)
     gw = g.with_weights(w)
