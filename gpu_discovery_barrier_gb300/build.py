@@ -41,6 +41,7 @@ CUDA_SOURCES = [
     "gdb_bc.cu",
     "gdb_mst.cu",
     "gdb_batch.cu",
+    "gdb_mlp.cu",
 ]
 
 

@@ -145,7 +145,8 @@ int gdb_batch_create(gdb_ctx* c, gdb_graph* g, uint32_t apps, const uint32_t* so
   e = cudaMemcpyAsync(b->d_srcs, sources, (size_t)nsrc * 4, cudaMemcpyHostToDevice, c->stream);
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "batch sources"));
   if ((rc = batch_arm(b))) return fail(rc);
-  if ((apps & GDB_BATCH_SSSP) && (rc = sssp_pick_delta(c, g, &b->delta))) return fail(rc);
+  bool relaunch = false;
+  if ((apps & GDB_BATCH_SSSP) && (rc = sssp_plan(c, g, nsrc, false, &b->delta, &relaunch))) return fail(rc);
 
   gdb::DiscoveryArgs proto;
   proto.ctx = b->dctx;
@@ -163,9 +164,7 @@ int gdb_batch_create(gdb_ctx* c, gdb_graph* g, uint32_t apps, const uint32_t* so
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "capture stream"));
   e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    const int adaptive = c->opt.schedule == GDB_SCHED_ADAPTIVE;
-    if (apps & GDB_BATCH_BFS)
-      rc = bfs_enqueue(c, g, b->ws_bfs, b->d_srcs, nsrc, b->d_bfs, cs, proto, adaptive);
+    if (apps & GDB_BATCH_BFS) rc = bfs_enqueue(c, g, b->ws_bfs, b->d_srcs, nsrc, b->d_bfs, cs, proto);
     if (rc == GDB_OK && (apps & GDB_BATCH_SSSP))
       rc = sssp_enqueue(c, g, b->ws_sssp, b->d_srcs, nsrc, b->d_sssp, cs, proto, b->delta);
     cudaError_t e2 = cudaStreamEndCapture(cs, &b->graph);

@@ -15,9 +15,15 @@
 //    (every unvisited vertex scans its arcs for a parent at L-1, stopping at
 //    the first) when the frontier's arcs exceed the unvisited arcs / 14, and
 //    back when the frontier shrinks below V/24.  Levels are identical.
+//  * learned: the master CTA evaluates the schedule selector's network
+//    inside every barrier (after the last arrival, before the release) on
+//    the next level's frontier features and picks push or pull for it;
+//  * forced push / pull (trace generation): the same hook records every
+//    level's features and duration with the mode fixed.
 #include <algorithm>
 
 #include "gdb_internal.h"
+#include "gdb_selector.cuh"
 
 namespace {
 
@@ -35,14 +41,74 @@ struct BfsWs {
   unsigned long long* stats;   // [0] arcs inspected, [1] levels, [2] unvisited arcs, [3] frontier arcs
   uint32_t* mode;              // [3] 0 = top-down, 1 = bottom-up, per level slot
   uint32_t qcap, hcap;
-  int adaptive;
+  int adaptive;                // kBfs* schedule below
   uint32_t alpha, beta;        // direction thresholds of the adaptive schedule
+  const float* mlp;            // selector parameters (learned schedule)
+  gdb_level_trace* trace;      // per-level records (nullable)
+  uint32_t trace_cap;
+  uint32_t maxdeg;
   const uint32_t* srcs;        // multi-source run when nsrc > 0
   uint32_t nsrc;
 };
 
+// BfsWs::adaptive: plain push, the threshold heuristic, the learned
+// selector, and the two fixed modes of trace generation.
+enum { kBfsPlain = 0, kBfsHeuristic = 1, kBfsLearned = 2, kBfsForcePush = 3, kBfsForcePull = 4 };
+
 __device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long* p) {
   return __ldcg(p);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Decision for level Lnext, taken by the master CTA inside the barrier
+// that ends level Lnext - 1 (all of that level's pushes are complete).
+// stats[2] / stats[3]: vertices / arcs visited so far (master-only),
+// stats[4 + slot]: arcs of the frontier in that slot, stats[7]: time of
+// the previous decision.  Warp 0 computes; lane 0 writes.
+__device__ __noinline__ void bfs_decide(const GraphView& G, const BfsWs& ws, const float* smlp,
+                                        uint32_t Lnext, uint32_t nwarps) {
+  if (threadIdx.x >= 32) return;
+  const int slot = Lnext % 3;
+  const unsigned long long now = globaltimer();
+  const uint32_t n = ld_cg(&ws.qcount[slot]);
+  const unsigned long long hp = ld_cg_u64(&ws.hcount[slot]);
+  const unsigned long long nfi = (unsigned long long)n + (hp >> 32);
+  const unsigned long long mfi = ld_cg_u64(&ws.stats[4 + slot]);
+  const unsigned long long vis_v = ld_cg_u64(&ws.stats[2]) + nfi;
+  const unsigned long long vis_a = ld_cg_u64(&ws.stats[3]) + mfi;
+  const unsigned long long mu = G.E > vis_a ? G.E - vis_a : 0ull;
+  const uint32_t prev = Lnext ? ld_cg(&ws.mode[(Lnext + 2) % 3]) : 0u;
+  float x[kFeat];
+  bfs_features(x, (float)nfi, (float)mfi, (float)mu, (float)G.V, (float)G.E,
+               (float)(G.V > vis_v ? G.V - vis_v : 0ull), Lnext, prev, (float)ws.maxdeg, (float)nwarps);
+  uint32_t mode = 0;
+  if (ws.adaptive == kBfsLearned) {
+    float out[kOut];
+    mlp_warp(smlp, x, out);
+    mode = out[kOutPull] < out[kOutPush] ? 1u : 0u;
+  } else if (ws.adaptive == kBfsForcePull) {
+    mode = 1;
+  }
+  if (threadIdx.x == 0) {
+    ws.mode[slot] = mode;
+    ws.stats[2] = vis_v;
+    ws.stats[3] = vis_a;
+    if (ws.trace) {
+      if (Lnext > 0 && Lnext - 1 < ws.trace_cap)
+        ws.trace[Lnext - 1].us = (float)(now - ws.stats[7]) * 1e-3f;
+      if (Lnext < ws.trace_cap && nfi > 0) {
+        for (int i = 0; i < kFeat; ++i) ws.trace[Lnext].x[i] = x[i];
+        ws.trace[Lnext].mode = mode;
+        ws.trace[Lnext].us = 0.f;
+      }
+    }
+    ws.stats[7] = now;
+  }
 }
 
 // Top-down expansion of level L into L+1.
@@ -105,10 +171,25 @@ __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& w
   }
 }
 
-template <class Sync>
-__device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsWs& ws, uint32_t src) {
+// Hooked: the learned and forced-mode schedules (a decision inside every
+// barrier); a separate instantiation keeps the plain kernels' registers.
+template <bool Hooked, class Sync>
+__device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsWs& ws, uint32_t src,
+                                         float* smlp) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
+  constexpr bool hooked = Hooked;
+  if (Hooked && ws.adaptive == kBfsLearned) {
+    for (int i = threadIdx.x; i < kParams; i += blockDim.x) smlp[i] = __ldg(&ws.mlp[i]);
+  }
+  // barrier ending level Lnext - 1; hooked schedules decide level Lnext in it
+  auto level_sync = [&](uint32_t Lnext) {
+    if constexpr (!Hooked) {
+      return s.sync();
+    } else {
+      return s.sync_hook([&] { bfs_decide(G, ws, smlp, Lnext, W.nwarps); });
+    }
+  };
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) ws.dist[v] = kInf;
   if (leader) {
     for (int i = 0; i < 3; ++i) {
@@ -124,12 +205,14 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
   if (!s.sync()) return;
   const Frontier f0{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap, ws.overflow};
   if (ws.nsrc) {
-    frontier_seed_many(G, f0, W, ws.srcs, ws.nsrc, ws.dist, kInf);
+    frontier_seed_many(G, f0, W, ws.srcs, ws.nsrc, ws.dist, kInf,
+                       hooked ? &ws.stats[4] : (unsigned long long*)nullptr);
   } else if (leader) {
     ws.dist[src] = 0;
     frontier_seed(G, f0, src);
+    if (hooked) ws.stats[4] = G.row[src + 1] - G.row[src];
   }
-  if (!s.sync()) return;
+  if (!level_sync(0)) return;
   unsigned long long arcs = 0;
   uint32_t L = 0;
   bool bottom_up = false;
@@ -143,7 +226,7 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
     const uint32_t n = ld_cg(&ws.qcount[cur]);
     const unsigned long long hp = ld_cg_u64(&ws.hcount[cur]);
     if (n == 0 && hp == 0) break;
-    if (ws.adaptive) {
+    if (ws.adaptive == kBfsHeuristic) {
       if (L > 0) {
         mf = ld_cg_u64(&ws.stats[4 + cur]);
         mu = mu > mf ? mu - mf : 0;
@@ -151,6 +234,8 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
       const uint32_t nf = n + (uint32_t)(hp >> 32);
       if (!bottom_up && mf > mu / ws.alpha) bottom_up = true;
       else if (bottom_up && nf < G.V / ws.beta) bottom_up = false;
+    } else if (hooked) {
+      bottom_up = ld_cg(&ws.mode[cur]) != 0;
     }
     if (leader) {
       ws.qcount[old] = 0;
@@ -167,7 +252,7 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
       for (int o = 16; o > 0; o >>= 1) farcs += __shfl_xor_sync(kFull, farcs, o);
       if (lane_id() == 0 && farcs) atomicAdd(&ws.stats[4 + (L + 1) % 3], farcs);
     }
-    if (!s.sync()) return;
+    if (!level_sync(L + 1)) return;
   }
   unsigned long long r = arcs;
 #pragma unroll
@@ -180,12 +265,27 @@ __global__ void __launch_bounds__(512, 3) k_bfs_xf(DiscoveryArgs a, GraphView G,
   __shared__ LocalCtx l;
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
-  bfs_body(s, G, ws, src);
+  bfs_body<false>(s, G, ws, src, nullptr);
 }
 
 __global__ void __launch_bounds__(512, 3) k_bfs_grid(GraphView G, BfsWs ws, uint32_t src) {
   GridSync s;
-  bfs_body(s, G, ws, src);
+  bfs_body<false>(s, G, ws, src, nullptr);
+}
+
+__global__ void __launch_bounds__(512, 3) k_bfs_xf_sel(DiscoveryArgs a, GraphView G, BfsWs ws,
+                                                       uint32_t src) {
+  __shared__ LocalCtx l;
+  __shared__ float smlp[kParams];
+  if (!discover(a, &l)) return;
+  XfSync s{&a, &l};
+  bfs_body<true>(s, G, ws, src, smlp);
+}
+
+__global__ void __launch_bounds__(512, 3) k_bfs_grid_sel(GraphView G, BfsWs ws, uint32_t src) {
+  __shared__ float smlp[kParams];
+  GridSync s;
+  bfs_body<true>(s, G, ws, src, smlp);
 }
 
 // Relaunch mode: init kernel, then one launch per level (no in-kernel barrier).
@@ -300,9 +400,13 @@ static size_t bfs_layout(const gdb_graph* g, char* base, uint32_t* d_dist, BfsWs
   ws->overflow = (int*)(cnt + 160);
   ws->qcap = V;
   ws->hcap = hcap;
-  ws->adaptive = 0;
+  ws->adaptive = kBfsPlain;
   ws->alpha = 14;
   ws->beta = 24;
+  ws->mlp = nullptr;
+  ws->trace = nullptr;
+  ws->trace_cap = 0;
+  ws->maxdeg = g->maxdeg;
   ws->srcs = nullptr;
   ws->nsrc = 0;
   *cnt_out = cnt;
@@ -313,33 +417,50 @@ size_t gdbi::bfs_workspace_bytes(const gdb_graph* g) {
   return bfs_layout(g, nullptr, nullptr, nullptr, nullptr);
 }
 
+// BfsWs::adaptive for c's schedule; the learned one needs a loaded selector.
+static int bfs_mode(gdb_ctx* c, int* mode) {
+  switch (c->opt.schedule) {
+    case GDB_SCHED_ADAPTIVE: *mode = kBfsHeuristic; return GDB_OK;
+    case GDB_SCHED_LEARNED:
+      if (!c->d_mlp) return set_error(c, GDB_ERR_INVALID, "learned schedule without a selector");
+      *mode = kBfsLearned;
+      return GDB_OK;
+    default: *mode = kBfsPlain; return GDB_OK;
+  }
+}
+
 // Enqueue one XF-barrier BFS (counter reset + persistent launch) on
 // `stream` without waiting, so that it can be stream-captured.  `proto`
 // carries the discovery context and flags the launch synchronises through.
 int gdbi::bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
-                      uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto,
-                      int adaptive) {
+                      uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto) {
   BfsWs ws;
   char* cnt = nullptr;
   bfs_layout(g, (char*)wsbase, d_dist, &ws, &cnt);
   ws.srcs = d_srcs;
   ws.nsrc = nsrc;
-  ws.adaptive = adaptive;
+  int rc = bfs_mode(c, &ws.adaptive);
+  if (rc) return rc;
+  ws.mlp = c->d_mlp;
   if (c->opt.pull_alpha) ws.alpha = c->opt.pull_alpha;
   if (c->opt.push_beta) ws.beta = c->opt.push_beta;
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, stream));
   Shape s;
-  int rc = persistent_shape(c, (const void*)k_bfs_xf, c->opt.block_size, 0, &s, false);
+  const bool sel = ws.adaptive >= kBfsLearned;
+  auto kx = sel ? k_bfs_xf_sel : k_bfs_xf;
+  rc = persistent_shape(c, (const void*)kx, c->opt.block_size, 0, &s, false);
   if (rc) return rc;
   DiscoveryArgs a = proto;
   a.expected = std::min(s.grid, s.fit);
-  k_bfs_xf<<<s.grid, c->opt.block_size, 0, stream>>>(a, g->view(), ws, 0u);
+  kx<<<s.grid, c->opt.block_size, 0, stream>>>(a, g->view(), ws, 0u);
   GDB_CUDA(c, cudaGetLastError());
   return GDB_OK;
 }
 
+// force: -1 = c's schedule, else a BfsWs::adaptive value (trace runs).
 static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_srcs, uint32_t nsrc,
-                   uint32_t* d_dist) {
+                   uint32_t* d_dist, int force = -1, gdb_level_trace* d_trace = nullptr,
+                   uint32_t trace_cap = 0) {
   if (!graph_ok(c, g) || !d_dist || (nsrc && !d_srcs)) return GDB_ERR_INVALID;
   if (!nsrc && src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
   BfsWs ws;
@@ -347,7 +468,15 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
   char* base = (char*)workspace(c, bfs_layout(g, nullptr, nullptr, nullptr, nullptr));
   if (!base) return GDB_ERR_OOM;
   bfs_layout(g, base, d_dist, &ws, &cnt);
-  ws.adaptive = c->opt.schedule == GDB_SCHED_ADAPTIVE;
+  if (force >= 0) {
+    ws.adaptive = force;
+  } else {
+    int rc0 = bfs_mode(c, &ws.adaptive);
+    if (rc0) return rc0;
+  }
+  ws.mlp = c->d_mlp;
+  ws.trace = d_trace;
+  ws.trace_cap = trace_cap;
   if (c->opt.pull_alpha) ws.alpha = c->opt.pull_alpha;
   if (c->opt.push_beta) ws.beta = c->opt.push_beta;
   ws.srcs = d_srcs;
@@ -363,11 +492,12 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
   int rc = GDB_OK;
   if (kind == GDB_BARRIER_XF || kind == GDB_BARRIER_XF_FIXED) {
     Shape s;
-    rc = persistent_shape(c, (const void*)k_bfs_xf, block, 0, &s, kind == GDB_BARRIER_XF);
+    auto kx = ws.adaptive >= kBfsLearned ? k_bfs_xf_sel : k_bfs_xf;
+    rc = persistent_shape(c, (const void*)kx, block, 0, &s, kind == GDB_BARRIER_XF);
     if (rc) return rc;
     DiscoveryArgs a = discovery_args(c, s);
     GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    k_bfs_xf<<<s.grid, block, 0, c->stream>>>(a, G, ws, src);
+    kx<<<s.grid, block, 0, c->stream>>>(a, G, ws, src);
     GDB_CUDA(c, cudaGetLastError());
     GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     rc = finish_run(c);
@@ -379,7 +509,8 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
     c->last.launches = 1;
   } else if (kind == GDB_BARRIER_GRID_SYNC) {
     int occ = 0;
-    GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs_grid, block, 0));
+    auto kg = ws.adaptive >= kBfsLearned ? k_bfs_grid_sel : k_bfs_grid;
+    GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kg, block, 0));
     int grid = occ * c->sm_count;
     if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
     GraphView Gc = G;
@@ -387,7 +518,7 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
     uint32_t srcc = src;
     void* args[] = {(void*)&Gc, (void*)&wsc, (void*)&srcc};
     GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    GDB_CUDA(c, cudaLaunchCooperativeKernel((const void*)k_bfs_grid, grid, block, args, 0, c->stream));
+    GDB_CUDA(c, cudaLaunchCooperativeKernel((const void*)kg, grid, block, args, 0, c->stream));
     GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     GDB_CUDA(c, cudaStreamSynchronize(c->stream));
     c->last.participating = grid;
@@ -473,6 +604,34 @@ int gdb_bfs_multi(gdb_ctx* c, gdb_graph* g, const uint32_t* sources, uint32_t ns
     e = cudaMemcpyAsync(dist, d, nb, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) rc = set_cuda_error(c, e, "dist read-back");
+  }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
+int gdb_bfs_trace(gdb_ctx* c, gdb_graph* g, uint32_t src, int mode, uint32_t* dist,
+                  gdb_level_trace* trace, uint32_t cap, uint32_t* levels) {
+  if (!graph_ok(c, g) || mode < 0 || mode > 2 || (cap && !trace)) return GDB_ERR_INVALID;
+  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED &&
+      c->opt.barrier != GDB_BARRIER_GRID_SYNC)
+    return set_error(c, GDB_ERR_UNSUPPORTED, "level traces need a persistent barrier");
+  if (mode == 2 && !c->d_mlp) return set_error(c, GDB_ERR_INVALID, "no selector loaded");
+  const int force = mode == 0 ? kBfsForcePush : mode == 1 ? kBfsForcePull : kBfsLearned;
+  const size_t nb = (size_t)g->V * 4, tb = (size_t)std::max<uint32_t>(cap, 1) * sizeof(gdb_level_trace);
+  char* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, nb + tb, c->stream));
+  cudaError_t e = cudaMemsetAsync(d + nb, 0, tb, c->stream);
+  int rc = e == cudaSuccess ? bfs_run(c, g, src, nullptr, 0, (uint32_t*)d, force,
+                                      (gdb_level_trace*)(d + nb), cap)
+                            : set_cuda_error(c, e, "trace buffer");
+  if (rc == GDB_OK) {
+    if (dist) e = cudaMemcpyAsync(dist, d, nb, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && cap) e = cudaMemcpyAsync(trace, d + nb, (size_t)cap * sizeof(gdb_level_trace),
+                                                      cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "trace read-back");
+    if (levels) *levels = c->last.supersteps;
   }
   cudaFreeAsync(d, c->stream);
   cudaStreamSynchronize(c->stream);
@@ -635,6 +794,10 @@ extern "C" int gdb_bfs_noalloc(const uint32_t* d_row_ptr, const uint32_t* d_col,
   ws.adaptive = 0;
   ws.alpha = 14;
   ws.beta = 24;
+  ws.mlp = nullptr;
+  ws.trace = nullptr;
+  ws.trace_cap = 0;
+  ws.maxdeg = 0;
   ws.srcs = nullptr;
   ws.nsrc = 0;
   DiscoveryArgs a;

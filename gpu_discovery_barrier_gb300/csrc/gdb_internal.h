@@ -33,6 +33,10 @@ struct gdb_ctx {
   size_t pinned_bytes = 0;
   gdb_run_stats last{};
   std::string err;
+  // schedule selector parameters (device copy for the kernels, host copy
+  // for run-level decisions); empty = none loaded
+  float* d_mlp = nullptr;
+  std::vector<float> h_mlp;
 };
 
 struct gdb_graph {
@@ -51,6 +55,7 @@ struct gdb_graph {
   uint4* heavy_chunk = nullptr;    // one entry per chunk: {v, chunk, heavy index, chunks}
   uint32_t* heavy_bits = nullptr;  // V-bit membership bitmap
   double wmean = -1.0;             // mean usable weight (< 0: not measured yet)
+  uint32_t maxdeg = 0;
   gdb::GraphView view() const;
 };
 
@@ -111,12 +116,16 @@ bool graph_ok(gdb_ctx* c, gdb_graph* g);
 size_t bfs_workspace_bytes(const gdb_graph* g);
 size_t sssp_workspace_bytes(const gdb_graph* g);
 int bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
-                uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto, int adaptive);
+                uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto);
 int sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
                  uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto,
                  uint32_t delta);
-// Near-far bucket width for g under c's options (0 = plain schedule).
-int sssp_pick_delta(gdb_ctx* c, gdb_graph* g, uint32_t* delta);
+// Schedule of one worklist SSSP run under c's options: near-far bucket
+// width (0 = label-correcting worklist) and graph relaunch (when allowed).
+int sssp_plan(gdb_ctx* c, gdb_graph* g, uint32_t nsrc, bool allow_relaunch, uint32_t* delta,
+              bool* relaunch);
+// Run-level selector features of an SSSP from nsrc sources.
+void sssp_features(gdb_ctx* c, const gdb_graph* g, uint32_t nsrc, float* x);
 
 // Build, run and free a graph: init<<<grid, block>>>(G, ws, src), then a
 // WHILE node whose body is level<<<grid, block>>>(G, ws, ctl, handle).

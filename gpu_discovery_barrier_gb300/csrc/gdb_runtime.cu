@@ -140,6 +140,7 @@ int build_heavy_table(gdb_graph* g, const uint32_t* hrow) {
   std::vector<uint32_t> bits((g->V + 31) / 32 + 1, 0);
   for (uint32_t v = 0; v < g->V; ++v) {
     const uint32_t d = hrow[v + 1] - hrow[v];
+    g->maxdeg = std::max(g->maxdeg, d);
     if (d > gdb::kHeavyDeg) {
       const uint32_t h = (uint32_t)hv.size(), n = gdb::chunks_of(d);
       hv.push_back(v);
@@ -225,7 +226,7 @@ static int check_options(const gdb_options* o) {
     return GDB_ERR_INVALID;
   if (o->lock < GDB_LOCK_TICKET || o->lock > GDB_LOCK_FREE) return GDB_ERR_INVALID;
   if (o->barrier < GDB_BARRIER_XF || o->barrier > GDB_BARRIER_RELAUNCH_GRAPH) return GDB_ERR_INVALID;
-  if (o->schedule < GDB_SCHED_PLAIN || o->schedule > GDB_SCHED_ADAPTIVE) return GDB_ERR_INVALID;
+  if (o->schedule < GDB_SCHED_PLAIN || o->schedule > GDB_SCHED_LEARNED) return GDB_ERR_INVALID;
   if (o->max_ctas < 0 || o->oversubscribe < 0) return GDB_ERR_INVALID;
   if (o->xf_release < 0 || o->xf_release > 1) return GDB_ERR_INVALID;
   return GDB_OK;
@@ -281,6 +282,7 @@ int gdb_ctx_destroy(gdb_ctx* c) {
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->dctx) cudaFree(c->dctx);
   if (c->flags) cudaFree(c->flags);
+  if (c->d_mlp) cudaFree(c->d_mlp);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);

@@ -29,6 +29,7 @@
 #include <algorithm>
 
 #include "gdb_internal.h"
+#include "gdb_selector.cuh"
 
 namespace {
 
@@ -504,16 +505,11 @@ size_t gdbi::sssp_workspace_bytes(const gdb_graph* g) {
   return sssp_layout(g, nullptr, nullptr, nullptr, nullptr);
 }
 
-// Bucket width of the near-far schedule: options.sssp_delta if set, else
-// 32 x mean weight / mean degree under the adaptive schedule (the
-// heuristic of Davidson et al.), else 0 (plain label-correcting).
-int gdbi::sssp_pick_delta(gdb_ctx* c, gdb_graph* g, uint32_t* delta) {
-  *delta = 0;
-  if (c->opt.sssp_delta) {
-    *delta = c->opt.sssp_delta;
-    return GDB_OK;
-  }
-  if (c->opt.schedule != GDB_SCHED_ADAPTIVE || !g->w || g->E == 0) return GDB_OK;
+// Automatic bucket width: 32 x mean weight / mean degree (the heuristic
+// of Davidson et al.); the mean weight is measured once per weight array.
+static int sssp_auto_delta(gdb_ctx* c, gdb_graph* g, uint32_t* delta) {
+  *delta = 1;
+  if (!g->w || g->E == 0) return GDB_OK;
   if (g->wmean < 0) {
     unsigned long long* d = nullptr;
     unsigned long long* h = (unsigned long long*)pinned(c, 4096);
@@ -533,6 +529,44 @@ int gdbi::sssp_pick_delta(gdb_ctx* c, gdb_graph* g, uint32_t* delta) {
   const double deg = (double)g->E / std::max<uint32_t>(g->V, 1);
   const double dl = 32.0 * g->wmean / std::max(deg, 1.0);
   *delta = (uint32_t)std::min(std::max(dl, 1.0), 1e9);
+  return GDB_OK;
+}
+
+// Schedule of one worklist SSSP run: the bucket width (0 = the
+// label-correcting worklist) and whether to run under graph relaunch.
+//  * options.sssp_delta > 0: that width;
+//  * learned: the selector's cheapest of worklist, near-far at the
+//    automatic width, near-far at 4x that width and (where allowed) the
+//    worklist under graph relaunch;
+//  * adaptive: the automatic width;  * plain: the worklist.
+int gdbi::sssp_plan(gdb_ctx* c, gdb_graph* g, uint32_t nsrc, bool allow_relaunch, uint32_t* delta,
+                    bool* relaunch) {
+  *delta = 0;
+  *relaunch = false;
+  if (c->opt.sssp_delta) {
+    *delta = c->opt.sssp_delta;
+    return GDB_OK;
+  }
+  if (c->opt.schedule == GDB_SCHED_ADAPTIVE) return sssp_auto_delta(c, g, delta);
+  if (c->opt.schedule != GDB_SCHED_LEARNED) return GDB_OK;
+  if (c->h_mlp.empty()) return set_error(c, GDB_ERR_INVALID, "learned schedule without a selector");
+  float x[kFeat], y[kOut];
+  sssp_features(c, g, std::max<uint32_t>(nsrc, 1), x);
+  mlp_host(c->h_mlp.data(), x, y);
+  int best = kOutSsspPlain;
+  for (int k = kOutSsspNearFar; k <= kOutSsspRelaunch; ++k) {
+    if (k == kOutSsspRelaunch && !allow_relaunch) continue;
+    if (y[k] < y[best]) best = k;
+  }
+  if (best == kOutSsspRelaunch) {
+    *relaunch = true;
+    return GDB_OK;
+  }
+  if (best == kOutSsspPlain) return GDB_OK;
+  uint32_t d = 1;
+  int rc = sssp_auto_delta(c, g, &d);
+  if (rc) return rc;
+  *delta = best == kOutSsspNearFarWide ? (uint32_t)std::min<uint64_t>(4ull * d, 1000000000ull) : d;
   return GDB_OK;
 }
 
@@ -565,7 +599,10 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   if (nsrc && c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH)
     return set_error(c, GDB_ERR_UNSUPPORTED, "multi-source SSSP needs a persistent barrier");
   uint32_t delta = 0;
-  int rc = c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH ? GDB_OK : sssp_pick_delta(c, g, &delta);
+  bool relaunch = false;
+  int rc = c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH
+               ? GDB_OK
+               : sssp_plan(c, g, nsrc ? nsrc : 1, nsrc == 0, &delta, &relaunch);
   if (rc) return rc;
   char* base = (char*)workspace(c, sssp_layout(g, nullptr, nullptr, nullptr, nullptr));
   if (!base) return GDB_ERR_OOM;
@@ -578,7 +615,7 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
   const GraphView G = g->view();
   const int block = c->opt.block_size;
-  const int kind = c->opt.barrier;
+  const int kind = relaunch ? GDB_BARRIER_RELAUNCH_GRAPH : c->opt.barrier;
   c->last = gdb_run_stats{};
   if (kind == GDB_BARRIER_XF || kind == GDB_BARRIER_XF_FIXED) {
     Shape s;

@@ -259,15 +259,23 @@ __device__ __forceinline__ void frontier_seed(const GraphView& G, const Frontier
 __device__ __forceinline__ void frontier_seed_many(const GraphView& G, const Frontier& F,
                                                    const Warps& W, const uint32_t* srcs,
                                                    uint32_t nsrc, uint32_t* dist,
-                                                   uint32_t unreached) {
+                                                   uint32_t unreached,
+                                                   unsigned long long* arcs_out = nullptr) {
   const int lane = lane_id();
+  unsigned long long arcs = 0;
   for (uint32_t base = W.gwarp * 32; base < nsrc; base += W.nwarps * 32) {
     const uint32_t i = base + lane;
     bool want = i < nsrc;
     const uint32_t v = want ? __ldg(&srcs[i]) : 0u;
     if (v >= G.V) want = false;  // out-of-range sources are ignored
     if (want) want = atomicCAS(&dist[v], unreached, 0u) == unreached;
+    if (want && arcs_out) arcs += __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
     frontier_push(G, F, want, v);
+  }
+  if (arcs_out) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(0xffffffffu, arcs, o);
+    if (lane == 0 && arcs) atomicAdd(arcs_out, arcs);
   }
 }
 
@@ -367,15 +375,28 @@ __device__ __forceinline__ double warp_sum_f64(double x) {
 
 // Barrier abstraction for the persistent kernels: XF over discovered CTAs
 // or cooperative_groups grid sync over a cooperative launch.
+// Grid barriers for the persistent bodies.  sync_hook(h): h runs once, in
+// CTA 0 (all its threads), between the last arrival and the release.
 struct XfSync {
   const DiscoveryArgs* a;
   LocalCtx* l;
   __device__ __forceinline__ bool sync() { return xf_barrier(*a, l); }
+  template <class H>
+  __device__ __forceinline__ bool sync_hook(H&& h) {
+    return xf_barrier(*a, l, h);
+  }
   __device__ __forceinline__ int id() const { return l->id; }
   __device__ __forceinline__ int P() const { return l->P; }
 };
 struct GridSync {
   __device__ __forceinline__ bool sync() {
+    cooperative_groups::this_grid().sync();
+    return true;
+  }
+  template <class H>
+  __device__ __forceinline__ bool sync_hook(H&& h) {
+    cooperative_groups::this_grid().sync();
+    if (blockIdx.x == 0) h();
     cooperative_groups::this_grid().sync();
     return true;
   }

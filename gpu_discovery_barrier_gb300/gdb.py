@@ -23,13 +23,14 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libgdb.so"
 
-ABI_VERSION = 3  # GDB_ABI_VERSION of include/gdb.h
+ABI_VERSION = 4  # GDB_ABI_VERSION of include/gdb.h
 LONESTAR_INF = 1_000_000_000
 PANNOTIA_BIG = 99_999_999
 
 LOCK_TICKET, LOCK_SPIN, LOCK_FREE = 0, 1, 2
 BARRIER_XF, BARRIER_GRID_SYNC, BARRIER_RELAUNCH, BARRIER_XF_FIXED, BARRIER_RELAUNCH_GRAPH = range(5)
-SCHED_PLAIN, SCHED_ADAPTIVE = 0, 1
+SCHED_PLAIN, SCHED_ADAPTIVE, SCHED_LEARNED = 0, 1, 2
+MLP_FEATURES, MLP_OUTPUTS, MLP_PARAMS = 12, 6, 1694
 
 STATUS = {0: "GDB_OK", -1: "GDB_ERR_INVALID", -2: "GDB_ERR_CUDA", -3: "GDB_ERR_OOM",
           -4: "GDB_ERR_TIMEOUT", -5: "GDB_ERR_CAPACITY", -6: "GDB_ERR_NOT_CORESIDENT",
@@ -62,6 +63,10 @@ class RunStats(C.Structure):
 class MstResult(C.Structure):
     _fields_ = [("weight64", C.c_uint64), ("weight32", C.c_uint32), ("components", C.c_uint32),
                 ("edges", C.c_uint32), ("rounds", C.c_uint32)]
+
+
+class LevelTrace(C.Structure):
+    _fields_ = [("x", C.c_float * 12), ("mode", C.c_uint32), ("us", C.c_float)]
 
 
 class DeviceInfo(C.Structure):
@@ -119,6 +124,14 @@ SIGNATURES = [
     ("gdb_bc_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
     ("gdb_mst", C.c_int, [_P, _P, C.POINTER(MstResult), _P]),
     ("gdb_mst_device", C.c_int, [_P, _P, _P, _P]),
+    ("gdb_selector_set", C.c_int, [_P, _P]),
+    ("gdb_bfs_trace", C.c_int, [_P, _P, C.c_uint32, C.c_int, _P, _P, C.c_uint32,
+                                C.POINTER(C.c_uint32)]),
+    ("gdb_sssp_features", C.c_int, [_P, _P, C.c_uint32, _P]),
+    ("gdb_mlp_forward", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_mlp_loss_grad", C.c_int, [_P, _P, _P, _P, _P, C.c_uint32, _P, C.POINTER(C.c_double)]),
+    ("gdb_mlp_train", C.c_int, [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_float, C.c_float,
+                                C.POINTER(C.c_double)]),
     ("gdb_bfs_multi", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
     ("gdb_bfs_multi_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
     ("gdb_sssp_multi", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
@@ -330,6 +343,60 @@ class Ctx:
         if with_arcs:
             out["arc_in_mst"] = flags[: g.E]
         return out
+
+    # -- schedule selector (no reference counterpart)
+    def selector_set(self, params: np.ndarray | None) -> None:
+        p = None if params is None else np.ascontiguousarray(params, dtype=np.float32)
+        if p is not None and p.size != MLP_PARAMS:
+            raise GdbError(-1, "gdb_selector_set", f"{p.size} parameters, want {MLP_PARAMS}")
+        self.check(self._lib.gdb_selector_set(self.h, _ptr(p)), "gdb_selector_set")
+
+    def bfs_trace(self, g: "Graph", src: int, mode: int, cap: int = 1 << 16):
+        """BFS with every level pushed (0), pulled (1) or chosen by the
+        selector (2); returns (levels, features[L, 12], modes[L], us[L])."""
+        rec = (LevelTrace * max(cap, 1))()
+        dist = np.empty(g.V, dtype=np.uint32)
+        n = C.c_uint32()
+        self.check(self._lib.gdb_bfs_trace(self.h, g.h, src, mode, _ptr(dist), rec, cap, C.byref(n)),
+                   "gdb_bfs_trace")
+        L = min(n.value, cap)
+        arr = np.frombuffer(rec, dtype=np.float32, count=14 * max(cap, 1)).reshape(-1, 14)[:L]
+        modes = np.frombuffer(rec, dtype=np.uint32, count=14 * max(cap, 1)).reshape(-1, 14)[:L, 12]
+        return dist, arr[:, :12].copy(), modes.copy(), arr[:, 13].copy()
+
+    def sssp_features(self, g: "Graph", nsrc: int = 1) -> np.ndarray:
+        x = np.empty(MLP_FEATURES, dtype=np.float32)
+        self.check(self._lib.gdb_sssp_features(self.h, g.h, nsrc, _ptr(x)), "gdb_sssp_features")
+        return x
+
+    def mlp_forward(self, params: np.ndarray, x: np.ndarray) -> np.ndarray:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        xx = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_FEATURES)
+        y = np.empty((xx.shape[0], MLP_OUTPUTS), dtype=np.float32)
+        self.check(self._lib.gdb_mlp_forward(self.h, _ptr(p), _ptr(xx), xx.shape[0], _ptr(y)),
+                   "gdb_mlp_forward")
+        return y
+
+    def mlp_loss_grad(self, params, x, t, m) -> tuple[float, np.ndarray]:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        xx = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_FEATURES)
+        tt = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, MLP_OUTPUTS)
+        mm = np.ascontiguousarray(m, dtype=np.float32).reshape(-1, MLP_OUTPUTS)
+        g = np.empty(MLP_PARAMS, dtype=np.float32)
+        loss = C.c_double()
+        self.check(self._lib.gdb_mlp_loss_grad(self.h, _ptr(p), _ptr(xx), _ptr(tt), _ptr(mm),
+                                               xx.shape[0], _ptr(g), C.byref(loss)), "gdb_mlp_loss_grad")
+        return loss.value, g
+
+    def mlp_train(self, params, x, t, m, epochs: int, lr: float = 1e-2, wd: float = 0.0):
+        p = np.array(params, dtype=np.float32, copy=True)
+        xx = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_FEATURES)
+        tt = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, MLP_OUTPUTS)
+        mm = np.ascontiguousarray(m, dtype=np.float32).reshape(-1, MLP_OUTPUTS)
+        loss = C.c_double()
+        self.check(self._lib.gdb_mlp_train(self.h, _ptr(p), _ptr(xx), _ptr(tt), _ptr(mm), xx.shape[0],
+                                           epochs, lr, wd, C.byref(loss)), "gdb_mlp_train")
+        return p, loss.value
 
     # -- multi-source and batched forms (no reference counterpart)
     def bfs_multi(self, g: "Graph", sources) -> np.ndarray:

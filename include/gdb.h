@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GDB_ABI_VERSION 3
+#define GDB_ABI_VERSION 4
 
 /* Sentinels of the reference kernels. */
 #define GDB_LONESTAR_INF 1000000000u /* lonestar/apps/bfs/kernel/bfs_common.cl:35 */
@@ -67,7 +67,12 @@ typedef enum {
 /* Schedule of the traversal options per superstep. */
 typedef enum {
   GDB_SCHED_PLAIN = 0,    /* fixed: push, queue frontier, persistent */
-  GDB_SCHED_ADAPTIVE = 1  /* per-superstep choice of push/pull (direction-optimising) */
+  GDB_SCHED_ADAPTIVE = 1, /* per-superstep choice of push/pull (direction-optimising
+                             thresholds); automatic near-far width for SSSP */
+  GDB_SCHED_LEARNED = 2   /* the schedule selector's network (gdb_selector_set):
+                             push/pull per BFS level, taken by the master CTA inside
+                             each barrier; SSSP worklist / near-far width / graph
+                             relaunch per run */
 } gdb_schedule;
 
 typedef struct {
@@ -234,6 +239,47 @@ int gdb_bc_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_
  * mst_common.cl:41-194, mst_port_kernel.cl:35-82). */
 int gdb_mst(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* result, uint8_t* arc_in_mst);
 int gdb_mst_device(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* d_result, uint8_t* d_arc_in_mst);
+
+/* ------------------------------------------------- schedule selector */
+/* No reference counterpart.  A 12-32-32-6 ReLU MLP in FP32 (GDB_MLP_PARAMS
+ * floats: feature shift[12], scale[12], W1[12][32], b1[32], W2[32][32],
+ * b2[32], W3[32][6], b3[6]); its outputs are predicted log2 costs of the
+ * options of a decision (0 push level, 1 pull level, 2 SSSP worklist,
+ * 3 SSSP near-far, 4 SSSP near-far 4x width, 5 SSSP graph relaunch). */
+#define GDB_MLP_FEATURES 12
+#define GDB_MLP_OUTPUTS 6
+#define GDB_MLP_PARAMS 1694
+
+/* One BFS level as seen by the selector: its features, the mode it ran in
+ * (0 push, 1 pull) and its duration (barrier to barrier, microseconds). */
+typedef struct {
+  float x[GDB_MLP_FEATURES];
+  uint32_t mode;
+  float us;
+} gdb_level_trace;
+
+/* Load (params != NULL) or clear the network used by GDB_SCHED_LEARNED. */
+int gdb_selector_set(gdb_ctx* ctx, const float* params);
+/* BFS with the mode of every level fixed (0 push, 1 pull) or chosen by
+ * the loaded network (2), recording up to cap levels; *levels = levels
+ * run.  Levels (dist) are the same for every mode. */
+int gdb_bfs_trace(gdb_ctx* ctx, gdb_graph* g, uint32_t src, int mode, uint32_t* dist,
+                  gdb_level_trace* trace, uint32_t cap, uint32_t* levels);
+/* Features of an SSSP run-level decision for g from nsrc sources. */
+int gdb_sssp_features(gdb_ctx* ctx, gdb_graph* g, uint32_t nsrc, float* x);
+/* Network outputs for n feature rows x[n][12] (host arrays). */
+int gdb_mlp_forward(gdb_ctx* ctx, const float* params, const float* x, uint32_t n, float* y);
+/* Masked squared loss L = sum(m * (y - t)^2) / sum(m) over rows x[n][12],
+ * targets t[n][6], mask m[n][6], and its gradient over the whole blob
+ * (the shift/scale entries get 0): CUDA forward/backward kernels with a
+ * fixed reduction order (deterministic). */
+int gdb_mlp_loss_grad(gdb_ctx* ctx, const float* params, const float* x, const float* t,
+                      const float* m, uint32_t n, float* grad, double* loss);
+/* Full-batch Adam on the GPU for `epochs` steps (lr, beta1 0.9, beta2
+ * 0.999, eps 1e-8, weight decay wd on W1..W3); params updated in place,
+ * *loss = loss before the last step (nullable). */
+int gdb_mlp_train(gdb_ctx* ctx, float* params, const float* x, const float* t, const float* m,
+                  uint32_t n, uint32_t epochs, float lr, float wd, double* loss);
 
 /* ------------------------------------------------ multi-source forms */
 /* No reference counterpart (they serve the batched form).  Every vertex

@@ -17,6 +17,8 @@
 // store publishes everything the whole grid wrote before the barrier.
 #pragma once
 
+#include <type_traits>
+
 #include <cuda/atomic>
 #include <stdint.h>
 
@@ -312,7 +314,17 @@ __device__ __forceinline__ int p_get_global_size(const LocalCtx* l) {
 // relaxed polls + fence.acq_rel.gpu on the acquiring side, CTA barriers
 // in between.  Returns false (uniformly across the CTA) after an error or
 // a timeout anywhere in the grid.
-__device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l) {
+//
+// `hook` runs in the master CTA (every thread calls it) after every
+// participant has arrived and before the release: it sees all the grid's
+// writes of the superstep, and its own writes are published by the release
+// (a superstep-boundary decision taken once, e.g. the schedule selector).
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+
+template <class Hook>
+__device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l, Hook&& hook) {
   DeviceCtx* c = a.ctx;
   const int P = l->P;
   const bool bcast = a.xf_release == kXfBroadcast;
@@ -349,6 +361,10 @@ __device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l) {
       ok = 0;
     }
     if (ok) {
+      if constexpr (!std::is_same<typename std::decay<Hook>::type, NoHook>::value) {
+        hook();
+        __syncthreads();
+      }
       if (bcast) {
         if (threadIdx.x == 0) {
           fence_acq_rel_gpu();  // release: the grid's writes before the word
@@ -386,6 +402,10 @@ __device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l) {
   }
   __syncthreads();
   return l->ok != 0;
+}
+
+__device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l) {
+  return xf_barrier(a, l, NoHook{});
 }
 
 }  // namespace gdb
