@@ -52,8 +52,13 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--apps", default="bfs,sssp,mis,color,bc,mst")
     p.add_argument("--batch-graphs", type=int, default=512)
+    p.add_argument("--schedule", choices=["plain", "adaptive", "learned"], default="learned",
+                   help="BFS/SSSP schedule of the suite (learned = the trained selector)")
     p.add_argument("--no-tune", action="store_true")
-    p.add_argument("--workload", choices=["rmat", "grid4096", "batch"], default="rmat",
+    p.add_argument("--requests", type=int, default=4000, help="serve: requests submitted")
+    p.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (req/s)")
+    p.add_argument("--slots", type=int, default=16, help="serve: concurrent slots")
+    p.add_argument("--workload", choices=["rmat", "grid4096", "batch", "serve"], default="rmat",
                    help="rmat: the R-MAT suite (default); grid4096: the barrier-bound "
                         "4096x4096 grid, BFS and SSSP from the corner per barrier kind")
     return p.parse_args()
@@ -173,8 +178,21 @@ class ClockSampler:
 # ------------------------------------------------------------- GPU suite
 
 
+def set_schedule(ctx, name: str) -> None:
+    """plain / adaptive / learned (loads the committed selector weights)."""
+    from gpu_discovery_barrier_gb300 import gdb, selector
+
+    if name == "learned":
+        p = selector.load()
+        if p is None:
+            raise SystemExit("learned schedule: selector_weights.json missing")
+        ctx.selector_set(p)
+    ctx.set_options(schedule={"plain": gdb.SCHED_PLAIN, "adaptive": gdb.SCHED_ADAPTIVE,
+                              "learned": gdb.SCHED_LEARNED}[name])
+
+
 class GpuSuite:
-    def __init__(self, wl, apps, device):
+    def __init__(self, wl, apps, device, schedule="plain"):
         import torch
 
         from gpu_discovery_barrier_gb300 import gdb
@@ -185,6 +203,7 @@ class GpuSuite:
         self.apps = apps
         g = wl["g"]
         self.ctx = gdb.Ctx(device=device)
+        set_schedule(self.ctx, schedule)
         self.G = self.ctx.graph(g.row_ptr, g.col, wl["w"])
         self.Gu = self.ctx.graph(g.row_ptr, g.col, wl["uw"])
         dev = torch.device("cuda", device)
@@ -398,7 +417,7 @@ def run_gdb(args, rank, world, local):
     apps = args.apps.split(",")
     wl = make_workload(args.scale, args.edge_factor)
     g = wl["g"]
-    suite = GpuSuite(wl, apps, local)
+    suite = GpuSuite(wl, apps, local, args.schedule)
     er_by_src, reached = {}, []
     for s in wl["src"]:
         vr, erv = reach(g, suite.ctx.bfs(suite.G, int(s)))
@@ -428,6 +447,20 @@ def run_gdb(args, rank, world, local):
     ms = reduce_max(ms, world)
     value = world * units_per_step * args.steps / (ms / 1e3)
     clocks = clk.summary()
+
+    # the plain schedule on the schedule-dependent apps, for comparison
+    plain_ms = None
+    if args.schedule != "plain" and any(a in apps for a in ("bfs", "sssp")):
+        set_schedule(suite.ctx, "plain")
+        saved = suite.apps
+        suite.apps = [a for a in apps if a in ("bfs", "sssp")]
+        suite.step_device({})
+        prec: dict = {}
+        for _ in range(args.steps):
+            suite.step_device(prec)
+        plain_ms = {a: prec[a]["ms"] / args.steps for a in prec}
+        suite.apps = saved
+        set_schedule(suite.ctx, args.schedule)
 
     # roofline of the kernel with the largest time share
     dom = max(rec, key=lambda a: rec[a]["ms"])
@@ -482,7 +515,8 @@ def run_gdb(args, rank, world, local):
         cfg = {"workload": f"rmat scale {args.scale} ef {args.edge_factor:g} suite", "V": g.V,
                "E": g.E, "sources": NSRC, "apps": apps, "global_batch": world,
                "parallelism": f"replicas x{world}", "l2": "inputs > L2 (no flush)",
-               "block": suite.ctx.opt.block_size, "barrier": "xf", "lock": "lock-free poll"}
+               "block": suite.ctx.opt.block_size, "barrier": "xf", "lock": "lock-free poll",
+               "schedule": args.schedule}
         line = base_line(args, world, value, ms / args.steps, cfg)
         line["clocks"] = clocks
         line["e2e"] = e2e
@@ -490,6 +524,8 @@ def run_gdb(args, rank, world, local):
         line["cpu_baseline"] = cpu
         line["gpu_launches"] = sum(r["launches"] for r in rec.values())
         line["per_app_ms"] = {a: rec[a]["ms"] / args.steps for a in rec}
+        line["schedule"] = args.schedule
+        line["plain_schedule_ms"] = plain_ms
         line["per_app_supersteps"] = {a: rec[a]["supersteps"] // args.steps for a in rec}
         print(json.dumps(line), flush=True)
 
@@ -605,6 +641,10 @@ def run_batch(args, rank, world, local):
         off = U.vertex_offset
         usrc = [int(off[i]) + s for i, s in enumerate(srcs)]
         tune = None
+        from gpu_discovery_barrier_gb300 import selector
+        sel = selector.load()
+        if sel is not None:
+            c.selector_set(sel)
         if not args.no_tune:
             tune = autotune.tune_batch(c, U, usrc, apps=3, reps=2)
         with c.batch(U, usrc) as B:
@@ -681,6 +721,115 @@ def run_batch(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def run_serve(args, rank, world, local):
+    """Request loop: 64 resident graphs drawn like the mixed batch (V
+    log-uniform in [1e3, 1e6], half R-MAT, half grids), BFS / SSSP /
+    single-source BC requests arriving as a seeded Poisson stream; reports
+    throughput and p50/p99 latency, and checks a sample of results against
+    the same requests run alone."""
+    import torch
+
+    from gpu_discovery_barrier_gb300 import gdb, graphgen as gg, selector
+
+    torch.cuda.set_device(local)
+    members = gg.mixed_batch(64, 1000, 1_000_000, seed=3 + rank)
+    rng = np.random.default_rng(17 + rank)
+    n = args.requests
+    gaps = rng.exponential(1.0 / args.rate, n)
+    graph_of = rng.integers(0, len(members), n)
+    app_of = rng.integers(1, 4, n)
+    src_of = [int(rng.integers(members[i].V)) for i in graph_of]
+    with gdb.Ctx() as c:
+        set_schedule(c, args.schedule)
+        Gs = [c.graph(m.row_ptr, m.col, m.w) for m in members]
+        deg = [np.diff(m.row_ptr.astype(np.int64)) for m in members]
+        with c.server(slots=args.slots, pool_bytes=8 << 30) as srv:
+            ids = [srv.add_graph(G) for G in Gs]
+            # warm-up: one request per app on the smallest graph
+            small = int(np.argmin([m.V for m in members]))
+            for app in (1, 2, 3):
+                srv.submit(ids[small], app, 0)
+            srv.drain(120.0)
+            srv.poll(16)
+            barrier(world)
+            with ClockSampler(local) as clk:
+                t0 = time.perf_counter()
+                due = t0
+                sub = {}
+                for k in range(n):
+                    due += gaps[k]
+                    while True:
+                        now = time.perf_counter()
+                        if now >= due:
+                            break
+                        if due - now > 2e-4:
+                            time.sleep(due - now - 1e-4)
+                    rid, out = srv.submit(ids[graph_of[k]], int(app_of[k]), src_of[k])
+                    sub[rid] = (k, out)
+                srv.drain(0)
+                wall = time.perf_counter() - t0
+            clocks = clk.summary()
+            done = srv.poll(n + 16)
+    lat = np.array([d["total_ms"] for d in done])
+    run = np.array([d["run_ms"] for d in done])
+    qms = np.array([d["queue_ms"] for d in done])
+    ok = all(d["status"] == 0 for d in done)
+    # work: arcs of the source's component (the reached arcs; BC counts its
+    # forward and backward pass)
+    from scipy.sparse import csr_matrix
+    from scipy.sparse.csgraph import connected_components
+
+    comp_arcs = []
+    for m, dg in zip(members, deg):
+        A = csr_matrix((np.ones(m.E, np.int8), m.col, m.row_ptr), shape=(m.V, m.V))
+        _, lab = connected_components(A, directed=False)
+        comp_arcs.append((lab, np.bincount(lab, weights=dg)))
+    units = 0
+    for d in done:
+        lab, arcs = comp_arcs[d["graph"]]
+        units += int(arcs[lab[d["src"]]]) * (2 if d["app"] == 3 else 1)
+    # sample check: alone == in the mix
+    identical = True
+    with gdb.Ctx() as c2:
+        set_schedule(c2, args.schedule)
+        for d in done[:: max(1, len(done) // 24)]:
+            k, out = sub[d["id"]]
+            m = members[graph_of[k]]
+            G = c2.graph(m.row_ptr, m.col, m.w)
+            app, src = d["app"], d["src"]
+            if app == 1:
+                identical &= bool(np.array_equal(out, c2.bfs(G, src)))
+            elif app == 2:
+                identical &= bool(np.array_equal(out, c2.sssp(G, src)))
+            else:
+                want = c2.bc(G, [src]).astype(np.float64)
+                scale = np.maximum(np.abs(want), 1e-6 * max(1.0, float(np.abs(want).max())))
+                identical &= bool(np.all(np.abs(out - want) <= 1e-4 * scale + 1e-6))
+            G.close()
+    cfg = {"workload": f"serving: {len(members)} resident graphs (mixed-batch distribution), "
+                       f"BFS/SSSP/BC-single-source, Poisson {args.rate:g} req/s",
+           "requests": n, "slots": args.slots, "global_batch": world, "parallelism": f"replicas x{world}",
+           "l2": "inputs > L2 (no flush)", "schedule": args.schedule}
+    value = world * units / wall
+    if rank == 0:
+        line = base_line(args, world, value, 1e3 * wall / max(args.steps, 1), cfg)
+        line["metric"] = "edges/sec (request loop, continuous batching)"
+        line["steps"] = 1
+        line["clocks"] = clocks
+        line["e2e"] = {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 4 * n,
+                       "d2h_bytes_per_step": int(sum(members[graph_of[sub[d['id']][0]]].V for d in done)) * 4}
+        line["roofline"] = None
+        line["cpu_baseline"] = None
+        line["gpu_launches"] = len(done)
+        line["serving"] = {
+            "offered_rps": args.rate, "achieved_rps": len(done) / wall, "wall_s": wall,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "run_p50_ms": float(np.percentile(run, 50)),
+            "run_p99_ms": float(np.percentile(run, 99)), "queue_p99_ms": float(np.percentile(qms, 99)),
+            "all_ok": ok, "alone_equals_mix_sample": identical}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup(args.gpus)
@@ -690,6 +839,8 @@ def main():
         run_grid(args, rank, world, local)
     elif args.workload == "batch":
         run_batch(args, rank, world, local)
+    elif args.workload == "serve":
+        run_serve(args, rank, world, local)
     else:
         run_gdb(args, rank, world, local)
     if world > 1:

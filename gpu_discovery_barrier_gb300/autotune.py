@@ -26,6 +26,7 @@ from . import gdb
 SHAPES = [(512, 3), (512, 2), (512, 1), (256, 6), (256, 4)]
 SCHEDULES = [(gdb.SCHED_PLAIN, 0, 0), (gdb.SCHED_ADAPTIVE, 14, 24), (gdb.SCHED_ADAPTIVE, 8, 24),
              (gdb.SCHED_ADAPTIVE, 24, 24), (gdb.SCHED_ADAPTIVE, 14, 64)]
+LEARNED = (gdb.SCHED_LEARNED, 0, 0)  # tried when the context holds a selector
 
 
 def cache_path() -> Path:
@@ -118,9 +119,8 @@ def tune_batch(ctx: gdb.Ctx, g: gdb.Graph, sources, apps: int = 3, reps: int = 3
         raise RuntimeError("autotune: no configuration ran")
     shape = best[0]
     best_opts, best_ms = _options(shape, SCHEDULES[0], sms), best[1]
-    for sched in SCHEDULES[1:]:
-        if not apps & gdb.BATCH_BFS:
-            break  # the thresholds steer BFS only
+    scheds = SCHEDULES[1:] + ([LEARNED] if getattr(ctx, "has_selector", False) else [])
+    for sched in scheds:
         opts = _options(shape, sched, sms)
         ms, _ = _time(ctx, g, sources, apps, opts, reps, ref)
         trials.append({"options": opts, "ms": ms})

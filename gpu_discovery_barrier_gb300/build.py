@@ -42,6 +42,7 @@ CUDA_SOURCES = [
     "gdb_mst.cu",
     "gdb_batch.cu",
     "gdb_mlp.cu",
+    "gdb_server.cu",
 ]
 
 

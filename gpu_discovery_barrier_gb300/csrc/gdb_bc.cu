@@ -320,10 +320,10 @@ __global__ void __launch_bounds__(512, 2) k_bc_xf(DiscoveryArgs a, GraphView G, 
 
 using namespace gdbi;
 
-static int bc_run(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc, float* d_bc) {
-  if (!graph_ok(c, g) || !d_bc || (nsrc && !d_sources)) return GDB_ERR_INVALID;
-  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED)
-    return set_error(c, GDB_ERR_UNSUPPORTED, "BC runs on the XF barrier");
+// Workspace of one BC run (distances, path counts, dependencies, the level
+// lists, heavy-chunk entries and their accumulators, the counter block).
+static size_t bc_layout(const gdb_graph* g, char* base, float* d_bc, const uint32_t* d_sources,
+                        uint32_t nsrc, BcWs* ws, char** cnt_out) {
   const uint32_t V = g->V;
   const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
   const uint32_t ccap = std::max<uint32_t>(g->nheavy_chunks, 1);
@@ -336,32 +336,63 @@ static int bc_run(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t 
   const size_t o_ll = b.take((size_t)maxlev * 4), o_lh = b.take((size_t)maxlev * 4),
                o_lhc = b.take((size_t)maxlev * 4), o_lhv = b.take((size_t)maxlev * 4);
   const size_t o_cnt = b.take(512);
-  char* base = (char*)workspace(c, b.off);
+  if (!base) return b.off;
+  ws->d = (int32_t*)(base + o_d);
+  ws->rho = (float*)(base + o_rho);
+  ws->sigma = (float*)(base + o_sg);
+  ws->bc = d_bc;
+  ws->order = (uint32_t*)(base + o_ord);
+  ws->hc = (uint4*)(base + o_hc);
+  ws->hc_cap = ccap;
+  ws->hacc = (double*)(base + o_hacc);
+  ws->hleft = (uint32_t*)(base + o_hleft);
+  ws->lev_l = (uint32_t*)(base + o_ll);
+  ws->lev_h = (uint32_t*)(base + o_lh);
+  ws->lev_hc = (uint32_t*)(base + o_lhc);
+  ws->lev_hv = (uint32_t*)(base + o_lhv);
+  char* cnt = base + o_cnt;
+  ws->stats = (unsigned long long*)cnt;
+  ws->hcnt = (unsigned long long*)(cnt + 64);
+  ws->lcnt = (uint32_t*)(cnt + 96);
+  ws->cursor = (uint32_t*)(cnt + 112);
+  ws->hcursor = (uint32_t*)(cnt + 128);
+  ws->overflow = (int*)(cnt + 160);
+  ws->sources = d_sources;
+  ws->nsrc = nsrc;
+  ws->max_levels = maxlev - 1;
+  *cnt_out = cnt;
+  return b.off;
+}
+
+size_t gdbi::bc_workspace_bytes(const gdb_graph* g) {
+  return bc_layout(g, nullptr, nullptr, nullptr, 0, nullptr, nullptr);
+}
+
+int gdbi::bc_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_sources, uint32_t nsrc,
+                     float* d_bc, cudaStream_t stream, const gdb::DiscoveryArgs& proto) {
+  BcWs ws;
+  char* cnt = nullptr;
+  bc_layout(g, (char*)wsbase, d_bc, d_sources, nsrc, &ws, &cnt);
+  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, stream));
+  Shape s;
+  int rc = persistent_shape(c, (const void*)k_bc_xf, c->opt.block_size, 0, &s, false);
+  if (rc) return rc;
+  DiscoveryArgs a = proto;
+  a.expected = std::min(s.grid, s.fit);
+  k_bc_xf<<<s.grid, c->opt.block_size, 0, stream>>>(a, g->view(), ws);
+  GDB_CUDA(c, cudaGetLastError());
+  return GDB_OK;
+}
+
+static int bc_run(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc, float* d_bc) {
+  if (!graph_ok(c, g) || !d_bc || (nsrc && !d_sources)) return GDB_ERR_INVALID;
+  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED)
+    return set_error(c, GDB_ERR_UNSUPPORTED, "BC runs on the XF barrier");
+  char* base = (char*)workspace(c, bc_layout(g, nullptr, nullptr, nullptr, 0, nullptr, nullptr));
   if (!base) return GDB_ERR_OOM;
   BcWs ws;
-  ws.d = (int32_t*)(base + o_d);
-  ws.rho = (float*)(base + o_rho);
-  ws.sigma = (float*)(base + o_sg);
-  ws.bc = d_bc;
-  ws.order = (uint32_t*)(base + o_ord);
-  ws.hc = (uint4*)(base + o_hc);
-  ws.hc_cap = ccap;
-  ws.hacc = (double*)(base + o_hacc);
-  ws.hleft = (uint32_t*)(base + o_hleft);
-  ws.lev_l = (uint32_t*)(base + o_ll);
-  ws.lev_h = (uint32_t*)(base + o_lh);
-  ws.lev_hc = (uint32_t*)(base + o_lhc);
-  ws.lev_hv = (uint32_t*)(base + o_lhv);
-  char* cnt = base + o_cnt;
-  ws.stats = (unsigned long long*)cnt;
-  ws.hcnt = (unsigned long long*)(cnt + 64);
-  ws.lcnt = (uint32_t*)(cnt + 96);
-  ws.cursor = (uint32_t*)(cnt + 112);
-  ws.hcursor = (uint32_t*)(cnt + 128);
-  ws.overflow = (int*)(cnt + 160);
-  ws.sources = d_sources;
-  ws.nsrc = nsrc;
-  ws.max_levels = maxlev - 1;
+  char* cnt = nullptr;
+  bc_layout(g, base, d_bc, d_sources, nsrc, &ws, &cnt);
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
   const int block = c->opt.block_size;
   Shape s;

@@ -413,6 +413,15 @@ static size_t bfs_layout(const gdb_graph* g, char* base, uint32_t* d_dist, BfsWs
   return b.off;
 }
 
+int gdbi::traversal_occupancy(gdb_ctx* c, int block) {
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs_xf, block, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return occ;
+}
+
 size_t gdbi::bfs_workspace_bytes(const gdb_graph* g) {
   return bfs_layout(g, nullptr, nullptr, nullptr, nullptr);
 }

@@ -113,6 +113,8 @@ bool graph_ok(gdb_ctx* c, gdb_graph* g);
 // form): bytes of one run's workspace, and an enqueue that only issues a
 // counter reset and the persistent launch on `stream`.  `proto` supplies the
 // discovery context, flags, lock, timeout and release form.
+// Resident CTAs per SM of the traversal kernels at `block` threads.
+int traversal_occupancy(gdb_ctx* c, int block);
 size_t bfs_workspace_bytes(const gdb_graph* g);
 size_t sssp_workspace_bytes(const gdb_graph* g);
 int bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
@@ -120,6 +122,9 @@ int bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, 
 int sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
                  uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto,
                  uint32_t delta);
+size_t bc_workspace_bytes(const gdb_graph* g);
+int bc_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_sources, uint32_t nsrc,
+               float* d_bc, cudaStream_t stream, const gdb::DiscoveryArgs& proto);
 // Schedule of one worklist SSSP run under c's options: near-far bucket
 // width (0 = label-correcting worklist) and graph relaunch (when allowed).
 int sssp_plan(gdb_ctx* c, gdb_graph* g, uint32_t nsrc, bool allow_relaunch, uint32_t* delta,

@@ -450,7 +450,7 @@ int gdb_device_info_get(gdb_ctx* c, gdb_device_info* info) {
   info->cc_minor = c->cc_minor;
   info->total_mem = c->total_mem;
   info->flag_capacity = c->flag_cap;
-  info->occupancy_per_sm = 0;
+  info->occupancy_per_sm = gdbi::traversal_occupancy(c, c->opt.block_size);
   return GDB_OK;
 }
 

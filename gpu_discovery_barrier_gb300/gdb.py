@@ -23,7 +23,7 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libgdb.so"
 
-ABI_VERSION = 4  # GDB_ABI_VERSION of include/gdb.h
+ABI_VERSION = 5  # GDB_ABI_VERSION of include/gdb.h
 LONESTAR_INF = 1_000_000_000
 PANNOTIA_BIG = 99_999_999
 
@@ -67,6 +67,15 @@ class MstResult(C.Structure):
 
 class LevelTrace(C.Structure):
     _fields_ = [("x", C.c_float * 12), ("mode", C.c_uint32), ("us", C.c_float)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int32), ("app", C.c_uint32), ("graph", C.c_uint32),
+                ("src", C.c_uint32), ("slot", C.c_uint32), ("queue_ms", C.c_double),
+                ("run_ms", C.c_double), ("total_ms", C.c_double), ("footprint", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class DeviceInfo(C.Structure):
@@ -146,8 +155,16 @@ SIGNATURES = [
     ("gdb_batch_device_result", _P, [_P, C.c_uint32]),
     ("gdb_batch_app_stats", C.c_int, [_P, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]),
     ("gdb_batch_destroy", C.c_int, [_P]),
+    ("gdb_server_create", C.c_int, [_P, C.c_uint32, C.c_uint64, C.POINTER(_P)]),
+    ("gdb_server_add_graph", C.c_int, [_P, _P, C.POINTER(C.c_uint32)]),
+    ("gdb_server_submit", C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P, C.POINTER(C.c_uint64)]),
+    ("gdb_server_poll", C.c_int, [_P, _P, C.c_uint32, C.POINTER(C.c_uint32)]),
+    ("gdb_server_drain", C.c_int, [_P, C.c_double]),
+    ("gdb_server_destroy", C.c_int, [_P]),
     ("gdb_bfs_noalloc", C.c_int, [_P, _P, C.c_uint32, C.c_uint64, C.c_uint32, _P, _P]),
 ]
+
+APP_BFS, APP_SSSP, APP_BC = 1, 2, 3
 
 BATCH_BFS, BATCH_SSSP = 1, 2
 
@@ -350,6 +367,7 @@ class Ctx:
         if p is not None and p.size != MLP_PARAMS:
             raise GdbError(-1, "gdb_selector_set", f"{p.size} parameters, want {MLP_PARAMS}")
         self.check(self._lib.gdb_selector_set(self.h, _ptr(p)), "gdb_selector_set")
+        self.has_selector = p is not None
 
     def bfs_trace(self, g: "Graph", src: int, mode: int, cap: int = 1 << 16):
         """BFS with every level pushed (0), pulled (1) or chosen by the
@@ -418,6 +436,9 @@ class Ctx:
 
     def batch(self, g: "Graph", sources, apps: int = 3) -> "Batch":
         return Batch(self, g, sources, apps)
+
+    def server(self, slots: int = 8, pool_bytes: int = 1 << 30) -> "Server":
+        return Server(self, slots, pool_bytes)
 
     # -- applications on device buffers (integer device pointers)
     def bfs_device(self, g: "Graph", src: int, d_dist: int) -> None:
@@ -575,6 +596,66 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "h", None) and self.ctx.h:
             self.ctx._lib.gdb_batch_destroy(self.h)
+        self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """A gdb_server: requests over resident graphs, continuously batched
+    into slots.  submit() returns the request id and the numpy array the
+    result is written into (uint32 levels / distances, float32 BC)."""
+
+    def __init__(self, ctx: Ctx, slots: int = 8, pool_bytes: int = 1 << 30):
+        self.ctx = ctx
+        self._out: dict[int, np.ndarray] = {}
+        self.graphs: list[Graph] = []
+        h = _P()
+        ctx.check(ctx._lib.gdb_server_create(ctx.h, slots, pool_bytes, C.byref(h)), "gdb_server_create")
+        self.h = h
+
+    def add_graph(self, g: Graph) -> int:
+        gid = C.c_uint32()
+        self.ctx.check(self.ctx._lib.gdb_server_add_graph(self.h, g.h, C.byref(gid)), "gdb_server_add_graph")
+        self.graphs.append(g)
+        return gid.value
+
+    def submit(self, graph: int, app: int, src: int) -> tuple[int, np.ndarray]:
+        V = self.graphs[graph].V
+        out = np.empty(V, dtype=np.float32 if app == APP_BC else np.uint32)
+        rid = C.c_uint64()
+        self.ctx.check(self.ctx._lib.gdb_server_submit(self.h, graph, app, src, _ptr(out), C.byref(rid)),
+                       "gdb_server_submit")
+        self._out[rid.value] = out
+        return rid.value, out
+
+    def poll(self, max_n: int = 1024) -> list[dict]:
+        buf = (RequestInfo * max_n)()
+        n = C.c_uint32()
+        self.ctx.check(self.ctx._lib.gdb_server_poll(self.h, buf, max_n, C.byref(n)), "gdb_server_poll")
+        out = []
+        for i in range(n.value):
+            d = buf[i].as_dict()
+            d["result"] = self._out.pop(d["id"], None)
+            out.append(d)
+        return out
+
+    def drain(self, timeout_s: float = 0.0) -> None:
+        self.ctx.check(self.ctx._lib.gdb_server_drain(self.h, timeout_s), "gdb_server_drain")
+
+    def close(self) -> None:
+        if getattr(self, "h", None) and self.ctx.h:
+            self.ctx._lib.gdb_server_destroy(self.h)
         self.h = None
 
     def __enter__(self):

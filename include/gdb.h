@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GDB_ABI_VERSION 4
+#define GDB_ABI_VERSION 5
 
 /* Sentinels of the reference kernels. */
 #define GDB_LONESTAR_INF 1000000000u /* lonestar/apps/bfs/kernel/bfs_common.cl:35 */
@@ -330,6 +330,46 @@ const uint32_t* gdb_batch_device_result(gdb_batch* b, uint32_t app);
 /* Arcs inspected and barrier intervals of one app in the last replay. */
 int gdb_batch_app_stats(gdb_batch* b, uint32_t app, uint64_t* arcs, uint32_t* supersteps);
 int gdb_batch_destroy(gdb_batch* b);
+
+/* ------------------------------------------------------------- serving */
+/* No reference counterpart.  A request loop over graphs resident in HBM
+ * with continuous batching: a dispatcher thread admits queued requests, in
+ * arrival order with bypass, into free slots as soon as a slot and the
+ * request's device-memory footprint (result + workspace, first-fit in a
+ * fixed pool) are free; each slot runs its request as a persistent launch
+ * on its own stream with its own discovery context and barrier flags, so
+ * requests admitted while others run overlap on the device.  Results are
+ * those of gdb_bfs / gdb_sssp / gdb_bc from the same source. */
+#define GDB_APP_BFS 1u
+#define GDB_APP_SSSP 2u
+#define GDB_APP_BC 3u
+typedef struct gdb_server gdb_server;
+typedef struct {
+  uint64_t id;
+  int32_t status;      /* GDB_OK or the request's error */
+  uint32_t app, graph, src, slot;
+  double queue_ms;     /* submit -> launch */
+  double run_ms;       /* device time of the launch (CUDA events) */
+  double total_ms;     /* submit -> result in the caller's buffer */
+  uint64_t footprint;  /* device bytes held while running */
+} gdb_request_info;
+/* slots: concurrent requests (0 = 8); pool_bytes: device memory for
+ * running requests (0 = 1 GiB); options (block size, CTA cap per launch,
+ * lock, schedule, timeout) and the selector are taken from ctx. */
+int gdb_server_create(gdb_ctx* ctx, uint32_t slots, uint64_t pool_bytes, gdb_server** out);
+/* Register a resident graph created on ctx (weights needed for SSSP). */
+int gdb_server_add_graph(gdb_server* s, gdb_graph* g, uint32_t* graph_id);
+/* Queue a request; `out` (host, V entries: uint32 levels / distances, or
+ * float BC scores) is written before the request completes.  Thread-safe.
+ * GDB_ERR_CAPACITY if the footprint exceeds the whole pool. */
+int gdb_server_submit(gdb_server* s, uint32_t graph_id, uint32_t app, uint32_t src, void* out,
+                      uint64_t* request_id);
+/* Completed requests since the last poll (up to max); *n = count. */
+int gdb_server_poll(gdb_server* s, gdb_request_info* info, uint32_t max, uint32_t* n);
+/* Block until every submitted request has completed (timeout_s <= 0: no
+ * limit); GDB_ERR_TIMEOUT otherwise. */
+int gdb_server_drain(gdb_server* s, double timeout_s);
+int gdb_server_destroy(gdb_server* s);
 
 /* -------------------------------------------- allocation-free BFS variant */
 /* No counterpart in the reference: an extra entry point for callers that
