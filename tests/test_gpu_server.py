@@ -34,8 +34,16 @@ def _alone(ctx, G, app, src):
 
 def _same(app, got, want):
     if app == gdb.APP_BC:
-        scale = np.maximum(np.abs(want), 1e-6 * max(1.0, float(np.abs(want).max())))
-        return bool(np.all(np.abs(got.astype(np.float64) - want) <= RTOL * scale + 1e-6))
+        # float32 path counts overflow on long grids (as in the reference):
+        # non-finite entries must match, finite ones agree within RTOL
+        fin = np.isfinite(want)
+        if not np.array_equal(fin, np.isfinite(got)):
+            return False
+        g, w = got[fin].astype(np.float64), want[fin].astype(np.float64)
+        if w.size == 0:
+            return True
+        scale = np.maximum(np.abs(w), 1e-6 * max(1.0, float(np.abs(w).max())))
+        return bool(np.all(np.abs(g - w) <= RTOL * scale + 1e-6))
     return bool(np.array_equal(got, want))
 
 
