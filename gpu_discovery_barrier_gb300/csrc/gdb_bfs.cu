@@ -140,8 +140,14 @@ __device__ __forceinline__ void bfs_top_down(const GraphView& G, const Warps& W,
 }
 
 // Bottom-up step for level L+1: every unvisited vertex looks for a parent
-// at level L among its arcs, stopping at the first.  Warp per 32 vertices,
-// each lane scanning its own vertex (degree-limited early exit).
+// at level L among its arcs, stopping at the first.  A warp takes 32
+// consecutive vertices.  Each lane first probes up to kPullProbe arcs of
+// its own vertex, four independent loads at a time; vertices whose lists
+// go on are then scanned by the whole warp, 32 arcs per step, one vertex
+// after another, leaving at the first step with a hit (so a long list
+// costs its length / 32 round trips instead of its length).
+constexpr uint32_t kPullProbe = 8;
+
 __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& ws, uint32_t L,
                                               const Warps& W, unsigned long long& arcs,
                                               unsigned long long& farcs) {
@@ -152,20 +158,48 @@ __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& w
   const uint32_t ngroups = (G.V + 31) / 32;
   for (uint32_t g = W.gwarp; g < ngroups; g += W.nwarps) {
     const uint32_t v = g * 32 + lane;
-    bool want = false;
+    bool want = false, open = false;
+    uint32_t b = 0, e = 0, deg = 0;
     if (v < G.V && ws.dist[v] == kInf) {
-      const uint32_t b = __ldg(&G.row[v]), e = __ldg(&G.row[v + 1]);
-      for (uint32_t a = b; a < e; ++a) {
-        ++arcs;
-        if (ld_cg(&ws.dist[__ldg(&G.col[a])]) == L) {
-          want = true;
+      b = __ldg(&G.row[v]);
+      e = __ldg(&G.row[v + 1]);
+      deg = e - b;
+      const uint32_t stop = min(e, b + kPullProbe);
+      for (uint32_t a = b; a < stop && !want; a += 4) {
+        uint32_t u[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) u[k] = a + k < stop ? __ldg(&G.col[a + k]) : kInf;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (u[k] != kInf) {
+            ++arcs;
+            if (ld_cg(&ws.dist[u[k]]) == L) want = true;
+          }
+        }
+      }
+      b = stop;
+      open = !want && stop < e;
+    }
+    for (unsigned m = __ballot_sync(kFull, open); m; m &= m - 1) {
+      const int o = __ffs(m) - 1;
+      const uint32_t bb = __shfl_sync(kFull, b, o), ee = __shfl_sync(kFull, e, o);
+      bool found = false;
+      for (uint32_t a = bb; a < ee; a += 32) {
+        bool hit = false;
+        if (a + lane < ee) {
+          ++arcs;
+          hit = ld_cg(&ws.dist[__ldg(&G.col[a + lane])]) == L;
+        }
+        if (__any_sync(kFull, hit)) {
+          found = true;
           break;
         }
       }
-      if (want) {
-        ws.dist[v] = L + 1;  // only this lane writes v
-        farcs += e - b;
-      }
+      if (lane == o) want = found;
+    }
+    if (want) {
+      ws.dist[v] = L + 1;  // only this lane writes v
+      farcs += deg;
     }
     frontier_push(G, out, want, v);
   }

@@ -27,6 +27,7 @@ __global__ void k_run_test(DiscoveryArgs a) {
   if (!gdb::discover(a, &l)) return;
   if (threadIdx.x == 0 && blockDim.x > 1) lms[0] = l.id;  // touch the dynamic allocation
   gdb::xf_barrier(a, &l);
+  gdb::xf_finish(a, &l);
 }
 
 // `iters` empty supersteps; participant 0 times barriers 2..iters+1 with
@@ -42,6 +43,7 @@ __global__ void k_bench_xf(DiscoveryArgs a, int iters, unsigned long long* out_n
     out_ns[0] = gdb::globaltimer() - t0;
     out_ns[1] = (unsigned long long)l.P;
   }
+  gdb::xf_finish(a, &l);
 }
 
 __global__ void k_bench_grid(int iters, unsigned long long* out_ns) {

@@ -313,7 +313,10 @@ void gdbi::sssp_features(gdb_ctx* c, const gdb_graph* g, uint32_t nsrc, float* x
   const double V = g->V, E = (double)g->E;
   const double nf = std::min<double>(nsrc, V);
   const double mf = nf * E / std::max(V, 1.0);
-  const double warps = (double)c->sm_count * 3.0 * (c->opt.block_size / 32);
+  // warps of the launch: the traversal kernels' resident CTAs, capped by max_ctas
+  double ctas = (double)c->sm_count * std::max(gdbi::traversal_occupancy(c, c->opt.block_size), 1);
+  if (c->opt.max_ctas > 0) ctas = std::min(ctas, (double)c->opt.max_ctas);
+  const double warps = ctas * (c->opt.block_size / 32);
   bfs_features(x, (float)nf, (float)mf, (float)std::max(E - mf, 0.0), (float)V, (float)E,
                (float)std::max(V - nf, 0.0), 0, 2, (float)g->maxdeg, (float)warps);
 }

@@ -380,6 +380,7 @@ __device__ __forceinline__ double warp_sum_f64(double x) {
 struct XfSync {
   const DiscoveryArgs* a;
   LocalCtx* l;
+  __device__ ~XfSync() { xf_finish(*a, l); }
   __device__ __forceinline__ bool sync() { return xf_barrier(*a, l); }
   template <class H>
   __device__ __forceinline__ bool sync_hook(H&& h) {

@@ -138,14 +138,21 @@ def training_graphs(small: bool = False):
     return out
 
 
-def collect(ctx: gdb.Ctx, graphs, reps: int = 2):
+def collect(ctx: gdb.Ctx, graphs, reps: int = 2, ctas=(0,)):
+    """Traces of every graph and source at every launch shape in `ctas`
+    (options.max_ctas values; 0 = all co-resident CTAs): the warps of the
+    launch are a feature, so the network sees how the options scale."""
     bfs, sssp = [], []
+    base = ctx.opt.max_ctas
     for name, g, srcs in graphs:
         G = ctx.graph(g.row_ptr, g.col, g.w)
-        for s in srcs:
-            bfs.append(bfs_trace(ctx, G, s, name, reps))
-            sssp.append(sssp_sample(ctx, G, s, name, reps))
+        for k in ctas:
+            ctx.set_options(max_ctas=k)
+            for s in srcs:
+                bfs.append(bfs_trace(ctx, G, s, f"{name}@{k}", reps))
+                sssp.append(sssp_sample(ctx, G, s, f"{name}@{k}", reps))
         G.close()
+    ctx.set_options(max_ctas=base)
     return bfs, sssp
 
 
@@ -238,19 +245,22 @@ def main(argv=None) -> None:
     ap.add_argument("--out", default=str(WEIGHTS))
     ap.add_argument("--small", action="store_true")
     ap.add_argument("--epochs", type=int, default=4000)
+    ap.add_argument("--ctas", default="152,304,0", help="launch shapes (max_ctas) to trace")
     args = ap.parse_args(argv)
+    ctas = tuple(int(k) for k in args.ctas.split(","))
     graphs = training_graphs(args.small)
     held = [graphs[i] for i in range(len(graphs)) if i % 5 == 4]
     fit = [graphs[i] for i in range(len(graphs)) if i % 5 != 4]
     with gdb.Ctx() as ctx:
-        bfs_fit, sssp_fit = collect(ctx, fit)
-        bfs_held, sssp_held = collect(ctx, held)
+        bfs_fit, sssp_fit = collect(ctx, fit, ctas=ctas)
+        bfs_held, sssp_held = collect(ctx, held, ctas=ctas)
         X, T, M = dataset(bfs_fit, sssp_fit)
         p, info = train(ctx, X, T, M, epochs=args.epochs)
         info["regret_fit"] = regret(ctx, p, bfs_fit, sssp_fit)
         info["regret_held_out"] = regret(ctx, p, bfs_held, sssp_held)
         info["fit_graphs"] = [n for n, _, _ in fit]
         info["held_out_graphs"] = [n for n, _, _ in held]
+        info["launch_shapes"] = list(ctas)
     save(p, info, Path(args.out))
     print(json.dumps(info, indent=1))
 

@@ -85,8 +85,12 @@ typedef struct {
   int lock;            /* gdb_lock_kind */
   int barrier;         /* gdb_barrier_kind */
   int schedule;        /* gdb_schedule */
-  int xf_release;      /* XF release form: 0 = master clears every slave's
-                          flag (the reference's), 1 = one broadcast epoch word */
+  int xf_release;      /* XF form: 0 = master polls every slave's padded flag
+                          and clears it (the reference's), 1 = same arrival,
+                          one broadcast epoch word as release, 2 = combining:
+                          slaves add to 16 padded arrival counters that one
+                          master warp watches, one generation word as release
+                          (the default) */
   uint64_t timeout_ns; /* limit for every device spin (0 = 2e9) */
   /* direction-optimising BFS thresholds (GDB_SCHED_ADAPTIVE): switch to
      pull when frontier arcs > unvisited arcs / pull_alpha, back to push
@@ -313,7 +317,7 @@ typedef struct gdb_batch gdb_batch;
  * workspace, result arrays, discovery context and barrier flags owned by
  * the batch.  Launch shape (block_size, max_ctas), lock, schedule and
  * timeout come from ctx's options at this call; the XF barrier uses the
- * per-slave release form (valid on every replay).  g must outlive b. */
+ * combining XF form (valid on every replay).  g must outlive b. */
 int gdb_batch_create(gdb_ctx* ctx, gdb_graph* g, uint32_t apps, const uint32_t* sources,
                      uint32_t nsrc, gdb_batch** out);
 /* Replace the sources (same count) read by the next replay. */

@@ -30,6 +30,8 @@ constexpr int kLineInts = 32;                 // one 128-byte line of ints
 constexpr int kPollClosed = 0x40000000;       // lock-free poll: closed bit
 constexpr int kPollCountMask = kPollClosed - 1;
 constexpr unsigned kBarrierSpin = 4096;        // polls before a barrier wait backs off
+constexpr int kArriveGroups = 16;              // combining XF: arrival counters
+constexpr int kReleaseCopies = 4;              // combining XF: generation word copies
 
 // discovery_kernel_ctx (common.h:33-48), one contended word per line.
 struct __align__(128) DeviceCtx {
@@ -54,6 +56,17 @@ struct __align__(128) DeviceCtx {
   // broadcast release word of the epoch form of the XF barrier
   unsigned long long release;
   unsigned long long _p7[15];
+  // combining form: slave s adds 1 to arrive[(s - 1) % kArriveGroups]; the
+  // master zeroes them when its launch ends.  gen: release generation,
+  // bumped once per barrier and never reset (waiters compare for change).
+  struct {
+    int v;
+    int _p[31];
+  } arrive[kArriveGroups];
+  struct {
+    unsigned v;
+    int _p[31];
+  } gen[kReleaseCopies];
 };
 
 // discovery_local_ctx (discovery.cl:67-71), in shared memory.
@@ -64,12 +77,14 @@ struct LocalCtx {
   int ok;             // 0 once this CTA saw an error / abort
   unsigned long long timeout_ns;  // limit of every single wait
   int barriers;       // barriers passed (master: for the stall test hook)
+  unsigned gen;       // combining form: release generation last seen
 };
 
 // XF release forms.
 enum XfRelease {
-  kXfPerSlave = 0,  // the master stores 0 into every slave's flag (discovery.cl:203-209)
-  kXfBroadcast = 1  // slaves store a launch-unique epoch; one broadcast release word
+  kXfPerSlave = 0,   // the master stores 0 into every slave's flag (discovery.cl:203-209)
+  kXfBroadcast = 1,  // slaves store a launch-unique epoch; one broadcast release word
+  kXfCombined = 2    // slaves add to 16 padded arrival counters; one generation word
 };
 
 // Launch parameters every discovery kernel receives.
@@ -284,6 +299,8 @@ __device__ inline bool discover(const DiscoveryArgs& a, LocalCtx* l) {
       l->ok = 0;
     }
     if (!l->ok) l->participating = 0;
+    // combining XF: no release can happen before this CTA's first arrival
+    l->gen = (unsigned)ld_relaxed((int*)&c->gen[0].v);
   }
   __syncthreads();
   return l->participating != 0;
@@ -297,6 +314,124 @@ __device__ __forceinline__ int p_get_global_id(const LocalCtx* l) {
 }
 __device__ __forceinline__ int p_get_global_size(const LocalCtx* l) {
   return l->P * blockDim.x;
+}
+
+// A barrier hook that does nothing (see xf_barrier).
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+
+// Warp-uniform bounded spin: done() must return the same value in every
+// lane; lane 0 watches the abort word and the deadline for the warp.
+template <class Done>
+__device__ __forceinline__ bool spin_until_warp(DeviceCtx* c, unsigned long long timeout_ns,
+                                                int where, Done done, unsigned pure) {
+  unsigned ns = 0;
+  unsigned long long deadline = 0;
+  for (unsigned k = 1;; ++k) {
+    if (done()) return true;
+    if ((k & 15) == 0) {
+      int stop = 0;
+      if ((threadIdx.x & 31) == 0) {
+        if (ld_relaxed(&c->abort)) {
+          stop = 1;
+        } else {
+          const unsigned long long now = globaltimer();
+          if (deadline == 0) {
+            deadline = now + timeout_ns;
+          } else if (now > deadline) {
+            raise_error(c, GDB_ERR_TIMEOUT, where);
+            stop = 1;
+          }
+        }
+      }
+      if (__shfl_sync(0xffffffffu, stop, 0)) return false;
+    }
+    if (k > pure) {
+      __nanosleep(ns);
+      ns = ns < 128 ? ns + 16 : 128;
+    }
+  }
+}
+
+// Combining form of the XF barrier.  The master/slave roles stay, but the
+// master no longer polls one padded flag per slave: slave s adds 1 to the
+// padded counter arrive[(s - 1) % 16] (fence + relaxed add: a release),
+// and the master's first warp watches the 16 counters (acquire loads)
+// until each holds (barrier + 1) x its group size.  The release is a
+// generation word bumped by the master (fence + relaxed store), written
+// to four padded copies so that each copy is polled (acquire loads) by a
+// quarter of the slaves.  Nothing has to be reset between
+// barriers: counts grow within a launch (the master zeroes them when it
+// leaves the launch, see xf_finish) and the generation only ever changes,
+// so captured launches can be replayed.
+template <class Hook>
+__device__ inline bool xf_barrier_combined(const DiscoveryArgs& a, LocalCtx* l, Hook&& hook) {
+  DeviceCtx* c = a.ctx;
+  int ok = 1;
+  if (l->id == 0) {
+    // no CTA barrier first: warp 0 starts watching at once, and the
+    // __syncthreads_and below holds the release until the whole master
+    // CTA has arrived
+    const int slaves = l->P - 1;
+    if (threadIdx.x < 32 && slaves > 0) {
+      const int lane = threadIdx.x;
+      const int n_g = lane < kArriveGroups
+                          ? slaves / kArriveGroups + (lane < slaves % kArriveGroups ? 1 : 0)
+                          : 0;
+      const int target = (l->barriers + 1) * n_g;
+      bool mine = n_g == 0;
+      ok = spin_until_warp(c, l->timeout_ns, 5, [&] {
+        if (!mine) mine = (int)((unsigned)ld_acquire(&c->arrive[lane].v) - (unsigned)target) >= 0;
+        return __all_sync(0xffffffffu, mine);
+      }, kBarrierSpin);
+    }
+    ok = __syncthreads_and(ok);
+    if (ok && c->stall_after >= 0 && l->barriers >= c->stall_after) {
+      if (threadIdx.x == 0) spin_until(c, l->timeout_ns, 6, [&] { return false; });
+      ok = 0;
+    }
+    if (ok) {
+      if constexpr (!std::is_same<typename std::decay<Hook>::type, NoHook>::value) {
+        hook();
+        __syncthreads();
+      }
+      if (threadIdx.x < kReleaseCopies) {
+        fence_acq_rel_gpu();  // release: the grid's writes before the generation
+        aref(*(int*)&c->gen[threadIdx.x].v).store((int)(l->gen + 1), cuda::memory_order_relaxed);
+      }
+      __syncwarp();
+      if (threadIdx.x == 0) l->gen += 1;
+    }
+  } else {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int g0 = (int)l->gen;
+      fence_acq_rel_gpu();  // release: this CTA's writes before its arrival
+      aref(c->arrive[(l->id - 1) % kArriveGroups].v).fetch_add(1, cuda::memory_order_relaxed);
+      int* word = (int*)&c->gen[l->id % kReleaseCopies].v;
+      ok = spin_until(c, l->timeout_ns, 7, [&] { return ld_acquire(word) != g0; }, kBarrierSpin);
+      if (ok) l->gen = (unsigned)(g0 + 1);  // one bump per barrier
+      l->ok = ok;
+    }
+    __syncthreads();
+    ok = l->ok;
+  }
+  if (threadIdx.x == 0) {
+    if (!ok) l->ok = 0;
+    l->barriers++;
+  }
+  __syncthreads();
+  return l->ok != 0;
+}
+
+// End of a launch that used the combining form: the master zeroes the
+// arrival counts (every arrival of its last barrier has been counted, and
+// no CTA arrives again).  After an error the host re-arms the context.
+__device__ inline void xf_finish(const DiscoveryArgs& a, const LocalCtx* l) {
+  if (a.xf_release == kXfCombined && l->participating && l->id == 0 && l->ok &&
+      threadIdx.x < kArriveGroups)
+    st_relaxed(&a.ctx->arrive[threadIdx.x].v, 0);
 }
 
 // XF barrier (discovery.cl:177-238) over the participating CTAs.  Slave: one
@@ -319,12 +454,9 @@ __device__ __forceinline__ int p_get_global_size(const LocalCtx* l) {
 // participant has arrived and before the release: it sees all the grid's
 // writes of the superstep, and its own writes are published by the release
 // (a superstep-boundary decision taken once, e.g. the schedule selector).
-struct NoHook {
-  __device__ __forceinline__ void operator()() const {}
-};
-
 template <class Hook>
 __device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l, Hook&& hook) {
+  if (a.xf_release == kXfCombined) return xf_barrier_combined(a, l, hook);
   DeviceCtx* c = a.ctx;
   const int P = l->P;
   const bool bcast = a.xf_release == kXfBroadcast;

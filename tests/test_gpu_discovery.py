@@ -50,7 +50,7 @@ def test_skip_refuses_oversubscription():
         c.init_discovery_kernel_ctx()
 
 
-@pytest.mark.parametrize("xf_release", [0, 1])
+@pytest.mark.parametrize("xf_release", [0, 1, 2])
 @pytest.mark.parametrize("kind", [gdb.BARRIER_XF, gdb.BARRIER_XF_FIXED, gdb.BARRIER_GRID_SYNC,
                                   gdb.BARRIER_RELAUNCH, gdb.BARRIER_RELAUNCH_GRAPH])
 def test_barrier_bench(kind, xf_release):
@@ -70,13 +70,13 @@ def test_release_modes_switch_in_one_context():
     with gdb.Ctx() as c:
         G = c.graph(g.row_ptr, g.col)
         want = oracle.bfs(g, 1)
-        for rel in (1, 0, 1, 0):
+        for rel in (1, 0, 2, 1, 2, 0):
             c.set_options(xf_release=rel)
             assert np.array_equal(c.bfs(G, 1), want)
             c.barrier_bench(gdb.BARRIER_XF, 256, 50)
 
 
-@pytest.mark.parametrize("xf_release", [0, 1])
+@pytest.mark.parametrize("xf_release", [0, 1, 2])
 def test_timeout_reports_and_recovers(xf_release):
     with gdb.Ctx(timeout_ns=50_000_000, xf_release=xf_release) as c:
         c.debug_stall_master(3)
@@ -86,3 +86,43 @@ def test_timeout_reports_and_recovers(xf_release):
         c.debug_stall_master(-1)
         ns, groups = c.barrier_bench(gdb.BARRIER_XF, 256, 20)
         assert ns > 0 and groups >= 1
+
+
+@pytest.mark.parametrize("ctas", [1, 2, 17, 152, 0])
+def test_combining_barrier_group_sizes(ctas):
+    """Arrival counts per group for every participant count, including a
+    lone master and counts that do not divide by the 16 groups; repeated
+    launches reuse the context (counts zeroed at the end of each)."""
+    with gdb.Ctx(xf_release=2, max_ctas=ctas) as c:
+        for _ in range(3):
+            ns, groups = c.barrier_bench(gdb.BARRIER_XF, 256, 300)
+            assert ns > 0 and groups >= 1
+            if ctas:
+                assert groups <= ctas
+
+
+@pytest.mark.parametrize("xf_release", [0, 1, 2])
+def test_all_apps_on_every_xf_form(xf_release):
+    import numpy as np
+
+    import oracle
+    from gpu_discovery_barrier_gb300 import graphgen as gg
+
+    g = gg.rmat(1 << 12, 12, seed=8)
+    w = gg.uniform_weights(g, 1, 255, seed=2)
+    uw = gg.unique_weights(g, seed=3)
+    prio = gg.priorities(g.V, seed=4)
+    gw = g.with_weights(w)
+    with gdb.Ctx(xf_release=xf_release) as c:
+        G = c.graph(g.row_ptr, g.col, w)
+        for _ in range(2):
+            assert np.array_equal(c.bfs(G, 3), oracle.bfs(g, 3))
+            assert np.array_equal(c.sssp(G, 3), oracle.sssp_worklist(gw, 3))
+            assert np.array_equal(c.sssp_jacobi(G, 3), oracle.sssp_jacobi(gw, 3, literal=True))
+            assert np.array_equal(c.mis(G, prio), oracle.mis(g, prio)[0])
+            assert np.array_equal(c.color(G, prio), oracle.color(g, prio)[0])
+            got = c.bc(G, [0, 5]).astype(np.float64)
+            want = oracle.bc_f64(g, [0, 5])
+            assert np.allclose(got, want, rtol=1e-4, atol=1e-3)
+        G.set_weights(uw)
+        assert c.mst(G)["weight64"] == oracle.mst(g.with_weights(uw))["weight64"]
