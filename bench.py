@@ -479,7 +479,7 @@ def run_gdb(args, rank, world, local):
     achieved = nbytes / (launch_ms / 1e3) / 1e9
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
+    if tf.exists() and args.scale == 22 and args.edge_factor == 16:  # the captured workload
         traffic = json.loads(tf.read_text()).get(dom)
     roof = {"bound": "hbm", "kernel": f"k_{dom}_xf", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
