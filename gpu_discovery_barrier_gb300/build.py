@@ -43,6 +43,7 @@ CUDA_SOURCES = [
     "gdb_batch.cu",
     "gdb_mlp.cu",
     "gdb_server.cu",
+    "gdb_io.cu",
 ]
 
 

@@ -23,7 +23,7 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libgdb.so"
 
-ABI_VERSION = 5  # GDB_ABI_VERSION of include/gdb.h
+ABI_VERSION = 6  # GDB_ABI_VERSION of include/gdb.h
 LONESTAR_INF = 1_000_000_000
 PANNOTIA_BIG = 99_999_999
 
@@ -67,6 +67,11 @@ class MstResult(C.Structure):
 
 class LevelTrace(C.Structure):
     _fields_ = [("x", C.c_float * 12), ("mode", C.c_uint32), ("us", C.c_float)]
+
+
+class Csr(C.Structure):
+    _fields_ = [("V", C.c_uint32), ("E", C.c_uint64), ("row_ptr", C.POINTER(C.c_uint32)),
+                ("col", C.POINTER(C.c_uint32)), ("w", C.POINTER(C.c_uint32))]
 
 
 class RequestInfo(C.Structure):
@@ -133,6 +138,10 @@ SIGNATURES = [
     ("gdb_bc_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
     ("gdb_mst", C.c_int, [_P, _P, C.POINTER(MstResult), _P]),
     ("gdb_mst_device", C.c_int, [_P, _P, _P, _P]),
+    ("gdb_csr_read", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(Csr)]),
+    ("gdb_csr_free", None, [C.POINTER(Csr)]),
+    ("gdb_csr_write_gr", C.c_int, [C.c_char_p, C.POINTER(Csr)]),
+    ("gdb_io_last_error", C.c_char_p, []),
     ("gdb_selector_set", C.c_int, [_P, _P]),
     ("gdb_bfs_trace", C.c_int, [_P, _P, C.c_uint32, C.c_int, _P, _P, C.c_uint32,
                                 C.POINTER(C.c_uint32)]),
@@ -165,6 +174,40 @@ SIGNATURES = [
 ]
 
 APP_BFS, APP_SSSP, APP_BC = 1, 2, 3
+FMT_AUTO, FMT_GR, FMT_DIMACS, FMT_METIS = 0, 1, 2, 3
+
+
+def read_graph(path, fmt: int = FMT_AUTO, directed: bool = False):
+    """gdb_csr_read: a .gr / DIMACS / METIS file as a graphgen.CSR
+    (weights in ``w`` when the file has them)."""
+    from .graphgen import CSR
+
+    c = Csr()
+    L = lib()
+    rc = L.gdb_csr_read(str(path).encode(), fmt, int(directed), C.byref(c))
+    if rc != 0:
+        raise GdbError(rc, "gdb_csr_read", L.gdb_io_last_error().decode())
+    try:
+        rp = np.ctypeslib.as_array(c.row_ptr, shape=(c.V + 1,)).copy()
+        col = np.ctypeslib.as_array(c.col, shape=(max(c.E, 1),))[: c.E].copy()
+        w = np.ctypeslib.as_array(c.w, shape=(max(c.E, 1),))[: c.E].copy() if c.w else None
+    finally:
+        L.gdb_csr_free(C.byref(c))
+    return CSR(rp, col, w, Path(path).name)
+
+
+def write_gr(path, g) -> None:
+    """gdb_csr_write_gr: write a CSR (row_ptr, col, optional w) as .gr v1."""
+    rp = np.ascontiguousarray(g.row_ptr, dtype=np.uint32)
+    col = np.ascontiguousarray(g.col, dtype=np.uint32)
+    w = None if g.w is None else np.ascontiguousarray(g.w, dtype=np.uint32)
+    u32 = C.POINTER(C.c_uint32)
+    c = Csr(rp.shape[0] - 1, col.shape[0], rp.ctypes.data_as(u32), col.ctypes.data_as(u32),
+            w.ctypes.data_as(u32) if w is not None else None)
+    L = lib()
+    rc = L.gdb_csr_write_gr(str(path).encode(), C.byref(c))
+    if rc != 0:
+        raise GdbError(rc, "gdb_csr_write_gr", L.gdb_io_last_error().decode())
 
 BATCH_BFS, BATCH_SSSP = 1, 2
 

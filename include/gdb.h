@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GDB_ABI_VERSION 5
+#define GDB_ABI_VERSION 6
 
 /* Sentinels of the reference kernels. */
 #define GDB_LONESTAR_INF 1000000000u /* lonestar/apps/bfs/kernel/bfs_common.cl:35 */
@@ -243,6 +243,39 @@ int gdb_bc_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_
  * mst_common.cl:41-194, mst_port_kernel.cl:35-82). */
 int gdb_mst(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* result, uint8_t* arc_in_mst);
 int gdb_mst_device(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* d_result, uint8_t* d_arc_in_mst);
+
+/* ---------------------------------------------------------- graph files */
+/* Readers of the reference's graph formats into host CSR arrays that the
+ * library allocates (free with gdb_csr_free); no GPU involved.
+ *   GDB_FMT_GR      Lonestar .gr version 1 binary
+ *                   (lonestar_gpu_opencl/include/graph.h:143-215);
+ *   GDB_FMT_DIMACS  "p sp V E" / "a u v w" text, 1-based
+ *                   (pannotia/graph_parser/parse.cpp:178-282); directed = 0
+ *                   adds every arc reversed too, as the reference's
+ *                   undirected mode does;
+ *   GDB_FMT_METIS   METIS adjacency text, 1-based, edge weights when the
+ *                   format field ends in 1 (parse.cpp:59-176).
+ * GDB_FMT_AUTO picks by extension (.gr, .graph/.metis, .dimacs/.txt/.coo).
+ * Arcs keep their file order within a source; every vertex has a row (the
+ * reference drops the rows of vertices without arcs).  w is NULL when the
+ * file carries no weights.  Errors: GDB_ERR_INVALID with the reason in
+ * gdb_io_last_error(), GDB_ERR_OOM. */
+#define GDB_FMT_AUTO 0
+#define GDB_FMT_GR 1
+#define GDB_FMT_DIMACS 2
+#define GDB_FMT_METIS 3
+typedef struct {
+  uint32_t V;
+  uint64_t E;
+  uint32_t* row_ptr; /* V + 1 */
+  uint32_t* col;     /* E */
+  uint32_t* w;       /* E or NULL */
+} gdb_csr;
+int gdb_csr_read(const char* path, int format, int directed, gdb_csr* out);
+void gdb_csr_free(gdb_csr* csr);
+/* Write a CSR as a .gr version 1 file (weights as 4-byte edge data). */
+int gdb_csr_write_gr(const char* path, const gdb_csr* csr);
+const char* gdb_io_last_error(void);
 
 /* ------------------------------------------------- schedule selector */
 /* No reference counterpart.  A 12-32-32-6 ReLU MLP in FP32 (GDB_MLP_PARAMS
