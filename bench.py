@@ -58,6 +58,9 @@ def parse():
     p.add_argument("--requests", type=int, default=4000, help="serve: requests submitted")
     p.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (req/s)")
     p.add_argument("--slots", type=int, default=16, help="serve: concurrent slots")
+    p.add_argument("--graph", default=None,
+                   help="rmat workload: run the suite on this .gr / DIMACS / METIS file instead "
+                        "(undirected; its weights for SSSP when it has them)")
     p.add_argument("--workload", choices=["rmat", "grid4096", "batch", "serve"], default="rmat",
                    help="rmat: the R-MAT suite (default); grid4096: the barrier-bound "
                         "4096x4096 grid, BFS and SSSP from the corner per barrier kind")
@@ -67,13 +70,19 @@ def parse():
 # ---------------------------------------------------------------- workload
 
 
-def make_workload(scale: int, ef: float):
-    from gpu_discovery_barrier_gb300 import graphgen as gg
+def make_workload(scale: int, ef: float, path: str | None = None):
+    from gpu_discovery_barrier_gb300 import gdb, graphgen as gg
 
-    g = gg.rmat_scale(scale, ef, seed=1)
+    if path:
+        g = gdb.read_graph(path, directed=False)
+        w = g.w if g.w is not None else gg.uniform_weights(g, 1, 255, seed=1)
+        g = gg.CSR(g.row_ptr, g.col, None, g.name)
+    else:
+        g = gg.rmat_scale(scale, ef, seed=1)
+        w = gg.uniform_weights(g, 1, 255, seed=1)
     return {
         "g": g,
-        "w": gg.uniform_weights(g, 1, 255, seed=1),
+        "w": w,
         "uw": gg.unique_weights(g, seed=3),
         "prio": gg.priorities(g.V, seed=4),
         "src": gg.sources(g, NSRC, seed=2),
@@ -385,7 +394,7 @@ def run_reference(args, rank, world):
 
     if rank != 0:
         return
-    wl = make_workload(args.scale, args.edge_factor)
+    wl = make_workload(args.scale, args.edge_factor, args.graph)
     g = wl["g"]
     er = {int(s): reach(g, O.par_bfs(g, int(s)))[1] for s in wl["src"]}
     threads = os.cpu_count() or 1
@@ -398,7 +407,7 @@ def run_reference(args, rank, world):
         units += units_of(names, srcs, er, g.E)
     total = sum(times)
     value = units / total
-    cfg = {"workload": f"rmat scale {args.scale} ef {args.edge_factor:g} suite", "V": g.V, "E": g.E,
+    cfg = {"workload": (f"file {args.graph} suite" if args.graph else f"rmat scale {args.scale} ef {args.edge_factor:g} suite"), "V": g.V, "E": g.E,
            "sources": NSRC, "global_batch": 1, "parallelism": "host threads", "l2": "inputs > L2"}
     line = base_line(args, 1, value, 1e3 * total / args.steps, cfg)
     line["impl"] = "reference"
@@ -415,7 +424,7 @@ def run_gdb(args, rank, world, local):
 
     torch.cuda.set_device(local)
     apps = args.apps.split(",")
-    wl = make_workload(args.scale, args.edge_factor)
+    wl = make_workload(args.scale, args.edge_factor, args.graph)
     g = wl["g"]
     suite = GpuSuite(wl, apps, local, args.schedule)
     er_by_src, reached = {}, []
@@ -479,7 +488,7 @@ def run_gdb(args, rank, world, local):
     achieved = nbytes / (launch_ms / 1e3) / 1e9
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists() and args.scale == 22 and args.edge_factor == 16:  # the captured workload
+    if tf.exists() and not args.graph and args.scale == 22 and args.edge_factor == 16:  # the captured workload
         traffic = json.loads(tf.read_text()).get(dom)
     roof = {"bound": "hbm", "kernel": f"k_{dom}_xf", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
@@ -512,7 +521,7 @@ def run_gdb(args, rank, world, local):
                                          f"same graph, serial CPU oracle ({dt:.1f} s)"}
 
     if rank == 0:
-        cfg = {"workload": f"rmat scale {args.scale} ef {args.edge_factor:g} suite", "V": g.V,
+        cfg = {"workload": (f"file {args.graph} suite" if args.graph else f"rmat scale {args.scale} ef {args.edge_factor:g} suite"), "V": g.V,
                "E": g.E, "sources": NSRC, "apps": apps, "global_batch": world,
                "parallelism": f"replicas x{world}", "l2": "inputs > L2 (no flush)",
                "block": suite.ctx.opt.block_size, "barrier": "xf", "lock": "lock-free poll",
