@@ -471,21 +471,26 @@ def run_gdb(args, rank, world, local):
         suite.apps = saved
         set_schedule(suite.ctx, args.schedule)
 
-    # roofline of the kernel with the largest time share
-    dom = max(rec, key=lambda a: rec[a]["ms"])
-    r = rec[dom]
-    launch_ms = r["ms"] / r["calls"]
-    rounds = max(1, r["supersteps"] // max(1, r["calls"]))
-    if dom in ("bfs", "sssp"):
-        # one source per launch: the mean over the 16 sources
-        mean = (sum(v for v, _ in reached) / len(reached), sum(e for _, e in reached) / len(reached))
-        nbytes = alg_bytes(dom, g, [mean], 0)
-    elif dom == "bc":
-        nbytes = alg_bytes("bc", g, reached, 0)
-    else:
-        nbytes = alg_bytes(dom, g, [], rounds)
+    # roofline of every kernel, reported for the one with the largest time share
     peak, peak_kind = peaks()
-    achieved = nbytes / (launch_ms / 1e3) / 1e9
+
+    def app_roofline(app):
+        r = rec[app]
+        launch_ms = r["ms"] / r["calls"]
+        rounds = max(1, r["supersteps"] // max(1, r["calls"]))
+        if app in ("bfs", "sssp"):
+            # one source per launch: the mean over the 16 sources
+            mean = (sum(v for v, _ in reached) / len(reached), sum(e for _, e in reached) / len(reached))
+            nbytes = alg_bytes(app, g, [mean], 0)
+        elif app == "bc":
+            nbytes = alg_bytes("bc", g, reached, 0)
+        else:
+            nbytes = alg_bytes(app, g, [], rounds)
+        return nbytes, launch_ms, nbytes / (launch_ms / 1e3) / 1e9
+
+    per_app_roof = {a: round(app_roofline(a)[2] / peak, 4) for a in rec}
+    dom = max(rec, key=lambda a: rec[a]["ms"])
+    nbytes, launch_ms, achieved = app_roofline(dom)
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists() and not args.graph and args.scale == 22 and args.edge_factor == 16:  # the captured workload
@@ -530,6 +535,7 @@ def run_gdb(args, rank, world, local):
         line["clocks"] = clocks
         line["e2e"] = e2e
         line["roofline"] = roof
+        line["per_app_hbm_frac"] = per_app_roof
         line["cpu_baseline"] = cpu
         line["gpu_launches"] = sum(r["launches"] for r in rec.values())
         line["per_app_ms"] = {a: rec[a]["ms"] / args.steps for a in rec}

@@ -683,8 +683,6 @@ int gdb_bfs_trace(gdb_ctx* c, gdb_graph* g, uint32_t src, int mode, uint32_t* di
 
 int gdb_bfs(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* dist) {
   if (!graph_ok(c, g) || !dist) return GDB_ERR_INVALID;
-  Bump b;
-  // the output lives after the kernel workspace, which bfs_run sizes itself
   uint32_t* d = nullptr;
   GDB_CUDA(c, cudaMallocAsync((void**)&d, (size_t)g->V * 4, c->stream));
   int rc = bfs_run(c, g, src, nullptr, 0, d);
