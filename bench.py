@@ -57,7 +57,7 @@ def parse():
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--requests", type=int, default=4000, help="serve: requests submitted")
     p.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (req/s)")
-    p.add_argument("--slots", type=int, default=16, help="serve: concurrent slots")
+    p.add_argument("--slots", type=int, default=64, help="serve: concurrent slots")
     p.add_argument("--graph", default=None,
                    help="rmat workload: run the suite on this .gr / DIMACS / METIS file instead "
                         "(undirected; its weights for SSSP when it has them)")
