@@ -197,6 +197,7 @@ __global__ void __launch_bounds__(512, 3) k_mis_xf(DiscoveryArgs a, GraphView G,
 struct ColorWs {
   int32_t* color;
   uint32_t* cnt;       // neighbours still to be coloured before this vertex
+  uint8_t* waitarc;    // per arc v -> u: 1 when u waits for v (set by the count pass)
   const float* prio;
   uint32_t* q[2];
   uint4* hc[2];                // heavy chunk entries
@@ -209,12 +210,8 @@ struct ColorWs {
   uint32_t qcap, hcap;
 };
 
-// u waits for v: u looks at its neighbours (degree != 1) and v's priority
-// is not below u's.
-__device__ __forceinline__ bool waits_for(const GraphView& G, const float* prio, uint32_t u,
-                                          float pv) {
-  return __ldg(&G.row[u + 1]) - __ldg(&G.row[u]) != 1 && pv >= __ldg(&prio[u]);
-}
+// u waits for v when u looks at its neighbours (degree != 1) and v's
+// priority is not below u's (the count pass stores it per arc v -> u).
 
 template <class Sync>
 __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const ColorWs& ws, uint32_t* smem) {
@@ -229,21 +226,31 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
     if (is_heavy(G, v)) ws.cnt[v] = 0;
   }
   if (!s.sync()) return;
+  // The same pass records, per arc v -> u, whether u waits for v, so that
+  // the rounds test one byte indexed by the arc instead of loading u's
+  // priority and degree after u itself.
   {
     float pv_lane = 0.f;
+    bool looks_lane = false;
     sweep_light(
         G, &ws.cursor[0],
         [&](uint32_t v, bool in_range) {
           my[lane] = 0;
           pv_lane = in_range ? __ldg(&ws.prio[v]) : 0.f;
-          // a degree-1 vertex never looks at its neighbour
-          return in_range && __ldg(&G.row[v + 1]) - __ldg(&G.row[v]) != 1;
+          // a degree-1 vertex never looks at its neighbour (but its arc
+          // still needs its waits-for byte)
+          looks_lane = in_range && __ldg(&G.row[v + 1]) - __ldg(&G.row[v]) != 1;
+          return in_range;
         },
         [&](bool valid, int owner, uint32_t arc) {
           const float pv = __shfl_sync(kFull, pv_lane, owner);
+          const bool looks = __shfl_sync(kFull, looks_lane, owner);
           if (valid) {
             ++arcs;
-            if (__ldg(&ws.prio[__ldg(&G.col[arc])]) >= pv) atomicAdd(&my[owner], 1u);
+            const uint32_t u = __ldg(&G.col[arc]);
+            const float pu = __ldg(&ws.prio[u]);
+            if (looks && pu >= pv) atomicAdd(&my[owner], 1u);
+            ws.waitarc[arc] = (pv >= pu && __ldg(&G.row[u + 1]) - __ldg(&G.row[u]) != 1) ? 1 : 0;
           }
         },
         [&](uint32_t v, bool) {
@@ -256,7 +263,10 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
         const uint32_t a = a0 + lane;
         if (a < e) {
           ++arcs;
-          n += __ldg(&ws.prio[__ldg(&G.col[a])]) >= pv;
+          const uint32_t u = __ldg(&G.col[a]);
+          const float pu = __ldg(&ws.prio[u]);
+          n += pu >= pv;
+          ws.waitarc[a] = (pv >= pu && __ldg(&G.row[u + 1]) - __ldg(&G.row[u]) != 1) ? 1 : 0;
         }
       }
       n = warp_add_u32(n);
@@ -303,7 +313,7 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
       if (valid) {
         ++arcs;
         u = __ldg(&G.col[arc]);
-        if (waits_for(G, ws.prio, u, pv) && atomicSub(&ws.cnt[u], 1u) == 1u) {
+        if (ws.waitarc[arc] && atomicSub(&ws.cnt[u], 1u) == 1u) {
           ws.color[u] = next_color;
           ready = true;
         }
@@ -355,14 +365,19 @@ __global__ void __launch_bounds__(512, 3) k_color_xf(DiscoveryArgs a, GraphView 
 
 using namespace gdbi;
 
+// default_ctas > 0: the launch's CTA count when options.max_ctas and
+// options.oversubscribe leave it open.
 template <class K, class Ws>
-static int launch_xf(gdb_ctx* c, K kernel, const GraphView& G, const Ws& ws, unsigned long long* d_stats) {
+static int launch_xf(gdb_ctx* c, K kernel, const GraphView& G, const Ws& ws, unsigned long long* d_stats,
+                     int default_ctas = 0) {
   if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED)
     return set_error(c, GDB_ERR_UNSUPPORTED, "this kernel runs on the XF barrier");
   const int block = c->opt.block_size;
   Shape s;
   int rc = persistent_shape(c, (const void*)kernel, block, 0, &s, c->opt.barrier == GDB_BARRIER_XF);
   if (rc) return rc;
+  if (default_ctas > 0 && c->opt.max_ctas == 0 && c->opt.oversubscribe == 0)
+    s.grid = std::min(s.grid, default_ctas);
   DiscoveryArgs a = discovery_args(c, s);
   c->last = gdb_run_stats{};
   GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
@@ -419,12 +434,14 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   const size_t o_cnt_v = b.take((size_t)V * 4);
   const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
   const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
+  const size_t o_wa = b.take(std::max<uint64_t>(g->E, 1));
   const size_t o_cnt = b.take(512);
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
   ColorWs ws;
   ws.color = d_color;
   ws.cnt = (uint32_t*)(base + o_cnt_v);
+  ws.waitarc = (uint8_t*)(base + o_wa);
   ws.prio = d_prio;
   ws.q[0] = (uint32_t*)(base + o_q0);
   ws.q[1] = (uint32_t*)(base + o_q1);
@@ -440,7 +457,11 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   ws.qcap = V;
   ws.hcap = hcap;
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
-  int rc = launch_xf(c, k_color_xf, g->view(), ws, ws.stats);
+  // after the count pass a round touches only the arcs of the vertices it
+  // colours (thousands of small rounds on power-law graphs): latency-bound,
+  // and faster on one CTA per SM (R-MAT-22: 42.8 ms against 47.4 ms on all
+  // 456 co-resident CTAs)
+  int rc = launch_xf(c, k_color_xf, g->view(), ws, ws.stats, c->sm_count);
   if (rc) return rc;
   unsigned long long* h = (unsigned long long*)pinned(c, 4096);
   GDB_CUDA(c, cudaMemcpy(h, cnt, 192, cudaMemcpyDeviceToHost));
