@@ -36,6 +36,7 @@ struct BcWs {
   int32_t* d;
   float* rho;
   float* sigma;
+  double* coef;                  // (1 + sigma[u]) / rho[u] of the last backward level
   float* bc;
   uint32_t* order;               // light vertices, level segments
   uint4* hc;                     // heavy chunk entries, level segments
@@ -206,7 +207,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
           [&](bool valid, int owner, uint32_t arc) {
             double a = 0.0;
             fwd_arc(valid, arc, a);
-            if (a != 0.0) atomicAdd(&my[owner], a);
+            segment_add(my, owner, a);
           },
           [&](uint32_t v, bool act) {
             if (act && L > 0) ws.rho[v] = (float)my[lane];
@@ -236,13 +237,13 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       const uint32_t lb = ld_cg(&ws.lev_l[Lb]), le = ld_cg(&ws.lev_l[Lb + 1]);
       const uint32_t hcb = ld_cg(&ws.lev_h[Lb]), hvb = ld_cg(&ws.lev_hv[Lb]);
       const uint32_t nch = ld_cg(&ws.lev_hc[Lb]);
+      // rho[v] / rho[u] * (1 + sigma[u]) with the u factor precomputed once
+      // per vertex (coef) instead of a division per arc
       auto bwd_arc = [&](bool valid, uint32_t arc, float rv, double& acc) {
         if (valid) {
           ++arcs;
           const uint32_t u = __ldg(&G.col[arc]);
-          if (ld_cg(&ws.d[u]) == Lb + 1) {
-            acc += (double)rv / (double)ld_cg(&ws.rho[u]) * (1.0 + (double)ld_cg(&ws.sigma[u]));
-          }
+          if (ld_cg(&ws.d[u]) == Lb + 1) acc += (double)rv * __ldcg(&ws.coef[u]);
         }
       };
       float rv_lane = 0.f;
@@ -255,12 +256,13 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
           [&](bool valid, int owner, uint32_t arc) {
             double a = 0.0;
             bwd_arc(valid, arc, __shfl_sync(kFull, rv_lane, owner), a);
-            if (a != 0.0) atomicAdd(&my[owner], a);
+            segment_add(my, owner, a);
           },
           [&](uint32_t v, bool act) {
             if (act) {
               const float sg = (float)my[lane];
               ws.sigma[v] = sg;
+              ws.coef[v] = (1.0 + (double)sg) / (double)rv_lane;
               if (v != src) ws.bc[v] += sg;
             }
           },
@@ -273,6 +275,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
             if (heavy_done(ws, slot, part, nchunks, &tot) && lane == 0) {
               const float sg = (float)tot;
               ws.sigma[v] = sg;
+              ws.coef[v] = (1.0 + (double)sg) / (double)rv;
               if (v != src) ws.bc[v] += sg;
             }
           });
@@ -330,6 +333,7 @@ static size_t bc_layout(const gdb_graph* g, char* base, float* d_bc, const uint3
   const uint32_t maxlev = V + 2;
   Bump b;
   const size_t o_d = b.take((size_t)V * 4), o_rho = b.take((size_t)V * 4), o_sg = b.take((size_t)V * 4);
+  const size_t o_coef = b.take((size_t)V * 8);
   const size_t o_ord = b.take((size_t)V * 4);
   const size_t o_hc = b.take((size_t)ccap * 16), o_hacc = b.take((size_t)hcap * 8),
                o_hleft = b.take((size_t)hcap * 4);
@@ -340,6 +344,7 @@ static size_t bc_layout(const gdb_graph* g, char* base, float* d_bc, const uint3
   ws->d = (int32_t*)(base + o_d);
   ws->rho = (float*)(base + o_rho);
   ws->sigma = (float*)(base + o_sg);
+  ws->coef = (double*)(base + o_coef);
   ws->bc = d_bc;
   ws->order = (uint32_t*)(base + o_ord);
   ws->hc = (uint4*)(base + o_hc);

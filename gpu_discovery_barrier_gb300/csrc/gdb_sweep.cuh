@@ -367,6 +367,23 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x)
   }
   return x;
 }
+// Per-owner sums of one group_arcs step.  Owners never decrease from lane
+// to lane, so each owner's lanes are contiguous: a segmented suffix scan
+// leaves every segment's total in its first lane, which adds it to
+// slot[owner] -- one lane per owner per step, no atomics.  Every lane of
+// the warp calls it.
+__device__ __forceinline__ void segment_add(double* slot, int owner, double x) {
+  const int lane = lane_id();
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double y = __shfl_down_sync(kFull, x, o);
+    const int ow = __shfl_down_sync(kFull, owner, o);
+    if (lane + o < 32 && ow == owner) x += y;
+  }
+  const int prev = __shfl_up_sync(kFull, owner, 1);
+  if ((lane == 0 || prev != owner) && x != 0.0) slot[owner] += x;
+}
+
 __device__ __forceinline__ double warp_sum_f64(double x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
