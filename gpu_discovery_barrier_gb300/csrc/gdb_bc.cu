@@ -311,7 +311,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
   if (leader) ws.stats[1] = t;
 }
 
-__global__ void __launch_bounds__(512, 2) k_bc_xf(DiscoveryArgs a, GraphView G, BcWs ws) {
+__global__ void __launch_bounds__(512, 3) k_bc_xf(DiscoveryArgs a, GraphView G, BcWs ws) {
   __shared__ LocalCtx l;
   __shared__ double sacc[1024];
   if (!discover(a, &l)) return;
