@@ -38,6 +38,11 @@ using namespace gdb;
 struct SsspWs {
   uint32_t* dist;
   uint32_t* stamp;             // superstep + 1 in which the vertex was pushed
+  // persistent kernels: distance and push stamp of a vertex in one word,
+  // (distance << 32) | stamp, so one 64-bit atomicMin both improves the
+  // distance and tells whether the vertex is already queued; the result is
+  // copied into dist at the end
+  unsigned long long* key;
   uint32_t* q[2];
   uint4* hc[2];                // heavy chunk entries
   uint32_t* qcount;            // [3]
@@ -82,6 +87,16 @@ __device__ __forceinline__ void pile_min(const SsspWs& ws, uint32_t phase, bool 
   if (lane_id() == 0 && dm != 0xFFFFFFFFu) atomicMin(&ws.farmin[phase % 3], dm);
 }
 
+template <bool Keyed>
+__device__ __forceinline__ uint32_t dist_of(const SsspWs& ws, uint32_t v) {
+  if constexpr (Keyed) {
+    return (uint32_t)(ld_cg(&ws.key[v]) >> 32);
+  } else {
+    return ld_cg(&ws.dist[v]);
+  }
+}
+
+template <bool Keyed>
 __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, const SsspWs& ws,
                                           uint32_t L, uint32_t split, uint32_t phase,
                                           unsigned long long& arcs) {
@@ -100,7 +115,20 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, co
       const uint32_t wt = __ldg(&G.w[arc]);
       if (wt < kInf) {
         nd = du + wt;
-        if (nd < ld_cg(&ws.dist[v])) {
+        if constexpr (Keyed) {
+          // the stamp part: L + 1 for a near push, 0 for a far one (so a
+          // later near improvement in the same superstep still pushes); at
+          // an equal distance the older, smaller stamp stays
+          if (nd < dist_of<true>(ws, v)) {
+            const unsigned long long k =
+                ((unsigned long long)nd << 32) | (nd < split ? (unsigned long long)(L + 1) : 0ull);
+            const unsigned long long old = atomicMin(&ws.key[v], k);
+            if (nd < (uint32_t)(old >> 32)) {
+              if (nd < split) want = (uint32_t)old != L + 1;
+              else far = true;  // the pile minimum must see every far improvement
+            }
+          }
+        } else if (nd < ld_cg(&ws.dist[v])) {
           const uint32_t old = atomicMin(&ws.dist[v], nd);
           if (nd < old) {
             if (nd < split) {
@@ -129,7 +157,7 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, co
     const uint32_t i = g * k + lane;
     const bool act = (uint32_t)lane < k && i < n;
     const uint32_t u = act ? ld_cg(&pick(ws.q, L)[i]) : 0u;
-    const uint32_t du = act ? ld_cg(&ws.dist[u]) : 0u;
+    const uint32_t du = act ? dist_of<Keyed>(ws, u) : 0u;
     group_arcs(G, act, u, [&](bool valid, int owner, uint32_t arc) {
       relax(valid, __shfl_sync(kFull, du, owner), arc);
     });
@@ -139,7 +167,7 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, co
   WorkTaker ht(nch, W, &ws.hcursor[cur]);
   for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
     const uint4 ent = ld_cg(&hc[c]);
-    const uint32_t du = ld_cg(&ws.dist[ent.x]);
+    const uint32_t du = dist_of<Keyed>(ws, ent.x);
     uint32_t b, en;
     chunk_range(G, ent, b, en);
     range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, du, arc); });
@@ -161,7 +189,7 @@ __device__ __forceinline__ void far_filter(const GraphView& G, const Warps& W, c
     const uint32_t i = base + lane;
     const bool act = i < fn;
     const uint32_t v = act ? ld_cg(&pile[i]) : 0u;
-    const uint32_t d = act ? ld_cg(&ws.dist[v]) : 0u;
+    const uint32_t d = act ? dist_of<true>(ws, v) : 0u;
     const bool near = act && d >= lo && d < split;
     const bool keep = act && d >= split;
     if (keep) ws.farmark[v] = phase + 2;
@@ -176,8 +204,7 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
-    ws.dist[v] = kInf;
-    ws.stamp[v] = 0;
+    ws.key[v] = (unsigned long long)kInf << 32;
     if (ws.delta) ws.farmark[v] = 0;
   }
   if (leader) {
@@ -197,10 +224,19 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
   if (!s.sync()) return;
   const Frontier f0{ws.q[0], ws.hc[0], &ws.qcount[0], &ws.hcount[0], ws.qcap, ws.hcap, ws.overflow};
   if (ws.nsrc) {
-    frontier_seed_many(G, f0, W, ws.srcs, ws.nsrc, ws.dist, kInf);
+    // one push per distinct in-range source (a CAS claims it)
+    const int lane = lane_id();
+    for (uint32_t base = W.gwarp * 32; base < ws.nsrc; base += W.nwarps * 32) {
+      const uint32_t i = base + lane;
+      bool want = i < ws.nsrc;
+      const uint32_t v = want ? __ldg(&ws.srcs[i]) : 0u;
+      if (v >= G.V) want = false;
+      if (want) want = atomicCAS(&ws.key[v], (unsigned long long)kInf << 32, 0ull) ==
+                       (unsigned long long)kInf << 32;
+      frontier_push(G, f0, want, v);
+    }
   } else if (leader) {
-    ws.dist[src] = 0;
-    ws.stamp[src] = 0;
+    ws.key[src] = 0;
     frontier_seed(G, f0, src);
   }
   if (!s.sync()) return;
@@ -232,10 +268,13 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
       far_filter(G, W, ws, L, phase, lo, split);
       ++phase;
     } else {
-      sssp_step(G, W, ws, L, split, phase, arcs);
+      sssp_step<true>(G, W, ws, L, split, phase, arcs);
     }
     if (!s.sync()) return;
   }
+  // the distances, out of the keys (every key is final after the last barrier)
+  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads)
+    ws.dist[v] = (uint32_t)(ld_cg(&ws.key[v]) >> 32);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
   if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
@@ -300,7 +339,7 @@ __global__ void __launch_bounds__(512, 3) k_sssp_glevel(GraphView G, SsspWs ws, 
   W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
   W.nthreads = gridDim.x * blockDim.x;
   unsigned long long arcs = 0;
-  sssp_step(G, W, ws, L, 0xFFFFFFFFu, 0, arcs);
+  sssp_step<false>(G, W, ws, L, 0xFFFFFFFFu, 0, arcs);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
   if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
@@ -471,10 +510,12 @@ static size_t sssp_layout(const gdb_graph* g, char* base, uint32_t* d_dist, Sssp
   const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
   const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
   const size_t o_f0 = b.take((size_t)V * 4), o_f1 = b.take((size_t)V * 4), o_fm = b.take((size_t)V * 4);
+  const size_t o_key = b.take((size_t)V * 8);
   const size_t o_cnt = b.take(512);
   if (!base) return b.off;
   ws->dist = d_dist;
   ws->stamp = (uint32_t*)(base + o_st);
+  ws->key = (unsigned long long*)(base + o_key);
   ws->far[0] = (uint32_t*)(base + o_f0);
   ws->far[1] = (uint32_t*)(base + o_f1);
   ws->farmark = (uint32_t*)(base + o_fm);
