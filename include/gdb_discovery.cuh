@@ -412,10 +412,12 @@ __device__ inline bool xf_barrier_combined(const DiscoveryArgs& a, LocalCtx* l, 
       int* word = (int*)&c->gen[l->id % kReleaseCopies].v;
       ok = spin_until(c, l->timeout_ns, 7, [&] { return ld_acquire(word) != g0; }, kBarrierSpin);
       if (ok) l->gen = (unsigned)(g0 + 1);  // one bump per barrier
-      l->ok = ok;
+      else l->ok = 0;
+      l->barriers++;
     }
+    // one CTA barrier between the release and the slave's next superstep
     __syncthreads();
-    ok = l->ok;
+    return l->ok != 0;
   }
   if (threadIdx.x == 0) {
     if (!ok) l->ok = 0;
