@@ -159,8 +159,12 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
     uint32_t lbase = 0, hcbase = 0, hvbase = 0, L = 0;
     for (;; ++L, ++t) {
       const int cur = t % 3, nx = (t + 1) % 3;
-      const uint32_t nl = ld_cg(&ws.lcnt[cur]);
-      const unsigned long long hp = __ldcg(&ws.hcnt[cur]);
+      const unsigned long long* sc = cta_words<2>([&](unsigned long long* w) {
+        w[0] = ld_cg(&ws.lcnt[cur]);
+        w[1] = __ldcg(&ws.hcnt[cur]);
+      });
+      const uint32_t nl = (uint32_t)sc[0];
+      const unsigned long long hp = sc[1];
       const uint32_t nhv = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
       if (leader && L < ws.max_levels) {
         ws.lev_l[L] = lbase;
@@ -234,9 +238,16 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
     for (int32_t Lb = (int32_t)levels - 1; Lb >= 0; --Lb, ++t) {
       const int cur = t % 3;
       reset_slot(t);
-      const uint32_t lb = ld_cg(&ws.lev_l[Lb]), le = ld_cg(&ws.lev_l[Lb + 1]);
-      const uint32_t hcb = ld_cg(&ws.lev_h[Lb]), hvb = ld_cg(&ws.lev_hv[Lb]);
-      const uint32_t nch = ld_cg(&ws.lev_hc[Lb]);
+      const unsigned long long* lv = cta_words<5>([&](unsigned long long* w) {
+        w[0] = ld_cg(&ws.lev_l[Lb]);
+        w[1] = ld_cg(&ws.lev_l[Lb + 1]);
+        w[2] = ld_cg(&ws.lev_h[Lb]);
+        w[3] = ld_cg(&ws.lev_hv[Lb]);
+        w[4] = ld_cg(&ws.lev_hc[Lb]);
+      });
+      const uint32_t lb = (uint32_t)lv[0], le = (uint32_t)lv[1];
+      const uint32_t hcb = (uint32_t)lv[2], hvb = (uint32_t)lv[3];
+      const uint32_t nch = (uint32_t)lv[4];
       // rho[v] / rho[u] * (1 + sigma[u]) with the u factor precomputed once
       // per vertex (coef) instead of a division per arc
       auto bwd_arc = [&](bool valid, uint32_t arc, float rv, double& acc) {

@@ -111,13 +111,28 @@ __device__ __noinline__ void bfs_decide(const GraphView& G, const BfsWs& ws, con
   }
 }
 
-// Top-down expansion of level L into L+1.
+// The queue counts of level slot `cur` (light count, packed heavy count),
+// loaded once per CTA into shared memory; every thread of the CTA calls it
+// and reads the two words until the next call.
+__device__ __forceinline__ const unsigned long long* level_counts(const BfsWs& ws, int cur) {
+  __shared__ unsigned long long s[2];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s[0] = ld_cg(&ws.qcount[cur]);
+    s[1] = ld_cg_u64(&ws.hcount[cur]);
+  }
+  __syncthreads();
+  return s;
+}
+
+// Top-down expansion of level L into L+1; sc: the level's counts from
+// level_counts.
 __device__ __forceinline__ void bfs_top_down(const GraphView& G, const Warps& W, const BfsWs& ws,
-                                             uint32_t L, unsigned long long& arcs,
-                                             unsigned long long& farcs) {
+                                             uint32_t L, const unsigned long long* sc,
+                                             unsigned long long& arcs, unsigned long long& farcs) {
   const int cur = L % 3, nxt = (L + 1) % 3;
-  const uint32_t n = ld_cg(&ws.qcount[cur]);
-  const unsigned long long hp = ld_cg_u64(&ws.hcount[cur]);
+  const uint32_t n = (uint32_t)sc[0];
+  const unsigned long long hp = sc[1];
   Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
                ws.qcap, ws.hcap, ws.overflow};
   auto edge = [&](bool valid, uint32_t arc) {
@@ -257,8 +272,9 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
   unsigned long long mu = G.E - mf;
   for (;; ++L) {
     const int cur = L % 3, old = (L + 2) % 3;
-    const uint32_t n = ld_cg(&ws.qcount[cur]);
-    const unsigned long long hp = ld_cg_u64(&ws.hcount[cur]);
+    const unsigned long long* sc = level_counts(ws, cur);
+    const uint32_t n = (uint32_t)sc[0];
+    const unsigned long long hp = sc[1];
     if (n == 0 && hp == 0) break;
     if (ws.adaptive == kBfsHeuristic) {
       if (L > 0) {
@@ -280,7 +296,7 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
     }
     unsigned long long farcs = 0;
     if (bottom_up) bfs_bottom_up(G, ws, L, W, arcs, farcs);
-    else bfs_top_down(G, W, ws, L, arcs, farcs);
+    else bfs_top_down(G, W, ws, L, sc, arcs, farcs);
     if (ws.adaptive) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) farcs += __shfl_xor_sync(kFull, farcs, o);
@@ -356,7 +372,7 @@ __global__ void __launch_bounds__(512, 3) k_bfs_level(GraphView G, BfsWs ws, uin
   W.nwarps = (gridDim.x * blockDim.x) >> 5;
   W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
   W.nthreads = gridDim.x * blockDim.x;
-  bfs_top_down(G, W, ws, L, arcs, farcs);
+  bfs_top_down(G, W, ws, L, level_counts(ws, L % 3), arcs, farcs);
   unsigned long long r = arcs;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(kFull, r, o);
@@ -385,7 +401,7 @@ __global__ void __launch_bounds__(512, 3) k_bfs_glevel(GraphView G, BfsWs ws, ui
   W.nwarps = (gridDim.x * blockDim.x) >> 5;
   W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
   W.nthreads = gridDim.x * blockDim.x;
-  bfs_top_down(G, W, ws, L, arcs, farcs);
+  bfs_top_down(G, W, ws, L, level_counts(ws, L % 3), arcs, farcs);
   unsigned long long r = arcs;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(kFull, r, o);

@@ -111,10 +111,10 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
         m = warp_min_u32(m);
         if (lane == 0 && m < big) atomicMin(&hmn[h], m);
       });
-      if (__any_sync(kFull, undecided_seen) && lane == 0) atomicOr(&ws.flag[cur], 1u);
+      cta_or(undecided_seen, &ws.flag[cur], 1u);
       if (!s.sync()) return;
       ++t;
-      if (ld_cg(&ws.flag[cur]) == 0) break;
+      if (cta_words<1>([&](unsigned long long* w) { w[0] = ld_cg(&ws.flag[cur]); })[0] == 0) break;
     }
     // ---- mis2: strict local minima join the set and decide their neighbours
     {
@@ -293,8 +293,12 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   unsigned long long coloured = 0;
   for (;; ++r) {
     const int cur = r % 3, nxt = (r + 1) % 3, old = (r + 2) % 3;
-    const uint32_t n = ld_cg(&ws.qcount[cur]);
-    const unsigned long long hp = __ldcg(&ws.hcount[cur]);
+    const unsigned long long* sc = cta_words<2>([&](unsigned long long* w) {
+      w[0] = ld_cg(&ws.qcount[cur]);
+      w[1] = __ldcg(&ws.hcount[cur]);
+    });
+    const uint32_t n = (uint32_t)sc[0];
+    const unsigned long long hp = sc[1];
     if (n == 0 && hp == 0) break;
     if (leader) {
       ws.qcount[old] = 0;

@@ -140,7 +140,7 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
       if (lane == 0 && hooked) atomicAdd(&ws.hooks[cur], hooked);
       if (!s.sync()) return;
       ++t;
-      if (ld_cg(&ws.hooks[cur]) == 0) break;
+      if (cta_words<1>([&](unsigned long long* w) { w[0] = ld_cg(&ws.hooks[cur]); })[0] == 0) break;
     }
     // ---- C: pointer jumping onto the roots
     for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {

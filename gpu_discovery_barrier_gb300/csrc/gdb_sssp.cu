@@ -96,13 +96,31 @@ __device__ __forceinline__ uint32_t dist_of(const SsspWs& ws, uint32_t v) {
   }
 }
 
+// The counts of superstep slot `cur` and of the far pile of `phase`
+// (light, packed heavy, pile size, pile minimum), loaded once per CTA into
+// shared memory; every thread of the CTA calls it and reads the words
+// until the next call.
+__device__ __forceinline__ const unsigned long long* step_counts(const SsspWs& ws, int cur,
+                                                                 uint32_t phase) {
+  __shared__ unsigned long long s[4];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s[0] = ld_cg(&ws.qcount[cur]);
+    s[1] = __ldcg(&ws.hcount[cur]);
+    s[2] = ws.delta ? ld_cg(&ws.farcount[phase % 3]) : 0u;
+    s[3] = ws.delta ? ld_cg(&ws.farmin[phase % 3]) : 0u;
+  }
+  __syncthreads();
+  return s;
+}
+
 template <bool Keyed>
 __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, const SsspWs& ws,
                                           uint32_t L, uint32_t split, uint32_t phase,
-                                          unsigned long long& arcs) {
+                                          const unsigned long long* sc, unsigned long long& arcs) {
   const int cur = L % 3, nxt = (L + 1) % 3;
-  const uint32_t n = ld_cg(&ws.qcount[cur]);
-  const unsigned long long hp = __ldcg(&ws.hcount[cur]);
+  const uint32_t n = (uint32_t)sc[0];
+  const unsigned long long hp = sc[1];
   Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
                ws.qcap, ws.hcap, ws.overflow};
   const uint32_t pile = phase + 1;
@@ -178,11 +196,11 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, co
 // into the next near frontier ([lo, split)), dropped settled entries
 // (< lo) and the pile of phase + 1 (>= split).
 __device__ __forceinline__ void far_filter(const GraphView& G, const Warps& W, const SsspWs& ws,
-                                           uint32_t L, uint32_t phase, uint32_t lo, uint32_t split) {
+                                           uint32_t L, uint32_t phase, uint32_t lo, uint32_t split,
+                                           uint32_t fn) {
   const int nxt = (L + 1) % 3;
   Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
                ws.qcap, ws.hcap, ws.overflow};
-  const uint32_t fn = ld_cg(&ws.farcount[phase % 3]);
   const uint32_t* pile = pick(ws.far, phase);
   const int lane = lane_id();
   for (uint32_t base = W.gwarp * 32; base < fn; base += W.nwarps * 32) {
@@ -247,8 +265,9 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
   uint32_t split = ws.delta ? ws.delta : 0xFFFFFFFFu, phase = 0;
   for (;; ++L) {
     const int cur = L % 3, old = (L + 2) % 3;
-    const bool dry = ld_cg(&ws.qcount[cur]) == 0 && __ldcg(&ws.hcount[cur]) == 0;
-    if (dry && (!ws.delta || ld_cg(&ws.farcount[phase % 3]) == 0)) break;
+    const unsigned long long* sc = step_counts(ws, cur, phase);
+    const bool dry = sc[0] == 0 && sc[1] == 0;
+    if (dry && (!ws.delta || sc[2] == 0)) break;
     if (leader) {
       ws.qcount[old] = 0;
       ws.hcount[old] = 0;
@@ -257,18 +276,17 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
     }
     if (dry) {
       const uint32_t lo = split;
-      const unsigned long long nx =
-          (unsigned long long)max(lo, ld_cg(&ws.farmin[phase % 3])) + ws.delta;
+      const unsigned long long nx = (unsigned long long)max(lo, (uint32_t)sc[3]) + ws.delta;
       split = (uint32_t)min(nx, 0xFFFFFFFFull);
       if (leader) {
         // slot (phase + 2) % 3 was last read by the previous phase change
         ws.farcount[(phase + 2) % 3] = 0;
         ws.farmin[(phase + 2) % 3] = 0xFFFFFFFFu;
       }
-      far_filter(G, W, ws, L, phase, lo, split);
+      far_filter(G, W, ws, L, phase, lo, split, (uint32_t)sc[2]);
       ++phase;
     } else {
-      sssp_step<true>(G, W, ws, L, split, phase, arcs);
+      sssp_step<true>(G, W, ws, L, split, phase, sc, arcs);
     }
     if (!s.sync()) return;
   }
@@ -339,7 +357,7 @@ __global__ void __launch_bounds__(512, 3) k_sssp_glevel(GraphView G, SsspWs ws, 
   W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
   W.nthreads = gridDim.x * blockDim.x;
   unsigned long long arcs = 0;
-  sssp_step<false>(G, W, ws, L, 0xFFFFFFFFu, 0, arcs);
+  sssp_step<false>(G, W, ws, L, 0xFFFFFFFFu, 0, step_counts(ws, L % 3, 0), arcs);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
   if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
@@ -449,9 +467,9 @@ __device__ __forceinline__ void jacobi_body(Sync& s, const GraphView& G, const J
     const int cur = k % 3, old = (k + 1) % 3;
     if (leader) ws.cursor[old] = ws.hcursor[old] = ws.changed[old] = 0;
     const bool ch = jacobi_iter(G, ws, k, smin, arcs);
-    if (__any_sync(kFull, ch) && lane_id() == 0) atomicOr(&ws.changed[cur], 1u);
+    cta_or(ch, &ws.changed[cur], 1u);
     if (!s.sync()) return;
-    if (ld_cg(&ws.changed[cur]) == 0) {
+    if (cta_words<1>([&](unsigned long long* w) { w[0] = ld_cg(&ws.changed[cur]); })[0] == 0) {
       ++k;
       break;
     }

@@ -367,6 +367,29 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x)
   }
   return x;
 }
+// Words every thread of the CTA needs at the start of a superstep (queue
+// counts, flags, level bounds): thread 0 loads them and the CTA shares
+// them through shared memory.  Thousands of warps loading one word at the
+// same moment queue on a single L2 slice; on the 4096^2 grid BFS that
+// queueing was more than a third of the level time.  Every thread of the
+// CTA calls it (two CTA barriers).
+// (Load fills N words; the words stay readable until the next call of the
+// same instantiation.)
+template <int N, class Load>
+__device__ __forceinline__ const unsigned long long* cta_words(Load&& load) {
+  __shared__ unsigned long long s[N];
+  __syncthreads();
+  if (threadIdx.x == 0) load(s);
+  __syncthreads();
+  return s;
+}
+
+// One atomicOr of `bit` into *word per CTA when any of its threads has `p`
+// (instead of one per warp).  Every thread of the CTA calls it.
+__device__ __forceinline__ void cta_or(bool p, uint32_t* word, uint32_t bit) {
+  if (__syncthreads_or(p) && threadIdx.x == 0) atomicOr(word, bit);
+}
+
 // Per-owner sums of one group_arcs step.  Owners never decrease from lane
 // to lane, so each owner's lanes are contiguous: a segmented suffix scan
 // leaves every segment's total in its first lane, which adds it to

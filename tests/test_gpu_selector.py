@@ -138,7 +138,30 @@ def test_selector_gains_over_plain(trained):
     p, _, _, (bfs_held, sssp_held) = trained
     with gdb.Ctx() as c:
         r = selector.regret(c, p, bfs_held, sssp_held)
-    # per-level push/pull on held-out graphs: faster than all-push, and
-    # within a bounded distance of the per-level optimum
-    assert r["bfs"]["gain_vs_plain"] > 1.05, r
-    assert r["bfs"]["regret"] < 0.5, r
+    b, s = r["bfs"], r["sssp"]
+    # on held-out graphs the network is never meaningfully slower than the
+    # plain schedule, and takes at least half of the gain the per-level
+    # (per-run) optimum offers over it
+    for d, t_sel, t_plain, t_opt in ((b, "selector_us", "plain_us", "optimal_us"),
+                                     (s, "selector_ms", "plain_ms", "optimal_ms")):
+        assert d[t_sel] <= 1.05 * d[t_plain], r  # sub-millisecond runs: 5 % of timing noise
+        if d[t_plain] > 1.05 * d[t_opt]:
+            assert d[t_plain] - d[t_sel] >= 0.5 * (d[t_plain] - d[t_opt]), r
+    assert b["regret"] < 0.5, r
+
+
+def test_learned_bfs_inspects_fewer_arcs(trained):
+    """Online, on a graph outside the training set: pull levels chosen by
+    the network skip most arcs of the big middle levels."""
+    p = trained[0]
+    g = gg.rmat(1 << 17, 16, seed=1234)
+    with gdb.Ctx() as c:
+        c.selector_set(p)
+        G = c.graph(g.row_ptr, g.col)
+        c.bfs(G, 1)
+        plain = c.last_stats()["edges_processed"]
+        c.set_options(schedule=gdb.SCHED_LEARNED)
+        got = c.bfs(G, 1)
+        learned = c.last_stats()["edges_processed"]
+    assert np.array_equal(got, oracle.bfs(g, 1))
+    assert learned < 0.7 * plain, (learned, plain)
