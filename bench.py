@@ -602,9 +602,11 @@ def run_grid(args, rank, world, local):
             r["barrier_ctas"] = groups
             res[name] = r
         c.set_options(barrier=gdb.BARRIER_XF, schedule=gdb.SCHED_PLAIN)
-    # the headline: the XF barrier under the learned schedule (plain when no
-    # selector weights are present); every kind and schedule is in the line
-    head = "xf_learned" if "xf_learned" in res else "xf"
+    # the headline: the XF barrier under its fastest schedule on this graph
+    # (plain, adaptive or learned, named in config); every barrier kind and
+    # schedule is in the line
+    xf_names = [k for k in ("xf", "xf_adaptive", "xf_learned") if k in res]
+    head = min(xf_names, key=lambda k: res[k]["bfs"]["ms"] + res[k]["sssp"]["ms"])
     xf = res[head]
     value = 2 * g.E / ((xf["bfs"]["ms"] + xf["sssp"]["ms"]) / 1e3)
     cfg = {"workload": "grid 4096x4096, BFS + SSSP from vertex 0", "V": g.V, "E": g.E,

@@ -65,49 +65,64 @@ __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
+// The master CTA's private decision state, in its shared memory: vertices
+// and arcs visited so far, the time of the previous decision (traces) and
+// the mode in force.
+struct DecideState {
+  unsigned long long vis_v, vis_a, tprev;
+  uint32_t mode;
+};
+
 // Decision for level Lnext, taken by the master CTA inside the barrier
-// that ends level Lnext - 1 (all of that level's pushes are complete).
-// stats[2] / stats[3]: vertices / arcs visited so far (master-only),
-// stats[4 + slot]: arcs of the frontier in that slot, stats[7]: time of
-// the previous decision.  Warp 0 computes; lane 0 writes.
+// that ends level Lnext - 1 (all of that level's pushes are complete):
+// stats[4 + slot] holds the arcs of the frontier in that slot.  Warp 0
+// computes; lane 0 writes the mode word ws.mode[0] -- only when the mode
+// changes, so that most releases wait for no store of the decision.
 __device__ __noinline__ void bfs_decide(const GraphView& G, const BfsWs& ws, const float* smlp,
-                                        uint32_t Lnext, uint32_t nwarps) {
+                                        DecideState* st, uint32_t Lnext, uint32_t nwarps) {
   if (threadIdx.x >= 32) return;
   const int slot = Lnext % 3;
-  const unsigned long long now = globaltimer();
   const uint32_t n = ld_cg(&ws.qcount[slot]);
   const unsigned long long hp = ld_cg_u64(&ws.hcount[slot]);
-  const unsigned long long nfi = (unsigned long long)n + (hp >> 32);
   const unsigned long long mfi = ld_cg_u64(&ws.stats[4 + slot]);
-  const unsigned long long vis_v = ld_cg_u64(&ws.stats[2]) + nfi;
-  const unsigned long long vis_a = ld_cg_u64(&ws.stats[3]) + mfi;
+  const unsigned long long nfi = (unsigned long long)n + (hp >> 32);
+  const unsigned long long vis_v = st->vis_v + nfi;
+  const unsigned long long vis_a = st->vis_a + mfi;
   const unsigned long long mu = G.E > vis_a ? G.E - vis_a : 0ull;
-  const uint32_t prev = Lnext ? ld_cg(&ws.mode[(Lnext + 2) % 3]) : 0u;
+  const uint32_t prev = st->mode;
   float x[kFeat];
   bfs_features(x, (float)nfi, (float)mfi, (float)mu, (float)G.V, (float)G.E,
                (float)(G.V > vis_v ? G.V - vis_v : 0ull), Lnext, prev, (float)ws.maxdeg, (float)nwarps);
   uint32_t mode = 0;
   if (ws.adaptive == kBfsLearned) {
-    float out[kOut];
-    mlp_warp(smlp, x, out);
-    mode = out[kOutPull] < out[kOutPush] ? 1u : 0u;
+    // a push level whose frontier holds under 1/1024 of the unvisited arcs
+    // stays push without evaluating the network: a pull level would scan
+    // every unvisited vertex for a handful of frontier vertices
+    if (prev != 0 || mfi * 1024ull >= mu) {
+      float out[kOut];
+      mlp_warp(smlp, x, out);
+      mode = out[kOutPull] < out[kOutPush] ? 1u : 0u;
+    }
   } else if (ws.adaptive == kBfsForcePull) {
     mode = 1;
   }
+  __syncwarp();
   if (threadIdx.x == 0) {
-    ws.mode[slot] = mode;
-    ws.stats[2] = vis_v;
-    ws.stats[3] = vis_a;
+    if (mode != prev) ws.mode[0] = mode;
+    st->mode = mode;
+    st->vis_v = vis_v;
+    st->vis_a = vis_a;
     if (ws.trace) {
+      const unsigned long long now = globaltimer();
       if (Lnext > 0 && Lnext - 1 < ws.trace_cap)
-        ws.trace[Lnext - 1].us = (float)(now - ws.stats[7]) * 1e-3f;
+        ws.trace[Lnext - 1].us = (float)(now - st->tprev) * 1e-3f;
       if (Lnext < ws.trace_cap && nfi > 0) {
         for (int i = 0; i < kFeat; ++i) ws.trace[Lnext].x[i] = x[i];
         ws.trace[Lnext].mode = mode;
         ws.trace[Lnext].us = 0.f;
       }
+      st->tprev = now;
     }
-    ws.stats[7] = now;
   }
 }
 
@@ -115,11 +130,13 @@ __device__ __noinline__ void bfs_decide(const GraphView& G, const BfsWs& ws, con
 // loaded once per CTA into shared memory; every thread of the CTA calls it
 // and reads the two words until the next call.
 __device__ __forceinline__ const unsigned long long* level_counts(const BfsWs& ws, int cur) {
-  __shared__ unsigned long long s[2];
+  __shared__ unsigned long long s[4];
   __syncthreads();
   if (threadIdx.x == 0) {
     s[0] = ld_cg(&ws.qcount[cur]);
     s[1] = ld_cg_u64(&ws.hcount[cur]);
+    s[2] = ws.adaptive >= kBfsLearned ? ld_cg(&ws.mode[0]) : 0u;  // the master's decision
+    s[3] = ws.adaptive == kBfsHeuristic ? ld_cg_u64(&ws.stats[4 + cur]) : 0ull;  // frontier arcs
   }
   __syncthreads();
   return s;
@@ -141,9 +158,18 @@ __device__ __forceinline__ void bfs_top_down(const GraphView& G, const Warps& W,
     if (valid) {
       u = __ldg(&G.col[arc]);
       ++arcs;
-      if (ld_cg(&ws.dist[u]) == kInf && atomicCAS(&ws.dist[u], kInf, L + 1) == kInf) {
-        want = true;
-        if (ws.adaptive) farcs += __ldg(&G.row[u + 1]) - __ldg(&G.row[u]);
+      if (ld_cg(&ws.dist[u]) == kInf) {
+        // the degree loads are issued before the claim, so that counting
+        // the next frontier's arcs adds no round trip after it
+        uint32_t r0 = 0, r1 = 0;
+        if (ws.adaptive) {
+          r0 = __ldg(&G.row[u]);
+          r1 = __ldg(&G.row[u + 1]);
+        }
+        if (atomicCAS(&ws.dist[u], kInf, L + 1) == kInf) {
+          want = true;
+          farcs += r1 - r0;
+        }
       }
     }
     frontier_push(G, out, want, u);
@@ -224,19 +250,21 @@ __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& w
 // barrier); a separate instantiation keeps the plain kernels' registers.
 template <bool Hooked, class Sync>
 __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsWs& ws, uint32_t src,
-                                         float* smlp) {
+                                         float* smlp, DecideState* dst) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
   constexpr bool hooked = Hooked;
-  if (Hooked && ws.adaptive == kBfsLearned) {
-    for (int i = threadIdx.x; i < kParams; i += blockDim.x) smlp[i] = __ldg(&ws.mlp[i]);
+  if constexpr (Hooked) {
+    if (ws.adaptive == kBfsLearned)
+      for (int i = threadIdx.x; i < kParams; i += blockDim.x) smlp[i] = __ldg(&ws.mlp[i]);
+    if (threadIdx.x == 0) *dst = DecideState{0, 0, 0, 0};  // read after the first barrier
   }
   // barrier ending level Lnext - 1; hooked schedules decide level Lnext in it
   auto level_sync = [&](uint32_t Lnext) {
     if constexpr (!Hooked) {
       return s.sync();
     } else {
-      return s.sync_hook([&] { bfs_decide(G, ws, smlp, Lnext, W.nwarps); });
+      return s.sync_hook([&] { bfs_decide(G, ws, smlp, dst, Lnext, W.nwarps); });
     }
   };
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) ws.dist[v] = kInf;
@@ -278,14 +306,14 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
     if (n == 0 && hp == 0) break;
     if (ws.adaptive == kBfsHeuristic) {
       if (L > 0) {
-        mf = ld_cg_u64(&ws.stats[4 + cur]);
+        mf = sc[3];
         mu = mu > mf ? mu - mf : 0;
       }
       const uint32_t nf = n + (uint32_t)(hp >> 32);
       if (!bottom_up && mf > mu / ws.alpha) bottom_up = true;
       else if (bottom_up && nf < G.V / ws.beta) bottom_up = false;
     } else if (hooked) {
-      bottom_up = ld_cg(&ws.mode[cur]) != 0;
+      bottom_up = sc[2] != 0;
     }
     if (leader) {
       ws.qcount[old] = 0;
@@ -315,27 +343,29 @@ __global__ void __launch_bounds__(512, 3) k_bfs_xf(DiscoveryArgs a, GraphView G,
   __shared__ LocalCtx l;
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
-  bfs_body<false>(s, G, ws, src, nullptr);
+  bfs_body<false>(s, G, ws, src, nullptr, nullptr);
 }
 
 __global__ void __launch_bounds__(512, 3) k_bfs_grid(GraphView G, BfsWs ws, uint32_t src) {
   GridSync s;
-  bfs_body<false>(s, G, ws, src, nullptr);
+  bfs_body<false>(s, G, ws, src, nullptr, nullptr);
 }
 
 __global__ void __launch_bounds__(512, 3) k_bfs_xf_sel(DiscoveryArgs a, GraphView G, BfsWs ws,
                                                        uint32_t src) {
   __shared__ LocalCtx l;
   __shared__ float smlp[kParams];
+  __shared__ DecideState dst;
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
-  bfs_body<true>(s, G, ws, src, smlp);
+  bfs_body<true>(s, G, ws, src, smlp, &dst);
 }
 
 __global__ void __launch_bounds__(512, 3) k_bfs_grid_sel(GraphView G, BfsWs ws, uint32_t src) {
   __shared__ float smlp[kParams];
+  __shared__ DecideState dst;
   GridSync s;
-  bfs_body<true>(s, G, ws, src, smlp);
+  bfs_body<true>(s, G, ws, src, smlp, &dst);
 }
 
 // Relaunch mode: init kernel, then one launch per level (no in-kernel barrier).
