@@ -37,6 +37,7 @@ CUDA_SOURCES = [
     "gdb_discovery.cu",
     "gdb_bfs.cu",
     "gdb_sssp.cu",
+    "gdb_arcsplit.cu",
     "gdb_mis_color.cu",
     "gdb_bc.cu",
     "gdb_mst.cu",

@@ -1,0 +1,382 @@
+// Light/heavy partition of a weighted CSR, the input of the near-far SSSP's
+// arc split (the edge classes of Meyer and Sanders' delta-stepping): for a
+// bound b, graph L holds every vertex's arcs of weight < b and graph H its
+// arcs of weight in [b, GDB_LONESTAR_INF), each in the original order, each
+// a complete CSR with its own heavy-vertex table, so the traversal kernels'
+// work distribution (warp groups of light vertices, 128-arc chunks of heavy
+// ones) applies to either half unchanged.  Arcs of weight >= the infinity
+// are never relaxed and belong to neither half.
+//
+// Everything is built on the device: per-vertex class counts (a warp per
+// vertex of degree <= 128, a CTA per heavier vertex), exclusive scans into
+// the two row arrays, an order-preserving scatter (ballot compaction), and
+// the heavy tables from scans of the halves' degrees.  Only totals come
+// back to the host.  The partition is cached on the graph per bound and
+// dropped when its weights change.
+#include <algorithm>
+
+#include "gdb_internal.h"
+
+namespace {
+
+using namespace gdb;
+
+constexpr int kScanThreads = 512;
+constexpr uint32_t kScanItems = 8;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;
+
+// Exclusive scan of one value per thread over the CTA; *total gets the sum.
+__device__ __forceinline__ uint32_t cta_exclusive(uint32_t x, uint32_t* total) {
+  __shared__ uint32_t wsum[32];
+  const int lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t inc = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = lane < nw ? wsum[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(kFull, s, o);
+      if (lane >= o) s += t;
+    }
+    if (lane < nw) wsum[lane] = s;  // inclusive warp totals
+  }
+  __syncthreads();
+  const uint32_t base = warp ? wsum[warp - 1] : 0u;
+  *total = wsum[nw - 1];
+  __syncthreads();
+  return base + inc - x;
+}
+
+// Scan, pass 1: the sum of every tile of kScanTile items.
+__global__ void __launch_bounds__(kScanThreads) k_tile_sums(const uint32_t* in, uint32_t n,
+                                                            uint32_t* sums) {
+  const uint64_t t0 = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+  uint32_t s = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kScanItems; ++k)
+    if (t0 + k < n) s += in[t0 + k];
+  uint32_t total;
+  cta_exclusive(s, &total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Scan, pass 2 (one CTA): exclusive scan of the tile sums in place;
+// sums[nt] = the grand total.
+__global__ void __launch_bounds__(kScanThreads) k_scan_sums(uint32_t* sums, uint32_t nt) {
+  uint32_t carry = 0;
+  for (uint32_t b = 0; b < nt; b += kScanThreads) {
+    const uint32_t i = b + threadIdx.x;
+    const uint32_t x = i < nt ? sums[i] : 0u;
+    uint32_t total;
+    const uint32_t ex = cta_exclusive(x, &total);
+    if (i < nt) sums[i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) sums[nt] = carry;
+}
+
+// Scan, pass 3: out[i] = exclusive prefix of in[i]; out[n] = the total.
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* in, uint32_t n,
+                                                             const uint32_t* sums, uint32_t nt,
+                                                             uint32_t* out) {
+  const uint64_t t0 = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems], s = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < kScanItems; ++k) {
+    v[k] = t0 + k < n ? in[t0 + k] : 0u;
+    s += v[k];
+  }
+  uint32_t total;
+  uint32_t run = sums[blockIdx.x] + cta_exclusive(s, &total);
+#pragma unroll
+  for (uint32_t k = 0; k < kScanItems; ++k) {
+    if (t0 + k < n) out[t0 + k] = run;
+    run += v[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = sums[nt];
+}
+
+__device__ __forceinline__ bool is_light(uint32_t w, uint32_t bound) { return w < bound; }
+__device__ __forceinline__ bool is_heavy_arc(uint32_t w, uint32_t bound) {
+  return w >= bound && w < kInf;
+}
+
+// Light and heavy arc counts of every vertex.
+__global__ void k_split_count(GraphView G, uint32_t bound, uint32_t* nl, uint32_t* nh) {
+  // vertices of degree > kHeavyDeg: one CTA each
+  for (uint32_t h = blockIdx.x; h < G.nheavy; h += gridDim.x) {
+    const uint32_t v = G.heavy_v[h];
+    const uint32_t b = G.row[v], e = G.row[v + 1];
+    uint32_t cl = 0, ch = 0;
+    for (uint32_t a = b + threadIdx.x; a < e; a += blockDim.x) {
+      const uint32_t w = __ldg(&G.w[a]);
+      cl += is_light(w, bound);
+      ch += is_heavy_arc(w, bound);
+    }
+    uint32_t tl, th;
+    cta_exclusive(cl, &tl);
+    cta_exclusive(ch, &th);
+    if (threadIdx.x == 0) {
+      nl[v] = tl;
+      nh[v] = th;
+    }
+  }
+  // the others: one warp each
+  const Warps W = warps_of(blockIdx.x, gridDim.x);
+  const int lane = lane_id();
+  for (uint32_t v = W.gwarp; v < G.V; v += W.nwarps) {
+    if (is_heavy(G, v)) continue;
+    const uint32_t b = G.row[v], e = G.row[v + 1];
+    uint32_t cl = 0, ch = 0;
+    for (uint32_t a0 = b; a0 < e; a0 += 32) {
+      const uint32_t a = a0 + lane;
+      const uint32_t w = a < e ? __ldg(&G.w[a]) : kInf;
+      cl += __popc(__ballot_sync(kFull, a < e && is_light(w, bound)));
+      ch += __popc(__ballot_sync(kFull, a < e && is_heavy_arc(w, bound)));
+    }
+    if (lane == 0) {
+      nl[v] = cl;
+      nh[v] = ch;
+    }
+  }
+}
+
+// Order-preserving scatter of every vertex's arcs into the two halves.
+__global__ void k_split_scatter(GraphView G, uint32_t bound, const uint32_t* rl, const uint32_t* rh,
+                                uint32_t* cl, uint32_t* wl, uint32_t* ch, uint32_t* wh) {
+  __shared__ uint32_t wsum[2][32];
+  const int lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (uint32_t h = blockIdx.x; h < G.nheavy; h += gridDim.x) {
+    const uint32_t v = G.heavy_v[h];
+    const uint32_t b = G.row[v], e = G.row[v + 1];
+    uint32_t ol = rl[v], oh = rh[v];
+    for (uint32_t a0 = b; a0 < e; a0 += blockDim.x) {
+      const uint32_t a = a0 + threadIdx.x;
+      const bool ok = a < e;
+      const uint32_t w = ok ? __ldg(&G.w[a]) : kInf;
+      const uint32_t c = ok ? __ldg(&G.col[a]) : 0u;
+      const bool il = ok && is_light(w, bound), ih = ok && is_heavy_arc(w, bound);
+      const unsigned ml = __ballot_sync(kFull, il), mh = __ballot_sync(kFull, ih);
+      if (lane == 0) {
+        wsum[0][warp] = __popc(ml);
+        wsum[1][warp] = __popc(mh);
+      }
+      __syncthreads();
+      uint32_t pl = 0, ph = 0, tl = 0, th = 0;
+      for (int k = 0; k < nw; ++k) {
+        if (k < warp) {
+          pl += wsum[0][k];
+          ph += wsum[1][k];
+        }
+        tl += wsum[0][k];
+        th += wsum[1][k];
+      }
+      if (il) {
+        const uint32_t p = ol + pl + __popc(ml & lanemask_lt());
+        cl[p] = c;
+        wl[p] = w;
+      }
+      if (ih) {
+        const uint32_t p = oh + ph + __popc(mh & lanemask_lt());
+        ch[p] = c;
+        wh[p] = w;
+      }
+      ol += tl;
+      oh += th;
+      __syncthreads();
+    }
+  }
+  const Warps W = warps_of(blockIdx.x, gridDim.x);
+  for (uint32_t v = W.gwarp; v < G.V; v += W.nwarps) {
+    if (is_heavy(G, v)) continue;
+    const uint32_t b = G.row[v], e = G.row[v + 1];
+    uint32_t ol = rl[v], oh = rh[v];
+    for (uint32_t a0 = b; a0 < e; a0 += 32) {
+      const uint32_t a = a0 + lane;
+      const bool ok = a < e;
+      const uint32_t w = ok ? __ldg(&G.w[a]) : kInf;
+      const uint32_t c = ok ? __ldg(&G.col[a]) : 0u;
+      const bool il = ok && is_light(w, bound), ih = ok && is_heavy_arc(w, bound);
+      const unsigned ml = __ballot_sync(kFull, il), mh = __ballot_sync(kFull, ih);
+      if (il) {
+        const uint32_t p = ol + __popc(ml & lanemask_lt());
+        cl[p] = c;
+        wl[p] = w;
+      }
+      if (ih) {
+        const uint32_t p = oh + __popc(mh & lanemask_lt());
+        ch[p] = c;
+        wh[p] = w;
+      }
+      ol += __popc(ml);
+      oh += __popc(mh);
+    }
+  }
+}
+
+// Heavy-vertex marks of a CSR given by its row array: flag (degree >
+// kHeavyDeg), chunk count, the membership bitmap and the largest degree.
+__global__ void k_heavy_marks(const uint32_t* row, uint32_t V, uint32_t* flag, uint32_t* nch,
+                              uint32_t* bits, uint32_t* maxdeg) {
+  const Warps W = warps_of(blockIdx.x, gridDim.x);
+  const int lane = lane_id();
+  uint32_t md = 0;
+  for (uint32_t base = W.gwarp * 32; base < V; base += W.nwarps * 32) {
+    const uint32_t v = base + lane;
+    const uint32_t d = v < V ? row[v + 1] - row[v] : 0u;
+    const bool hv = d > kHeavyDeg;
+    if (v < V) {
+      flag[v] = hv;
+      nch[v] = hv ? chunks_of(d) : 0u;
+    }
+    const unsigned m = __ballot_sync(kFull, hv);
+    if (lane == 0) bits[base >> 5] = m;
+    md = max(md, d);
+  }
+  md = __reduce_max_sync(kFull, md);
+  if (lane == 0 && md) atomicMax(maxdeg, md);
+}
+
+// Heavy vertex list and chunk entries {vertex, chunk, heavy index, chunks}.
+__global__ void k_heavy_fill(const uint32_t* row, uint32_t V, const uint32_t* flag,
+                             const uint32_t* hidx, const uint32_t* cbase, uint32_t* heavy_v,
+                             uint4* chunks) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    if (!flag[v]) continue;
+    const uint32_t h = hidx[v], n = chunks_of(row[v + 1] - row[v]), cb = cbase[v];
+    heavy_v[h] = v;
+    for (uint32_t j = 0; j < n; ++j) chunks[cb + j] = make_uint4(v, j, h, n);
+  }
+}
+
+}  // namespace
+
+namespace gdbi {
+
+// out[0..n] = exclusive scan of in[0..n) and the total; `tmp` holds
+// scan_tmp_words(n) words.
+static uint32_t scan_tiles(uint32_t n) { return std::max<uint32_t>((n + kScanTile - 1) / kScanTile, 1); }
+static size_t scan_tmp_words(uint32_t n) { return (size_t)scan_tiles(n) + 1; }
+
+static cudaError_t exclusive_scan(const uint32_t* in, uint32_t n, uint32_t* out, uint32_t* tmp,
+                                  cudaStream_t st) {
+  const uint32_t nt = scan_tiles(n);
+  k_tile_sums<<<nt, kScanThreads, 0, st>>>(in, n, tmp);
+  k_scan_sums<<<1, kScanThreads, 0, st>>>(tmp, nt);
+  k_scan_tiles<<<nt, kScanThreads, 0, st>>>(in, n, tmp, nt, out);
+  return cudaGetLastError();
+}
+
+void arc_split_drop(gdb_graph* g) {
+  if (g->split_l) gdb_graph_destroy(g->split_l);
+  if (g->split_h) gdb_graph_destroy(g->split_h);
+  g->split_l = g->split_h = nullptr;
+  g->split_bound = 0;
+}
+
+// Heavy table of a derived CSR whose row array is on the device; `t0`,
+// `t1` (V + 1 words each) and `tmp` are scratch.
+static int heavy_table_device(gdb_ctx* c, gdb_graph* x, uint32_t* t0, uint32_t* t1, uint32_t* t2,
+                              uint32_t* t3, uint32_t* tmp, uint32_t* hs) {
+  const uint32_t V = x->V;
+  cudaStream_t st = c->stream;
+  const size_t nb = ((size_t)(V + 31) / 32 + 1) * 4;
+  GDB_CUDA(c, cudaMalloc(&x->heavy_bits, nb));
+  GDB_CUDA(c, cudaMemsetAsync(x->heavy_bits, 0, nb, st));
+  GDB_CUDA(c, cudaMemsetAsync(hs, 0, 16, st));
+  const int grid = 4 * c->sm_count;
+  k_heavy_marks<<<grid, 256, 0, st>>>(x->row, V, t0, t1, x->heavy_bits, hs + 2);
+  GDB_CUDA(c, cudaGetLastError());
+  GDB_CUDA(c, exclusive_scan(t0, V, t2, tmp, st));
+  GDB_CUDA(c, exclusive_scan(t1, V, t3, tmp, st));
+  GDB_CUDA(c, cudaMemcpyAsync(hs, t2 + V, 4, cudaMemcpyDeviceToDevice, st));
+  GDB_CUDA(c, cudaMemcpyAsync(hs + 1, t3 + V, 4, cudaMemcpyDeviceToDevice, st));
+  uint32_t* hh = (uint32_t*)pinned(c, 64);
+  if (!hh) return GDB_ERR_OOM;
+  GDB_CUDA(c, cudaMemcpyAsync(hh, hs, 12, cudaMemcpyDeviceToHost, st));
+  GDB_CUDA(c, cudaStreamSynchronize(st));
+  x->nheavy = hh[0];
+  x->nheavy_chunks = hh[1];
+  x->maxdeg = hh[2];
+  GDB_CUDA(c, cudaMalloc(&x->heavy_v, std::max<size_t>(x->nheavy, 1) * 4));
+  GDB_CUDA(c, cudaMalloc(&x->heavy_chunk, std::max<size_t>(x->nheavy_chunks, 1) * sizeof(uint4)));
+  k_heavy_fill<<<grid, 256, 0, st>>>(x->row, V, t0, t2, t3, x->heavy_v, x->heavy_chunk);
+  GDB_CUDA(c, cudaGetLastError());
+  return GDB_OK;
+}
+
+static gdb_graph* new_half(gdb_ctx* c, uint32_t V) {
+  gdb_graph* x = new gdb_graph();
+  x->ctx = c;
+  x->V = V;
+  return x;
+}
+
+int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
+  if (!g->w) return set_error(c, GDB_ERR_INVALID, "arc split needs weights");
+  if (g->split_l && g->split_bound == bound) return GDB_OK;
+  arc_split_drop(g);
+  const uint32_t V = g->V;
+  cudaStream_t st = c->stream;
+  gdb_graph* L = new_half(c, V);
+  gdb_graph* H = new_half(c, V);
+  // scratch: four V + 1 word arrays, the scan's tile sums, totals
+  const size_t vw = (size_t)V + 1;
+  uint32_t* scratch = nullptr;
+  const size_t words = 4 * vw + scan_tmp_words(V) + 8;
+  int rc = GDB_OK;
+  auto fail = [&](int r) {
+    if (scratch) cudaFreeAsync(scratch, st);
+    cudaStreamSynchronize(st);
+    gdb_graph_destroy(L);
+    gdb_graph_destroy(H);
+    return r;
+  };
+  cudaError_t e = cudaMallocAsync((void**)&scratch, words * 4, st);
+  if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split scratch"));
+  uint32_t *t0 = scratch, *t1 = t0 + vw, *t2 = t1 + vw, *t3 = t2 + vw, *tmp = t3 + vw,
+           *hs = tmp + scan_tmp_words(V);
+  e = cudaMalloc(&L->row, vw * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&H->row, vw * 4);
+  if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split rows"));
+  const GraphView G = g->view();
+  const int grid = 4 * c->sm_count;
+  k_split_count<<<grid, 256, 0, st>>>(G, bound, t0, t1);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = exclusive_scan(t0, V, L->row, tmp, st);
+  if (e == cudaSuccess) e = exclusive_scan(t1, V, H->row, tmp, st);
+  uint32_t* hh = (uint32_t*)pinned(c, 64);
+  if (!hh) return fail(GDB_ERR_OOM);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hh, L->row + V, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hh + 1, H->row + V, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split counts"));
+  L->E = hh[0];
+  H->E = hh[1];
+  e = cudaMalloc(&L->col, std::max<uint64_t>(L->E, 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&L->w, std::max<uint64_t>(L->E, 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&H->col, std::max<uint64_t>(H->E, 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&H->w, std::max<uint64_t>(H->E, 1) * 4);
+  if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split arcs"));
+  k_split_scatter<<<grid, 256, 0, st>>>(G, bound, L->row, H->row, L->col, L->w, H->col, H->w);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split scatter"));
+  if ((rc = heavy_table_device(c, L, t0, t1, t2, t3, tmp, hs))) return fail(rc);
+  if ((rc = heavy_table_device(c, H, t0, t1, t2, t3, tmp, hs))) return fail(rc);
+  cudaFreeAsync(scratch, st);
+  e = cudaStreamSynchronize(st);
+  scratch = nullptr;
+  if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split"));
+  g->split_l = L;
+  g->split_h = H;
+  g->split_bound = bound;
+  return GDB_OK;
+}
+
+}  // namespace gdbi

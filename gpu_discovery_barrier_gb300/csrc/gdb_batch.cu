@@ -43,6 +43,7 @@ struct gdb_batch {
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   uint32_t delta = 0;         // near-far bucket width of the SSSP launch
+  uint32_t light = GDB_LONESTAR_INF;  // its light-arc bound (split when < inf)
   unsigned long long host_stats[2][8] = {};
 };
 
@@ -147,7 +148,7 @@ int gdb_batch_create(gdb_ctx* c, gdb_graph* g, uint32_t apps, const uint32_t* so
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "batch sources"));
   if ((rc = batch_arm(b))) return fail(rc);
   bool relaunch = false;
-  if ((apps & GDB_BATCH_SSSP) && (rc = sssp_plan(c, g, nsrc, false, &b->delta, &relaunch))) return fail(rc);
+  if ((apps & GDB_BATCH_SSSP) && (rc = sssp_plan(c, g, nsrc, false, &b->delta, &relaunch, &b->light))) return fail(rc);
 
   gdb::DiscoveryArgs proto;
   proto.ctx = b->dctx;
@@ -167,7 +168,7 @@ int gdb_batch_create(gdb_ctx* c, gdb_graph* g, uint32_t apps, const uint32_t* so
   if (e == cudaSuccess) {
     if (apps & GDB_BATCH_BFS) rc = bfs_enqueue(c, g, b->ws_bfs, b->d_srcs, nsrc, b->d_bfs, cs, proto);
     if (rc == GDB_OK && (apps & GDB_BATCH_SSSP))
-      rc = sssp_enqueue(c, g, b->ws_sssp, b->d_srcs, nsrc, b->d_sssp, cs, proto, b->delta);
+      rc = sssp_enqueue(c, g, b->ws_sssp, b->d_srcs, nsrc, b->d_sssp, cs, proto, b->delta, b->light);
     cudaError_t e2 = cudaStreamEndCapture(cs, &b->graph);
     if (rc == GDB_OK && e2 != cudaSuccess) rc = set_cuda_error(c, e2, "batch capture");
   } else {

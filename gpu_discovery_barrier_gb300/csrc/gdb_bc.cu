@@ -183,6 +183,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       Frontier out{ws.order + nlbase, ws.hc + nhcbase, &ws.lcnt[nx], &ws.hcnt[nx], G.V - nlbase,
                    ws.hc_cap - nhcbase, ws.overflow, G.nheavy - nhvbase, ws.hleft + nhvbase,
                    ws.hacc + nhvbase};
+      WarpStage qs = frontier_stage(out, 0);
       const int32_t Li = (int32_t)L;
       // one arc of a level-L vertex: claim level L+1 or pull a parent's count
       auto fwd_arc = [&](bool valid, uint32_t arc, double& acc) {
@@ -200,7 +201,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
           }
         }
         // a claimed heavy vertex gets its chunk countdown armed by the push
-        frontier_push(G, out, want, u);
+        frontier_push_staged(G, out, qs, want, u);
       };
       visit_level(
           G, W, ws, lbase, nl, hcbase, hvbase, nch, &ws.cursor[cur], &ws.hcursor[cur],
@@ -225,6 +226,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
             if (heavy_done(ws, slot, part, nchunks, &tot) && lane == 0 && L > 0)
               ws.rho[v] = (float)tot;
           });
+      qs.flush();
       if (!s.sync()) return;
       lbase = nlbase;
       hcbase = nhcbase;

@@ -152,6 +152,7 @@ __device__ __forceinline__ void bfs_top_down(const GraphView& G, const Warps& W,
   const unsigned long long hp = sc[1];
   Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
                ws.qcap, ws.hcap, ws.overflow};
+  WarpStage qs = frontier_stage(out, 0);
   auto edge = [&](bool valid, uint32_t arc) {
     uint32_t u = 0;
     bool want = false;
@@ -172,12 +173,13 @@ __device__ __forceinline__ void bfs_top_down(const GraphView& G, const Warps& W,
         }
       }
     }
-    frontier_push(G, out, want, u);
+    frontier_push_staged(G, out, qs, want, u);
   };
   visit_frontier(
       G, W, pick(ws.q, L), n, pick(ws.hc, L), hp, &ws.cursor[cur], &ws.hcursor[cur],
       [&](bool valid, int, uint32_t, uint32_t arc) { edge(valid, arc); },
       [&](bool valid, uint32_t, uint32_t arc) { edge(valid, arc); });
+  qs.flush();
 }
 
 // Bottom-up step for level L+1: every unvisited vertex looks for a parent
@@ -195,6 +197,7 @@ __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& w
   const int nxt = (L + 1) % 3;
   Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
                ws.qcap, ws.hcap, ws.overflow};
+  WarpStage qs = frontier_stage(out, 0);
   const int lane = lane_id();
   const uint32_t ngroups = (G.V + 31) / 32;
   for (uint32_t g = W.gwarp; g < ngroups; g += W.nwarps) {
@@ -242,8 +245,9 @@ __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& w
       ws.dist[v] = L + 1;  // only this lane writes v
       farcs += deg;
     }
-    frontier_push(G, out, want, v);
+    frontier_push_staged(G, out, qs, want, v);
   }
+  qs.flush();
 }
 
 // Hooked: the learned and forced-mode schedules (a decision inside every

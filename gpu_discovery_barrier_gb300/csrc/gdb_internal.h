@@ -55,7 +55,13 @@ struct gdb_graph {
   uint4* heavy_chunk = nullptr;    // one entry per chunk: {v, chunk, heavy index, chunks}
   uint32_t* heavy_bits = nullptr;  // V-bit membership bitmap
   double wmean = -1.0;             // mean usable weight (< 0: not measured yet)
+  uint32_t wmax = 0;               // largest usable weight (with wmean)
   uint32_t maxdeg = 0;
+  // light/heavy partition of the arcs for the near-far SSSP's arc split
+  // (built on demand for bound split_bound; dropped with the weights)
+  gdb_graph* split_l = nullptr;
+  gdb_graph* split_h = nullptr;
+  uint32_t split_bound = 0;
   gdb::GraphView view() const;
 };
 
@@ -103,6 +109,11 @@ int finish_run(gdb_ctx* c);
 int reset_device_ctx(gdb_ctx* c, int skip);
 int read_participating(gdb_ctx* c, int* n);
 
+// Light (weight < bound) and heavy (bound <= weight < infinity) halves of
+// g's arcs as two CSRs with their own heavy tables, cached on g.
+int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound);
+void arc_split_drop(gdb_graph* g);
+
 // Heavy table construction from a host copy of row_ptr.
 int build_heavy_table(gdb_graph* g, const uint32_t* host_row);
 uint32_t chunk_capacity(const gdb_graph* g);
@@ -121,14 +132,15 @@ int bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, 
                 uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto);
 int sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
                  uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto,
-                 uint32_t delta);
+                 uint32_t delta, uint32_t light);
 size_t bc_workspace_bytes(const gdb_graph* g);
 int bc_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_sources, uint32_t nsrc,
                float* d_bc, cudaStream_t stream, const gdb::DiscoveryArgs& proto);
 // Schedule of one worklist SSSP run under c's options: near-far bucket
-// width (0 = label-correcting worklist) and graph relaunch (when allowed).
+// width (0 = label-correcting worklist), graph relaunch (when allowed) and
+// the light-arc bound of the light/heavy split (GDB_LONESTAR_INF = none).
 int sssp_plan(gdb_ctx* c, gdb_graph* g, uint32_t nsrc, bool allow_relaunch, uint32_t* delta,
-              bool* relaunch);
+              bool* relaunch, uint32_t* light);
 // Run-level selector features of an SSSP from nsrc sources.
 void sssp_features(gdb_ctx* c, const gdb_graph* g, uint32_t nsrc, float* x);
 

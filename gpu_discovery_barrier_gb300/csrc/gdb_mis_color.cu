@@ -278,12 +278,14 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   {
     Frontier out{pick(ws.q, 1), pick(ws.hc, 1), &ws.qcount[1], &ws.hcount[1], ws.qcap, ws.hcap,
                  ws.overflow};
+    WarpStage qs = frontier_stage(out, 0);
     for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
       const uint32_t v = g * 32 + lane;
       const bool first = v < G.V && ld_cg(&ws.cnt[v]) == 0;
       if (first) ws.color[v] = 1;
-      frontier_push(G, out, first, v);
+      frontier_push_staged(G, out, qs, first, v);
     }
+    qs.flush();
     if (leader) ws.cursor[2] = ws.hcursor[2] = 0;
   }
   if (!s.sync()) return;
@@ -309,6 +311,7 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
     coloured += (leader ? n + (uint32_t)(hp >> 32) : 0);
     Frontier out{pick(ws.q, r + 1), pick(ws.hc, r + 1), &ws.qcount[nxt], &ws.hcount[nxt],
                  ws.qcap, ws.hcap, ws.overflow};
+    WarpStage qs = frontier_stage(out, 0);
     const int32_t next_color = (int32_t)r + 1;
     float pv_lane = 0.f;
     auto relax = [&](bool valid, float pv, uint32_t arc) {
@@ -322,7 +325,7 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
           ready = true;
         }
       }
-      frontier_push(G, out, ready, u);
+      frontier_push_staged(G, out, qs, ready, u);
     };
     const uint32_t* q = pick(ws.q, r);
     const uint32_t k = group_width(n, W.nwarps);
@@ -346,6 +349,7 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
       chunk_range(G, ent, b, en);
       range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, pv, arc); });
     }
+    qs.flush();
     if (!s.sync()) return;
   }
 #pragma unroll

@@ -230,6 +230,7 @@ static int check_options(const gdb_options* o) {
   if (o->schedule < GDB_SCHED_PLAIN || o->schedule > GDB_SCHED_LEARNED) return GDB_ERR_INVALID;
   if (o->max_ctas < 0 || o->oversubscribe < 0) return GDB_ERR_INVALID;
   if (o->xf_release < 0 || o->xf_release > 2) return GDB_ERR_INVALID;
+  if (o->sssp_split < -1 || o->sssp_split > 1) return GDB_ERR_INVALID;
   return GDB_OK;
 }
 
@@ -414,6 +415,7 @@ int gdb_graph_set_weights(gdb_graph* g, const uint32_t* w) {
     g->owns_w = true;
   }
   g->wmean = -1.0;
+  arc_split_drop(g);
   if (g->E) GDB_CUDA(c, cudaMemcpyAsync(g->w, w, g->E * 4, cudaMemcpyHostToDevice, c->stream));
   GDB_CUDA(c, cudaStreamSynchronize(c->stream));
   return GDB_OK;
@@ -422,6 +424,7 @@ int gdb_graph_set_weights(gdb_graph* g, const uint32_t* w) {
 int gdb_graph_destroy(gdb_graph* g) {
   if (!g) return GDB_ERR_INVALID;
   if (g->ctx && g->ctx->stream) cudaStreamSynchronize(g->ctx->stream);
+  arc_split_drop(g);
   if (g->owns) {
     cudaFree(g->row);
     cudaFree(g->col);

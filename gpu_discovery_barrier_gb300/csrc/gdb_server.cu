@@ -64,6 +64,7 @@ struct Req {
 struct GraphEntry {
   gdb_graph* g = nullptr;
   uint32_t delta = 0;  // SSSP bucket width under the server's schedule
+  uint32_t light = GDB_LONESTAR_INF;  // and its light-arc bound
 };
 
 }  // namespace
@@ -187,7 +188,7 @@ int launch(gdb_server* s, Slot& sl, Req& r) {
   if (r.app == GDB_APP_BFS)
     rc = bfs_enqueue(c, g, ws, d_src, 1, (uint32_t*)out, sl.stream, proto);
   else if (r.app == GDB_APP_SSSP)
-    rc = sssp_enqueue(c, g, ws, d_src, 1, (uint32_t*)out, sl.stream, proto, ge.delta);
+    rc = sssp_enqueue(c, g, ws, d_src, 1, (uint32_t*)out, sl.stream, proto, ge.delta, ge.light);
   else
     rc = bc_enqueue(c, g, ws, d_src, 1, (float*)out, sl.stream, proto);
   if (rc) return rc;
@@ -353,7 +354,7 @@ int gdb_server_add_graph(gdb_server* s, gdb_graph* g, uint32_t* graph_id) {
   ge.g = g;
   if (g->w) {
     bool relaunch = false;
-    int rc = sssp_plan(s->sc, g, 1, false, &ge.delta, &relaunch);
+    int rc = sssp_plan(s->sc, g, 1, false, &ge.delta, &relaunch, &ge.light);
     if (rc) return rc;
   }
   std::lock_guard<std::mutex> lk(s->mu);

@@ -20,6 +20,15 @@
 //    rework to one bucket's width; the fixed point, and so every distance,
 //    is the same as the plain schedule's.
 //
+//    Light/heavy arc split (the edge classification of Meyer and Sanders'
+//    delta-stepping, J. Algorithms 49(1), 2003): an arc of weight >= the
+//    width cannot end inside the current bucket, so near supersteps relax
+//    only the light arcs (weight < width) of their frontier; every vertex a
+//    near superstep expands is appended once to a settle list, and when the
+//    bucket runs dry one superstep relaxes the heavy arcs of the bucket's
+//    vertices, each exactly once, at their final distance.  Re-expansions
+//    inside a bucket then touch only light arcs.
+//
 // 2. Pannotia Jacobi SSSP (mega_kernel, pannotia/graph_app/sssp/kernel/sssp_kernel.cl:170-244):
 //    y[v] = min(x[v], min_j data[j] + x[col[j]]) over the CSR given (the
 //    reference pulls over the transpose) until nothing changes.  The copy
@@ -61,6 +70,15 @@ struct SsspWs {
   uint32_t* farcount;          // [3]
   uint32_t* farmin;            // [3]
   uint32_t* farmark;           // phase + 1 of the pile holding the vertex
+  // light/heavy split (light < kInf): near supersteps relax arcs of weight
+  // < light; expanded vertices go once to the settle list (stamp = phase +
+  // 1 marks them), a run-long append-only frontier whose entries of one
+  // bucket are relaxed over their heavy arcs when the bucket runs dry
+  uint32_t light;
+  uint32_t* sq;
+  uint4* shc;
+  uint32_t* sqcount;
+  unsigned long long* shcount;
 };
 
 // Warp-aggregated append of the lanes' `want` vertices to the far pile of
@@ -79,14 +97,6 @@ __device__ __forceinline__ void far_push(const SsspWs& ws, uint32_t phase, bool 
   }
 }
 
-// Lower the minimum distance of the pile of `phase` by the lanes' `has` d.
-__device__ __forceinline__ void pile_min(const SsspWs& ws, uint32_t phase, bool has, uint32_t d) {
-  uint32_t dm = has ? d : 0xFFFFFFFFu;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) dm = min(dm, __shfl_xor_sync(kFull, dm, o));
-  if (lane_id() == 0 && dm != 0xFFFFFFFFu) atomicMin(&ws.farmin[phase % 3], dm);
-}
-
 template <bool Keyed>
 __device__ __forceinline__ uint32_t dist_of(const SsspWs& ws, uint32_t v) {
   if constexpr (Keyed) {
@@ -102,36 +112,53 @@ __device__ __forceinline__ uint32_t dist_of(const SsspWs& ws, uint32_t v) {
 // until the next call.
 __device__ __forceinline__ const unsigned long long* step_counts(const SsspWs& ws, int cur,
                                                                  uint32_t phase) {
-  __shared__ unsigned long long s[4];
+  __shared__ unsigned long long s[6];
   __syncthreads();
   if (threadIdx.x == 0) {
     s[0] = ld_cg(&ws.qcount[cur]);
     s[1] = __ldcg(&ws.hcount[cur]);
     s[2] = ws.delta ? ld_cg(&ws.farcount[phase % 3]) : 0u;
     s[3] = ws.delta ? ld_cg(&ws.farmin[phase % 3]) : 0u;
+    const bool split = ws.light < kInf;
+    s[4] = split ? ld_cg(ws.sqcount) : 0u;
+    s[5] = split ? (uint32_t)__ldcg(ws.shcount) : 0u;
   }
   __syncthreads();
   return s;
 }
 
+// One relaxation superstep over frontier (q[0, n), chunk entries hc[0,
+// nch)): arcs of weight in [wlo, whi) are relaxed; improvements below
+// `split` are pushed to the next frontier (slot L + 1), the others to the
+// far pile of `phase`.  With `record`, every expanded vertex not yet in the
+// settle list of this phase is appended to it (its work entries laid out
+// for graph GR, the view the settle superstep walks).
 template <bool Keyed>
-__device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, const SsspWs& ws,
-                                          uint32_t L, uint32_t split, uint32_t phase,
-                                          const unsigned long long* sc, unsigned long long& arcs) {
+__device__ __forceinline__ void sssp_sweep(const GraphView& G, const GraphView& GR, const Warps& W,
+                                           const SsspWs& ws, uint32_t L, uint32_t split,
+                                           uint32_t phase,
+                                           const uint32_t* q, uint32_t n, const uint4* hc,
+                                           uint32_t nch, uint32_t wlo, uint32_t whi, bool record,
+                                           unsigned long long& arcs) {
   const int cur = L % 3, nxt = (L + 1) % 3;
-  const uint32_t n = (uint32_t)sc[0];
-  const unsigned long long hp = sc[1];
   Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
                ws.qcap, ws.hcap, ws.overflow};
   const uint32_t pile = phase + 1;
+  const int lane = lane_id();
+  // queue appends (next frontier, far pile, settle list) are staged per
+  // warp in shared memory; the pile minimum is a per-lane register folded
+  // in once at the end
+  WarpStage qs = frontier_stage(out, 0);
+  WarpStage fs{warp_stage(1), pick(ws.far, phase), &ws.farcount[phase % 3], ws.qcap, ws.overflow};
+  uint32_t fmin = 0xFFFFFFFFu;   // lane's smallest far improvement
   auto relax = [&](bool valid, uint32_t du, uint32_t arc) {
     uint32_t v = 0, nd = 0;
     bool want = false, far = false;
     if (valid) {
-      ++arcs;
       v = __ldg(&G.col[arc]);
       const uint32_t wt = __ldg(&G.w[arc]);
-      if (wt < kInf) {
+      if (wt >= wlo && wt < whi) {
+        ++arcs;
         nd = du + wt;
         if constexpr (Keyed) {
           // the stamp part: L + 1 for a near push, 0 for a far one (so a
@@ -159,36 +186,51 @@ __device__ __forceinline__ void sssp_step(const GraphView& G, const Warps& W, co
         }
       }
     }
-    frontier_push(G, out, want, v);
+    frontier_push_staged(G, out, qs, want, v);
     if (ws.delta && __any_sync(kFull, far)) {
-      const bool add = far && ld_cg(&ws.farmark[v]) != pile && atomicExch(&ws.farmark[v], pile) != pile;
-      far_push(ws, phase, add, v);
       // improvements of vertices already in the pile lower its minimum too
-      pile_min(ws, phase, far, nd);
+      if (far) fmin = min(fmin, nd);
+      const bool add = far && ld_cg(&ws.farmark[v]) != pile && atomicExch(&ws.farmark[v], pile) != pile;
+      fs.add(add, v);
     }
   };
+  const Frontier settle{ws.sq, ws.shc, ws.sqcount, ws.shcount, ws.qcap, ws.hcap, ws.overflow};
+  WarpStage ss = frontier_stage(settle, 2);
+  // a vertex is in a superstep's frontier at most once, so a plain mark
+  // store dedupes expansions across the bucket's supersteps
+  auto remember = [&](bool act, uint32_t u) {
+    const bool add = act && ld_cg(&ws.stamp[u]) != pile;
+    if (add) ws.stamp[u] = pile;
+    frontier_push_staged(GR, settle, ss, add, u);
+  };
   // light groups: each lane reads its own vertex's distance once
-  const int lane = lane_id();
   const uint32_t k = group_width(n, W.nwarps);
   WorkTaker lt((n + k - 1) / k, W, &ws.cursor[cur]);
   for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
     const uint32_t i = g * k + lane;
     const bool act = (uint32_t)lane < k && i < n;
-    const uint32_t u = act ? ld_cg(&pick(ws.q, L)[i]) : 0u;
+    const uint32_t u = act ? ld_cg(&q[i]) : 0u;
     const uint32_t du = act ? dist_of<Keyed>(ws, u) : 0u;
+    if (record) remember(act, u);
     group_arcs(G, act, u, [&](bool valid, int owner, uint32_t arc) {
       relax(valid, __shfl_sync(kFull, du, owner), arc);
     });
   }
-  const uint32_t nch = (uint32_t)hp;
-  const uint4* hc = pick(ws.hc, L);
   WorkTaker ht(nch, W, &ws.hcursor[cur]);
   for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
     const uint4 ent = ld_cg(&hc[c]);
     const uint32_t du = dist_of<Keyed>(ws, ent.x);
+    if (record) remember(lane == 0 && ent.y == 0, ent.x);
     uint32_t b, en;
     chunk_range(G, ent, b, en);
     range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, du, arc); });
+  }
+  qs.flush();
+  if (record) ss.flush();
+  if (ws.delta) {
+    fs.flush();
+    fmin = __reduce_min_sync(kFull, fmin);
+    if (lane == 0 && fmin != 0xFFFFFFFFu) atomicMin(&ws.farmin[phase % 3], fmin);
   }
 }
 
@@ -203,6 +245,7 @@ __device__ __forceinline__ void far_filter(const GraphView& G, const Warps& W, c
                ws.qcap, ws.hcap, ws.overflow};
   const uint32_t* pile = pick(ws.far, phase);
   const int lane = lane_id();
+  uint32_t fmin = 0xFFFFFFFFu;  // lane's smallest kept distance
   for (uint32_t base = W.gwarp * 32; base < fn; base += W.nwarps * 32) {
     const uint32_t i = base + lane;
     const bool act = i < fn;
@@ -213,17 +256,24 @@ __device__ __forceinline__ void far_filter(const GraphView& G, const Warps& W, c
     if (keep) ws.farmark[v] = phase + 2;
     frontier_push(G, out, near, v);
     far_push(ws, phase + 1, keep, v);
-    pile_min(ws, phase + 1, keep, d);
+    if (keep) fmin = min(fmin, d);
   }
+  fmin = __reduce_min_sync(kFull, fmin);
+  if (lane == 0 && fmin != 0xFFFFFFFFu) atomicMin(&ws.farmin[(phase + 1) % 3], fmin);
 }
 
+// G: the arcs near supersteps relax (all arcs, or the light half under
+// the split); GH: the heavy half the settle supersteps relax (split only).
 template <class Sync>
-__device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const SsspWs& ws, uint32_t src) {
+__device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const GraphView& GH,
+                                          const SsspWs& ws, uint32_t src) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
+  const bool split_arcs = ws.light < kInf;
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.key[v] = (unsigned long long)kInf << 32;
     if (ws.delta) ws.farmark[v] = 0;
+    if (split_arcs) ws.stamp[v] = 0;
   }
   if (leader) {
     for (int i = 0; i < 3; ++i) {
@@ -237,6 +287,8 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
       }
     }
     *ws.overflow = 0;
+    *ws.sqcount = 0;
+    *ws.shcount = 0;
     ws.stats[0] = ws.stats[1] = ws.stats[2] = 0;
   }
   if (!s.sync()) return;
@@ -263,18 +315,29 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
   // every CTA derives split and phase from the same counters after each
   // barrier, so they stay uniform across the grid
   uint32_t split = ws.delta ? ws.delta : 0xFFFFFFFFu, phase = 0;
+  // settle-list entries (light vertices, chunk entries) already relaxed
+  uint32_t sdone = 0, hdone = 0;
+  const uint32_t whi = split_arcs ? ws.light : kInf;
   for (;; ++L) {
     const int cur = L % 3, old = (L + 2) % 3;
     const unsigned long long* sc = step_counts(ws, cur, phase);
     const bool dry = sc[0] == 0 && sc[1] == 0;
-    if (dry && (!ws.delta || sc[2] == 0)) break;
+    const uint32_t sn = (uint32_t)sc[4], hn = (uint32_t)sc[5];
+    const bool unsettled = sn > sdone || hn > hdone;
+    if (dry && !unsettled && (!ws.delta || sc[2] == 0)) break;
     if (leader) {
       ws.qcount[old] = 0;
       ws.hcount[old] = 0;
       ws.cursor[old] = 0;
       ws.hcursor[old] = 0;
     }
-    if (dry) {
+    if (dry && unsettled) {
+      // the bucket is settled: relax the heavy arcs of its vertices once
+      sssp_sweep<true>(GH, GH, W, ws, L, split, phase, ws.sq + sdone, sn - sdone, ws.shc + hdone,
+                       hn - hdone, ws.light, kInf, false, arcs);
+      sdone = sn;
+      hdone = hn;
+    } else if (dry) {
       const uint32_t lo = split;
       const unsigned long long nx = (unsigned long long)max(lo, (uint32_t)sc[3]) + ws.delta;
       split = (uint32_t)min(nx, 0xFFFFFFFFull);
@@ -286,7 +349,8 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
       far_filter(G, W, ws, L, phase, lo, split, (uint32_t)sc[2]);
       ++phase;
     } else {
-      sssp_step<true>(G, W, ws, L, split, phase, sc, arcs);
+      sssp_sweep<true>(G, GH, W, ws, L, split, phase, pick(ws.q, L), (uint32_t)sc[0],
+                       pick(ws.hc, L), (uint32_t)sc[1], 0u, whi, split_arcs, arcs);
     }
     if (!s.sync()) return;
   }
@@ -302,16 +366,18 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Sss
   }
 }
 
-__global__ void __launch_bounds__(512, 3) k_sssp_xf(DiscoveryArgs a, GraphView G, SsspWs ws, uint32_t src) {
+__global__ void __launch_bounds__(512, 3) k_sssp_xf(DiscoveryArgs a, GraphView G, GraphView GH,
+                                                     SsspWs ws, uint32_t src) {
   __shared__ LocalCtx l;
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
-  sssp_body(s, G, ws, src);
+  sssp_body(s, G, GH, ws, src);
 }
 
-__global__ void __launch_bounds__(512, 3) k_sssp_grid(GraphView G, SsspWs ws, uint32_t src) {
+__global__ void __launch_bounds__(512, 3) k_sssp_grid(GraphView G, GraphView GH, SsspWs ws,
+                                                       uint32_t src) {
   GridSync s;
-  sssp_body(s, G, ws, src);
+  sssp_body(s, G, GH, ws, src);
 }
 
 // Graph-relaunch mode (CUDA-graph WHILE node): an init launch, then one
@@ -357,7 +423,9 @@ __global__ void __launch_bounds__(512, 3) k_sssp_glevel(GraphView G, SsspWs ws, 
   W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
   W.nthreads = gridDim.x * blockDim.x;
   unsigned long long arcs = 0;
-  sssp_step<false>(G, W, ws, L, 0xFFFFFFFFu, 0, step_counts(ws, L % 3, 0), arcs);
+  const unsigned long long* sc = step_counts(ws, L % 3, 0);
+  sssp_sweep<false>(G, G, W, ws, L, 0xFFFFFFFFu, 0, pick(ws.q, L), (uint32_t)sc[0], pick(ws.hc, L),
+                    (uint32_t)sc[1], 0u, kInf, false, arcs);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
   if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
@@ -491,26 +559,30 @@ __global__ void __launch_bounds__(512, 3) k_jacobi_xf(DiscoveryArgs a, GraphView
   jacobi_body(s, G, ws, src, smin);
 }
 
-// Sum and count of the usable weights (< kInf), for the automatic bucket
-// width of the near-far schedule.
+// Sum, count and maximum of the usable weights (< kInf), for the automatic
+// bucket width of the near-far schedule and its light/heavy split.
 __global__ void k_weight_sum(const uint32_t* w, unsigned long long E, unsigned long long* out) {
   unsigned long long sum = 0, cnt = 0;
+  uint32_t mx = 0;
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < E;
        i += (unsigned long long)gridDim.x * blockDim.x) {
     const uint32_t x = __ldg(&w[i]);
     if (x < kInf) {
       sum += x;
       ++cnt;
+      mx = max(mx, x);
     }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     sum += __shfl_xor_sync(kFull, sum, o);
     cnt += __shfl_xor_sync(kFull, cnt, o);
+    mx = max(mx, __shfl_xor_sync(kFull, mx, o));
   }
   if (lane_id() == 0 && cnt) {
     atomicAdd(&out[0], sum);
     atomicAdd(&out[1], cnt);
+    atomicMax(&out[2], (unsigned long long)mx);
   }
 }
 
@@ -519,7 +591,8 @@ __global__ void k_weight_sum(const uint32_t* w, unsigned long long E, unsigned l
 using namespace gdbi;
 
 // Workspace of one worklist SSSP run: stamps, two light queues, two
-// chunk-entry queues, the 512-byte counter block.
+// chunk-entry queues, far piles and marks, the distance keys, the settle
+// list (light queue + chunk entries), the 512-byte counter block.
 static size_t sssp_layout(const gdb_graph* g, char* base, uint32_t* d_dist, SsspWs* ws, char** cnt_out) {
   const uint32_t V = g->V;
   const uint32_t hcap = chunk_capacity(g);
@@ -529,6 +602,7 @@ static size_t sssp_layout(const gdb_graph* g, char* base, uint32_t* d_dist, Sssp
   const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
   const size_t o_f0 = b.take((size_t)V * 4), o_f1 = b.take((size_t)V * 4), o_fm = b.take((size_t)V * 4);
   const size_t o_key = b.take((size_t)V * 8);
+  const size_t o_sq = b.take((size_t)V * 4), o_shc = b.take((size_t)hcap * 16);
   const size_t o_cnt = b.take(512);
   if (!base) return b.off;
   ws->dist = d_dist;
@@ -551,6 +625,11 @@ static size_t sssp_layout(const gdb_graph* g, char* base, uint32_t* d_dist, Sssp
   // cnt + 192: graph-relaunch control words
   ws->farcount = (uint32_t*)(cnt + 224);               // 3
   ws->farmin = (uint32_t*)(cnt + 240);                 // 3
+  ws->sqcount = (uint32_t*)(cnt + 256);
+  ws->shcount = (unsigned long long*)(cnt + 264);
+  ws->sq = (uint32_t*)(base + o_sq);
+  ws->shc = (uint4*)(base + o_shc);
+  ws->light = kInf;
   ws->qcap = V;
   ws->hcap = hcap;
   ws->srcs = nullptr;
@@ -564,74 +643,125 @@ size_t gdbi::sssp_workspace_bytes(const gdb_graph* g) {
   return sssp_layout(g, nullptr, nullptr, nullptr, nullptr);
 }
 
+// Mean and maximum usable weight, measured once per weight array.
+static int weight_summary(gdb_ctx* c, gdb_graph* g) {
+  if (g->wmean >= 0) return GDB_OK;
+  unsigned long long* d = nullptr;
+  unsigned long long* h = (unsigned long long*)pinned(c, 4096);
+  if (!h) return GDB_ERR_OOM;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, 24, c->stream));
+  cudaError_t e = cudaMemsetAsync(d, 0, 24, c->stream);
+  if (e == cudaSuccess && g->E) {
+    k_weight_sum<<<4 * c->sm_count, 256, 0, c->stream>>>(g->w, g->E, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, 24, cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(d, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return set_cuda_error(c, e, "weight summary");
+  g->wmean = h[1] ? (double)h[0] / (double)h[1] : 1.0;
+  g->wmax = (uint32_t)h[2];
+  return GDB_OK;
+}
+
 // Automatic bucket width: 32 x mean weight / mean degree (the heuristic
-// of Davidson et al.); the mean weight is measured once per weight array.
+// of Davidson et al.).
 static int sssp_auto_delta(gdb_ctx* c, gdb_graph* g, uint32_t* delta) {
   *delta = 1;
   if (!g->w || g->E == 0) return GDB_OK;
-  if (g->wmean < 0) {
-    unsigned long long* d = nullptr;
-    unsigned long long* h = (unsigned long long*)pinned(c, 4096);
-    if (!h) return GDB_ERR_OOM;
-    GDB_CUDA(c, cudaMallocAsync((void**)&d, 16, c->stream));
-    cudaError_t e = cudaMemsetAsync(d, 0, 16, c->stream);
-    if (e == cudaSuccess) {
-      k_weight_sum<<<4 * c->sm_count, 256, 0, c->stream>>>(g->w, g->E, d);
-      e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, c->stream);
-    cudaFreeAsync(d, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return set_cuda_error(c, e, "weight mean");
-    g->wmean = h[1] ? (double)h[0] / (double)h[1] : 1.0;
-  }
+  const int rc = weight_summary(c, g);
+  if (rc) return rc;
   const double deg = (double)g->E / std::max<uint32_t>(g->V, 1);
   const double dl = 32.0 * g->wmean / std::max(deg, 1.0);
   *delta = (uint32_t)std::min(std::max(dl, 1.0), 1e9);
   return GDB_OK;
 }
 
+// Automatic width: the Davidson et al. width, halved when the light/heavy
+// split is allowed and some arc weighs at least half of it (with heavy arcs
+// relaxed once per vertex, narrower buckets pay: on R-MAT-22 with U[1,255]
+// weights the split run takes 3.0 ms per source at widths 48-64 against 3.7
+// ms at the full width 128 and 4.2 ms for the worklist).
+static int sssp_auto_width(gdb_ctx* c, gdb_graph* g, uint32_t* delta) {
+  int rc = sssp_auto_delta(c, g, delta);
+  if (rc || c->opt.sssp_split < 0 || *delta < 2) return rc;
+  if (c->opt.sssp_split == 1 || g->wmax >= *delta / 2) *delta /= 2;
+  return GDB_OK;
+}
+
+// Light-arc bound of a near-far run of width `delta`: arcs of weight >=
+// delta are deferred to the settle superstep when options.sssp_split asks
+// for it (1) or, automatically (0), when the graph has such arcs; kInf =
+// no split.
+static int sssp_light_bound(gdb_ctx* c, gdb_graph* g, uint32_t delta, uint32_t* light) {
+  *light = kInf;
+  if (delta == 0 || c->opt.sssp_split < 0) return GDB_OK;
+  if (c->opt.sssp_split == 0) {
+    const int rc = weight_summary(c, g);
+    if (rc) return rc;
+    if (g->wmax < delta) return GDB_OK;
+  }
+  *light = std::min<uint32_t>(delta, kInf);
+  return arc_split(c, g, *light);
+}
+
+// The views a run walks: the light and heavy halves under the split, the
+// graph itself (twice) otherwise.
+static void split_views(gdb_graph* g, uint32_t light, GraphView* gn, GraphView* gh) {
+  if (light < kInf && g->split_l && g->split_bound == light) {
+    *gn = g->split_l->view();
+    *gh = g->split_h->view();
+  } else {
+    *gn = *gh = g->view();
+  }
+}
+
 // Schedule of one worklist SSSP run: the bucket width (0 = the
-// label-correcting worklist) and whether to run under graph relaunch.
+// label-correcting worklist), its light-arc bound and whether to run under
+// graph relaunch.
 //  * options.sssp_delta > 0: that width;
 //  * learned: the selector's cheapest of worklist, near-far at the
 //    automatic width, near-far at 4x that width and (where allowed) the
 //    worklist under graph relaunch;
-//  * adaptive: the automatic width;  * plain: the worklist.
+//  * adaptive: the automatic width;  * plain: the worklist;
+// and under options.sssp_split the light-arc bound of a near-far width.
 int gdbi::sssp_plan(gdb_ctx* c, gdb_graph* g, uint32_t nsrc, bool allow_relaunch, uint32_t* delta,
-                    bool* relaunch) {
+                    bool* relaunch, uint32_t* light) {
   *delta = 0;
   *relaunch = false;
+  *light = kInf;
+  int rc = GDB_OK;
   if (c->opt.sssp_delta) {
     *delta = c->opt.sssp_delta;
-    return GDB_OK;
+  } else if (c->opt.schedule == GDB_SCHED_ADAPTIVE) {
+    rc = sssp_auto_width(c, g, delta);
+  } else if (c->opt.schedule == GDB_SCHED_LEARNED) {
+    if (c->h_mlp.empty()) return set_error(c, GDB_ERR_INVALID, "learned schedule without a selector");
+    float x[kFeat], y[kOut];
+    sssp_features(c, g, std::max<uint32_t>(nsrc, 1), x);
+    mlp_host(c->h_mlp.data(), x, y);
+    int best = kOutSsspPlain;
+    for (int k = kOutSsspNearFar; k <= kOutSsspRelaunch; ++k) {
+      if (k == kOutSsspRelaunch && !allow_relaunch) continue;
+      if (y[k] < y[best]) best = k;
+    }
+    if (best == kOutSsspRelaunch) {
+      *relaunch = true;
+      return GDB_OK;
+    }
+    if (best != kOutSsspPlain) {
+      uint32_t d = 1;
+      rc = sssp_auto_width(c, g, &d);
+      *delta = best == kOutSsspNearFarWide ? (uint32_t)std::min<uint64_t>(4ull * d, 1000000000ull) : d;
+    }
   }
-  if (c->opt.schedule == GDB_SCHED_ADAPTIVE) return sssp_auto_delta(c, g, delta);
-  if (c->opt.schedule != GDB_SCHED_LEARNED) return GDB_OK;
-  if (c->h_mlp.empty()) return set_error(c, GDB_ERR_INVALID, "learned schedule without a selector");
-  float x[kFeat], y[kOut];
-  sssp_features(c, g, std::max<uint32_t>(nsrc, 1), x);
-  mlp_host(c->h_mlp.data(), x, y);
-  int best = kOutSsspPlain;
-  for (int k = kOutSsspNearFar; k <= kOutSsspRelaunch; ++k) {
-    if (k == kOutSsspRelaunch && !allow_relaunch) continue;
-    if (y[k] < y[best]) best = k;
-  }
-  if (best == kOutSsspRelaunch) {
-    *relaunch = true;
-    return GDB_OK;
-  }
-  if (best == kOutSsspPlain) return GDB_OK;
-  uint32_t d = 1;
-  int rc = sssp_auto_delta(c, g, &d);
   if (rc) return rc;
-  *delta = best == kOutSsspNearFarWide ? (uint32_t)std::min<uint64_t>(4ull * d, 1000000000ull) : d;
-  return GDB_OK;
+  return sssp_light_bound(c, g, *delta, light);
 }
 
 int gdbi::sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
                        uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto,
-                       uint32_t delta) {
+                       uint32_t delta, uint32_t light) {
   if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
   SsspWs ws;
   char* cnt = nullptr;
@@ -639,13 +769,17 @@ int gdbi::sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d
   ws.srcs = d_srcs;
   ws.nsrc = nsrc;
   ws.delta = delta;
+  // a plan whose partition was dropped since (new weights) runs unsplit
+  ws.light = delta && light < kInf && g->split_l && g->split_bound == light ? light : kInf;
+  GraphView GN, GH;
+  split_views(g, ws.light, &GN, &GH);
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, stream));
   Shape s;
   int rc = persistent_shape(c, (const void*)k_sssp_xf, c->opt.block_size, 0, &s, false);
   if (rc) return rc;
   DiscoveryArgs a = proto;
   a.expected = std::min(s.grid, s.fit);
-  k_sssp_xf<<<s.grid, c->opt.block_size, 0, stream>>>(a, g->view(), ws, 0u);
+  k_sssp_xf<<<s.grid, c->opt.block_size, 0, stream>>>(a, GN, GH, ws, 0u);
   GDB_CUDA(c, cudaGetLastError());
   return GDB_OK;
 }
@@ -657,11 +791,11 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
   if (nsrc && c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH)
     return set_error(c, GDB_ERR_UNSUPPORTED, "multi-source SSSP needs a persistent barrier");
-  uint32_t delta = 0;
+  uint32_t delta = 0, light = kInf;
   bool relaunch = false;
   int rc = c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH
                ? GDB_OK
-               : sssp_plan(c, g, nsrc ? nsrc : 1, nsrc == 0, &delta, &relaunch);
+               : sssp_plan(c, g, nsrc ? nsrc : 1, nsrc == 0, &delta, &relaunch, &light);
   if (rc) return rc;
   char* base = (char*)workspace(c, sssp_layout(g, nullptr, nullptr, nullptr, nullptr));
   if (!base) return GDB_ERR_OOM;
@@ -671,8 +805,13 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   ws.srcs = d_srcs;
   ws.nsrc = nsrc;
   ws.delta = delta;
-  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
+  // the split lives in the persistent kernels only (graph relaunch runs
+  // the plain worklist)
+  ws.light = relaunch ? kInf : light;
   const GraphView G = g->view();
+  GraphView GN, GH;
+  split_views(g, ws.light, &GN, &GH);
+  GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
   const int block = c->opt.block_size;
   const int kind = relaunch ? GDB_BARRIER_RELAUNCH_GRAPH : c->opt.barrier;
   c->last = gdb_run_stats{};
@@ -682,7 +821,7 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
     if (rc) return rc;
     DiscoveryArgs a = discovery_args(c, s);
     GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    k_sssp_xf<<<s.grid, block, 0, c->stream>>>(a, G, ws, src);
+    k_sssp_xf<<<s.grid, block, 0, c->stream>>>(a, GN, GH, ws, src);
     GDB_CUDA(c, cudaGetLastError());
     GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     rc = finish_run(c);
@@ -696,10 +835,10 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
     GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sssp_grid, block, 0));
     int grid = occ * c->sm_count;
     if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
-    GraphView Gc = G;
+    GraphView Gc = GN, GHc = GH;
     SsspWs wsc = ws;
     uint32_t srcc = src;
-    void* args[] = {(void*)&Gc, (void*)&wsc, (void*)&srcc};
+    void* args[] = {(void*)&Gc, (void*)&GHc, (void*)&wsc, (void*)&srcc};
     GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
     GDB_CUDA(c, cudaLaunchCooperativeKernel((const void*)k_sssp_grid, grid, block, args, 0, c->stream));
     GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
@@ -733,6 +872,7 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   c->last.supersteps = (uint32_t)hs[1];
   c->last.phases = (uint32_t)hs[2];
   c->last.sssp_delta = delta;
+  c->last.sssp_light = ws.light < kInf ? ws.light : 0u;
   return GDB_OK;
 }
 

@@ -31,6 +31,8 @@ constexpr uint32_t kInf = GDB_LONESTAR_INF;
 // groups of 32 vertices a warp takes per atomic on a work cursor (one
 // cursor word is shared by every warp of the grid, so grabs are batched)
 constexpr uint32_t kGrab = 4;
+// warps per CTA of the graph kernels (launch bounds of 512 threads)
+constexpr int kMaxGraphWarps = 16;
 
 struct GraphView {
   uint32_t V;
@@ -193,25 +195,11 @@ struct Frontier {
   double* hacc = nullptr;       // optional: FP64 accumulator per slot, cleared at push
 };
 
-// Warp-aggregated push of the lanes' `want` vertices; the warp writes each
-// heavy vertex's chunk entries together.
-__device__ __forceinline__ void frontier_push(const GraphView& G, const Frontier& F, bool want,
-                                              uint32_t v) {
+// The lanes' `heavy` vertices: the warp writes each one's chunk entries
+// together after one packed atomic on the frontier's heavy counter.
+__device__ __forceinline__ void frontier_push_heavy(const GraphView& G, const Frontier& F,
+                                                    bool heavy, uint32_t v) {
   const int lane = lane_id();
-  const bool heavy = want && is_heavy(G, v);
-  const bool light = want && !heavy;
-  const unsigned m = __ballot_sync(kFull, light);
-  if (m) {
-    const int leader = __ffs(m) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(F.qcount, (uint32_t)__popc(m));
-    base = __shfl_sync(kFull, base, leader);
-    if (light) {
-      const uint32_t slot = base + __popc(m & lanemask_lt());
-      if (slot < F.qcap) F.q[slot] = v;
-      else atomicExch(F.overflow, 1);
-    }
-  }
   for (unsigned hm = __ballot_sync(kFull, heavy); hm; hm &= hm - 1) {
     const int l = __ffs(hm) - 1;
     const uint32_t hvx = __shfl_sync(kFull, v, l);
@@ -234,6 +222,95 @@ __device__ __forceinline__ void frontier_push(const GraphView& G, const Frontier
       F.hacc[vslot] = 0.0;
     }
   }
+}
+
+// Warp-aggregated push of the lanes' `want` vertices (one atomic per warp
+// step on the light counter).
+__device__ __forceinline__ void frontier_push(const GraphView& G, const Frontier& F, bool want,
+                                              uint32_t v) {
+  const int lane = lane_id();
+  const bool heavy = want && is_heavy(G, v);
+  const bool light = want && !heavy;
+  const unsigned m = __ballot_sync(kFull, light);
+  if (m) {
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(F.qcount, (uint32_t)__popc(m));
+    base = __shfl_sync(kFull, base, leader);
+    if (light) {
+      const uint32_t slot = base + __popc(m & lanemask_lt());
+      if (slot < F.qcap) F.q[slot] = v;
+      else atomicExch(F.overflow, 1);
+    }
+  }
+  frontier_push_heavy(G, F, heavy, v);
+}
+
+// Per-warp staging of queue appends in shared memory: the lanes' entries
+// collect in the warp's 64-slot buffer and leave 32 at a time with one
+// counter atomic, instead of one atomic per warp step -- a counter word
+// that every warp of the grid hits is an L2 hot spot.  flush() before the
+// superstep's barrier.
+struct WarpStage {
+  uint32_t* buf;     // this warp's 64 slots
+  uint32_t* q;       // the queue and its counter
+  uint32_t* count;
+  uint32_t cap;
+  int* overflow;
+  uint32_t n = 0;    // staged entries (warp-uniform)
+
+  __device__ __forceinline__ void out(uint32_t x, uint32_t m) {
+    const int lane = lane_id();
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(count, m);
+    base = __shfl_sync(kFull, base, 0);
+    if ((uint32_t)lane < m) {
+      if (base + lane < cap) q[base + lane] = x;
+      else atomicExch(overflow, 1);
+    }
+  }
+  __device__ __forceinline__ void add(bool want, uint32_t v) {
+    const unsigned m = __ballot_sync(kFull, want);
+    if (!m) return;
+    const int lane = lane_id();
+    if (want) buf[n + __popc(m & lanemask_lt())] = v;
+    n += __popc(m);
+    if (n >= 32) {
+      __syncwarp();
+      const uint32_t x = buf[lane], r = n - 32;
+      const uint32_t y = (uint32_t)lane < r ? buf[32 + lane] : 0u;
+      __syncwarp();
+      if ((uint32_t)lane < r) buf[lane] = y;
+      __syncwarp();
+      out(x, 32);
+      n = r;
+    }
+  }
+  __device__ __forceinline__ void flush() {
+    __syncwarp();
+    if (n) out((uint32_t)lane_id() < n ? buf[lane_id()] : 0u, n);
+    n = 0;
+  }
+};
+
+// This warp's 64-slot staging buffer number k (0-2), shared by the
+// staged queues of a superstep.
+__device__ __forceinline__ uint32_t* warp_stage(int k) {
+  __shared__ uint32_t buf[3][kMaxGraphWarps][64];
+  return buf[k][threadIdx.x >> 5];
+}
+
+// A staged frontier: light entries through the warp's buffer k.
+__device__ __forceinline__ WarpStage frontier_stage(const Frontier& F, int k) {
+  return WarpStage{warp_stage(k), F.q, F.qcount, F.qcap, F.overflow};
+}
+
+// frontier_push with the light entries staged.
+__device__ __forceinline__ void frontier_push_staged(const GraphView& G, const Frontier& F,
+                                                     WarpStage& st, bool want, uint32_t v) {
+  const bool heavy = want && is_heavy(G, v);
+  st.add(want && !heavy, v);
+  frontier_push_heavy(G, F, heavy, v);
 }
 
 // One thread seeds a frontier with vertex v (the traversal's source).

@@ -23,7 +23,7 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libgdb.so"
 
-ABI_VERSION = 6  # GDB_ABI_VERSION of include/gdb.h
+ABI_VERSION = 7  # GDB_ABI_VERSION of include/gdb.h
 LONESTAR_INF = 1_000_000_000
 PANNOTIA_BIG = 99_999_999
 
@@ -47,14 +47,16 @@ class Options(C.Structure):
     _fields_ = [("device", C.c_int), ("block_size", C.c_int), ("max_ctas", C.c_int),
                 ("oversubscribe", C.c_int), ("lock", C.c_int), ("barrier", C.c_int),
                 ("schedule", C.c_int), ("xf_release", C.c_int), ("timeout_ns", C.c_uint64),
-                ("pull_alpha", C.c_uint32), ("push_beta", C.c_uint32), ("sssp_delta", C.c_uint32)]
+                ("pull_alpha", C.c_uint32), ("push_beta", C.c_uint32), ("sssp_delta", C.c_uint32),
+                ("sssp_split", C.c_int)]
 
 
 class RunStats(C.Structure):
     _fields_ = [("supersteps", C.c_uint32), ("participating", C.c_uint32),
                 ("launched", C.c_uint32), ("launches", C.c_uint32),
                 ("edges_processed", C.c_uint64), ("work_units", C.c_uint64),
-                ("kernel_ms", C.c_double), ("phases", C.c_uint32), ("sssp_delta", C.c_uint32)]
+                ("kernel_ms", C.c_double), ("phases", C.c_uint32), ("sssp_delta", C.c_uint32),
+                ("sssp_light", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

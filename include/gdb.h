@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GDB_ABI_VERSION 6
+#define GDB_ABI_VERSION 7
 
 /* Sentinels of the reference kernels. */
 #define GDB_LONESTAR_INF 1000000000u /* lonestar/apps/bfs/kernel/bfs_common.cl:35 */
@@ -102,6 +102,11 @@ typedef struct {
      GDB_SCHED_ADAPTIVE, the reference's label-correcting worklist under
      GDB_SCHED_PLAIN.  Distances are the same for every width. */
   uint32_t sssp_delta;
+  /* light/heavy arc split of the near-far schedule (delta-stepping's edge
+     classes): near supersteps relax only arcs lighter than the width, each
+     bucket's heavy arcs are relaxed once when it runs dry.  0 = automatic
+     (split when some weight >= the width), 1 = always, -1 = never. */
+  int sssp_split;
 } gdb_options;
 
 typedef struct {
@@ -114,6 +119,7 @@ typedef struct {
   double kernel_ms;          /* device time of the last run (CUDA events) */
   uint32_t phases;           /* SSSP near-far phase changes of the last run */
   uint32_t sssp_delta;       /* SSSP bucket width used (0 = plain worklist) */
+  uint32_t sssp_light;       /* light-arc bound of the split (0 = no split) */
 } gdb_run_stats;
 
 typedef struct {

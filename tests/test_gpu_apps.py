@@ -86,17 +86,57 @@ def test_sssp_barrier_kinds(barrier):
 
 @pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
 @pytest.mark.parametrize("delta", [1, 37, 300, 1 << 20])
-def test_sssp_near_far(name, g, delta):
-    """The near-far schedule reaches the same distances for every bucket width."""
+@pytest.mark.parametrize("split", [0, -1, 1])
+def test_sssp_near_far(name, g, delta, split):
+    """The near-far schedule reaches the same distances for every bucket
+    width, with and without the light/heavy arc split."""
     w = gg.uniform_weights(g, 1, 255, seed=1)
     gw = g.with_weights(w)
-    with gdb.Ctx(sssp_delta=delta) as c:
+    with gdb.Ctx(sssp_delta=delta, sssp_split=split) as c:
         G = c.graph(g.row_ptr, g.col, w)
         for src in sorted(set([0] + list(gg.sources(g, 2, seed=3)))):
             got = c.sssp(G, int(src))
             assert np.array_equal(got, oracle.sssp_worklist(gw, int(src))), (name, src, delta)
             st = c.last_stats()
             assert st["sssp_delta"] == delta
+            # automatic: split only when some arc is at least as heavy as the width
+            on = split == 1 or (split == 0 and g.E > 0 and delta <= int(w.max()))
+            assert st["sssp_light"] == (delta if on else 0)
+
+
+@pytest.mark.parametrize("split", [-1, 1])
+def test_sssp_split_skips_heavy_rework(split):
+    """On R-MAT with U[1,255] weights the split relaxes far fewer arcs than
+    plain near-far at the same width (heavy arcs once per vertex)."""
+    g = gg.rmat(1 << 15, 16, seed=21)
+    w = gg.uniform_weights(g, 1, 255, seed=4)
+    want = oracle.sssp_worklist(g.with_weights(w), 3)
+    with gdb.Ctx(sssp_delta=32, sssp_split=split) as c:
+        G = c.graph(g.row_ptr, g.col, w)
+        assert np.array_equal(c.sssp(G, 3), want)
+        st = c.last_stats()
+    reached = int(np.diff(g.row_ptr.astype(np.int64))[want < gdb.LONESTAR_INF].sum())
+    if split == 1:
+        assert st["edges_processed"] < 1.5 * reached, (st, reached)
+    else:
+        assert st["edges_processed"] > 1.5 * reached, (st, reached)
+
+
+def test_sssp_split_zero_and_infinite_weights():
+    """Weight-0 arcs are light, arcs of weight >= 1e9 are never relaxed --
+    in near and settle supersteps alike."""
+    g = gg.rmat(1 << 12, 12, seed=5)
+    rng = np.random.default_rng(6)
+    w = rng.integers(0, 400, g.E).astype(np.uint32)
+    w[rng.random(g.E) < 0.1] = 0
+    w[rng.random(g.E) < 0.05] = gdb.LONESTAR_INF
+    w[rng.random(g.E) < 0.02] = 4_000_000_000
+    gw = g.with_weights(w)
+    for delta in (1, 16, 200):
+        with gdb.Ctx(sssp_delta=delta, sssp_split=1) as c:
+            G = c.graph(g.row_ptr, g.col, w)
+            for src in (0, 7, 100):
+                assert np.array_equal(c.sssp(G, src), oracle.sssp_worklist(gw, src)), (delta, src)
 
 
 @pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC])
@@ -122,10 +162,11 @@ def test_sssp_near_far_multi_source():
     g = gg.rmat(1 << 12, 16, seed=8)
     w = gg.uniform_weights(g, 1, 255, seed=8)
     srcs = [int(s) for s in gg.sources(g, 4, seed=1)]
-    with gdb.Ctx(sssp_delta=50) as c:
-        G = c.graph(g.row_ptr, g.col, w)
-        want = np.minimum.reduce([oracle.sssp_worklist(g.with_weights(w), s) for s in srcs])
-        assert np.array_equal(c.sssp_multi(G, srcs), want)
+    want = np.minimum.reduce([oracle.sssp_worklist(g.with_weights(w), s) for s in srcs])
+    for split in (-1, 1):
+        with gdb.Ctx(sssp_delta=50, sssp_split=split) as c:
+            G = c.graph(g.row_ptr, g.col, w)
+            assert np.array_equal(c.sssp_multi(G, srcs), want)
 
 
 @pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)

@@ -150,10 +150,13 @@ def test_selector_gains_over_plain(trained):
     assert b["regret"] < 0.5, r
 
 
-def test_learned_bfs_inspects_fewer_arcs(trained):
-    """Online, on a graph outside the training set: pull levels chosen by
-    the network skip most arcs of the big middle levels."""
-    p = trained[0]
+def test_learned_bfs_inspects_fewer_arcs():
+    """Online, with the shipped network on a graph outside its training set:
+    pull levels chosen by the network skip most arcs of the big middle
+    levels.  (The network the tests above train on small graphs alone has
+    seen too few levels where pull pays to be held to this.)"""
+    p = selector.load()
+    assert p is not None, "selector_weights.json missing"
     g = gg.rmat(1 << 17, 16, seed=1234)
     with gdb.Ctx() as c:
         c.selector_set(p)
