@@ -15,13 +15,18 @@
 //    reference's float CAS-loop atomics becomes a per-vertex pull;
 //  * backward, level L (deepest first): every vertex of the level pulls
 //    rho[v]/rho[u] * (1 + sigma[u]) from its level L+1 neighbours;
-//  * each vertex's sum is accumulated in FP64 and rounded to float once,
-//    so the result does not depend on thread order; heavy vertices sum
-//    their chunks with FP64 atomics and the last chunk to finish (a
-//    countdown) writes the vertex;
+//  * per-arc arithmetic is FP32 (as the reference's): each 32-arc step
+//    sums a vertex's terms with a segmented warp reduction in FP32, and
+//    only the per-step segment totals are added in FP64 -- FP64 issues at
+//    a small fraction of the FP32 rate on this GPU, and an FP64 scan per
+//    arc made BC FP64-bound; heavy vertices sum their chunks with FP64
+//    atomics and the last chunk to finish (a countdown) writes the vertex;
 //  * levels are kept as segments of one light list and one heavy list, so
 //    the backward pass visits exactly the reached vertices, and only those
-//    are reset between sources.
+//    are reset between sources;
+//  * a vertex's level, path count and backward coefficient share one
+//    16-byte record: each arc costs one random load in either pass;
+//  * sigma itself is never stored: each vertex adds it to bc[v] directly.
 // The pull form reads in-arcs forward and out-arcs backward; on the
 // symmetric graphs this library targets both are the CSR itself.
 #include <algorithm>
@@ -32,11 +37,12 @@ namespace {
 
 using namespace gdb;
 
+// Per-vertex state in one 16-byte record, so that an arc's random access
+// is one load of one sector: x = level (int32, -1 = unreached), y = path
+// count rho (float bits), z = (1 + sigma) / rho (float bits), written by
+// the backward pass for the level below to read, w unused.
 struct BcWs {
-  int32_t* d;
-  float* rho;
-  float* sigma;
-  double* coef;                  // (1 + sigma[u]) / rho[u] of the last backward level
+  uint4* st;
   float* bc;
   uint32_t* order;               // light vertices, level segments
   uint4* hc;                     // heavy chunk entries, level segments
@@ -88,6 +94,19 @@ __device__ __forceinline__ void visit_level(const GraphView& G, const Warps& W, 
   }
 }
 
+__device__ __forceinline__ int32_t st_level(const uint4& s) { return (int32_t)s.x; }
+__device__ __forceinline__ float st_coef(const uint4& s) { return __uint_as_float(s.z); }
+__device__ __forceinline__ float rho_of(const BcWs& ws, uint32_t v) {
+  return __uint_as_float(__ldcg(reinterpret_cast<const uint32_t*>(&ws.st[v]) + 1));
+}
+__device__ __forceinline__ void set_rho(const BcWs& ws, uint32_t v, float r) {
+  reinterpret_cast<uint32_t*>(&ws.st[v])[1] = __float_as_uint(r);
+}
+__device__ __forceinline__ void set_coef(const BcWs& ws, uint32_t v, float c) {
+  reinterpret_cast<uint32_t*>(&ws.st[v])[2] = __float_as_uint(c);
+}
+constexpr uint4 kUnreached = {0xFFFFFFFFu, 0u, 0u, 0u};
+
 // Heavy-vertex completion: add this chunk's partial sum; the last chunk
 // returns true (with the vertex total in *total) and re-arms the counter.
 __device__ __forceinline__ bool heavy_done(const BcWs& ws, uint32_t slot, double part,
@@ -114,9 +133,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
   const int lane = lane_id();
   double* my = sacc + (threadIdx.x & ~31u);
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
-    ws.d[v] = -1;
-    ws.rho[v] = 0.f;
-    ws.sigma[v] = 0.f;
+    ws.st[v] = kUnreached;
     ws.bc[v] = 0.f;
   }
   if (leader) {
@@ -146,8 +163,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
     // -- superstep: seed the source into slot (t+1)
     reset_slot(t);
     if (leader) {
-      ws.d[src] = 0;
-      ws.rho[src] = 1.f;
+      ws.st[src] = make_uint4(0u, __float_as_uint(1.f), 0u, 0u);
       const int nx = (t + 1) % 3;
       frontier_seed(G, Frontier{ws.order, ws.hc, &ws.lcnt[nx], &ws.hcnt[nx], G.V, ws.hc_cap,
                                 ws.overflow, G.nheavy, ws.hleft, ws.hacc},
@@ -186,18 +202,20 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       WarpStage qs = frontier_stage(out, 0);
       const int32_t Li = (int32_t)L;
       // one arc of a level-L vertex: claim level L+1 or pull a parent's count
-      auto fwd_arc = [&](bool valid, uint32_t arc, double& acc) {
+      auto fwd_arc = [&](bool valid, uint32_t arc, float& acc) {
         uint32_t u = 0;
         bool want = false;
         if (valid) {
           ++arcs;
           u = __ldg(&G.col[arc]);
-          const int32_t du = ld_cg(&ws.d[u]);
+          // level and path count of u in one 8-byte load
+          const uint2 su = __ldcg(reinterpret_cast<const uint2*>(&ws.st[u]));
+          const int32_t du = (int32_t)su.x;
           if (du == -1) {
             // unvisited (-1 is also L - 1 at level 0: test it first)
-            want = atomicCAS(&ws.d[u], -1, Li + 1) == -1;
+            want = atomicCAS(reinterpret_cast<int*>(&ws.st[u]), -1, Li + 1) == -1;
           } else if (Li > 0 && du == Li - 1) {
-            acc += (double)ld_cg(&ws.rho[u]);
+            acc += __uint_as_float(su.y);
           }
         }
         // a claimed heavy vertex gets its chunk countdown armed by the push
@@ -210,21 +228,21 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
             if (act) reached_arcs += __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
           },
           [&](bool valid, int owner, uint32_t arc) {
-            double a = 0.0;
+            float a = 0.f;
             fwd_arc(valid, arc, a);
             segment_add(my, owner, a);
           },
           [&](uint32_t v, bool act) {
-            if (act && L > 0) ws.rho[v] = (float)my[lane];
+            if (act && L > 0) set_rho(ws, v, (float)my[lane]);
           },
           [&](uint32_t v, uint32_t slot, uint32_t nchunks, uint32_t b, uint32_t e) {
-            double part = 0.0;
+            float part = 0.f;
             for (uint32_t a0 = b; a0 < e; a0 += 32) fwd_arc(a0 + lane < e, a0 + lane, part);
-            part = warp_sum_f64(part);
+            part = warp_sum_f32(part);
             if (lane == 0 && b == __ldg(&G.row[v])) reached_arcs += __ldg(&G.row[v + 1]) - b;
             double tot = 0.0;
             if (heavy_done(ws, slot, part, nchunks, &tot) && lane == 0 && L > 0)
-              ws.rho[v] = (float)tot;
+              set_rho(ws, v, (float)tot);
           });
       qs.flush();
       if (!s.sync()) return;
@@ -252,11 +270,12 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       const uint32_t nch = (uint32_t)lv[4];
       // rho[v] / rho[u] * (1 + sigma[u]) with the u factor precomputed once
       // per vertex (coef) instead of a division per arc
-      auto bwd_arc = [&](bool valid, uint32_t arc, float rv, double& acc) {
+      auto bwd_arc = [&](bool valid, uint32_t arc, float rv, float& acc) {
         if (valid) {
           ++arcs;
           const uint32_t u = __ldg(&G.col[arc]);
-          if (ld_cg(&ws.d[u]) == Lb + 1) acc += (double)rv * __ldcg(&ws.coef[u]);
+          const uint4 su = ld_cg(&ws.st[u]);  // level and coefficient together
+          if (st_level(su) == Lb + 1) acc = fmaf(rv, st_coef(su), acc);
         }
       };
       float rv_lane = 0.f;
@@ -264,49 +283,40 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
           G, W, ws, lb, le - lb, hcb, hvb, nch, &ws.cursor[cur], &ws.hcursor[cur],
           [&](uint32_t v, bool act) {
             my[lane] = 0.0;
-            rv_lane = act ? ld_cg(&ws.rho[v]) : 0.f;
+            rv_lane = act ? rho_of(ws, v) : 0.f;
           },
           [&](bool valid, int owner, uint32_t arc) {
-            double a = 0.0;
+            float a = 0.f;
             bwd_arc(valid, arc, __shfl_sync(kFull, rv_lane, owner), a);
             segment_add(my, owner, a);
           },
           [&](uint32_t v, bool act) {
             if (act) {
               const float sg = (float)my[lane];
-              ws.sigma[v] = sg;
-              ws.coef[v] = (1.0 + (double)sg) / (double)rv_lane;
+              set_coef(ws, v, (1.0f + sg) / rv_lane);
               if (v != src) ws.bc[v] += sg;
             }
           },
           [&](uint32_t v, uint32_t slot, uint32_t nchunks, uint32_t b, uint32_t e) {
-            const float rv = ld_cg(&ws.rho[v]);
-            double part = 0.0;
+            const float rv = rho_of(ws, v);
+            float part = 0.f;
             for (uint32_t a0 = b; a0 < e; a0 += 32) bwd_arc(a0 + lane < e, a0 + lane, rv, part);
-            part = warp_sum_f64(part);
+            part = warp_sum_f32(part);
             double tot = 0.0;
             if (heavy_done(ws, slot, part, nchunks, &tot) && lane == 0) {
               const float sg = (float)tot;
-              ws.sigma[v] = sg;
-              ws.coef[v] = (1.0 + (double)sg) / (double)rv;
+              set_coef(ws, v, (1.0f + sg) / rv);
               if (v != src) ws.bc[v] += sg;
             }
           });
       if (!s.sync()) return;
     }
     // -- reset the reached vertices for the next source
-    for (uint32_t k = W.gthread; k < total_l; k += W.nthreads) {
-      const uint32_t v = ws.order[k];
-      ws.d[v] = -1;
-      ws.rho[v] = 0.f;
-      ws.sigma[v] = 0.f;
-    }
+    for (uint32_t k = W.gthread; k < total_l; k += W.nthreads) ws.st[ws.order[k]] = kUnreached;
     for (uint32_t k = W.gthread; k < total_hc; k += W.nthreads) {
       const uint4 ent = ws.hc[k];
       if (ent.y != 0) continue;  // one entry per vertex: its first chunk
-      ws.d[ent.x] = -1;
-      ws.rho[ent.x] = 0.f;
-      ws.sigma[ent.x] = 0.f;
+      ws.st[ent.x] = kUnreached;
     }
     reset_slot(t);
     if (!s.sync()) return;
@@ -336,8 +346,8 @@ __global__ void __launch_bounds__(512, 3) k_bc_xf(DiscoveryArgs a, GraphView G, 
 
 using namespace gdbi;
 
-// Workspace of one BC run (distances, path counts, dependencies, the level
-// lists, heavy-chunk entries and their accumulators, the counter block).
+// Workspace of one BC run (the per-vertex records, the level lists,
+// heavy-chunk entries and their accumulators, the counter block).
 static size_t bc_layout(const gdb_graph* g, char* base, float* d_bc, const uint32_t* d_sources,
                         uint32_t nsrc, BcWs* ws, char** cnt_out) {
   const uint32_t V = g->V;
@@ -345,8 +355,7 @@ static size_t bc_layout(const gdb_graph* g, char* base, float* d_bc, const uint3
   const uint32_t ccap = std::max<uint32_t>(g->nheavy_chunks, 1);
   const uint32_t maxlev = V + 2;
   Bump b;
-  const size_t o_d = b.take((size_t)V * 4), o_rho = b.take((size_t)V * 4), o_sg = b.take((size_t)V * 4);
-  const size_t o_coef = b.take((size_t)V * 8);
+  const size_t o_st = b.take((size_t)V * 16);
   const size_t o_ord = b.take((size_t)V * 4);
   const size_t o_hc = b.take((size_t)ccap * 16), o_hacc = b.take((size_t)hcap * 8),
                o_hleft = b.take((size_t)hcap * 4);
@@ -354,10 +363,7 @@ static size_t bc_layout(const gdb_graph* g, char* base, float* d_bc, const uint3
                o_lhc = b.take((size_t)maxlev * 4), o_lhv = b.take((size_t)maxlev * 4);
   const size_t o_cnt = b.take(512);
   if (!base) return b.off;
-  ws->d = (int32_t*)(base + o_d);
-  ws->rho = (float*)(base + o_rho);
-  ws->sigma = (float*)(base + o_sg);
-  ws->coef = (double*)(base + o_coef);
+  ws->st = (uint4*)(base + o_st);
   ws->bc = d_bc;
   ws->order = (uint32_t*)(base + o_ord);
   ws->hc = (uint4*)(base + o_hc);

@@ -471,20 +471,22 @@ __device__ __forceinline__ void cta_or(bool p, uint32_t* word, uint32_t bit) {
 // to lane, so each owner's lanes are contiguous: a segmented suffix scan
 // leaves every segment's total in its first lane, which adds it to
 // slot[owner] -- one lane per owner per step, no atomics.  Every lane of
-// the warp calls it.
-__device__ __forceinline__ void segment_add(double* slot, int owner, double x) {
+// the warp calls it.  The scan runs in FP32 and only the segment totals
+// are added in FP64 (one FP64 add per owner per step instead of five per
+// arc: FP64 issues at a small fraction of the FP32 rate on this GPU).
+__device__ __forceinline__ void segment_add(double* slot, int owner, float x) {
   const int lane = lane_id();
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const double y = __shfl_down_sync(kFull, x, o);
+    const float y = __shfl_down_sync(kFull, x, o);
     const int ow = __shfl_down_sync(kFull, owner, o);
     if (lane + o < 32 && ow == owner) x += y;
   }
   const int prev = __shfl_up_sync(kFull, owner, 1);
-  if ((lane == 0 || prev != owner) && x != 0.0) slot[owner] += x;
+  if ((lane == 0 || prev != owner) && x != 0.f) slot[owner] += (double)x;
 }
 
-__device__ __forceinline__ double warp_sum_f64(double x) {
+__device__ __forceinline__ float warp_sum_f32(float x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
   return x;
