@@ -194,10 +194,14 @@ __global__ void __launch_bounds__(512, 3) k_mis_xf(DiscoveryArgs a, GraphView G,
 // -- as in the reference, which never terminates then -- they stay
 // uncoloured; the host reports that as an error.
 
+// waitarc bits of arc v -> u
+constexpr uint8_t kWaits = 1;   // u waits for v
+constexpr uint8_t kHeavyT = 2;  // u has degree > kHeavyDeg (a chunked frontier entry)
+
 struct ColorWs {
   int32_t* color;
   uint32_t* cnt;       // neighbours still to be coloured before this vertex
-  uint8_t* waitarc;    // per arc v -> u: 1 when u waits for v (set by the count pass)
+  uint8_t* waitarc;    // per arc v -> u: kWaits | kHeavyT (set by the count pass)
   const float* prio;
   uint32_t* q[2];
   uint4* hc[2];                // heavy chunk entries
@@ -250,7 +254,8 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
             const uint32_t u = __ldg(&G.col[arc]);
             const float pu = __ldg(&ws.prio[u]);
             if (looks && pu >= pv) atomicAdd(&my[owner], 1u);
-            ws.waitarc[arc] = (pv >= pu && __ldg(&G.row[u + 1]) - __ldg(&G.row[u]) != 1) ? 1 : 0;
+            const uint32_t du = __ldg(&G.row[u + 1]) - __ldg(&G.row[u]);
+            ws.waitarc[arc] = (pv >= pu && du != 1 ? kWaits : 0) | (du > kHeavyDeg ? kHeavyT : 0);
           }
         },
         [&](uint32_t v, bool) {
@@ -266,7 +271,8 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
           const uint32_t u = __ldg(&G.col[a]);
           const float pu = __ldg(&ws.prio[u]);
           n += pu >= pv;
-          ws.waitarc[a] = (pv >= pu && __ldg(&G.row[u + 1]) - __ldg(&G.row[u]) != 1) ? 1 : 0;
+          const uint32_t du = __ldg(&G.row[u + 1]) - __ldg(&G.row[u]);
+          ws.waitarc[a] = (pv >= pu && du != 1 ? kWaits : 0) | (du > kHeavyDeg ? kHeavyT : 0);
         }
       }
       n = warp_add_u32(n);
@@ -313,19 +319,29 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
                  ws.qcap, ws.hcap, ws.overflow};
     WarpStage qs = frontier_stage(out, 0);
     const int32_t next_color = (int32_t)r + 1;
-    float pv_lane = 0.f;
-    auto relax = [&](bool valid, float pv, uint32_t arc) {
-      uint32_t u = 0;
-      bool ready = false;
-      if (valid) {
-        ++arcs;
-        u = __ldg(&G.col[arc]);
-        if (ws.waitarc[arc] && atomicSub(&ws.cnt[u], 1u) == 1u) {
-          ws.color[u] = next_color;
-          ready = true;
-        }
+    // up to four 32-arc steps at once: their column, wait-byte loads and
+    // count-downs are all in flight together (a round is a chain of
+    // dependent round trips, and thousands of rounds run one after another)
+    auto relax4 = [&](const bool* valid, const uint32_t* arc) {
+      uint32_t u[4];
+      uint8_t wa[4];
+#pragma unroll
+      for (int s4 = 0; s4 < 4; ++s4) {
+        u[s4] = valid[s4] ? __ldg(&G.col[arc[s4]]) : 0u;
+        wa[s4] = valid[s4] ? ws.waitarc[arc[s4]] : (uint8_t)0;
+        arcs += valid[s4];
       }
-      frontier_push_staged(G, out, qs, ready, u);
+      uint32_t old4[4];
+#pragma unroll
+      for (int s4 = 0; s4 < 4; ++s4) old4[s4] = (wa[s4] & kWaits) ? atomicSub(&ws.cnt[u[s4]], 1u) : 0u;
+#pragma unroll
+      for (int s4 = 0; s4 < 4; ++s4) {
+        const bool ready = (wa[s4] & kWaits) && old4[s4] == 1u;
+        if (ready) ws.color[u[s4]] = next_color;
+        const bool heavy = ready && (wa[s4] & kHeavyT);
+        qs.add(ready && !heavy, u[s4]);
+        frontier_push_heavy(G, out, heavy, u[s4]);
+      }
     };
     const uint32_t* q = pick(ws.q, r);
     const uint32_t k = group_width(n, W.nwarps);
@@ -334,20 +350,25 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
       const uint32_t i = g * k + lane;
       const bool act = (uint32_t)lane < k && i < n;
       const uint32_t v = act ? ld_cg(&q[i]) : 0u;
-      pv_lane = act ? __ldg(&ws.prio[v]) : 0.f;
-      group_arcs(G, act, v, [&](bool valid, int owner, uint32_t arc) {
-        relax(valid, __shfl_sync(kFull, pv_lane, owner), arc);
-      });
+      group_arcs4(G, act, v, relax4);
     }
     const uint32_t nch = (uint32_t)hp;
     const uint4* hc = pick(ws.hc, r);
     WorkTaker ht(nch, W, &ws.hcursor[cur]);
     for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
       const uint4 ent = ld_cg(&hc[c]);
-      const float pv = __ldg(&ws.prio[ent.x]);
       uint32_t b, en;
       chunk_range(G, ent, b, en);
-      range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, pv, arc); });
+      // a chunk holds kChunk = 128 arcs: one four-step batch
+      static_assert(kChunk == 4 * 32, "a colour chunk is one batch of four steps");
+      bool valid[4];
+      uint32_t arc[4];
+#pragma unroll
+      for (int s4 = 0; s4 < 4; ++s4) {
+        arc[s4] = b + 32 * s4 + lane;
+        valid[s4] = arc[s4] < en;
+      }
+      relax4(valid, arc);
     }
     qs.flush();
     if (!s.sync()) return;
