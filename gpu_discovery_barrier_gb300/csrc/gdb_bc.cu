@@ -114,10 +114,10 @@ __device__ __forceinline__ bool heavy_done(const BcWs& ws, uint32_t slot, double
   bool last = false;
   if (lane_id() == 0) {
     atomicAdd(&ws.hacc[slot], part);
-    __threadfence();
-    last = atomicSub(&ws.hleft[slot], 1u) == 1u;
+    // release orders the add before the count-down; the last chunk's
+    // acquire makes every chunk's add visible to its read
+    last = countdown_acq_rel(&ws.hleft[slot]) == 1u;
     if (last) {
-      __threadfence();
       *total = __ldcg(&ws.hacc[slot]);
       ws.hacc[slot] = 0.0;
       ws.hleft[slot] = nchunks;

@@ -322,7 +322,7 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
     // up to four 32-arc steps at once: their column, wait-byte loads and
     // count-downs are all in flight together (a round is a chain of
     // dependent round trips, and thousands of rounds run one after another)
-    auto relax4 = [&](const bool* valid, const uint32_t* arc) {
+    auto relax4 = [&](const bool* valid, const int*, const uint32_t* arc) {
       uint32_t u[4];
       uint8_t wa[4];
 #pragma unroll
@@ -368,7 +368,7 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
         arc[s4] = b + 32 * s4 + lane;
         valid[s4] = arc[s4] < en;
       }
-      relax4(valid, arc);
+      relax4(valid, nullptr, arc);
     }
     qs.flush();
     if (!s.sync()) return;

@@ -159,10 +159,10 @@ __device__ __forceinline__ void group_arcs(const GraphView& G, bool active, uint
   }
 }
 
-// group_arcs four steps at a time: fn(valid[4], arc[4]) receives the arcs
-// of up to four consecutive 32-arc steps, so that the caller can issue
-// their loads and atomics together -- one round trip per four steps on
-// latency-bound paths instead of one per step.
+// group_arcs four steps at a time: fn(valid[4], owner[4], arc[4]) receives
+// the arcs (and owner lanes) of up to four consecutive 32-arc steps, so
+// that the caller can issue their loads and atomics together -- one round
+// trip per four steps on latency-bound paths instead of one per step.
 template <class Fn>
 __device__ __forceinline__ void group_arcs4(const GraphView& G, bool active, uint32_t v, Fn&& fn) {
   const int lane = lane_id();
@@ -181,6 +181,7 @@ __device__ __forceinline__ void group_arcs4(const GraphView& G, bool active, uin
   pre -= deg;
   for (uint32_t base = 0; base < total; base += 128) {
     bool valid[4];
+    int owner[4];
     uint32_t arc[4];
 #pragma unroll
     for (int s4 = 0; s4 < 4; ++s4) {
@@ -194,9 +195,10 @@ __device__ __forceinline__ void group_arcs4(const GraphView& G, bool active, uin
       const uint32_t obeg = __shfl_sync(kFull, beg, lo);
       const uint32_t opre = __shfl_sync(kFull, pre, lo);
       valid[s4] = k < total;
+      owner[s4] = lo;
       arc[s4] = obeg + (k - opre);
     }
-    fn(valid, arc);
+    fn(valid, owner, arc);
   }
 }
 
@@ -236,32 +238,46 @@ struct Frontier {
   double* hacc = nullptr;       // optional: FP64 accumulator per slot, cleared at push
 };
 
-// The lanes' `heavy` vertices: the warp writes each one's chunk entries
-// together after one packed atomic on the frontier's heavy counter.
+// The lanes' `heavy` vertices: their degrees are loaded together, one
+// packed atomic on the frontier's heavy counter reserves every vertex slot
+// and chunk entry of the warp's heavy vertices at once, and the warp then
+// writes each vertex's entries together -- no round trip per vertex (a
+// level whose arcs claim thousands of hubs otherwise serialises on them).
 __device__ __forceinline__ void frontier_push_heavy(const GraphView& G, const Frontier& F,
                                                     bool heavy, uint32_t v) {
+  const unsigned hm = __ballot_sync(kFull, heavy);
+  if (!hm) return;
   const int lane = lane_id();
-  for (unsigned hm = __ballot_sync(kFull, heavy); hm; hm &= hm - 1) {
-    const int l = __ffs(hm) - 1;
-    const uint32_t hvx = __shfl_sync(kFull, v, l);
-    unsigned long long old = 0;
-    uint32_t nch = 0;
-    if (lane == l) {
-      nch = chunks_of(__ldg(&G.row[hvx + 1]) - __ldg(&G.row[hvx]));
-      old = atomicAdd(F.hcount, (1ull << 32) | (unsigned long long)nch);
-    }
-    old = __shfl_sync(kFull, old, l);
-    nch = __shfl_sync(kFull, nch, l);
-    const uint32_t vslot = (uint32_t)(old >> 32), cbase = (uint32_t)old;
-    if (cbase + nch > F.hcap || vslot >= F.vcap) {
-      if (lane == l) atomicExch(F.overflow, 1);
-      continue;
-    }
-    for (uint32_t j = lane; j < nch; j += 32) F.hc[cbase + j] = make_uint4(hvx, j, vslot, nch);
-    if (lane == l && F.hleft) {
-      F.hleft[vslot] = nch;
-      F.hacc[vslot] = 0.0;
-    }
+  const uint32_t nch = heavy ? chunks_of(__ldg(&G.row[v + 1]) - __ldg(&G.row[v])) : 0u;
+  uint32_t inc = nch;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += t;
+  }
+  const uint32_t total = __shfl_sync(kFull, inc, 31);
+  const uint32_t cofs = inc - nch;  // this lane's first entry, relative
+  const uint32_t nh = __popc(hm);
+  const int leader = __ffs(hm) - 1;
+  unsigned long long old = 0;
+  if (lane == leader) old = atomicAdd(F.hcount, ((unsigned long long)nh << 32) | total);
+  old = __shfl_sync(kFull, old, leader);
+  const uint32_t vslot0 = (uint32_t)(old >> 32), cbase0 = (uint32_t)old;
+  if (cbase0 + total > F.hcap || vslot0 + nh > F.vcap) {
+    if (lane == leader) atomicExch(F.overflow, 1);
+    return;
+  }
+  if (heavy && F.hleft) {
+    const uint32_t vs = vslot0 + __popc(hm & lanemask_lt());
+    F.hleft[vs] = nch;
+    F.hacc[vs] = 0.0;
+  }
+  for (unsigned m = hm; m; m &= m - 1) {
+    const int l = __ffs(m) - 1;
+    const uint32_t hvx = __shfl_sync(kFull, v, l), n = __shfl_sync(kFull, nch, l);
+    const uint32_t cb = cbase0 + __shfl_sync(kFull, cofs, l);
+    const uint32_t vs = vslot0 + __popc(hm & ((1u << l) - 1u));
+    for (uint32_t j = lane; j < n; j += 32) F.hc[cb + j] = make_uint4(hvx, j, vs, n);
   }
 }
 
@@ -500,6 +516,19 @@ __device__ __forceinline__ const unsigned long long* cta_words(Load&& load) {
   if (threadIdx.x == 0) load(s);
   __syncthreads();
   return s;
+}
+
+// Count-down of *p by one with acquire-release semantics: this thread's
+// earlier writes are ordered before it, and the thread that takes the
+// count to zero sees the writes of every thread that counted down before
+// it (a fence-free completion pattern; __threadfence is a full fence).
+__device__ __forceinline__ uint32_t countdown_acq_rel(uint32_t* p) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;"
+               : "=r"(old)
+               : "l"(p), "r"(0xFFFFFFFFu)
+               : "memory");
+  return old;
 }
 
 // One atomicOr of `bit` into *word per CTA when any of its threads has `p`
