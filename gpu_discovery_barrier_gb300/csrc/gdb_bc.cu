@@ -5,29 +5,35 @@
 // mega_bfs_kernel_func :295-371), dependencies sigma with
 // sigma[w] += rho[w]/rho[i] * (1 + sigma[i]) for every predecessor w of i
 // (backward, mega_backtrack_kernel_func :373-428), and bc[i] += sigma[i]
-// for i != s; no halving for undirected graphs.
+// for i != s; no halving for undirected graphs.  Path counts are float32
+// as in the reference, so they overflow where the reference's do.
 //
 // GB300 form, one persistent kernel for all sources, one XF barrier per
-// level:
-//  * forward, level L: every vertex of the level walks its arcs once,
-//    claiming unvisited neighbours for level L+1 (CAS on d) and pulling the
-//    path counts of its level L-1 neighbours into rho -- the push of the
-//    reference's float CAS-loop atomics becomes a per-vertex pull;
-//  * backward, level L (deepest first): every vertex of the level pulls
-//    rho[v]/rho[u] * (1 + sigma[u]) from its level L+1 neighbours;
-//  * per-arc arithmetic is FP32 (as the reference's): each 32-arc step
-//    sums a vertex's terms with a segmented warp reduction in FP32, and
-//    only the per-step segment totals are added in FP64 -- FP64 issues at
-//    a small fraction of the FP32 rate on this GPU, and an FP64 scan per
-//    arc made BC FP64-bound; heavy vertices sum their chunks with FP64
-//    atomics and the last chunk to finish (a countdown) writes the vertex;
+// level, and each level pair (L, L+1) handled from whichever side has
+// fewer arcs -- on power-law graphs one middle level holds most arcs, and
+// neither pass walks it:
+//  * forward, level L -> L+1, direction-optimising: push -- the level's
+//    vertices claim unvisited neighbours (CAS on d) and add their path
+//    count into every level-L+1 neighbour's FP64 accumulator (an L2
+//    atomic); pull -- every unvisited vertex sums the path counts of its
+//    level-L neighbours and claims itself when the sum is positive.  A
+//    pull has no early exit (every parent counts), so it runs only when the
+//    unvisited vertices' arcs are fewer than the level's own;
+//  * backward, level L (deepest first): levels below the level with the
+//    most arcs pull (1 + sigma[w]) / rho[w] from their level-L+1
+//    neighbours, levels above it push their own coefficient into their
+//    level-L-1 neighbours' FP64 accumulators, and that level itself only
+//    finalises: sigma[v] = rho[v] x the sum;
+//  * per-arc arithmetic is FP32; pulled sums go through a segmented warp
+//    reduction in FP32 whose per-step totals are added in FP64 -- FP64
+//    issues at a small fraction of the FP32 rate on this GPU; heavy
+//    vertices that pull sum their chunks with FP64 atomics and the last
+//    chunk to finish (an acquire-release count-down) writes the vertex;
 //  * levels are kept as segments of one light list and one heavy list, so
 //    the backward pass visits exactly the reached vertices, and only those
 //    are reset between sources;
-//  * a vertex's level, path count and backward coefficient share one
-//    16-byte record: each arc costs one random load in either pass;
 //  * sigma itself is never stored: each vertex adds it to bc[v] directly.
-// The pull form reads in-arcs forward and out-arcs backward; on the
+// The pull forms read in-arcs forward and out-arcs backward; on the
 // symmetric graphs this library targets both are the CSR itself.
 #include <algorithm>
 
@@ -37,12 +43,14 @@ namespace {
 
 using namespace gdb;
 
-// Per-vertex state in one 16-byte record, so that an arc's random access
-// is one load of one sector: x = level (int32, -1 = unreached), y = path
-// count rho (float bits), z = (1 + sigma) / rho (float bits), written by
-// the backward pass for the level below to read, w unused.
+// Per-vertex state.  st: x = level (int32, -1 = unreached), y = the
+// backward coefficient (1 + sigma) / rho (float bits), one 8-byte load for
+// the arcs of either pass; rho: FP64 accumulator of the path count (read
+// as float); sacc: FP64 accumulator of the backward sum of pushed levels.
 struct BcWs {
-  uint4* st;
+  uint2* st;
+  double* rho;
+  double* sacc;
   float* bc;
   uint32_t* order;               // light vertices, level segments
   uint4* hc;                     // heavy chunk entries, level segments
@@ -53,6 +61,7 @@ struct BcWs {
   uint32_t* lev_h;               // heavy chunk-entry start per level
   uint32_t* lev_hc;              // heavy chunks per level
   uint32_t* lev_hv;              // heavy vertex-slot start per level
+  unsigned long long* lev_arcs;  // arcs out of each level's vertices
   uint32_t* lcnt;                // [3] light pushes of the next level
   unsigned long long* hcnt;      // [3] (entries << 32) | chunks
   uint32_t* cursor;              // [3]
@@ -94,18 +103,18 @@ __device__ __forceinline__ void visit_level(const GraphView& G, const Warps& W, 
   }
 }
 
-__device__ __forceinline__ int32_t st_level(const uint4& s) { return (int32_t)s.x; }
-__device__ __forceinline__ float st_coef(const uint4& s) { return __uint_as_float(s.z); }
-__device__ __forceinline__ float rho_of(const BcWs& ws, uint32_t v) {
-  return __uint_as_float(__ldcg(reinterpret_cast<const uint32_t*>(&ws.st[v]) + 1));
+__device__ __forceinline__ int32_t level_of(const BcWs& ws, uint32_t v) {
+  return (int32_t)__ldcg(reinterpret_cast<const uint32_t*>(&ws.st[v]));
 }
-__device__ __forceinline__ void set_rho(const BcWs& ws, uint32_t v, float r) {
-  reinterpret_cast<uint32_t*>(&ws.st[v])[1] = __float_as_uint(r);
+__device__ __forceinline__ float rho_of(const BcWs& ws, uint32_t v) {
+  return (float)__ldcg(&ws.rho[v]);
 }
 __device__ __forceinline__ void set_coef(const BcWs& ws, uint32_t v, float c) {
-  reinterpret_cast<uint32_t*>(&ws.st[v])[2] = __float_as_uint(c);
+  reinterpret_cast<uint32_t*>(&ws.st[v])[1] = __float_as_uint(c);
 }
-constexpr uint4 kUnreached = {0xFFFFFFFFu, 0u, 0u, 0u};
+constexpr uint2 kUnreached = {0xFFFFFFFFu, 0u};
+// an empty sum: sums start at -0.0, and -0.0 + x = x for every x >= +0.0
+__device__ __forceinline__ bool no_terms(double s) { return s == 0.0 && signbit(s); }
 
 // Heavy-vertex completion: add this chunk's partial sum; the last chunk
 // returns true (with the vertex total in *total) and re-arms the counter.
@@ -119,7 +128,7 @@ __device__ __forceinline__ bool heavy_done(const BcWs& ws, uint32_t slot, double
     last = countdown_acq_rel(&ws.hleft[slot]) == 1u;
     if (last) {
       *total = __ldcg(&ws.hacc[slot]);
-      ws.hacc[slot] = 0.0;
+      ws.hacc[slot] = -0.0;
       ws.hleft[slot] = nchunks;
     }
   }
@@ -127,13 +136,15 @@ __device__ __forceinline__ bool heavy_done(const BcWs& ws, uint32_t slot, double
 }
 
 template <class Sync>
-__device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs& ws, double* sacc) {
+__device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs& ws, double* smem) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
   const int lane = lane_id();
-  double* my = sacc + (threadIdx.x & ~31u);
+  double* my = smem + (threadIdx.x & ~31u);
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.st[v] = kUnreached;
+    ws.rho[v] = 0.0;
+    ws.sacc[v] = -0.0;
     ws.bc[v] = 0.f;
   }
   if (leader) {
@@ -158,12 +169,16 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       ws.hcursor[old] = 0;
     }
   };
+  auto degree = [&](uint32_t v) { return __ldg(&G.row[v + 1]) - __ldg(&G.row[v]); };
   for (uint32_t si = 0; si < ws.nsrc; ++si) {
     const uint32_t src = ws.sources[si];
     // -- superstep: seed the source into slot (t+1)
     reset_slot(t);
     if (leader) {
-      ws.st[src] = make_uint4(0u, __float_as_uint(1.f), 0u, 0u);
+      ws.st[src] = make_uint2(0u, 0u);
+      ws.rho[src] = 1.0;
+      ws.lev_arcs[0] = degree(src);
+      ws.lev_arcs[1] = 0;
       const int nx = (t + 1) % 3;
       frontier_seed(G, Frontier{ws.order, ws.hc, &ws.lcnt[nx], &ws.hcnt[nx], G.V, ws.hc_cap,
                                 ws.overflow, G.nheavy, ws.hleft, ws.hacc},
@@ -173,14 +188,17 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
     ++t;
     // -- forward levels
     uint32_t lbase = 0, hcbase = 0, hvbase = 0, L = 0;
+    unsigned long long vis_arcs = 0, peak_arcs = 0;
+    uint32_t peak = 0;
     for (;; ++L, ++t) {
       const int cur = t % 3, nx = (t + 1) % 3;
-      const unsigned long long* sc = cta_words<2>([&](unsigned long long* w) {
+      const unsigned long long* sc = cta_words<3>([&](unsigned long long* w) {
         w[0] = ld_cg(&ws.lcnt[cur]);
         w[1] = __ldcg(&ws.hcnt[cur]);
+        w[2] = __ldcg(&ws.lev_arcs[L]);
       });
       const uint32_t nl = (uint32_t)sc[0];
-      const unsigned long long hp = sc[1];
+      const unsigned long long hp = sc[1], mf = sc[2];
       const uint32_t nhv = (uint32_t)(hp >> 32), nch = (uint32_t)hp;
       if (leader && L < ws.max_levels) {
         ws.lev_l[L] = lbase;
@@ -195,56 +213,97 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
         if (leader) *ws.overflow = 1;
         break;
       }
+      // level L+2's arc counter fills during the next superstep
+      if (leader) ws.lev_arcs[L + 2] = 0;
+      vis_arcs += mf;
+      if (mf > peak_arcs) {
+        peak_arcs = mf;
+        peak = L;
+      }
+      // direction of L -> L+1, from the same counters in every CTA: a push
+      // walks the level's mf arcs, a pull (no early exit: every parent
+      // counts) the arcs of every unvisited vertex plus one look at each
+      // vertex's level -- the cheaper one runs
+      const unsigned long long mu = G.E > vis_arcs ? G.E - vis_arcs : 0ull;
+      const bool pull = mu + G.V < mf;
       const uint32_t nlbase = lbase + nl, nhcbase = hcbase + nch, nhvbase = hvbase + nhv;
       Frontier out{ws.order + nlbase, ws.hc + nhcbase, &ws.lcnt[nx], &ws.hcnt[nx], G.V - nlbase,
                    ws.hc_cap - nhcbase, ws.overflow, G.nheavy - nhvbase, ws.hleft + nhvbase,
                    ws.hacc + nhvbase};
       WarpStage qs = frontier_stage(out, 0);
       const int32_t Li = (int32_t)L;
-      // one arc of a level-L vertex: claim level L+1 or pull a parent's count
-      auto fwd_arc = [&](bool valid, uint32_t arc, float& acc) {
-        uint32_t u = 0;
-        bool want = false;
-        if (valid) {
-          ++arcs;
-          u = __ldg(&G.col[arc]);
-          // level and path count of u in one 8-byte load
-          const uint2 su = __ldcg(reinterpret_cast<const uint2*>(&ws.st[u]));
-          const int32_t du = (int32_t)su.x;
-          if (du == -1) {
-            // unvisited (-1 is also L - 1 at level 0: test it first)
-            want = atomicCAS(reinterpret_cast<int*>(&ws.st[u]), -1, Li + 1) == -1;
-          } else if (Li > 0 && du == Li - 1) {
-            acc += __uint_as_float(su.y);
+      unsigned long long next_arcs = 0;  // arcs out of the vertices this lane claims
+      if (!pull) {
+        // push: one arc of a level-L vertex of path count rv -- claim an
+        // unvisited neighbour, add rv to every level-L+1 neighbour
+        auto fwd = [&](bool valid, float rv, uint32_t arc) {
+          uint32_t u = 0;
+          bool claimed = false;
+          if (valid) {
+            ++arcs;
+            u = __ldg(&G.col[arc]);
+            const int32_t du = level_of(ws, u);
+            bool add = du == Li + 1;
+            if (du == -1) {
+              // the degree loads go out with the claim, not after it
+              const uint32_t r0 = __ldg(&G.row[u]), r1 = __ldg(&G.row[u + 1]);
+              const int old = atomicCAS(reinterpret_cast<int*>(&ws.st[u]), -1, Li + 1);
+              claimed = old == -1;
+              add = claimed || old == Li + 1;
+              if (claimed) next_arcs += r1 - r0;
+            }
+            if (add) atomicAdd(&ws.rho[u], (double)rv);
           }
-        }
-        // a claimed heavy vertex gets its chunk countdown armed by the push
-        frontier_push_staged(G, out, qs, want, u);
-      };
-      visit_level(
-          G, W, ws, lbase, nl, hcbase, hvbase, nch, &ws.cursor[cur], &ws.hcursor[cur],
-          [&](uint32_t v, bool act) {
-            my[lane] = 0.0;
-            if (act) reached_arcs += __ldg(&G.row[v + 1]) - __ldg(&G.row[v]);
-          },
-          [&](bool valid, int owner, uint32_t arc) {
-            float a = 0.f;
-            fwd_arc(valid, arc, a);
+          frontier_push_staged(G, out, qs, claimed, u);
+        };
+        float rv_lane = 0.f;
+        visit_level(
+            G, W, ws, lbase, nl, hcbase, hvbase, nch, &ws.cursor[cur], &ws.hcursor[cur],
+            [&](uint32_t v, bool act) {
+              rv_lane = act ? rho_of(ws, v) : 0.f;
+              if (act) reached_arcs += degree(v);
+            },
+            [&](bool valid, int owner, uint32_t arc) {
+              fwd(valid, __shfl_sync(kFull, rv_lane, owner), arc);
+            },
+            [&](uint32_t, bool) {},
+            [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
+              const float rv = rho_of(ws, v);
+              for (uint32_t a0 = b; a0 < e; a0 += 32) fwd(a0 + lane < e, rv, a0 + lane);
+              if (lane == 0 && b == __ldg(&G.row[v])) reached_arcs += degree(v);
+            });
+      } else {
+        // pull: every unvisited vertex sums the path counts of its level-L
+        // neighbours (all of them) and claims itself when there are any
+        for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
+          const uint32_t u = g * 32 + lane;
+          const bool unv = u < G.V && level_of(ws, u) == -1;
+          my[lane] = 0.0;
+          __syncwarp();
+          group_arcs(G, unv, u, [&](bool valid, int owner, uint32_t arc) {
+            float a = -0.f;  // no term
+            if (valid) {
+              ++arcs;
+              const uint32_t w = __ldg(&G.col[arc]);
+              if (level_of(ws, w) == Li) a = rho_of(ws, w);
+            }
             segment_add(my, owner, a);
-          },
-          [&](uint32_t v, bool act) {
-            if (act && L > 0) set_rho(ws, v, (float)my[lane]);
-          },
-          [&](uint32_t v, uint32_t slot, uint32_t nchunks, uint32_t b, uint32_t e) {
-            float part = 0.f;
-            for (uint32_t a0 = b; a0 < e; a0 += 32) fwd_arc(a0 + lane < e, a0 + lane, part);
-            part = warp_sum_f32(part);
-            if (lane == 0 && b == __ldg(&G.row[v])) reached_arcs += __ldg(&G.row[v + 1]) - b;
-            double tot = 0.0;
-            if (heavy_done(ws, slot, part, nchunks, &tot) && lane == 0 && L > 0)
-              set_rho(ws, v, (float)tot);
           });
+          __syncwarp();
+          const double sum = my[lane];
+          const bool claimed = unv && sum > 0.0;
+          if (claimed) {
+            ws.st[u].x = (uint32_t)(Li + 1);  // only this lane writes u
+            ws.rho[u] = sum;
+            next_arcs += degree(u);
+          }
+          frontier_push_staged(G, out, qs, claimed, u);
+        }
+        if (leader) reached_arcs += mf;
+      }
       qs.flush();
+      next_arcs = warp_add_u64(next_arcs);
+      if (lane == 0 && next_arcs) atomicAdd(&ws.lev_arcs[L + 1], next_arcs);
       if (!s.sync()) return;
       lbase = nlbase;
       hcbase = nhcbase;
@@ -254,7 +313,8 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
     const uint32_t levels = L;  // levels 0 .. L-1 are non-empty
     const uint32_t total_l = lbase, total_hc = hcbase;
     if (!s.sync()) return;
-    // -- backward levels, deepest first
+    // -- backward levels, deepest first.  Pair (L, L+1) is pulled by level
+    // L below the peak level and pushed by level L+1 above it.
     for (int32_t Lb = (int32_t)levels - 1; Lb >= 0; --Lb, ++t) {
       const int cur = t % 3;
       reset_slot(t);
@@ -268,55 +328,104 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       const uint32_t lb = (uint32_t)lv[0], le = (uint32_t)lv[1];
       const uint32_t hcb = (uint32_t)lv[2], hvb = (uint32_t)lv[3];
       const uint32_t nch = (uint32_t)lv[4];
-      // rho[v] / rho[u] * (1 + sigma[u]) with the u factor precomputed once
-      // per vertex (coef) instead of a division per arc
-      auto bwd_arc = [&](bool valid, uint32_t arc, float rv, float& acc) {
-        if (valid) {
-          ++arcs;
-          const uint32_t u = __ldg(&G.col[arc]);
-          const uint4 su = ld_cg(&ws.st[u]);  // level and coefficient together
-          if (st_level(su) == Lb + 1) acc = fmaf(rv, st_coef(su), acc);
-        }
+      // sigma of v from the sum of its successors' coefficients.  Sums
+      // start at -0.0 and every successor adds at least +0.0, so -0.0 means
+      // no successor: sigma stays 0 then even when rho overflowed to inf, as
+      // in the reference, which adds nothing; a successor whose own count
+      // overflowed (coefficient 0) still gives inf x 0 = NaN, as there
+      auto finalize = [&](uint32_t v, float rv, double sum) {
+        const float sg = no_terms(sum) ? 0.f : (float)((double)rv * sum);
+        set_coef(ws, v, (1.0f + sg) / rv);
+        if (v != src) ws.bc[v] += sg;
+        return (1.0f + sg) / rv;
       };
-      float rv_lane = 0.f;
-      visit_level(
-          G, W, ws, lb, le - lb, hcb, hvb, nch, &ws.cursor[cur], &ws.hcursor[cur],
-          [&](uint32_t v, bool act) {
-            my[lane] = 0.0;
-            rv_lane = act ? rho_of(ws, v) : 0.f;
-          },
-          [&](bool valid, int owner, uint32_t arc) {
-            float a = 0.f;
-            bwd_arc(valid, arc, __shfl_sync(kFull, rv_lane, owner), a);
-            segment_add(my, owner, a);
-          },
-          [&](uint32_t v, bool act) {
-            if (act) {
-              const float sg = (float)my[lane];
-              set_coef(ws, v, (1.0f + sg) / rv_lane);
-              if (v != src) ws.bc[v] += sg;
-            }
-          },
-          [&](uint32_t v, uint32_t slot, uint32_t nchunks, uint32_t b, uint32_t e) {
-            const float rv = rho_of(ws, v);
-            float part = 0.f;
-            for (uint32_t a0 = b; a0 < e; a0 += 32) bwd_arc(a0 + lane < e, a0 + lane, rv, part);
-            part = warp_sum_f32(part);
-            double tot = 0.0;
-            if (heavy_done(ws, slot, part, nchunks, &tot) && lane == 0) {
-              const float sg = (float)tot;
-              set_coef(ws, v, (1.0f + sg) / rv);
-              if (v != src) ws.bc[v] += sg;
-            }
-          });
+      if ((uint32_t)Lb < peak) {
+        // pull the coefficients of the level-Lb+1 neighbours
+        auto bwd = [&](bool valid, uint32_t arc) {
+          float a = -0.f;  // no term
+          if (valid) {
+            ++arcs;
+            const uint2 su = __ldcg(&ws.st[__ldg(&G.col[arc])]);  // level and coefficient
+            if ((int32_t)su.x == Lb + 1) a = __uint_as_float(su.y);
+          }
+          return a;
+        };
+        float rv_lane = 0.f;
+        visit_level(
+            G, W, ws, lb, le - lb, hcb, hvb, nch, &ws.cursor[cur], &ws.hcursor[cur],
+            [&](uint32_t v, bool act) {
+              my[lane] = -0.0;
+              rv_lane = act ? rho_of(ws, v) : 0.f;
+            },
+            [&](bool valid, int owner, uint32_t arc) { segment_add(my, owner, bwd(valid, arc)); },
+            [&](uint32_t v, bool act) {
+              if (act) finalize(v, rv_lane, my[lane]);
+            },
+            [&](uint32_t v, uint32_t slot, uint32_t nchunks, uint32_t b, uint32_t e) {
+              float part = -0.f;
+              for (uint32_t a0 = b; a0 < e; a0 += 32) part += bwd(a0 + lane < e, a0 + lane);
+              part = warp_sum_f32(part);
+              double tot = 0.0;
+              if (heavy_done(ws, slot, part, nchunks, &tot) && lane == 0) finalize(v, rho_of(ws, v), tot);
+            });
+      } else if ((uint32_t)Lb == peak) {
+        // the peak level only finalises: its sums were pushed by level
+        // peak + 1 (none when it is the deepest level)
+        for (uint32_t k = lb + W.gthread; k < le; k += W.nthreads) {
+          const uint32_t v = ws.order[k];
+          finalize(v, rho_of(ws, v), __ldcg(&ws.sacc[v]));
+        }
+        for (uint32_t k = W.gthread; k < nch; k += W.nthreads) {
+          const uint4 ent = ld_cg(&ws.hc[hcb + k]);
+          if (ent.y == 0) finalize(ent.x, rho_of(ws, ent.x), __ldcg(&ws.sacc[ent.x]));
+        }
+      } else {
+        // finalise from the pushed sum, then push the coefficient into the
+        // level-Lb-1 neighbours
+        auto push = [&](bool valid, float cf, uint32_t arc) {
+          if (valid) {
+            ++arcs;
+            const uint32_t u = __ldg(&G.col[arc]);
+            if (level_of(ws, u) == Lb - 1) atomicAdd(&ws.sacc[u], (double)cf);
+          }
+        };
+        float cf_lane = 0.f;
+        visit_level(
+            G, W, ws, lb, le - lb, hcb, hvb, nch, &ws.cursor[cur], &ws.hcursor[cur],
+            [&](uint32_t v, bool act) {
+              cf_lane = act ? finalize(v, rho_of(ws, v), __ldcg(&ws.sacc[v])) : 0.f;
+            },
+            [&](bool valid, int owner, uint32_t arc) {
+              push(valid, __shfl_sync(kFull, cf_lane, owner), arc);
+            },
+            [&](uint32_t, bool) {},
+            [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
+              // every chunk derives the same coefficient; the first writes it
+              const float rv = rho_of(ws, v);
+              const double sum = __ldcg(&ws.sacc[v]);
+              float cf;
+              if (b == __ldg(&G.row[v])) {
+                cf = lane == 0 ? finalize(v, rv, sum) : 0.f;
+                cf = __shfl_sync(kFull, cf, 0);
+              } else {
+                const float sg = no_terms(sum) ? 0.f : (float)((double)rv * sum);
+                cf = (1.0f + sg) / rv;
+              }
+              for (uint32_t a0 = b; a0 < e; a0 += 32) push(a0 + lane < e, cf, a0 + lane);
+            });
+      }
       if (!s.sync()) return;
     }
     // -- reset the reached vertices for the next source
-    for (uint32_t k = W.gthread; k < total_l; k += W.nthreads) ws.st[ws.order[k]] = kUnreached;
+    auto reset = [&](uint32_t v) {
+      ws.st[v] = kUnreached;
+      ws.rho[v] = 0.0;
+      ws.sacc[v] = -0.0;
+    };
+    for (uint32_t k = W.gthread; k < total_l; k += W.nthreads) reset(ws.order[k]);
     for (uint32_t k = W.gthread; k < total_hc; k += W.nthreads) {
       const uint4 ent = ws.hc[k];
-      if (ent.y != 0) continue;  // one entry per vertex: its first chunk
-      ws.st[ent.x] = kUnreached;
+      if (ent.y == 0) reset(ent.x);  // one entry per vertex: its first chunk
     }
     reset_slot(t);
     if (!s.sync()) return;
@@ -346,8 +455,9 @@ __global__ void __launch_bounds__(512, 3) k_bc_xf(DiscoveryArgs a, GraphView G, 
 
 using namespace gdbi;
 
-// Workspace of one BC run (the per-vertex records, the level lists,
-// heavy-chunk entries and their accumulators, the counter block).
+// Workspace of one BC run (the per-vertex records and accumulators, the
+// level lists, heavy-chunk entries and their accumulators, per-level arc
+// counts, the counter block).
 static size_t bc_layout(const gdb_graph* g, char* base, float* d_bc, const uint32_t* d_sources,
                         uint32_t nsrc, BcWs* ws, char** cnt_out) {
   const uint32_t V = g->V;
@@ -355,15 +465,19 @@ static size_t bc_layout(const gdb_graph* g, char* base, float* d_bc, const uint3
   const uint32_t ccap = std::max<uint32_t>(g->nheavy_chunks, 1);
   const uint32_t maxlev = V + 2;
   Bump b;
-  const size_t o_st = b.take((size_t)V * 16);
+  const size_t o_st = b.take((size_t)V * 8), o_rho = b.take((size_t)V * 8),
+               o_sacc = b.take((size_t)V * 8);
   const size_t o_ord = b.take((size_t)V * 4);
   const size_t o_hc = b.take((size_t)ccap * 16), o_hacc = b.take((size_t)hcap * 8),
                o_hleft = b.take((size_t)hcap * 4);
   const size_t o_ll = b.take((size_t)maxlev * 4), o_lh = b.take((size_t)maxlev * 4),
                o_lhc = b.take((size_t)maxlev * 4), o_lhv = b.take((size_t)maxlev * 4);
+  const size_t o_la = b.take((size_t)(maxlev + 2) * 8);
   const size_t o_cnt = b.take(512);
   if (!base) return b.off;
-  ws->st = (uint4*)(base + o_st);
+  ws->st = (uint2*)(base + o_st);
+  ws->rho = (double*)(base + o_rho);
+  ws->sacc = (double*)(base + o_sacc);
   ws->bc = d_bc;
   ws->order = (uint32_t*)(base + o_ord);
   ws->hc = (uint4*)(base + o_hc);
@@ -374,6 +488,7 @@ static size_t bc_layout(const gdb_graph* g, char* base, float* d_bc, const uint3
   ws->lev_h = (uint32_t*)(base + o_lh);
   ws->lev_hc = (uint32_t*)(base + o_lhc);
   ws->lev_hv = (uint32_t*)(base + o_lhv);
+  ws->lev_arcs = (unsigned long long*)(base + o_la);
   char* cnt = base + o_cnt;
   ws->stats = (unsigned long long*)cnt;
   ws->hcnt = (unsigned long long*)(cnt + 64);

@@ -270,7 +270,7 @@ __device__ __forceinline__ void frontier_push_heavy(const GraphView& G, const Fr
   if (heavy && F.hleft) {
     const uint32_t vs = vslot0 + __popc(hm & lanemask_lt());
     F.hleft[vs] = nch;
-    F.hacc[vs] = 0.0;
+    F.hacc[vs] = -0.0;  // an empty sum (segment_add)
   }
   for (unsigned m = hm; m; m &= m - 1) {
     const int l = __ffs(m) - 1;
@@ -377,7 +377,7 @@ __device__ __forceinline__ void frontier_seed(const GraphView& G, const Frontier
     for (uint32_t j = 0; j < nch; ++j) F.hc[j] = make_uint4(v, j, 0u, nch);
     if (F.hleft) {
       F.hleft[0] = nch;
-      F.hacc[0] = 0.0;
+      F.hacc[0] = -0.0;  // an empty sum (segment_add)
     }
     *F.hcount = (1ull << 32) | nch;
   } else {
@@ -493,6 +493,11 @@ __device__ __forceinline__ uint32_t warp_min_u32(uint32_t x) { return __reduce_m
 __device__ __forceinline__ uint32_t warp_max_u32(uint32_t x) { return __reduce_max_sync(kFull, x); }
 __device__ __forceinline__ uint32_t warp_or_u32(uint32_t x) { return __reduce_or_sync(kFull, x); }
 __device__ __forceinline__ uint32_t warp_add_u32(uint32_t x) { return __reduce_add_sync(kFull, x); }
+__device__ __forceinline__ unsigned long long warp_add_u64(unsigned long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
+  return x;
+}
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -544,6 +549,8 @@ __device__ __forceinline__ void cta_or(bool p, uint32_t* word, uint32_t bit) {
 // the warp calls it.  The scan runs in FP32 and only the segment totals
 // are added in FP64 (one FP64 add per owner per step instead of five per
 // arc: FP64 issues at a small fraction of the FP32 rate on this GPU).
+// -0.0 is the neutral term: a segment of -0.0 leaves its slot untouched, so
+// a slot that starts at -0.0 still reads -0.0 when nothing was added.
 __device__ __forceinline__ void segment_add(double* slot, int owner, float x) {
   const int lane = lane_id();
 #pragma unroll
@@ -553,7 +560,7 @@ __device__ __forceinline__ void segment_add(double* slot, int owner, float x) {
     if (lane + o < 32 && ow == owner) x += y;
   }
   const int prev = __shfl_up_sync(kFull, owner, 1);
-  if ((lane == 0 || prev != owner) && x != 0.f) slot[owner] += (double)x;
+  if ((lane == 0 || prev != owner) && __float_as_uint(x) != 0x80000000u) slot[owner] += (double)x;
 }
 
 __device__ __forceinline__ float warp_sum_f32(float x) {
