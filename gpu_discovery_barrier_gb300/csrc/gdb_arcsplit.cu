@@ -4,8 +4,9 @@
 // arcs of weight in [b, GDB_LONESTAR_INF), each in the original order, each
 // a complete CSR with its own heavy-vertex table, so the traversal kernels'
 // work distribution (warp groups of light vertices, 128-arc chunks of heavy
-// ones) applies to either half unchanged.  Arcs of weight >= the infinity
-// are never relaxed and belong to neither half.
+// ones) applies to either half unchanged; graph T is H transposed (in-arcs
+// and their weights, no heavy table), for pulls over heavy arcs.  Arcs of
+// weight >= the infinity are never relaxed and belong to neither half.
 //
 // Everything is built on the device: per-vertex class counts (a warp per
 // vertex of degree <= 128, a CTA per heavier vertex), exclusive scans into
@@ -220,6 +221,36 @@ __global__ void k_split_scatter(GraphView G, uint32_t bound, const uint32_t* rl,
   }
 }
 
+// In-arc counts of graph H (for its transpose).
+__global__ void k_in_degree(GraphView H, uint32_t* indeg) {
+  for (uint64_t a = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; a < H.E;
+       a += (uint64_t)gridDim.x * blockDim.x)
+    atomicAdd(&indeg[__ldg(&H.col[a])], 1u);
+}
+
+// Transpose of graph H: every arc u -> v (weight w) becomes v -> u in
+// row v of (rt, ct, wt); fill[v] hands out the places in row v, so the
+// order within a row is arbitrary.  A CTA per heavy vertex of H, a warp
+// per other vertex.
+__global__ void k_transpose(GraphView H, const uint32_t* rt, uint32_t* fill, uint32_t* ct,
+                            uint32_t* wt) {
+  auto arc = [&](uint32_t u, uint32_t a) {
+    const uint32_t v = __ldg(&H.col[a]);
+    const uint32_t p = rt[v] + atomicAdd(&fill[v], 1u);
+    ct[p] = u;
+    wt[p] = __ldg(&H.w[a]);
+  };
+  for (uint32_t h = blockIdx.x; h < H.nheavy; h += gridDim.x) {
+    const uint32_t u = H.heavy_v[h];
+    for (uint32_t a = H.row[u] + threadIdx.x; a < H.row[u + 1]; a += blockDim.x) arc(u, a);
+  }
+  const Warps W = warps_of(blockIdx.x, gridDim.x);
+  for (uint32_t u = W.gwarp; u < H.V; u += W.nwarps) {
+    if (is_heavy(H, u)) continue;
+    for (uint32_t a = H.row[u] + lane_id(); a < H.row[u + 1]; a += 32) arc(u, a);
+  }
+}
+
 // Heavy-vertex marks of a CSR given by its row array: flag (degree >
 // kHeavyDeg), chunk count, the membership bitmap and the largest degree.
 __global__ void k_heavy_marks(const uint32_t* row, uint32_t V, uint32_t* flag, uint32_t* nch,
@@ -276,7 +307,8 @@ static cudaError_t exclusive_scan(const uint32_t* in, uint32_t n, uint32_t* out,
 void arc_split_drop(gdb_graph* g) {
   if (g->split_l) gdb_graph_destroy(g->split_l);
   if (g->split_h) gdb_graph_destroy(g->split_h);
-  g->split_l = g->split_h = nullptr;
+  if (g->split_t) gdb_graph_destroy(g->split_t);
+  g->split_l = g->split_h = g->split_t = nullptr;
   g->split_bound = 0;
 }
 
@@ -326,6 +358,7 @@ int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
   cudaStream_t st = c->stream;
   gdb_graph* L = new_half(c, V);
   gdb_graph* H = new_half(c, V);
+  gdb_graph* T = nullptr;  // transpose of H, built last
   // scratch: four V + 1 word arrays, the scan's tile sums, totals
   const size_t vw = (size_t)V + 1;
   uint32_t* scratch = nullptr;
@@ -336,6 +369,7 @@ int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
     cudaStreamSynchronize(st);
     gdb_graph_destroy(L);
     gdb_graph_destroy(H);
+    if (T) gdb_graph_destroy(T);
     return r;
   };
   cudaError_t e = cudaMallocAsync((void**)&scratch, words * 4, st);
@@ -369,12 +403,32 @@ int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split scatter"));
   if ((rc = heavy_table_device(c, L, t0, t1, t2, t3, tmp, hs))) return fail(rc);
   if ((rc = heavy_table_device(c, H, t0, t1, t2, t3, tmp, hs))) return fail(rc);
+  // the transpose of the heavy half: in-arcs with their weights, for the
+  // pull form of a settle superstep (the weights need not be symmetric)
+  T = new_half(c, V);
+  T->E = H->E;
+  e = cudaMalloc(&T->row, vw * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&T->col, std::max<uint64_t>(T->E, 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&T->w, std::max<uint64_t>(T->E, 1) * 4);
+  if (e == cudaSuccess) e = cudaMemsetAsync(t0, 0, vw * 4, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(t1, 0, vw * 4, st);
+  if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split transpose"));
+  const GraphView HV = H->view();
+  k_in_degree<<<grid, 256, 0, st>>>(HV, t0);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = exclusive_scan(t0, V, T->row, tmp, st);
+  if (e == cudaSuccess) {
+    k_transpose<<<grid, 256, 0, st>>>(HV, T->row, t1, T->col, T->w);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split transpose"));
   cudaFreeAsync(scratch, st);
   e = cudaStreamSynchronize(st);
   scratch = nullptr;
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split"));
   g->split_l = L;
   g->split_h = H;
+  g->split_t = T;
   g->split_bound = bound;
   return GDB_OK;
 }

@@ -61,6 +61,7 @@ struct gdb_graph {
   // (built on demand for bound split_bound; dropped with the weights)
   gdb_graph* split_l = nullptr;
   gdb_graph* split_h = nullptr;
+  gdb_graph* split_t = nullptr;  // split_h transposed (in-arcs, no heavy table)
   uint32_t split_bound = 0;
   gdb::GraphView view() const;
 };

@@ -79,6 +79,7 @@ struct SsspWs {
   uint4* shc;
   uint32_t* sqcount;
   unsigned long long* shcount;
+  unsigned long long* sarcs;   // heavy arcs of the settle list's vertices
 };
 
 // Warp-aggregated append of the lanes' `want` vertices to the far pile of
@@ -112,7 +113,7 @@ __device__ __forceinline__ uint32_t dist_of(const SsspWs& ws, uint32_t v) {
 // until the next call.
 __device__ __forceinline__ const unsigned long long* step_counts(const SsspWs& ws, int cur,
                                                                  uint32_t phase) {
-  __shared__ unsigned long long s[6];
+  __shared__ unsigned long long s[7];
   __syncthreads();
   if (threadIdx.x == 0) {
     s[0] = ld_cg(&ws.qcount[cur]);
@@ -122,6 +123,7 @@ __device__ __forceinline__ const unsigned long long* step_counts(const SsspWs& w
     const bool split = ws.light < kInf;
     s[4] = split ? ld_cg(ws.sqcount) : 0u;
     s[5] = split ? (uint32_t)__ldcg(ws.shcount) : 0u;
+    s[6] = split ? __ldcg(ws.sarcs) : 0ull;
   }
   __syncthreads();
   return s;
@@ -198,9 +200,13 @@ __device__ __forceinline__ void sssp_sweep(const GraphView& G, const GraphView& 
   WarpStage ss = frontier_stage(settle, 2);
   // a vertex is in a superstep's frontier at most once, so a plain mark
   // store dedupes expansions across the bucket's supersteps
+  unsigned long long rec_arcs = 0;  // heavy arcs of the vertices this lane records
   auto remember = [&](bool act, uint32_t u) {
     const bool add = act && ld_cg(&ws.stamp[u]) != pile;
-    if (add) ws.stamp[u] = pile;
+    if (add) {
+      ws.stamp[u] = pile;
+      rec_arcs += __ldg(&GR.row[u + 1]) - __ldg(&GR.row[u]);
+    }
     frontier_push_staged(GR, settle, ss, add, u);
   };
   // light groups: each lane reads its own vertex's distance once
@@ -226,12 +232,62 @@ __device__ __forceinline__ void sssp_sweep(const GraphView& G, const GraphView& 
     range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, du, arc); });
   }
   qs.flush();
-  if (record) ss.flush();
+  if (record) {
+    ss.flush();
+    rec_arcs = warp_add_u64(rec_arcs);
+    if (lane == 0 && rec_arcs) atomicAdd(ws.sarcs, rec_arcs);
+  }
   if (ws.delta) {
     fs.flush();
     fmin = __reduce_min_sync(kFull, fmin);
     if (lane == 0 && fmin != 0xFFFFFFFFu) atomicMin(&ws.farmin[phase % 3], fmin);
   }
+}
+
+// Settle by pull, the other direction of a settle superstep: every vertex
+// at or beyond the split takes the minimum of dist(v) + w over its heavy
+// in-arcs v -> u (GT: the heavy half transposed) from vertices below the
+// split (all final).  It replaces walking the
+// heavy arcs of the bucket's vertices when the unsettled vertices hold
+// fewer heavy arcs -- on power-law graphs the first bucket holds the hubs
+// and most arcs.  Same fixed point: each relaxation it applies is one the
+// push would apply, and arcs from earlier buckets can no longer improve.
+__device__ __forceinline__ void settle_pull(const GraphView& GT, const Warps& W, const SsspWs& ws,
+                                            uint32_t split, uint32_t phase, uint32_t* smin,
+                                            unsigned long long& arcs) {
+  const int lane = lane_id();
+  const uint32_t pile = phase + 1;
+  WarpStage fs{warp_stage(1), pick(ws.far, phase), &ws.farcount[phase % 3], ws.qcap, ws.overflow};
+  uint32_t fmin = 0xFFFFFFFFu;
+  uint32_t* my = smin + (threadIdx.x & ~31u);
+  for (uint32_t g = W.gwarp; g * 32 < GT.V; g += W.nwarps) {
+    const uint32_t u = g * 32 + lane;
+    const uint32_t du = u < GT.V ? dist_of<true>(ws, u) : 0u;
+    const bool open = u < GT.V && du >= split;
+    my[lane] = 0xFFFFFFFFu;
+    __syncwarp();
+    group_arcs(GT, open, u, [&](bool valid, int owner, uint32_t arc) {
+      if (valid) {
+        ++arcs;
+        const uint32_t v = __ldg(&GT.col[arc]), w = __ldg(&GT.w[arc]);
+        const uint32_t dv = dist_of<true>(ws, v);
+        if (dv < split) atomicMin(&my[owner], dv + w);
+      }
+    });
+    __syncwarp();
+    const uint32_t nd = my[lane];
+    const bool better = open && nd < du;
+    if (better) {
+      ws.key[u] = (unsigned long long)nd << 32;  // a far improvement; only this lane writes u
+      fmin = min(fmin, nd);
+    }
+    const bool add = better && ld_cg(&ws.farmark[u]) != pile;
+    if (add) ws.farmark[u] = pile;
+    fs.add(add, u);
+  }
+  fs.flush();
+  fmin = __reduce_min_sync(kFull, fmin);
+  if (lane == 0 && fmin != 0xFFFFFFFFu) atomicMin(&ws.farmin[phase % 3], fmin);
 }
 
 // Phase change of the near-far schedule: split the far pile of `phase`
@@ -263,10 +319,12 @@ __device__ __forceinline__ void far_filter(const GraphView& G, const Warps& W, c
 }
 
 // G: the arcs near supersteps relax (all arcs, or the light half under
-// the split); GH: the heavy half the settle supersteps relax (split only).
+// the split); GH: the heavy half the settle supersteps relax, GT the same
+// transposed (split only).
 template <class Sync>
 __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const GraphView& GH,
-                                          const SsspWs& ws, uint32_t src) {
+                                          const GraphView& GT, const SsspWs& ws, uint32_t src,
+                                          uint32_t* smin) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
   const bool split_arcs = ws.light < kInf;
@@ -289,6 +347,7 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Gra
     *ws.overflow = 0;
     *ws.sqcount = 0;
     *ws.shcount = 0;
+    *ws.sarcs = 0;
     ws.stats[0] = ws.stats[1] = ws.stats[2] = 0;
   }
   if (!s.sync()) return;
@@ -315,8 +374,10 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Gra
   // every CTA derives split and phase from the same counters after each
   // barrier, so they stay uniform across the grid
   uint32_t split = ws.delta ? ws.delta : 0xFFFFFFFFu, phase = 0;
-  // settle-list entries (light vertices, chunk entries) already relaxed
+  // settle-list entries (light vertices, chunk entries) already relaxed,
+  // and the heavy arcs of all vertices recorded by then
   uint32_t sdone = 0, hdone = 0;
+  unsigned long long adone = 0;
   const uint32_t whi = split_arcs ? ws.light : kInf;
   for (;; ++L) {
     const int cur = L % 3, old = (L + 2) % 3;
@@ -332,11 +393,20 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Gra
       ws.hcursor[old] = 0;
     }
     if (dry && unsettled) {
-      // the bucket is settled: relax the heavy arcs of its vertices once
-      sssp_sweep<true>(GH, GH, W, ws, L, split, phase, ws.sq + sdone, sn - sdone, ws.shc + hdone,
-                       hn - hdone, ws.light, kInf, false, arcs);
+      // the bucket is settled: relax the heavy arcs of its vertices once,
+      // from whichever side holds fewer of them (the pull also looks at
+      // every vertex's distance once)
+      const unsigned long long an = sc[6];
+      const unsigned long long open_arcs = GH.E > an ? GH.E - an : 0ull;
+      if (open_arcs + GH.V < an - adone) {
+        settle_pull(GT, W, ws, split, phase, smin, arcs);
+      } else {
+        sssp_sweep<true>(GH, GH, W, ws, L, split, phase, ws.sq + sdone, sn - sdone, ws.shc + hdone,
+                         hn - hdone, ws.light, kInf, false, arcs);
+      }
       sdone = sn;
       hdone = hn;
+      adone = an;
     } else if (dry) {
       const uint32_t lo = split;
       const unsigned long long nx = (unsigned long long)max(lo, (uint32_t)sc[3]) + ws.delta;
@@ -367,17 +437,19 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Gra
 }
 
 __global__ void __launch_bounds__(512, 3) k_sssp_xf(DiscoveryArgs a, GraphView G, GraphView GH,
-                                                     SsspWs ws, uint32_t src) {
+                                                     GraphView GT, SsspWs ws, uint32_t src) {
   __shared__ LocalCtx l;
+  __shared__ uint32_t smin[512];
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
-  sssp_body(s, G, GH, ws, src);
+  sssp_body(s, G, GH, GT, ws, src, smin);
 }
 
-__global__ void __launch_bounds__(512, 3) k_sssp_grid(GraphView G, GraphView GH, SsspWs ws,
-                                                       uint32_t src) {
+__global__ void __launch_bounds__(512, 3) k_sssp_grid(GraphView G, GraphView GH, GraphView GT,
+                                                       SsspWs ws, uint32_t src) {
+  __shared__ uint32_t smin[512];
   GridSync s;
-  sssp_body(s, G, GH, ws, src);
+  sssp_body(s, G, GH, GT, ws, src, smin);
 }
 
 // Graph-relaunch mode (CUDA-graph WHILE node): an init launch, then one
@@ -627,6 +699,7 @@ static size_t sssp_layout(const gdb_graph* g, char* base, uint32_t* d_dist, Sssp
   ws->farmin = (uint32_t*)(cnt + 240);                 // 3
   ws->sqcount = (uint32_t*)(cnt + 256);
   ws->shcount = (unsigned long long*)(cnt + 264);
+  ws->sarcs = (unsigned long long*)(cnt + 272);
   ws->sq = (uint32_t*)(base + o_sq);
   ws->shc = (uint4*)(base + o_shc);
   ws->light = kInf;
@@ -705,14 +778,15 @@ static int sssp_light_bound(gdb_ctx* c, gdb_graph* g, uint32_t delta, uint32_t* 
   return arc_split(c, g, *light);
 }
 
-// The views a run walks: the light and heavy halves under the split, the
-// graph itself (twice) otherwise.
-static void split_views(gdb_graph* g, uint32_t light, GraphView* gn, GraphView* gh) {
+// The views a run walks: the light half, the heavy half and its transpose
+// under the split, the graph itself (three times) otherwise.
+static void split_views(gdb_graph* g, uint32_t light, GraphView* gn, GraphView* gh, GraphView* gt) {
   if (light < kInf && g->split_l && g->split_bound == light) {
     *gn = g->split_l->view();
     *gh = g->split_h->view();
+    *gt = g->split_t->view();
   } else {
-    *gn = *gh = g->view();
+    *gn = *gh = *gt = g->view();
   }
 }
 
@@ -771,15 +845,15 @@ int gdbi::sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d
   ws.delta = delta;
   // a plan whose partition was dropped since (new weights) runs unsplit
   ws.light = delta && light < kInf && g->split_l && g->split_bound == light ? light : kInf;
-  GraphView GN, GH;
-  split_views(g, ws.light, &GN, &GH);
+  GraphView GN, GH, GT;
+  split_views(g, ws.light, &GN, &GH, &GT);
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, stream));
   Shape s;
   int rc = persistent_shape(c, (const void*)k_sssp_xf, c->opt.block_size, 0, &s, false);
   if (rc) return rc;
   DiscoveryArgs a = proto;
   a.expected = std::min(s.grid, s.fit);
-  k_sssp_xf<<<s.grid, c->opt.block_size, 0, stream>>>(a, GN, GH, ws, 0u);
+  k_sssp_xf<<<s.grid, c->opt.block_size, 0, stream>>>(a, GN, GH, GT, ws, 0u);
   GDB_CUDA(c, cudaGetLastError());
   return GDB_OK;
 }
@@ -809,8 +883,8 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   // the plain worklist)
   ws.light = relaunch ? kInf : light;
   const GraphView G = g->view();
-  GraphView GN, GH;
-  split_views(g, ws.light, &GN, &GH);
+  GraphView GN, GH, GT;
+  split_views(g, ws.light, &GN, &GH, &GT);
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
   const int block = c->opt.block_size;
   const int kind = relaunch ? GDB_BARRIER_RELAUNCH_GRAPH : c->opt.barrier;
@@ -821,7 +895,7 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
     if (rc) return rc;
     DiscoveryArgs a = discovery_args(c, s);
     GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    k_sssp_xf<<<s.grid, block, 0, c->stream>>>(a, GN, GH, ws, src);
+    k_sssp_xf<<<s.grid, block, 0, c->stream>>>(a, GN, GH, GT, ws, src);
     GDB_CUDA(c, cudaGetLastError());
     GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     rc = finish_run(c);
@@ -835,10 +909,10 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
     GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sssp_grid, block, 0));
     int grid = occ * c->sm_count;
     if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
-    GraphView Gc = GN, GHc = GH;
+    GraphView Gc = GN, GHc = GH, GTc = GT;
     SsspWs wsc = ws;
     uint32_t srcc = src;
-    void* args[] = {(void*)&Gc, (void*)&GHc, (void*)&wsc, (void*)&srcc};
+    void* args[] = {(void*)&Gc, (void*)&GHc, (void*)&GTc, (void*)&wsc, (void*)&srcc};
     GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
     GDB_CUDA(c, cudaLaunchCooperativeKernel((const void*)k_sssp_grid, grid, block, args, 0, c->stream));
     GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
