@@ -343,6 +343,24 @@ static int heavy_table_device(gdb_ctx* c, gdb_graph* x, uint32_t* t0, uint32_t* 
   return GDB_OK;
 }
 
+// The heavy table of a graph whose row array is on the device (every graph
+// the library creates): scratch of its own, one synchronisation for the
+// totals.
+int build_heavy_table(gdb_graph* g) {
+  gdb_ctx* c = g->ctx;
+  const uint32_t V = g->V;
+  const size_t vw = (size_t)V + 1;
+  uint32_t* scratch = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&scratch, (4 * vw + scan_tmp_words(V) + 8) * 4, c->stream));
+  uint32_t *t0 = scratch, *t1 = t0 + vw, *t2 = t1 + vw, *t3 = t2 + vw, *tmp = t3 + vw,
+           *hs = tmp + scan_tmp_words(V);
+  const int rc = heavy_table_device(c, g, t0, t1, t2, t3, tmp, hs);
+  cudaFreeAsync(scratch, c->stream);
+  const cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (rc) return rc;
+  return e == cudaSuccess ? GDB_OK : set_cuda_error(c, e, "heavy table");
+}
+
 static gdb_graph* new_half(gdb_ctx* c, uint32_t V) {
   gdb_graph* x = new gdb_graph();
   x->ctx = c;

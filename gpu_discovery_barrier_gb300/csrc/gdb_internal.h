@@ -115,8 +115,8 @@ int read_participating(gdb_ctx* c, int* n);
 int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound);
 void arc_split_drop(gdb_graph* g);
 
-// Heavy table construction from a host copy of row_ptr.
-int build_heavy_table(gdb_graph* g, const uint32_t* host_row);
+// Heavy table construction on the device from g's row array.
+int build_heavy_table(gdb_graph* g);
 uint32_t chunk_capacity(const gdb_graph* g);
 
 bool graph_ok(gdb_ctx* c, gdb_graph* g);

@@ -133,36 +133,6 @@ int read_participating(gdb_ctx* c, int* n) {
   return GDB_OK;
 }
 
-int build_heavy_table(gdb_graph* g, const uint32_t* hrow) {
-  gdb_ctx* c = g->ctx;
-  std::vector<uint32_t> hv;
-  std::vector<uint4> chunks;
-  std::vector<uint32_t> bits((g->V + 31) / 32 + 1, 0);
-  for (uint32_t v = 0; v < g->V; ++v) {
-    const uint32_t d = hrow[v + 1] - hrow[v];
-    g->maxdeg = std::max(g->maxdeg, d);
-    if (d > gdb::kHeavyDeg) {
-      const uint32_t h = (uint32_t)hv.size(), n = gdb::chunks_of(d);
-      hv.push_back(v);
-      for (uint32_t j = 0; j < n; ++j) chunks.push_back(make_uint4(v, j, h, n));
-      bits[v >> 5] |= 1u << (v & 31);
-    }
-  }
-  g->nheavy = (uint32_t)hv.size();
-  g->nheavy_chunks = (uint32_t)chunks.size();
-  const size_t nb = bits.size() * 4, nv = std::max<size_t>(hv.size(), 1) * 4,
-               nc = std::max<size_t>(chunks.size(), 1) * sizeof(uint4);
-  GDB_CUDA(c, cudaMalloc(&g->heavy_bits, nb));
-  GDB_CUDA(c, cudaMalloc(&g->heavy_v, nv));
-  GDB_CUDA(c, cudaMalloc(&g->heavy_chunk, nc));
-  GDB_CUDA(c, cudaMemcpy(g->heavy_bits, bits.data(), nb, cudaMemcpyHostToDevice));
-  if (!hv.empty()) GDB_CUDA(c, cudaMemcpy(g->heavy_v, hv.data(), hv.size() * 4, cudaMemcpyHostToDevice));
-  if (!chunks.empty())
-    GDB_CUDA(c, cudaMemcpy(g->heavy_chunk, chunks.data(), chunks.size() * sizeof(uint4),
-                           cudaMemcpyHostToDevice));
-  return GDB_OK;
-}
-
 // Capacity of a frontier's chunk entries: sum of ceil(d / kChunk) over the
 // heavy vertices, at most E / kChunk + nheavy.
 uint32_t chunk_capacity(const gdb_graph* g) {
@@ -369,7 +339,7 @@ int gdb_graph_create(gdb_ctx* c, uint32_t V, uint64_t E, const uint32_t* row, co
     gdb_graph_destroy(g);
     return rc;
   }
-  rc = build_heavy_table(g, row);
+  rc = build_heavy_table(g);
   if (rc) {
     gdb_graph_destroy(g);
     return rc;
@@ -384,10 +354,11 @@ int gdb_graph_create_device(gdb_ctx* c, uint32_t V, uint64_t E, const uint32_t* 
   *out = nullptr;
   int rc = graph_common(c, V, E);
   if (rc) return rc;
-  std::vector<uint32_t> hrow((size_t)V + 1);
-  cudaError_t e = cudaMemcpy(hrow.data(), d_row, (size_t)(V + 1) * 4, cudaMemcpyDeviceToHost);
+  uint32_t ends[2] = {1, 0};
+  cudaError_t e = cudaMemcpy(&ends[0], d_row, 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&ends[1], d_row + V, 4, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return set_cuda_error(c, e, "row_ptr read-back");
-  if (hrow[0] != 0 || hrow[V] != E) return set_error(c, GDB_ERR_INVALID, "row_ptr[0] != 0 or row_ptr[V] != E");
+  if (ends[0] != 0 || ends[1] != E) return set_error(c, GDB_ERR_INVALID, "row_ptr[0] != 0 or row_ptr[V] != E");
   gdb_graph* g = new gdb_graph();
   g->ctx = c;
   g->V = V;
@@ -397,7 +368,7 @@ int gdb_graph_create_device(gdb_ctx* c, uint32_t V, uint64_t E, const uint32_t* 
   g->w = const_cast<uint32_t*>(d_w);
   g->owns = false;
   g->owns_w = false;
-  rc = build_heavy_table(g, hrow.data());
+  rc = build_heavy_table(g);
   if (rc) {
     gdb_graph_destroy(g);
     return rc;
