@@ -382,7 +382,10 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   }
 }
 
-__global__ void __launch_bounds__(512, 3) k_color_xf(DiscoveryArgs a, GraphView G, ColorWs ws) {
+// One CTA per SM (the rounds are latency-bound; see color_run), so the
+// bound leaves the compiler all the registers it wants for the four-step
+// batches (R-MAT-22: 33.7 ms at a three-per-SM bound, 31.3 ms).
+__global__ void __launch_bounds__(512, 1) k_color_xf(DiscoveryArgs a, GraphView G, ColorWs ws) {
   __shared__ LocalCtx l;
   __shared__ uint32_t smem[1024];
   if (!discover(a, &l)) return;

@@ -196,6 +196,46 @@ __device__ __forceinline__ void sssp_sweep(const GraphView& G, const GraphView& 
       fs.add(add, v);
     }
   };
+  // four 32-arc steps at once (Keyed): column/weight loads, key loads and
+  // atomicMins of the four steps in flight together
+  auto relax4 = [&](const bool* valid, const uint32_t* du4, const uint32_t* arc) {
+    uint32_t v[4], nd[4];
+    bool in[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      v[k] = valid[k] ? __ldg(&G.col[arc[k]]) : 0u;
+      const uint32_t wt = valid[k] ? __ldg(&G.w[arc[k]]) : kInf;
+      in[k] = valid[k] && wt >= wlo && wt < whi;
+      nd[k] = du4[k] + wt;
+      arcs += in[k];
+    }
+    uint32_t cur[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) cur[k] = in[k] ? dist_of<true>(ws, v[k]) : 0u;
+    unsigned long long old[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const bool t = in[k] && nd[k] < cur[k];
+      old[k] = t ? atomicMin(&ws.key[v[k]], ((unsigned long long)nd[k] << 32) |
+                                                 (nd[k] < split ? (unsigned long long)(L + 1) : 0ull))
+                 : 0ull;
+      in[k] = t;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      bool want = false, far = false;
+      if (in[k] && nd[k] < (uint32_t)(old[k] >> 32)) {
+        if (nd[k] < split) want = (uint32_t)old[k] != L + 1;
+        else far = true;
+      }
+      frontier_push_staged(G, out, qs, want, v[k]);
+      if (ws.delta && __any_sync(kFull, far)) {
+        if (far) fmin = min(fmin, nd[k]);
+        const bool add = far && ld_cg(&ws.farmark[v[k]]) != pile && atomicExch(&ws.farmark[v[k]], pile) != pile;
+        fs.add(add, v[k]);
+      }
+    }
+  };
   const Frontier settle{ws.sq, ws.shc, ws.sqcount, ws.shcount, ws.qcap, ws.hcap, ws.overflow};
   WarpStage ss = frontier_stage(settle, 2);
   // a vertex is in a superstep's frontier at most once, so a plain mark
@@ -218,9 +258,18 @@ __device__ __forceinline__ void sssp_sweep(const GraphView& G, const GraphView& 
     const uint32_t u = act ? ld_cg(&q[i]) : 0u;
     const uint32_t du = act ? dist_of<Keyed>(ws, u) : 0u;
     if (record) remember(act, u);
-    group_arcs(G, act, u, [&](bool valid, int owner, uint32_t arc) {
-      relax(valid, __shfl_sync(kFull, du, owner), arc);
-    });
+    if constexpr (Keyed) {
+      group_arcs4(G, act, u, [&](const bool* valid, const int* owner, const uint32_t* arc) {
+        uint32_t d4[4];
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) d4[kk] = __shfl_sync(kFull, du, owner[kk]);
+        relax4(valid, d4, arc);
+      });
+    } else {
+      group_arcs(G, act, u, [&](bool valid, int owner, uint32_t arc) {
+        relax(valid, __shfl_sync(kFull, du, owner), arc);
+      });
+    }
   }
   WorkTaker ht(nch, W, &ws.hcursor[cur]);
   for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
@@ -229,7 +278,19 @@ __device__ __forceinline__ void sssp_sweep(const GraphView& G, const GraphView& 
     if (record) remember(lane == 0 && ent.y == 0, ent.x);
     uint32_t b, en;
     chunk_range(G, ent, b, en);
-    range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, du, arc); });
+    if constexpr (Keyed) {
+      bool valid[4];
+      uint32_t arc[4], d4[4];
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        arc[kk] = b + 32 * kk + lane;
+        valid[kk] = arc[kk] < en;
+        d4[kk] = du;
+      }
+      relax4(valid, d4, arc);
+    } else {
+      range_arcs(b, en, [&](bool valid, uint32_t arc) { relax(valid, du, arc); });
+    }
   }
   qs.flush();
   if (record) {
@@ -436,7 +497,10 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Gra
   }
 }
 
-__global__ void __launch_bounds__(512, 3) k_sssp_xf(DiscoveryArgs a, GraphView G, GraphView GH,
+// Two CTAs per SM at up to 64 registers: the four-step batches and the
+// bucket state keep more values live than 40 registers hold (R-MAT-22 at
+// the automatic width: 2.20 ms per source at three CTAs per SM, 1.97 ms).
+__global__ void __launch_bounds__(512, 2) k_sssp_xf(DiscoveryArgs a, GraphView G, GraphView GH,
                                                      GraphView GT, SsspWs ws, uint32_t src) {
   __shared__ LocalCtx l;
   __shared__ uint32_t smin[512];
@@ -445,7 +509,7 @@ __global__ void __launch_bounds__(512, 3) k_sssp_xf(DiscoveryArgs a, GraphView G
   sssp_body(s, G, GH, GT, ws, src, smin);
 }
 
-__global__ void __launch_bounds__(512, 3) k_sssp_grid(GraphView G, GraphView GH, GraphView GT,
+__global__ void __launch_bounds__(512, 2) k_sssp_grid(GraphView G, GraphView GH, GraphView GT,
                                                        SsspWs ws, uint32_t src) {
   __shared__ uint32_t smin[512];
   GridSync s;
