@@ -75,14 +75,19 @@ def make_workload(scale: int, ef: float, path: str | None = None):
 
     if path:
         g = gdb.read_graph(path, directed=False)
+        # generated weights are one per undirected edge; a file's own
+        # weights are taken as given (not declared symmetric)
+        symmetric = g.w is None
         w = g.w if g.w is not None else gg.uniform_weights(g, 1, 255, seed=1)
         g = gg.CSR(g.row_ptr, g.col, None, g.name)
     else:
         g = gg.rmat_scale(scale, ef, seed=1)
         w = gg.uniform_weights(g, 1, 255, seed=1)
+        symmetric = True  # undirected R-MAT, one weight per edge
     return {
         "g": g,
         "w": w,
+        "symmetric": symmetric,
         "uw": gg.unique_weights(g, seed=3),
         "prio": gg.priorities(g.V, seed=4),
         "src": gg.sources(g, NSRC, seed=2),
@@ -213,7 +218,7 @@ class GpuSuite:
         g = wl["g"]
         self.ctx = gdb.Ctx(device=device)
         set_schedule(self.ctx, schedule)
-        self.G = self.ctx.graph(g.row_ptr, g.col, wl["w"])
+        self.G = self.ctx.graph(g.row_ptr, g.col, wl["w"], symmetric=wl["symmetric"])
         self.Gu = self.ctx.graph(g.row_ptr, g.col, wl["uw"])
         dev = torch.device("cuda", device)
         V = g.V
@@ -262,20 +267,22 @@ class GpuSuite:
         """The same suite through the host-buffer API, graph upload included."""
         gdb = self.gdb
         c, g, src = self.ctx, self.wl["g"], self.wl["src"]
-        G = gdb.Graph(c, host["row"], host["col"], host["w"])
+        G = gdb.Graph(c, host["row"], host["col"], host["w"], symmetric=self.wl["symmetric"])
         outs = 0
+        # results land in page-locked host buffers the caller owns (reused
+        # from call to call, as a serving loop would)
         if "bfs" in self.apps:
             for s in src:
-                outs += c.bfs(G, int(s)).nbytes
+                outs += c.bfs(G, int(s), out=host["out_u32"]).nbytes
         if "sssp" in self.apps:
             for s in src:
-                outs += c.sssp(G, int(s)).nbytes
+                outs += c.sssp(G, int(s), out=host["out_u32"]).nbytes
         if "mis" in self.apps:
-            outs += c.mis(G, host["prio"]).nbytes
+            outs += c.mis(G, host["prio"], out=host["out_i32"]).nbytes
         if "color" in self.apps:
-            outs += c.color(G, host["prio"]).nbytes
+            outs += c.color(G, host["prio"], out=host["out_i32"]).nbytes
         if "bc" in self.apps:
-            outs += c.bc(G, src).nbytes
+            outs += c.bc(G, src, out=host["out_f32"]).nbytes
         if "mst" in self.apps:
             G.set_weights(host["uw"])
             c.mst(G)
@@ -289,7 +296,7 @@ _PINNED_KEEP: list = []
 
 def pinned_copy(torch, a: np.ndarray) -> np.ndarray:
     """Copy into page-locked host memory (kept alive for the process)."""
-    t = torch.empty(a.shape, dtype={np.dtype(np.uint32): torch.int32,
+    t = torch.empty(a.shape, dtype={np.dtype(np.uint32): torch.int32, np.dtype(np.int32): torch.int32,
                                     np.dtype(np.float32): torch.float32}[a.dtype], pin_memory=True)
     _PINNED_KEEP.append(t)
     out = t.numpy().view(a.dtype)
@@ -506,6 +513,9 @@ def run_gdb(args, rank, world, local):
                 "w": pinned_copy(torch, wl["w"]), "uw": pinned_copy(torch, wl["uw"]),
                 "prio": pinned_copy(torch, wl["prio"])}
         h2d = sum(host[k].nbytes for k in host) + 4 * NSRC
+        host.update(out_u32=pinned_copy(torch, np.zeros(g.V, np.uint32)),
+                    out_i32=pinned_copy(torch, np.zeros(g.V, np.int32)),
+                    out_f32=pinned_copy(torch, np.zeros(g.V, np.float32)))
         suite.step_e2e(host)
         barrier(world)
         torch.cuda.synchronize()
@@ -574,7 +584,7 @@ def run_grid(args, rank, world, local):
             c.selector_set(p)
         else:
             kinds.pop("xf_learned")
-        G = c.graph(g.row_ptr, g.col, w)
+        G = c.graph(g.row_ptr, g.col, w, symmetric=True)  # grid, one weight per edge
         for name, (kind, sched) in kinds.items():
             c.set_options(barrier=kind, schedule=sched)
             r = {}

@@ -319,7 +319,7 @@ static int heavy_table_device(gdb_ctx* c, gdb_graph* x, uint32_t* t0, uint32_t* 
   const uint32_t V = x->V;
   cudaStream_t st = c->stream;
   const size_t nb = ((size_t)(V + 31) / 32 + 1) * 4;
-  GDB_CUDA(c, cudaMalloc(&x->heavy_bits, nb));
+  GDB_CUDA(c, dev_alloc(c, (void**)&x->heavy_bits, nb));
   GDB_CUDA(c, cudaMemsetAsync(x->heavy_bits, 0, nb, st));
   GDB_CUDA(c, cudaMemsetAsync(hs, 0, 16, st));
   const int grid = 4 * c->sm_count;
@@ -336,8 +336,8 @@ static int heavy_table_device(gdb_ctx* c, gdb_graph* x, uint32_t* t0, uint32_t* 
   x->nheavy = hh[0];
   x->nheavy_chunks = hh[1];
   x->maxdeg = hh[2];
-  GDB_CUDA(c, cudaMalloc(&x->heavy_v, std::max<size_t>(x->nheavy, 1) * 4));
-  GDB_CUDA(c, cudaMalloc(&x->heavy_chunk, std::max<size_t>(x->nheavy_chunks, 1) * sizeof(uint4)));
+  GDB_CUDA(c, dev_alloc(c, (void**)&x->heavy_v, std::max<size_t>(x->nheavy, 1) * 4));
+  GDB_CUDA(c, dev_alloc(c, (void**)&x->heavy_chunk, std::max<size_t>(x->nheavy_chunks, 1) * sizeof(uint4)));
   k_heavy_fill<<<grid, 256, 0, st>>>(x->row, V, t0, t2, t3, x->heavy_v, x->heavy_chunk);
   GDB_CUDA(c, cudaGetLastError());
   return GDB_OK;
@@ -394,8 +394,8 @@ int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split scratch"));
   uint32_t *t0 = scratch, *t1 = t0 + vw, *t2 = t1 + vw, *t3 = t2 + vw, *tmp = t3 + vw,
            *hs = tmp + scan_tmp_words(V);
-  e = cudaMalloc(&L->row, vw * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&H->row, vw * 4);
+  e = dev_alloc(c, (void**)&L->row, vw * 4);
+  if (e == cudaSuccess) e = dev_alloc(c, (void**)&H->row, vw * 4);
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split rows"));
   const GraphView G = g->view();
   const int grid = 4 * c->sm_count;
@@ -411,10 +411,10 @@ int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split counts"));
   L->E = hh[0];
   H->E = hh[1];
-  e = cudaMalloc(&L->col, std::max<uint64_t>(L->E, 1) * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&L->w, std::max<uint64_t>(L->E, 1) * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&H->col, std::max<uint64_t>(H->E, 1) * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&H->w, std::max<uint64_t>(H->E, 1) * 4);
+  e = dev_alloc(c, (void**)&L->col, std::max<uint64_t>(L->E, 1) * 4);
+  if (e == cudaSuccess) e = dev_alloc(c, (void**)&L->w, std::max<uint64_t>(L->E, 1) * 4);
+  if (e == cudaSuccess) e = dev_alloc(c, (void**)&H->col, std::max<uint64_t>(H->E, 1) * 4);
+  if (e == cudaSuccess) e = dev_alloc(c, (void**)&H->w, std::max<uint64_t>(H->E, 1) * 4);
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split arcs"));
   k_split_scatter<<<grid, 256, 0, st>>>(G, bound, L->row, H->row, L->col, L->w, H->col, H->w);
   e = cudaGetLastError();
@@ -422,24 +422,27 @@ int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
   if ((rc = heavy_table_device(c, L, t0, t1, t2, t3, tmp, hs))) return fail(rc);
   if ((rc = heavy_table_device(c, H, t0, t1, t2, t3, tmp, hs))) return fail(rc);
   // the transpose of the heavy half: in-arcs with their weights, for the
-  // pull form of a settle superstep (the weights need not be symmetric)
-  T = new_half(c, V);
-  T->E = H->E;
-  e = cudaMalloc(&T->row, vw * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&T->col, std::max<uint64_t>(T->E, 1) * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&T->w, std::max<uint64_t>(T->E, 1) * 4);
-  if (e == cudaSuccess) e = cudaMemsetAsync(t0, 0, vw * 4, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(t1, 0, vw * 4, st);
-  if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split transpose"));
-  const GraphView HV = H->view();
-  k_in_degree<<<grid, 256, 0, st>>>(HV, t0);
-  e = cudaGetLastError();
-  if (e == cudaSuccess) e = exclusive_scan(t0, V, T->row, tmp, st);
-  if (e == cudaSuccess) {
-    k_transpose<<<grid, 256, 0, st>>>(HV, T->row, t1, T->col, T->w);
+  // pull form of a settle superstep -- a graph declared symmetric (with
+  // symmetric weights) is its own transpose
+  if (!g->symmetric) {
+    T = new_half(c, V);
+    T->E = H->E;
+    e = dev_alloc(c, (void**)&T->row, vw * 4);
+    if (e == cudaSuccess) e = dev_alloc(c, (void**)&T->col, std::max<uint64_t>(T->E, 1) * 4);
+    if (e == cudaSuccess) e = dev_alloc(c, (void**)&T->w, std::max<uint64_t>(T->E, 1) * 4);
+    if (e == cudaSuccess) e = cudaMemsetAsync(t0, 0, vw * 4, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(t1, 0, vw * 4, st);
+    if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split transpose"));
+    const GraphView HV = H->view();
+    k_in_degree<<<grid, 256, 0, st>>>(HV, t0);
     e = cudaGetLastError();
+    if (e == cudaSuccess) e = exclusive_scan(t0, V, T->row, tmp, st);
+    if (e == cudaSuccess) {
+      k_transpose<<<grid, 256, 0, st>>>(HV, T->row, t1, T->col, T->w);
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split transpose"));
   }
-  if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split transpose"));
   cudaFreeAsync(scratch, st);
   e = cudaStreamSynchronize(st);
   scratch = nullptr;

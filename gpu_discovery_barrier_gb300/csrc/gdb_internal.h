@@ -61,7 +61,9 @@ struct gdb_graph {
   // (built on demand for bound split_bound; dropped with the weights)
   gdb_graph* split_l = nullptr;
   gdb_graph* split_h = nullptr;
-  gdb_graph* split_t = nullptr;  // split_h transposed (in-arcs, no heavy table)
+  gdb_graph* split_t = nullptr;  // split_h transposed (in-arcs, no heavy table);
+                                 // none for a graph declared symmetric
+  bool symmetric = false;         // declared: u -> v (w) iff v -> u (w)
   uint32_t split_bound = 0;
   gdb::GraphView view() const;
 };
@@ -120,6 +122,11 @@ int build_heavy_table(gdb_graph* g);
 uint32_t chunk_capacity(const gdb_graph* g);
 
 bool graph_ok(gdb_ctx* c, gdb_graph* g);
+
+// Device memory of graphs and their derived structures: the context
+// stream's stream-ordered pool.
+cudaError_t dev_alloc(gdb_ctx* c, void** p, size_t bytes);
+void dev_free(gdb_ctx* c, void* p);
 
 // Stream-capturable XF launches over a caller-owned workspace (the batch
 // form): bytes of one run's workspace, and an enqueue that only issues a

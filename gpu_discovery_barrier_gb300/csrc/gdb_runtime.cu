@@ -141,6 +141,14 @@ uint32_t chunk_capacity(const gdb_graph* g) {
 
 bool graph_ok(gdb_ctx* c, gdb_graph* g) { return c && g && g->ctx == c; }
 
+cudaError_t dev_alloc(gdb_ctx* c, void** p, size_t bytes) {
+  return cudaMallocAsync(p, bytes, c->stream);
+}
+
+void dev_free(gdb_ctx* c, void* p) {
+  if (p) cudaFreeAsync(p, c->stream);
+}
+
 }  // namespace gdbi
 
 gdb::GraphView gdb_graph::view() const {
@@ -234,6 +242,15 @@ int gdb_ctx_create(const gdb_options* opt, gdb_ctx** out) {
   c->total_mem = prop.totalGlobalMem;
   // at most 32 resident CTAs per SM on this architecture family
   c->flag_cap = std::max(64, c->sm_count * 32);
+  // graphs, their partitions and per-call buffers come from the device's
+  // stream-ordered pool; keep freed blocks cached in it (a graph created
+  // and destroyed per request then costs no page mapping)
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  cudaGetLastError();
   bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess &&
             cudaEventCreate(&c->ev0) == cudaSuccess && cudaEventCreate(&c->ev1) == cudaSuccess &&
             cudaMalloc(&c->dctx, sizeof(gdb::DeviceCtx)) == cudaSuccess &&
@@ -327,9 +344,9 @@ int gdb_graph_create(gdb_ctx* c, uint32_t V, uint64_t E, const uint32_t* row, co
   g->V = V;
   g->E = E;
   const size_t eb = std::max<uint64_t>(E, 1) * 4;
-  cudaError_t e = cudaMalloc(&g->row, (size_t)(V + 1) * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&g->col, eb);
-  if (e == cudaSuccess && w) e = cudaMalloc(&g->w, eb);
+  cudaError_t e = dev_alloc(c, (void**)&g->row, (size_t)(V + 1) * 4);
+  if (e == cudaSuccess) e = dev_alloc(c, (void**)&g->col, eb);
+  if (e == cudaSuccess && w) e = dev_alloc(c, (void**)&g->w, eb);
   if (e == cudaSuccess) e = cudaMemcpyAsync(g->row, row, (size_t)(V + 1) * 4, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && E) e = cudaMemcpyAsync(g->col, col, E * 4, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && w && E) e = cudaMemcpyAsync(g->w, w, E * 4, cudaMemcpyHostToDevice, c->stream);
@@ -382,7 +399,7 @@ int gdb_graph_set_weights(gdb_graph* g, const uint32_t* w) {
   gdb_ctx* c = g->ctx;
   if (!g->w || !g->owns_w) {
     g->w = nullptr;
-    GDB_CUDA(c, cudaMalloc(&g->w, std::max<uint64_t>(g->E, 1) * 4));
+    GDB_CUDA(c, dev_alloc(c, (void**)&g->w, std::max<uint64_t>(g->E, 1) * 4));
     g->owns_w = true;
   }
   g->wmean = -1.0;
@@ -392,18 +409,30 @@ int gdb_graph_set_weights(gdb_graph* g, const uint32_t* w) {
   return GDB_OK;
 }
 
+int gdb_graph_set_symmetric(gdb_graph* g, int symmetric) {
+  if (!g || (symmetric != 0 && symmetric != 1)) return GDB_ERR_INVALID;
+  if ((bool)symmetric != g->symmetric) {
+    cudaStreamSynchronize(g->ctx->stream);
+    arc_split_drop(g);  // the partition's transposed half depends on it
+    g->symmetric = symmetric != 0;
+  }
+  return GDB_OK;
+}
+
 int gdb_graph_destroy(gdb_graph* g) {
   if (!g) return GDB_ERR_INVALID;
-  if (g->ctx && g->ctx->stream) cudaStreamSynchronize(g->ctx->stream);
+  gdb_ctx* c = g->ctx;
+  // work on any stream may still read the graph (batches, server slots)
+  cudaDeviceSynchronize();
   arc_split_drop(g);
   if (g->owns) {
-    cudaFree(g->row);
-    cudaFree(g->col);
+    dev_free(c, g->row);
+    dev_free(c, g->col);
   }
-  if (g->owns_w && g->w) cudaFree(g->w);
-  cudaFree(g->heavy_v);
-  cudaFree(g->heavy_chunk);
-  cudaFree(g->heavy_bits);
+  if (g->owns_w) dev_free(c, g->w);
+  dev_free(c, g->heavy_v);
+  dev_free(c, g->heavy_chunk);
+  dev_free(c, g->heavy_bits);
   cudaGetLastError();
   delete g;
   return GDB_OK;

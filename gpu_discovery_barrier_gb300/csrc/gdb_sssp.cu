@@ -848,7 +848,7 @@ static void split_views(gdb_graph* g, uint32_t light, GraphView* gn, GraphView* 
   if (light < kInf && g->split_l && g->split_bound == light) {
     *gn = g->split_l->view();
     *gh = g->split_h->view();
-    *gt = g->split_t->view();
+    *gt = g->split_t ? g->split_t->view() : *gh;  // a symmetric graph is its own transpose
   } else {
     *gn = *gh = *gt = g->view();
   }

@@ -23,7 +23,7 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libgdb.so"
 
-ABI_VERSION = 7  # GDB_ABI_VERSION of include/gdb.h
+ABI_VERSION = 8  # GDB_ABI_VERSION of include/gdb.h
 LONESTAR_INF = 1_000_000_000
 PANNOTIA_BIG = 99_999_999
 
@@ -123,6 +123,7 @@ SIGNATURES = [
     ("gdb_graph_create", C.c_int, [_P, C.c_uint32, C.c_uint64, _P, _P, _P, C.POINTER(_P)]),
     ("gdb_graph_create_device", C.c_int, [_P, C.c_uint32, C.c_uint64, _P, _P, _P, C.POINTER(_P)]),
     ("gdb_graph_set_weights", C.c_int, [_P, _P]),
+    ("gdb_graph_set_symmetric", C.c_int, [_P, C.c_int]),
     ("gdb_graph_destroy", C.c_int, [_P]),
     ("gdb_graph_info", C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64),
                                  C.POINTER(C.c_uint32)]),
@@ -259,6 +260,16 @@ def default_options(**kw) -> Options:
     return o
 
 
+def _out(out, n: int, dtype) -> np.ndarray:
+    """The result array of a call: a fresh one, or the caller's (checked)."""
+    if out is None:
+        return np.empty(n, dtype=dtype)
+    if out.dtype != np.dtype(dtype) or out.shape != (n,) or not out.flags["C_CONTIGUOUS"] \
+            or not out.flags["WRITEABLE"]:
+        raise ValueError(f"out must be a writable contiguous {np.dtype(dtype).name}[{n}] array")
+    return out
+
+
 def _ptr(a: np.ndarray | None):
     if a is None:
         return None
@@ -360,17 +371,21 @@ class Ctx:
         self.check(self._lib.gdb_debug_stall_master(self.h, after_barriers), "debug_stall_master")
 
     # -- graphs
-    def graph(self, row_ptr: np.ndarray, col: np.ndarray, w: np.ndarray | None = None) -> "Graph":
-        return Graph(self, row_ptr, col, w)
+    def graph(self, row_ptr: np.ndarray, col: np.ndarray, w: np.ndarray | None = None,
+              symmetric: bool = False) -> "Graph":
+        return Graph(self, row_ptr, col, w, symmetric=symmetric)
 
     # -- applications (host buffers)
-    def bfs(self, g: "Graph", src: int) -> np.ndarray:
-        out = np.empty(g.V, dtype=np.uint32)
+    def bfs(self, g: "Graph", src: int, out: np.ndarray | None = None) -> np.ndarray:
+        """BFS levels from src.  `out`: an optional caller-owned result
+        array (V uint32); page-locked host memory makes the read-back a
+        direct DMA instead of a staged copy."""
+        out = _out(out, g.V, np.uint32)
         self.check(self._lib.gdb_bfs(self.h, g.h, src, _ptr(out)), "gdb_bfs")
         return out
 
-    def sssp(self, g: "Graph", src: int) -> np.ndarray:
-        out = np.empty(g.V, dtype=np.uint32)
+    def sssp(self, g: "Graph", src: int, out: np.ndarray | None = None) -> np.ndarray:
+        out = _out(out, g.V, np.uint32)
         self.check(self._lib.gdb_sssp(self.h, g.h, src, _ptr(out)), "gdb_sssp")
         return out
 
@@ -379,21 +394,21 @@ class Ctx:
         self.check(self._lib.gdb_sssp_jacobi(self.h, g.h, src, _ptr(out)), "gdb_sssp_jacobi")
         return out
 
-    def mis(self, g: "Graph", node_value: np.ndarray) -> np.ndarray:
+    def mis(self, g: "Graph", node_value: np.ndarray, out: np.ndarray | None = None) -> np.ndarray:
         nv = np.ascontiguousarray(node_value, dtype=np.float32)
-        out = np.empty(g.V, dtype=np.int32)
+        out = _out(out, g.V, np.int32)
         self.check(self._lib.gdb_mis(self.h, g.h, _ptr(nv), _ptr(out)), "gdb_mis")
         return out
 
-    def color(self, g: "Graph", node_value: np.ndarray) -> np.ndarray:
+    def color(self, g: "Graph", node_value: np.ndarray, out: np.ndarray | None = None) -> np.ndarray:
         nv = np.ascontiguousarray(node_value, dtype=np.float32)
-        out = np.empty(g.V, dtype=np.int32)
+        out = _out(out, g.V, np.int32)
         self.check(self._lib.gdb_color(self.h, g.h, _ptr(nv), _ptr(out)), "gdb_color")
         return out
 
-    def bc(self, g: "Graph", sources) -> np.ndarray:
+    def bc(self, g: "Graph", sources, out: np.ndarray | None = None) -> np.ndarray:
         s = np.ascontiguousarray(sources, dtype=np.uint32)
-        out = np.empty(g.V, dtype=np.float32)
+        out = _out(out, g.V, np.float32)
         self.check(self._lib.gdb_bc(self.h, g.h, _ptr(s), len(s), _ptr(out)), "gdb_bc")
         return out
 
@@ -519,7 +534,10 @@ class Ctx:
 class Graph:
     """A gdb_graph: CSR copied from host arrays (or borrowed device arrays)."""
 
-    def __init__(self, ctx: Ctx, row_ptr, col, w=None, device: bool = False):
+    def __init__(self, ctx: Ctx, row_ptr, col, w=None, device: bool = False,
+                 symmetric: bool = False):
+        """symmetric: declare that arc u -> v of weight w exists exactly when
+        v -> u of weight w does (gdb_graph_set_symmetric)."""
         self.ctx = ctx
         h = _P()
         if device:
@@ -542,6 +560,12 @@ class Graph:
             ctx.check(ctx._lib.gdb_graph_create(ctx.h, self.V, self.E, _ptr(self._rp), _ptr(self._col),
                                                 _ptr(self._w), C.byref(h)), "gdb_graph_create")
         self.h = h
+        if symmetric:
+            self.set_symmetric(True)
+
+    def set_symmetric(self, symmetric: bool) -> None:
+        self.ctx.check(self.ctx._lib.gdb_graph_set_symmetric(self.h, int(bool(symmetric))),
+                       "gdb_graph_set_symmetric")
 
     @classmethod
     def batch(cls, ctx: Ctx, graphs, weights: bool = True) -> "Graph":

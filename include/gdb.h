@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GDB_ABI_VERSION 7
+#define GDB_ABI_VERSION 8
 
 /* Sentinels of the reference kernels. */
 #define GDB_LONESTAR_INF 1000000000u /* lonestar/apps/bfs/kernel/bfs_common.cl:35 */
@@ -199,6 +199,13 @@ int gdb_graph_create_device(gdb_ctx* ctx, uint32_t V, uint64_t E, const uint32_t
                             const uint32_t* d_col, const uint32_t* d_w, gdb_graph** out);
 /* Replace the weight array (host array copied). */
 int gdb_graph_set_weights(gdb_graph* g, const uint32_t* w);
+/* Declare (1) that the graph is symmetric with symmetric weights: arc
+   u -> v of weight w exists exactly when arc v -> u of weight w does (the
+   undirected inputs of the reference's applications).  Pulls over in-arcs
+   then read the out-arcs themselves instead of a transposed copy.  Results
+   on a graph that does not satisfy the declaration are undefined.
+   Default 0. */
+int gdb_graph_set_symmetric(gdb_graph* g, int symmetric);
 int gdb_graph_destroy(gdb_graph* g);
 int gdb_graph_info(gdb_graph* g, uint32_t* V, uint64_t* E, uint32_t* heavy_vertices);
 

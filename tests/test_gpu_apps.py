@@ -122,6 +122,25 @@ def test_sssp_split_skips_heavy_rework(split):
         assert st["edges_processed"] > 1.5 * reached, (st, reached)
 
 
+def test_sssp_split_on_a_declared_symmetric_graph():
+    """A graph declared symmetric (one weight per undirected edge) pulls
+    over its own heavy half instead of a transposed copy: the same
+    distances, and undeclaring rebuilds the partition with the transpose."""
+    g = gg.rmat(1 << 14, 16, seed=31)
+    w = gg.uniform_weights(g, 1, 255, seed=6)
+    gw = g.with_weights(w)
+    with gdb.Ctx(schedule=gdb.SCHED_ADAPTIVE) as c:
+        G = c.graph(g.row_ptr, g.col, w, symmetric=True)
+        for delta in (8, 32, 0):
+            c.set_options(sssp_delta=delta)
+            for src in (0, 17):
+                assert np.array_equal(c.sssp(G, src), oracle.sssp_worklist(gw, src)), (delta, src)
+        G.set_symmetric(False)
+        assert np.array_equal(c.sssp(G, 3), oracle.sssp_worklist(gw, 3))
+        G.set_symmetric(True)
+        assert np.array_equal(c.sssp(G, 3), oracle.sssp_worklist(gw, 3))
+
+
 def test_sssp_split_zero_and_infinite_weights():
     """Weight-0 arcs are light, arcs of weight >= 1e9 are never relaxed --
     in near and settle supersteps alike."""
