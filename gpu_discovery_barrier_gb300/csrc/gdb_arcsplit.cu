@@ -322,7 +322,7 @@ static int heavy_table_device(gdb_ctx* c, gdb_graph* x, uint32_t* t0, uint32_t* 
   GDB_CUDA(c, dev_alloc(c, (void**)&x->heavy_bits, nb));
   GDB_CUDA(c, cudaMemsetAsync(x->heavy_bits, 0, nb, st));
   GDB_CUDA(c, cudaMemsetAsync(hs, 0, 16, st));
-  const int grid = 4 * c->sm_count;
+  const int grid = 8 * c->sm_count;  // every 256-thread CTA resident: the loops are latency-bound
   k_heavy_marks<<<grid, 256, 0, st>>>(x->row, V, t0, t1, x->heavy_bits, hs + 2);
   GDB_CUDA(c, cudaGetLastError());
   GDB_CUDA(c, exclusive_scan(t0, V, t2, tmp, st));
@@ -398,7 +398,7 @@ int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
   if (e == cudaSuccess) e = dev_alloc(c, (void**)&H->row, vw * 4);
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split rows"));
   const GraphView G = g->view();
-  const int grid = 4 * c->sm_count;
+  const int grid = 8 * c->sm_count;  // every 256-thread CTA resident: the loops are latency-bound
   k_split_count<<<grid, 256, 0, st>>>(G, bound, t0, t1);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = exclusive_scan(t0, V, L->row, tmp, st);

@@ -13,10 +13,12 @@
 //
 // A batch owns its workspace, its discovery context and its barrier flags,
 // so its graph replays on the context's stream without touching the
-// context's own device state.  The captured launches use the combining XF
-// form, which needs no launch-unique epoch (arrival counts are zeroed when
-// a launch ends, the release generation only changes) and is therefore
-// valid on every replay.
+// context's own device state.  The captured launches use the counting XF
+// forms (flat or combining by participant count), which need no
+// launch-unique epoch -- combining arrival counts are zeroed when a launch
+// ends and its release generation only changes; the flat count carries
+// over from launch to launch through the context -- so they are valid on
+// every replay.
 #include <algorithm>
 #include <cstdio>
 #include <vector>
@@ -159,7 +161,7 @@ int gdb_batch_create(gdb_ctx* c, gdb_graph* g, uint32_t apps, const uint32_t* so
   proto.timeout_ns = c->opt.timeout_ns ? c->opt.timeout_ns : 2000000000ull;
   proto.close_wait_ns = 50000ull;
   proto.launch_id = 1;
-  proto.xf_release = gdb::kXfCombined;
+  proto.xf_release = gdb::kXfAuto;
 
   cudaStream_t cs = nullptr;
   e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);

@@ -182,7 +182,7 @@ void gdb_options_default(gdb_options* o) {
   o->lock = GDB_LOCK_FREE;
   o->barrier = GDB_BARRIER_XF;
   o->schedule = GDB_SCHED_PLAIN;
-  o->xf_release = gdb::kXfCombined;
+  o->xf_release = gdb::kXfAuto;
   o->timeout_ns = 2000000000ull;
 }
 
@@ -207,7 +207,7 @@ static int check_options(const gdb_options* o) {
   if (o->barrier < GDB_BARRIER_XF || o->barrier > GDB_BARRIER_RELAUNCH_GRAPH) return GDB_ERR_INVALID;
   if (o->schedule < GDB_SCHED_PLAIN || o->schedule > GDB_SCHED_LEARNED) return GDB_ERR_INVALID;
   if (o->max_ctas < 0 || o->oversubscribe < 0) return GDB_ERR_INVALID;
-  if (o->xf_release < 0 || o->xf_release > 2) return GDB_ERR_INVALID;
+  if (o->xf_release < 0 || o->xf_release > 4) return GDB_ERR_INVALID;
   if (o->sssp_split < -1 || o->sssp_split > 1) return GDB_ERR_INVALID;
   return GDB_OK;
 }

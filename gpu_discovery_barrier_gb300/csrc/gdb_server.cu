@@ -182,7 +182,7 @@ int launch(gdb_server* s, Slot& sl, Req& r) {
   proto.timeout_ns = c->opt.timeout_ns ? c->opt.timeout_ns : 2000000000ull;
   proto.close_wait_ns = 50000ull;
   proto.launch_id = 1;
-  proto.xf_release = gdb::kXfCombined;
+  proto.xf_release = gdb::kXfAuto;
   GDB_CUDA(c, cudaEventRecord(sl.ev0, sl.stream));
   int rc;
   if (r.app == GDB_APP_BFS)

@@ -89,8 +89,11 @@ typedef struct {
                           and clears it (the reference's), 1 = same arrival,
                           one broadcast epoch word as release, 2 = combining:
                           slaves add to 16 padded arrival counters that one
-                          master warp watches, one generation word as release
-                          (the default) */
+                          master warp watches, one generation word as release,
+                          3 = flat: every CTA adds to one counter and waits
+                          for the barrier's count (the master arrives last
+                          when a hook runs), 4 = flat up to 480 CTAs and
+                          combining above (the default) */
   uint64_t timeout_ns; /* limit for every device spin (0 = 2e9) */
   /* direction-optimising BFS thresholds (GDB_SCHED_ADAPTIVE): switch to
      pull when frontier arcs > unvisited arcs / pull_alpha, back to push

@@ -67,6 +67,13 @@ struct __align__(128) DeviceCtx {
     unsigned v;
     int _p[31];
   } gen[kReleaseCopies];
+  // flat form: every CTA adds 1 to one arrival counter and waits for the
+  // barrier's count; the counter is never reset within a context, and the
+  // master leaves its final value in flat_base for the next launch
+  struct {
+    unsigned v;
+    int _p[31];
+  } flat, flat_base;
 };
 
 // discovery_local_ctx (discovery.cl:67-71), in shared memory.
@@ -78,14 +85,28 @@ struct LocalCtx {
   unsigned long long timeout_ns;  // limit of every single wait
   int barriers;       // barriers passed (master: for the stall test hook)
   unsigned gen;       // combining form: release generation last seen
+  unsigned flat;      // flat form: the arrival count every CTA reached so far
 };
 
 // XF release forms.
 enum XfRelease {
   kXfPerSlave = 0,   // the master stores 0 into every slave's flag (discovery.cl:203-209)
   kXfBroadcast = 1,  // slaves store a launch-unique epoch; one broadcast release word
-  kXfCombined = 2    // slaves add to 16 padded arrival counters; one generation word
+  kXfCombined = 2,   // slaves add to 16 padded arrival counters; one generation word
+  kXfFlat = 3,       // every CTA adds to one counter and waits for the barrier's count
+  kXfAuto = 4        // flat up to kXfFlatMax participants, combining above
 };
+
+// Participants up to which the flat form beats the combining one (GB300,
+// CTAs of 512 threads: flat 1.36 / 1.54 / 1.80 / 2.30 us at 152 / 304 /
+// 456 / 608 CTAs, combining 2.02-2.05 us at every count): the one counter
+// every CTA polls is the flat form's limit.
+constexpr int kXfFlatMax = 480;
+
+// The form a launch's barriers take (uniform: P is the same in every CTA).
+__device__ __forceinline__ int xf_form(int release, int P) {
+  return release == kXfAuto ? (P <= kXfFlatMax ? kXfFlat : kXfCombined) : release;
+}
 
 // Launch parameters every discovery kernel receives.
 struct DiscoveryArgs {
@@ -301,6 +322,8 @@ __device__ inline bool discover(const DiscoveryArgs& a, LocalCtx* l) {
     if (!l->ok) l->participating = 0;
     // combining XF: no release can happen before this CTA's first arrival
     l->gen = (unsigned)ld_relaxed((int*)&c->gen[0].v);
+    // flat XF: the count the previous launch ended at
+    l->flat = (unsigned)ld_relaxed((int*)&c->flat_base.v);
   }
   __syncthreads();
   return l->participating != 0;
@@ -427,13 +450,69 @@ __device__ inline bool xf_barrier_combined(const DiscoveryArgs& a, LocalCtx* l, 
   return l->ok != 0;
 }
 
-// End of a launch that used the combining form: the master zeroes the
-// arrival counts (every arrival of its last barrier has been counted, and
-// no CTA arrives again).  After an error the host re-arms the context.
+// End of a launch.  Combining form: the master zeroes the arrival counts
+// (every arrival of its last barrier has been counted, and no CTA arrives
+// again).  Flat form: the master records the count reached, which the next
+// launch's CTAs start from (CTAs still polling this launch's last barrier
+// read the counter, not this word).  After an error the host re-arms the
+// context.
 __device__ inline void xf_finish(const DiscoveryArgs& a, const LocalCtx* l) {
-  if (a.xf_release == kXfCombined && l->participating && l->id == 0 && l->ok &&
-      threadIdx.x < kArriveGroups)
+  if (!l->participating || l->id != 0 || !l->ok) return;
+  const int form = xf_form(a.xf_release, l->P);
+  if (form == kXfCombined && threadIdx.x < kArriveGroups)
     st_relaxed(&a.ctx->arrive[threadIdx.x].v, 0);
+  if (form == kXfFlat && threadIdx.x == 0) st_relaxed((int*)&a.ctx->flat_base.v, (int)l->flat);
+}
+
+// Flat form: thread 0 of every CTA publishes its CTA's writes and adds 1
+// to the arrival counter, then polls it (acquire) until it holds this
+// barrier's count -- one round trip after the last arrival, as a grid-wide
+// counter barrier.  A hook (or the stall test hook) makes the master
+// arrive last: it waits for the other P - 1, runs the hook, then arrives.
+template <class Hook>
+__device__ inline bool xf_barrier_flat(const DiscoveryArgs& a, LocalCtx* l, Hook&& hook) {
+  DeviceCtx* c = a.ctx;
+  constexpr bool hooked = !std::is_same<typename std::decay<Hook>::type, NoHook>::value;
+  int* counter = (int*)&c->flat.v;
+  const unsigned target = l->flat + (unsigned)l->P;
+  int ok = 1;
+  __syncthreads();
+  if (l->id == 0 && (hooked || c->stall_after >= 0)) {
+    if (threadIdx.x == 0)
+      ok = spin_until(c, l->timeout_ns, 5, [&] {
+        return (int)((unsigned)ld_acquire(counter) - (target - 1u)) >= 0;
+      }, kBarrierSpin);
+    ok = __syncthreads_and(ok);
+    if (ok && c->stall_after >= 0 && l->barriers >= c->stall_after) {
+      // test hook: never arrive; every other CTA's wait must end with
+      // GDB_ERR_TIMEOUT at its deadline
+      if (threadIdx.x == 0) spin_until(c, l->timeout_ns, 6, [&] { return false; });
+      ok = 0;
+    }
+    if (ok) {
+      if constexpr (hooked) {
+        hook();
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        fence_acq_rel_gpu();  // release: the grid's writes before the last arrival
+        aref(*counter).fetch_add(1, cuda::memory_order_relaxed);
+      }
+    }
+  } else if (threadIdx.x == 0) {
+    fence_acq_rel_gpu();  // release: this CTA's writes before its arrival
+    aref(*counter).fetch_add(1, cuda::memory_order_relaxed);
+    ok = spin_until(c, l->timeout_ns, 7, [&] {
+      return (int)((unsigned)ld_acquire(counter) - target) >= 0;
+    }, kBarrierSpin);
+  }
+  if (threadIdx.x == 0) {
+    if (!ok) l->ok = 0;
+    l->barriers++;
+    l->flat = target;
+  }
+  __syncthreads();
+  return l->ok != 0;
 }
 
 // XF barrier (discovery.cl:177-238) over the participating CTAs.  Slave: one
@@ -458,7 +537,9 @@ __device__ inline void xf_finish(const DiscoveryArgs& a, const LocalCtx* l) {
 // (a superstep-boundary decision taken once, e.g. the schedule selector).
 template <class Hook>
 __device__ inline bool xf_barrier(const DiscoveryArgs& a, LocalCtx* l, Hook&& hook) {
-  if (a.xf_release == kXfCombined) return xf_barrier_combined(a, l, hook);
+  const int form = xf_form(a.xf_release, l->P);
+  if (form == kXfCombined) return xf_barrier_combined(a, l, hook);
+  if (form == kXfFlat) return xf_barrier_flat(a, l, hook);
   DeviceCtx* c = a.ctx;
   const int P = l->P;
   const bool bcast = a.xf_release == kXfBroadcast;

@@ -50,7 +50,7 @@ def test_skip_refuses_oversubscription():
         c.init_discovery_kernel_ctx()
 
 
-@pytest.mark.parametrize("xf_release", [0, 1, 2])
+@pytest.mark.parametrize("xf_release", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("kind", [gdb.BARRIER_XF, gdb.BARRIER_XF_FIXED, gdb.BARRIER_GRID_SYNC,
                                   gdb.BARRIER_RELAUNCH, gdb.BARRIER_RELAUNCH_GRAPH])
 def test_barrier_bench(kind, xf_release):
@@ -70,13 +70,13 @@ def test_release_modes_switch_in_one_context():
     with gdb.Ctx() as c:
         G = c.graph(g.row_ptr, g.col)
         want = oracle.bfs(g, 1)
-        for rel in (1, 0, 2, 1, 2, 0):
+        for rel in (1, 0, 2, 3, 1, 4, 3, 2, 0, 3, 4):
             c.set_options(xf_release=rel)
             assert np.array_equal(c.bfs(G, 1), want)
             c.barrier_bench(gdb.BARRIER_XF, 256, 50)
 
 
-@pytest.mark.parametrize("xf_release", [0, 1, 2])
+@pytest.mark.parametrize("xf_release", [0, 1, 2, 3, 4])
 def test_timeout_reports_and_recovers(xf_release):
     with gdb.Ctx(timeout_ns=50_000_000, xf_release=xf_release) as c:
         c.debug_stall_master(3)
@@ -88,12 +88,14 @@ def test_timeout_reports_and_recovers(xf_release):
         assert ns > 0 and groups >= 1
 
 
+@pytest.mark.parametrize("xf_release", [2, 3, 4])
 @pytest.mark.parametrize("ctas", [1, 2, 17, 152, 0])
-def test_combining_barrier_group_sizes(ctas):
-    """Arrival counts per group for every participant count, including a
-    lone master and counts that do not divide by the 16 groups; repeated
-    launches reuse the context (counts zeroed at the end of each)."""
-    with gdb.Ctx(xf_release=2, max_ctas=ctas) as c:
+def test_counting_barrier_group_sizes(ctas, xf_release):
+    """Arrival counts for every participant count, including a lone master
+    and counts that do not divide by the 16 groups; repeated launches reuse
+    the context (combining: counts zeroed at the end of each; flat: the
+    next launch starts from the count the last one reached)."""
+    with gdb.Ctx(xf_release=xf_release, max_ctas=ctas) as c:
         for _ in range(3):
             ns, groups = c.barrier_bench(gdb.BARRIER_XF, 256, 300)
             assert ns > 0 and groups >= 1
@@ -101,7 +103,7 @@ def test_combining_barrier_group_sizes(ctas):
                 assert groups <= ctas
 
 
-@pytest.mark.parametrize("xf_release", [0, 1, 2])
+@pytest.mark.parametrize("xf_release", [0, 1, 2, 3, 4])
 def test_all_apps_on_every_xf_form(xf_release):
     import numpy as np
 
@@ -124,5 +126,14 @@ def test_all_apps_on_every_xf_form(xf_release):
             got = c.bc(G, [0, 5]).astype(np.float64)
             want = oracle.bc_f64(g, [0, 5])
             assert np.allclose(got, want, rtol=1e-4, atol=1e-3)
+        # the learned schedule's decision runs as a hook inside every barrier
+        from gpu_discovery_barrier_gb300 import selector
+
+        p = selector.load()
+        if p is not None:
+            c.selector_set(p)
+            c.set_options(schedule=gdb.SCHED_LEARNED)
+            assert np.array_equal(c.bfs(G, 3), oracle.bfs(g, 3))
+            c.set_options(schedule=gdb.SCHED_PLAIN)
         G.set_weights(uw)
         assert c.mst(G)["weight64"] == oracle.mst(g.with_weights(uw))["weight64"]
