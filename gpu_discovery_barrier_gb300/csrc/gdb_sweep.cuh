@@ -180,11 +180,12 @@ __device__ __forceinline__ void group_arcs4(const GraphView& G, bool active, uin
   const uint32_t total = __shfl_sync(kFull, pre, 31);
   pre -= deg;
   for (uint32_t base = 0; base < total; base += 128) {
-    bool valid[4];
-    int owner[4];
-    uint32_t arc[4];
+    bool valid[4] = {false, false, false, false};
+    int owner[4] = {0, 0, 0, 0};
+    uint32_t arc[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int s4 = 0; s4 < 4; ++s4) {
+      if (base + 32 * s4 >= total) break;  // warp-uniform: no owner search for empty steps
       const uint32_t k = base + 32 * s4 + lane;
       int lo = 0;
 #pragma unroll

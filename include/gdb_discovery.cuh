@@ -97,11 +97,14 @@ enum XfRelease {
   kXfAuto = 4        // flat up to kXfFlatMax participants, combining above
 };
 
-// Participants up to which the flat form beats the combining one (GB300,
-// CTAs of 512 threads: flat 1.36 / 1.54 / 1.80 / 2.30 us at 152 / 304 /
-// 456 / 608 CTAs, combining 2.02-2.05 us at every count): the one counter
-// every CTA polls is the flat form's limit.
-constexpr int kXfFlatMax = 480;
+// Participants up to which the flat form is used.  In isolation (empty
+// supersteps, every CTA arriving at once) it beats the combining form up
+// to 456 CTAs of 512 threads (flat 1.36 / 1.54 / 1.80 / 2.30 us at 152 /
+// 304 / 456 / 608, combining 2.02-2.05 us at every count), but inside real
+// kernels, whose arrivals spread out, it also wins at 608 (4096^2 grid BFS,
+// 8,191 levels: 46.4 ms flat, 53.3 ms combining); the one counter every
+// CTA polls is its limit beyond a GPU's worth of CTAs.
+constexpr int kXfFlatMax = 1024;
 
 // The form a launch's barriers take (uniform: P is the same in every CTA).
 __device__ __forceinline__ int xf_form(int release, int P) {
