@@ -1,10 +1,11 @@
 """Autotuner for the batched form.
 
-Chooses the launch shape (threads per CTA, CTAs per SM) and the schedule
-(plain push, or direction-optimising with its two frontier thresholds) of a
-captured batch by timing replays, with a coordinate search: the shape
-first under the plain schedule, then the schedule and thresholds at the
-best shape.  Every candidate's results are compared with the first
+Chooses the launch shape (threads per CTA, CTAs per SM), the schedule
+(plain push, or direction-optimising with its two frontier thresholds) and
+whether SSSP splits its arcs into light and heavy classes, for a captured
+batch, by timing replays with a coordinate search: the shape first under
+the plain schedule, then the schedule and thresholds at the best shape,
+then the split.  Every candidate's results are compared with the first
 candidate's on the device: a configuration only changes speed, never an
 answer, and the tuner raises if one does.
 
@@ -56,10 +57,10 @@ def key(ctx: gdb.Ctx, g: gdb.Graph, nsrc: int, apps: int) -> str:
     return f"sm{info['sm_count']}_cc{info['cc_major']}{info['cc_minor']}|V{g.V}|E{g.E}|q{nsrc}|apps{apps}"
 
 
-def _options(shape, sched, sms: int) -> dict:
+def _options(shape, sched, sms: int, split: int = 0) -> dict:
     (block, per_sm), (schedule, alpha, beta) = shape, sched
     return {"block_size": block, "max_ctas": per_sm * sms, "schedule": schedule,
-            "pull_alpha": alpha, "push_beta": beta}
+            "pull_alpha": alpha, "push_beta": beta, "sssp_split": split}
 
 
 def _time(ctx: gdb.Ctx, g: gdb.Graph, sources, apps: int, opts: dict, reps: int, ref):
@@ -98,7 +99,7 @@ def tune_batch(ctx: gdb.Ctx, g: gdb.Graph, sources, apps: int = 3, reps: int = 3
         return dict(cache[k], cached=True)
     sms = ctx.device_info()["sm_count"]
     base = {f: getattr(ctx.opt, f) for f in ("block_size", "max_ctas", "schedule", "pull_alpha",
-                                             "push_beta")}
+                                             "push_beta", "sssp_split")}
     trials = []
     ref = None
     best = None
@@ -120,8 +121,17 @@ def tune_batch(ctx: gdb.Ctx, g: gdb.Graph, sources, apps: int = 3, reps: int = 3
     shape = best[0]
     best_opts, best_ms = _options(shape, SCHEDULES[0], sms), best[1]
     scheds = SCHEDULES[1:] + ([LEARNED] if getattr(ctx, "has_selector", False) else [])
+    best_sched = SCHEDULES[0]
     for sched in scheds:
         opts = _options(shape, sched, sms)
+        ms, _ = _time(ctx, g, sources, apps, opts, reps, ref)
+        trials.append({"options": opts, "ms": ms})
+        if ms < best_ms:
+            best_opts, best_ms, best_sched = opts, ms, sched
+    # the SSSP light/heavy arc split (automatic by default): a batch whose
+    # members include high-diameter graphs can do better without it
+    if apps & gdb.BATCH_SSSP and best_sched[0] != gdb.SCHED_PLAIN:
+        opts = _options(shape, best_sched, sms, split=-1)
         ms, _ = _time(ctx, g, sources, apps, opts, reps, ref)
         trials.append({"options": opts, "ms": ms})
         if ms < best_ms:
