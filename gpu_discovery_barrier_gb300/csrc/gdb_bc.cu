@@ -14,8 +14,8 @@
 // neither pass walks it:
 //  * forward, level L -> L+1, direction-optimising: push -- the level's
 //    vertices claim unvisited neighbours (CAS on d) and add their path
-//    count into every level-L+1 neighbour's FP64 accumulator (an L2
-//    atomic); pull -- every unvisited vertex sums the path counts of its
+//    count into every level-L+1 neighbour's (an FP32 L2 atomic, as the
+//    reference's float adds; FP64 ones cost 6 % more of the BC time); pull -- every unvisited vertex sums the path counts of its
 //    level-L neighbours and claims itself when the sum is positive.  A
 //    pull has no early exit (every parent counts), so it runs only when the
 //    unvisited vertices' arcs are fewer than the level's own;
@@ -45,11 +45,12 @@ using namespace gdb;
 
 // Per-vertex state.  st: x = level (int32, -1 = unreached), y = the
 // backward coefficient (1 + sigma) / rho (float bits), one 8-byte load for
-// the arcs of either pass; rho: FP64 accumulator of the path count (read
-// as float); sacc: FP64 accumulator of the backward sum of pushed levels.
+// the arcs of either pass; rho: the path count, float as the reference's
+// (pushes add into it with FP32 L2 atomics); sacc: FP64 accumulator of the
+// backward sum of pushed levels.
 struct BcWs {
   uint2* st;
-  double* rho;
+  float* rho;
   double* sacc;
   float* bc;
   uint32_t* order;               // light vertices, level segments
@@ -107,7 +108,7 @@ __device__ __forceinline__ int32_t level_of(const BcWs& ws, uint32_t v) {
   return (int32_t)__ldcg(reinterpret_cast<const uint32_t*>(&ws.st[v]));
 }
 __device__ __forceinline__ float rho_of(const BcWs& ws, uint32_t v) {
-  return (float)__ldcg(&ws.rho[v]);
+  return __ldcg(&ws.rho[v]);
 }
 __device__ __forceinline__ void set_coef(const BcWs& ws, uint32_t v, float c) {
   reinterpret_cast<uint32_t*>(&ws.st[v])[1] = __float_as_uint(c);
@@ -143,7 +144,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
   double* my = smem + (threadIdx.x & ~31u);
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.st[v] = kUnreached;
-    ws.rho[v] = 0.0;
+    ws.rho[v] = 0.f;
     ws.sacc[v] = -0.0;
     ws.bc[v] = 0.f;
   }
@@ -176,7 +177,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
     reset_slot(t);
     if (leader) {
       ws.st[src] = make_uint2(0u, 0u);
-      ws.rho[src] = 1.0;
+      ws.rho[src] = 1.f;
       ws.lev_arcs[0] = degree(src);
       ws.lev_arcs[1] = 0;
       const int nx = (t + 1) % 3;
@@ -252,7 +253,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
               add = claimed || old == Li + 1;
               if (claimed) next_arcs += r1 - r0;
             }
-            if (add) atomicAdd(&ws.rho[u], (double)rv);
+            if (add) atomicAdd(&ws.rho[u], rv);
           }
           frontier_push_staged(G, out, qs, claimed, u);
         };
@@ -294,7 +295,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
           const bool claimed = unv && sum > 0.0;
           if (claimed) {
             ws.st[u].x = (uint32_t)(Li + 1);  // only this lane writes u
-            ws.rho[u] = sum;
+            ws.rho[u] = (float)sum;
             next_arcs += degree(u);
           }
           frontier_push_staged(G, out, qs, claimed, u);
@@ -419,7 +420,7 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
     // -- reset the reached vertices for the next source
     auto reset = [&](uint32_t v) {
       ws.st[v] = kUnreached;
-      ws.rho[v] = 0.0;
+      ws.rho[v] = 0.f;
       ws.sacc[v] = -0.0;
     };
     for (uint32_t k = W.gthread; k < total_l; k += W.nthreads) reset(ws.order[k]);
@@ -476,7 +477,7 @@ static size_t bc_layout(const gdb_graph* g, char* base, float* d_bc, const uint3
   const size_t o_cnt = b.take(512);
   if (!base) return b.off;
   ws->st = (uint2*)(base + o_st);
-  ws->rho = (double*)(base + o_rho);
+  ws->rho = (float*)(base + o_rho);
   ws->sacc = (double*)(base + o_sacc);
   ws->bc = d_bc;
   ws->order = (uint32_t*)(base + o_ord);
