@@ -36,6 +36,7 @@
 // The pull forms read in-arcs forward and out-arcs backward; on the
 // symmetric graphs this library targets both are the CSR itself.
 #include <algorithm>
+#include <vector>
 
 #include "gdb_internal.h"
 
@@ -452,6 +453,19 @@ __global__ void __launch_bounds__(512, 3) k_bc_xf(DiscoveryArgs a, GraphView G, 
   bc_body(s, G, ws, sacc);
 }
 
+// out[v] = the lanes' partial sums, in lane order (deterministic).
+struct LaneParts {
+  const float* p[gdbi::kLanes];
+  int k;
+};
+__global__ void k_bc_sum(float* out, LaneParts parts, uint32_t V) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int j = 0; j < parts.k; ++j) s += parts.p[j][v];
+    out[v] = s;
+  }
+}
+
 }  // namespace
 
 using namespace gdbi;
@@ -524,10 +538,45 @@ int gdbi::bc_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_s
   return GDB_OK;
 }
 
+// Several sources: contiguous groups of them on concurrent lanes, each
+// lane summing into its own array, then one pass adds the lanes' arrays.
+static int bc_lanes(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc, float* d_bc) {
+  const uint32_t k = std::min<uint32_t>(kLanes, nsrc);
+  const size_t vb = ((size_t)g->V * 4 + 255) & ~size_t(255);
+  int occ = 0;
+  GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bc_xf, c->opt.block_size, 0));
+  std::vector<unsigned long long> st((size_t)k * 4);
+  int rc = run_on_lanes(c, k, vb + bc_workspace_bytes(g), occ * c->sm_count,
+                        [&](gdb_lane& L, uint32_t j) {
+                          const uint32_t b = j * nsrc / k, e = (j + 1) * nsrc / k;
+                          return bc_enqueue(c, g, L.ws + vb, d_sources + b, e - b, (float*)L.ws,
+                                            L.stream, lane_args(c, L));
+                        },
+                        st.data());
+  if (rc) return rc;
+  const float ms = (float)c->last.kernel_ms;
+  LaneParts parts;
+  parts.k = (int)k;
+  for (uint32_t j = 0; j < k; ++j) parts.p[j] = (const float*)c->lanes[j].ws;
+  GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  k_bc_sum<<<4 * c->sm_count, 256, 0, c->stream>>>(d_bc, parts, g->V);
+  GDB_CUDA(c, cudaGetLastError());
+  GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  float sum_ms = 0;
+  GDB_CUDA(c, cudaEventElapsedTime(&sum_ms, c->ev0, c->ev1));
+  c->last.kernel_ms = ms + sum_ms;
+  c->last.launches = k + 1;
+  c->last.work_units = 0;
+  for (uint32_t j = 0; j < k; ++j) c->last.work_units += st[4 * j + 2];
+  return GDB_OK;
+}
+
 static int bc_run(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc, float* d_bc) {
   if (!graph_ok(c, g) || !d_bc || (nsrc && !d_sources)) return GDB_ERR_INVALID;
   if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED)
     return set_error(c, GDB_ERR_UNSUPPORTED, "BC runs on the XF barrier");
+  if (nsrc >= 2) return bc_lanes(c, g, d_sources, nsrc, d_bc);
   char* base = (char*)workspace(c, bc_layout(g, nullptr, nullptr, nullptr, 0, nullptr, nullptr));
   if (!base) return GDB_ERR_OOM;
   BcWs ws;

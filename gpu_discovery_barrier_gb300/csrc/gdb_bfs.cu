@@ -703,6 +703,47 @@ int gdb_bfs_multi(gdb_ctx* c, gdb_graph* g, const uint32_t* sources, uint32_t ns
   return rc;
 }
 
+int gdb_bfs_sources_device(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t n,
+                           uint32_t* d_dist) {
+  if (!graph_ok(c, g) || !d_sources || !d_dist || n == 0) return GDB_ERR_INVALID;
+  const size_t V = g->V;
+  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED) {
+    // the other barrier kinds: one run after another
+    for (uint32_t i = 0; i < n; ++i) {
+      const int rc = bfs_run(c, g, 0, d_sources + i, 1, d_dist + i * V);
+      if (rc) return rc;
+    }
+    return GDB_OK;
+  }
+  int mode = 0;
+  int rc = bfs_mode(c, &mode);
+  if (rc) return rc;
+  const int fit = traversal_occupancy(c, c->opt.block_size) * c->sm_count;
+  return run_on_lanes(c, n, bfs_workspace_bytes(g), fit, [&](gdb_lane& L, uint32_t i) {
+    return bfs_enqueue(c, g, L.ws, d_sources + i, 1, d_dist + i * V, L.stream, lane_args(c, L));
+  });
+}
+
+int gdb_bfs_sources(gdb_ctx* c, gdb_graph* g, const uint32_t* sources, uint32_t n, uint32_t* dist) {
+  if (!graph_ok(c, g) || !dist || !sources || n == 0) return GDB_ERR_INVALID;
+  for (uint32_t i = 0; i < n; ++i)
+    if (sources[i] >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  const size_t nb = (size_t)g->V * 4 * n;
+  char* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, nb + (size_t)n * 4, c->stream));
+  cudaError_t e = cudaMemcpyAsync(d + nb, sources, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+  int rc = e == cudaSuccess ? gdb_bfs_sources_device(c, g, (const uint32_t*)(d + nb), n, (uint32_t*)d)
+                            : set_cuda_error(c, e, "sources upload");
+  if (rc == GDB_OK) {
+    e = cudaMemcpyAsync(dist, d, nb, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "dist read-back");
+  }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
 int gdb_bfs_trace(gdb_ctx* c, gdb_graph* g, uint32_t src, int mode, uint32_t* dist,
                   gdb_level_trace* trace, uint32_t cap, uint32_t* levels) {
   if (!graph_ok(c, g) || mode < 0 || mode > 2 || (cap && !trace)) return GDB_ERR_INVALID;

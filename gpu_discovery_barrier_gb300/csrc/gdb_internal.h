@@ -5,12 +5,24 @@
 
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
 #include "gdb.h"
 #include "gdb_discovery.cuh"
 #include "gdb_sweep.cuh"
+
+// A lane: a stream with its own discovery context, barrier flags and
+// workspace, so that several persistent launches of one context run at
+// once (independent sources of one graph).
+struct gdb_lane {
+  cudaStream_t stream = nullptr;
+  gdb::DeviceCtx* dctx = nullptr;
+  int* flags = nullptr;
+  char* ws = nullptr;
+  size_t ws_bytes = 0;
+};
 
 struct gdb_ctx {
   gdb_options opt{};
@@ -37,6 +49,10 @@ struct gdb_ctx {
   // for run-level decisions); empty = none loaded
   float* d_mlp = nullptr;
   std::vector<float> h_mlp;
+  // concurrent lanes (created on first use) and, while their launches are
+  // enqueued, the CTA cap each of them takes (0 = none)
+  std::vector<gdb_lane> lanes;
+  int cap_override = 0;
 };
 
 struct gdb_graph {
@@ -110,6 +126,24 @@ gdb::DiscoveryArgs discovery_args(gdb_ctx* c, const Shape& s);
 // discovery context and return the status.
 int finish_run(gdb_ctx* c);
 int reset_device_ctx(gdb_ctx* c, int skip);
+// Arm a discovery context and its flags on `st` (no synchronisation).
+cudaError_t arm_device_ctx(gdb_ctx* c, gdb::DeviceCtx* d, int* flags, cudaStream_t st, int skip);
+
+// Independent runs of one graph spread over concurrent lanes: `run(lane,
+// i)` enqueues run i (of n) on the lane's stream with the lane's discovery
+// context and workspace (ws_bytes each); every lane takes fit / lanes CTAs
+// of the kernel (fit: its co-resident CTAs on the whole GPU).  Waits for
+// every lane, checks each lane's device status, records the elapsed time
+// in c->last.kernel_ms.
+// stats_out (optional, n x 4): the first four statistics words of each
+// run's counter block (the last 512 bytes of its workspace).
+int run_on_lanes(gdb_ctx* c, uint32_t n, size_t ws_bytes, int fit,
+                 const std::function<int(gdb_lane&, uint32_t)>& run,
+                 unsigned long long* stats_out = nullptr);
+// Discovery arguments of a launch on lane L.
+gdb::DiscoveryArgs lane_args(gdb_ctx* c, const gdb_lane& L);
+void lanes_destroy(gdb_ctx* c);
+constexpr int kLanes = 4;
 int read_participating(gdb_ctx* c, int* n);
 
 // Light (weight < bound) and heavy (bound <= weight < infinity) halves of

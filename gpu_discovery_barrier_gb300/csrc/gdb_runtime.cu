@@ -63,6 +63,7 @@ int persistent_shape(gdb_ctx* c, const void* kernel, int block, size_t smem, Sha
   s->fit = occ * c->sm_count;
   int grid = s->fit;
   if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
+  if (c->cap_override > 0) grid = std::min(grid, c->cap_override);  // a lane's share
   if (allow_oversubscribe && c->opt.oversubscribe > 0) grid = c->opt.oversubscribe;
   // the XF master retires at most 32 peers per thread; flags bound P
   const int cap = std::min(c->flag_cap, 32 * block + 1);
@@ -85,16 +86,143 @@ gdb::DiscoveryArgs discovery_args(gdb_ctx* c, const Shape& s) {
   return a;
 }
 
-int reset_device_ctx(gdb_ctx* c, int skip) {
+cudaError_t arm_device_ctx(gdb_ctx* c, gdb::DeviceCtx* d, int* flags, cudaStream_t st, int skip) {
   gdb::DeviceCtx h;
   std::memset(&h, 0, sizeof(h));
   h.poll_open = 1;
   h.skip = skip;
   h.stall_after = c->stall_after;
-  GDB_CUDA(c, cudaMemcpyAsync(c->dctx, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
-  GDB_CUDA(c, cudaMemsetAsync(c->flags, 0, (size_t)c->flag_cap * gdb::kLineInts * sizeof(int),
-                              c->stream));
+  // pageable source: the copy has taken h before the call returns
+  cudaError_t e = cudaMemcpyAsync(d, &h, sizeof(h), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(flags, 0, (size_t)c->flag_cap * gdb::kLineInts * sizeof(int), st);
+  return e;
+}
+
+int reset_device_ctx(gdb_ctx* c, int skip) {
+  GDB_CUDA(c, arm_device_ctx(c, c->dctx, c->flags, c->stream, skip));
   GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GDB_OK;
+}
+
+void lanes_destroy(gdb_ctx* c) {
+  for (gdb_lane& L : c->lanes) {
+    if (L.stream) cudaStreamSynchronize(L.stream);
+    cudaFree(L.ws);
+    cudaFree(L.dctx);
+    cudaFree(L.flags);
+    if (L.stream) cudaStreamDestroy(L.stream);
+  }
+  c->lanes.clear();
+  cudaGetLastError();
+}
+
+gdb::DiscoveryArgs lane_args(gdb_ctx* c, const gdb_lane& L) {
+  gdb::DiscoveryArgs a;
+  a.ctx = L.dctx;
+  a.flags = L.flags;
+  a.flag_capacity = c->flag_cap;
+  a.lock_kind = c->opt.lock;
+  a.expected = 0;
+  a.timeout_ns = c->opt.timeout_ns ? c->opt.timeout_ns : 2000000000ull;
+  a.close_wait_ns = 50000ull;
+  a.launch_id = ++c->launches;
+  a.xf_release = c->opt.xf_release;
+  return a;
+}
+
+int run_on_lanes(gdb_ctx* c, uint32_t n, size_t ws_bytes, int fit,
+                 const std::function<int(gdb_lane&, uint32_t)>& run,
+                 unsigned long long* stats_out) {
+  const int k = (int)std::min<uint32_t>(kLanes, std::max<uint32_t>(n, 1u));
+  while ((int)c->lanes.size() < k) {
+    gdb_lane L;
+    cudaError_t e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&L.dctx, sizeof(gdb::DeviceCtx));
+    if (e == cudaSuccess) e = cudaMalloc(&L.flags, (size_t)c->flag_cap * gdb::kLineInts * sizeof(int));
+    if (e == cudaSuccess) e = arm_device_ctx(c, L.dctx, L.flags, L.stream, 0);
+    if (e != cudaSuccess) {
+      c->lanes.push_back(L);  // freed with the others
+      lanes_destroy(c);
+      return set_cuda_error(c, e, "lane creation");
+    }
+    c->lanes.push_back(L);
+  }
+  for (int i = 0; i < k; ++i) {
+    gdb_lane& L = c->lanes[i];
+    if (L.ws_bytes < ws_bytes) {
+      GDB_CUDA(c, cudaStreamSynchronize(L.stream));
+      cudaFree(L.ws);
+      L.ws = nullptr;
+      L.ws_bytes = 0;
+      GDB_CUDA(c, cudaMalloc(&L.ws, ws_bytes));
+      L.ws_bytes = ws_bytes;
+    }
+  }
+  // per run: its 32 statistics bytes and overflow word, read back after
+  unsigned long long* stage = (unsigned long long*)pinned(c, 4096 + (size_t)n * 64);
+  if (!stage) return GDB_ERR_OOM;
+  stage += 512;  // past the staging the single runs use
+  // the lanes start after the work already queued on the context's stream
+  GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  for (int i = 0; i < k; ++i) GDB_CUDA(c, cudaStreamWaitEvent(c->lanes[i].stream, c->ev0, 0));
+  c->cap_override = std::max(1, fit / k);
+  int rc = GDB_OK;
+  for (uint32_t i = 0; i < n && rc == GDB_OK; ++i) {
+    gdb_lane& L = c->lanes[i % k];
+    rc = run(L, i);
+    const char* cnt = L.ws + ws_bytes - 512;
+    if (rc == GDB_OK) {
+      cudaError_t e = cudaMemcpyAsync(stage + 8 * i, cnt, 32, cudaMemcpyDeviceToHost, L.stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(stage + 8 * i + 4, cnt + 160, 4, cudaMemcpyDeviceToHost, L.stream);
+      if (e != cudaSuccess) rc = set_cuda_error(c, e, "lane statistics");
+    }
+  }
+  c->cap_override = 0;
+  // join: the context's stream waits for every lane
+  for (int i = 0; i < k; ++i) {
+    gdb_lane& L = c->lanes[i];
+    cudaEvent_t done;
+    GDB_CUDA(c, cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    cudaEventRecord(done, L.stream);
+    cudaStreamWaitEvent(c->stream, done, 0);
+    cudaEventDestroy(done);
+  }
+  GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  const cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return set_cuda_error(c, e, "lane execution");
+  if (rc) return rc;
+  // device status of every lane; a lane that saw an error is re-armed
+  int* st = (int*)pinned(c, 4096 + (size_t)n * 64);
+  for (int i = 0; i < k; ++i) {
+    gdb_lane& L = c->lanes[i];
+    GDB_CUDA(c, cudaMemcpy(st, &L.dctx->status, 4 * sizeof(int), cudaMemcpyDeviceToHost));
+    if (st[0] != 0) {
+      const int status = st[0], where = st[2];
+      GDB_CUDA(c, arm_device_ctx(c, L.dctx, L.flags, L.stream, 0));
+      GDB_CUDA(c, cudaStreamSynchronize(L.stream));
+      char buf[160];
+      snprintf(buf, sizeof buf, "lane %d: device reported %s at site %d", i, gdb_status_string(status),
+               where);
+      return set_error(c, status, buf);
+    }
+  }
+  stage = (unsigned long long*)pinned(c, 4096 + (size_t)n * 64) + 512;
+  c->last = gdb_run_stats{};
+  for (uint32_t i = 0; i < n; ++i) {
+    if (*(int*)(stage + 8 * i + 4)) return set_error(c, GDB_ERR_CAPACITY, "queue overflow in a lane");
+    c->last.edges_processed += stage[8 * i];
+    c->last.supersteps += (uint32_t)stage[8 * i + 1];
+    if (stats_out)
+      for (int j = 0; j < 4; ++j) stats_out[4 * i + j] = stage[8 * i + j];
+  }
+  float ms = 0;
+  GDB_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->last.kernel_ms = ms;
+  c->last.launches = n;
+  c->last.launched = (uint32_t)std::max(1, fit / k);
+  c->last.participating = c->last.launched;
   return GDB_OK;
 }
 
@@ -267,6 +395,7 @@ int gdb_ctx_create(const gdb_options* opt, gdb_ctx** out) {
 int gdb_ctx_destroy(gdb_ctx* c) {
   if (!c) return GDB_ERR_INVALID;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  lanes_destroy(c);
   if (c->ws) cudaFree(c->ws);
   if (c->pinned) cudaFreeHost(c->pinned);
   if (c->dctx) cudaFree(c->dctx);

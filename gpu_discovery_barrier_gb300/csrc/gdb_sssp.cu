@@ -1121,6 +1121,53 @@ int gdb_sssp_multi(gdb_ctx* c, gdb_graph* g, const uint32_t* sources, uint32_t n
   return rc;
 }
 
+int gdb_sssp_sources_device(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t n,
+                            uint32_t* d_dist) {
+  if (!graph_ok(c, g) || !d_sources || !d_dist || n == 0) return GDB_ERR_INVALID;
+  if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
+  const size_t V = g->V;
+  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED) {
+    for (uint32_t i = 0; i < n; ++i) {
+      const int rc = sssp_run(c, g, 0, d_sources + i, 1, d_dist + i * V);
+      if (rc) return rc;
+    }
+    return GDB_OK;
+  }
+  uint32_t delta = 0, light = kInf;
+  bool relaunch = false;
+  int rc = sssp_plan(c, g, 1, false, &delta, &relaunch, &light);
+  if (rc) return rc;
+  int occ = 0;
+  GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sssp_xf, c->opt.block_size, 0));
+  rc = run_on_lanes(c, n, sssp_workspace_bytes(g), occ * c->sm_count, [&](gdb_lane& L, uint32_t i) {
+    return sssp_enqueue(c, g, L.ws, d_sources + i, 1, d_dist + i * V, L.stream, lane_args(c, L),
+                        delta, light);
+  });
+  c->last.sssp_delta = delta;
+  c->last.sssp_light = delta && light < kInf ? light : 0u;
+  return rc;
+}
+
+int gdb_sssp_sources(gdb_ctx* c, gdb_graph* g, const uint32_t* sources, uint32_t n, uint32_t* dist) {
+  if (!graph_ok(c, g) || !dist || !sources || n == 0) return GDB_ERR_INVALID;
+  for (uint32_t i = 0; i < n; ++i)
+    if (sources[i] >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  const size_t nb = (size_t)g->V * 4 * n;
+  char* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, nb + (size_t)n * 4, c->stream));
+  cudaError_t e = cudaMemcpyAsync(d + nb, sources, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+  int rc = e == cudaSuccess ? gdb_sssp_sources_device(c, g, (const uint32_t*)(d + nb), n, (uint32_t*)d)
+                            : set_cuda_error(c, e, "sources upload");
+  if (rc == GDB_OK) {
+    e = cudaMemcpyAsync(dist, d, nb, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "dist read-back");
+  }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
 int gdb_sssp(gdb_ctx* c, gdb_graph* g, uint32_t src, uint32_t* dist) {
   if (!graph_ok(c, g) || !dist) return GDB_ERR_INVALID;
   uint32_t* d = nullptr;

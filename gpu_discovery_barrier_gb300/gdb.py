@@ -23,7 +23,7 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libgdb.so"
 
-ABI_VERSION = 8  # GDB_ABI_VERSION of include/gdb.h
+ABI_VERSION = 9  # GDB_ABI_VERSION of include/gdb.h
 LONESTAR_INF = 1_000_000_000
 PANNOTIA_BIG = 99_999_999
 
@@ -154,6 +154,10 @@ SIGNATURES = [
     ("gdb_mlp_train", C.c_int, [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_float, C.c_float,
                                 C.POINTER(C.c_double)]),
     ("gdb_bfs_multi", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_bfs_sources", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_bfs_sources_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_sssp_sources", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    ("gdb_sssp_sources_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
     ("gdb_bfs_multi_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
     ("gdb_sssp_multi", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
     ("gdb_sssp_multi_device", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
@@ -521,6 +525,29 @@ class Ctx:
 
     def mst_device(self, g: "Graph", d_result: int, d_flags: int | None = None) -> None:
         self.check(self._lib.gdb_mst_device(self.h, g.h, d_result, d_flags), "gdb_mst_device")
+
+    def bfs_sources(self, g: "Graph", sources, out: np.ndarray | None = None) -> np.ndarray:
+        """Independent BFS from each source: row i = levels from sources[i]."""
+        s = np.ascontiguousarray(sources, dtype=np.uint32)
+        out = _out(None if out is None else out.reshape(-1), len(s) * g.V, np.uint32)
+        self.check(self._lib.gdb_bfs_sources(self.h, g.h, _ptr(s), len(s), _ptr(out)), "gdb_bfs_sources")
+        return out.reshape(len(s), g.V)
+
+    def sssp_sources(self, g: "Graph", sources, out: np.ndarray | None = None) -> np.ndarray:
+        """Independent SSSP from each source: row i = distances from sources[i]."""
+        s = np.ascontiguousarray(sources, dtype=np.uint32)
+        out = _out(None if out is None else out.reshape(-1), len(s) * g.V, np.uint32)
+        self.check(self._lib.gdb_sssp_sources(self.h, g.h, _ptr(s), len(s), _ptr(out)),
+                   "gdb_sssp_sources")
+        return out.reshape(len(s), g.V)
+
+    def bfs_sources_device(self, g: "Graph", d_sources: int, n: int, d_dist: int) -> None:
+        self.check(self._lib.gdb_bfs_sources_device(self.h, g.h, d_sources, n, d_dist),
+                   "gdb_bfs_sources_device")
+
+    def sssp_sources_device(self, g: "Graph", d_sources: int, n: int, d_dist: int) -> None:
+        self.check(self._lib.gdb_sssp_sources_device(self.h, g.h, d_sources, n, d_dist),
+                   "gdb_sssp_sources_device")
 
     def bfs_multi_device(self, g: "Graph", d_sources: int, nsrc: int, d_dist: int) -> None:
         self.check(self._lib.gdb_bfs_multi_device(self.h, g.h, d_sources, nsrc, d_dist),

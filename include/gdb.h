@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GDB_ABI_VERSION 8
+#define GDB_ABI_VERSION 9
 
 /* Sentinels of the reference kernels. */
 #define GDB_LONESTAR_INF 1000000000u /* lonestar/apps/bfs/kernel/bfs_common.cl:35 */
@@ -348,6 +348,22 @@ int gdb_bfs_multi_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, 
 int gdb_sssp_multi(gdb_ctx* ctx, gdb_graph* g, const uint32_t* sources, uint32_t nsrc, uint32_t* dist);
 int gdb_sssp_multi_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc,
                           uint32_t* d_dist);
+
+/* ------------------------------------------- independent many-source runs */
+/* The single-source BFS / SSSP of each of n sources, source i's answer in
+ * dist[i * V .. i * V + V): what n calls of gdb_bfs / gdb_sssp return (the
+ * reference runs one source per call).  Under the XF barriers the runs are
+ * spread over concurrent lanes -- streams with their own discovery
+ * contexts, each launch with a share of the GPU's CTAs -- so that the
+ * latency-bound supersteps of several sources overlap; other barrier kinds
+ * run them one after another.  The host forms check the sources; the
+ * device forms ignore sources >= V (their rows stay unreached). */
+int gdb_bfs_sources(gdb_ctx* ctx, gdb_graph* g, const uint32_t* sources, uint32_t n, uint32_t* dist);
+int gdb_bfs_sources_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_t n,
+                           uint32_t* d_dist);
+int gdb_sssp_sources(gdb_ctx* ctx, gdb_graph* g, const uint32_t* sources, uint32_t n, uint32_t* dist);
+int gdb_sssp_sources_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_t n,
+                            uint32_t* d_dist);
 
 /* ---------------------------------------------------------- batched form */
 /* No reference counterpart.  n host CSR graphs packed into one disjoint

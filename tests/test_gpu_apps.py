@@ -233,6 +233,46 @@ def test_bc(ctx, name, g):
     assert not np.any(np.isfinite(got[~fin])), name
 
 
+@pytest.mark.parametrize("n", [1, 3, 7])
+@pytest.mark.parametrize("schedule", [gdb.SCHED_PLAIN, gdb.SCHED_ADAPTIVE])
+def test_many_sources_on_lanes(n, schedule):
+    """Independent runs of several sources on concurrent lanes: row i is the
+    single-source answer of sources[i]."""
+    g = gg.rmat(1 << 13, 16, seed=41)
+    w = gg.uniform_weights(g, 1, 255, seed=7)
+    gw = g.with_weights(w)
+    srcs = [int(x) for x in gg.sources(g, n, seed=5)]
+    with gdb.Ctx(schedule=schedule) as c:
+        G = c.graph(g.row_ptr, g.col, w, symmetric=True)
+        for _ in range(2):  # lanes are reused
+            lv = c.bfs_sources(G, srcs)
+            ds = c.sssp_sources(G, srcs)
+            for i, s in enumerate(srcs):
+                assert np.array_equal(lv[i], oracle.bfs(g, s)), (i, s)
+                assert np.array_equal(ds[i], oracle.sssp_worklist(gw, s)), (i, s)
+        assert c.last_stats()["launches"] == n
+
+
+def test_many_sources_device_form_ignores_out_of_range():
+    import torch
+
+    g = gg.grid(40, 30)
+    w = gg.uniform_weights(g, 1, 9, seed=2)
+    with gdb.Ctx() as c:
+        G = c.graph(g.row_ptr, g.col, w)
+        src = torch.tensor([0, g.V + 5, 17], dtype=torch.int32, device="cuda")
+        out = torch.zeros((3, g.V), dtype=torch.int32, device="cuda")
+        c.sssp_sources_device(G, src.data_ptr(), 3, out.data_ptr())
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().view(np.uint32)
+        gw = g.with_weights(w)
+        assert np.array_equal(got[0], oracle.sssp_worklist(gw, 0))
+        assert np.all(got[1] == gdb.LONESTAR_INF)
+        assert np.array_equal(got[2], oracle.sssp_worklist(gw, 17))
+        with pytest.raises(gdb.GdbError):
+            c.sssp_sources(G, [0, g.V])
+
+
 @pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
 def test_mst(ctx, name, g):
     uw = gg.unique_weights(g, seed=9)
