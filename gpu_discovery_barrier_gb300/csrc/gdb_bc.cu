@@ -540,8 +540,13 @@ int gdbi::bc_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_s
 
 // Several sources: contiguous groups of them on concurrent lanes, each
 // lane summing into its own array, then one pass adds the lanes' arrays.
+// Two lanes: BC's launches are longer and fuller than BFS's and SSSP's
+// (R-MAT-22, 16 sources: 20.9 ms on one launch, 17.7 ms on two lanes, 19.9
+// on four, 25.7 on six).
+constexpr uint32_t kBcLanes = 2;
+
 static int bc_lanes(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc, float* d_bc) {
-  const uint32_t k = std::min<uint32_t>(kLanes, nsrc);
+  const uint32_t k = std::min<uint32_t>(kBcLanes, nsrc);
   const size_t vb = ((size_t)g->V * 4 + 255) & ~size_t(255);
   int occ = 0;
   GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bc_xf, c->opt.block_size, 0));
