@@ -203,8 +203,8 @@ struct ColorWs {
   uint32_t* cnt;       // neighbours still to be coloured before this vertex
   uint8_t* waitarc;    // per arc v -> u: kWaits | kHeavyT (set by the count pass)
   const float* prio;
-  uint32_t* q[2];
-  uint4* hc[2];                // heavy chunk entries
+  uint2* q[2];                 // light vertices as their arc ranges {begin, end}
+  uint4* hc[2];                // heavy chunks as {vertex, first arc, end arc, chunk}
   uint32_t* qcount;            // [3]
   unsigned long long* hcount;  // [3]
   uint32_t* cursor;            // [3]
@@ -217,13 +217,99 @@ struct ColorWs {
 // u waits for v when u looks at its neighbours (degree != 1) and v's
 // priority is not below u's (the count pass stores it per arc v -> u).
 
+// The colouring's frontier entries carry arc ranges, so a round's consumer
+// needs no row load: the producer loads the rows of every vertex it counts
+// down, in flight with the count-down itself.  Light entries are staged per
+// warp in shared memory and leave 32 at a time; a heavy vertex's chunks are
+// reserved with one packed atomic per warp step.
+struct RangeStage {
+  uint2* buf;    // this warp's 64 slots
+  uint2* q;
+  uint32_t* count;
+  uint32_t cap;
+  int* overflow;
+  uint32_t n = 0;
+  __device__ __forceinline__ void out(uint2 x, uint32_t m) {
+    const int lane = lane_id();
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(count, m);
+    base = __shfl_sync(kFull, base, 0);
+    if ((uint32_t)lane < m) {
+      if (base + lane < cap) q[base + lane] = x;
+      else atomicExch(overflow, 1);
+    }
+  }
+  __device__ __forceinline__ void add(bool want, uint2 x) {
+    const unsigned m = __ballot_sync(kFull, want);
+    if (!m) return;
+    const int lane = lane_id();
+    if (want) buf[n + __popc(m & lanemask_lt())] = x;
+    n += __popc(m);
+    if (n >= 32) {
+      __syncwarp();
+      const uint2 y = buf[lane];
+      const uint32_t r = n - 32;
+      const uint2 z = (uint32_t)lane < r ? buf[32 + lane] : make_uint2(0u, 0u);
+      __syncwarp();
+      if ((uint32_t)lane < r) buf[lane] = z;
+      __syncwarp();
+      out(y, 32);
+      n = r;
+    }
+  }
+  __device__ __forceinline__ void flush() {
+    __syncwarp();
+    if (n) out((uint32_t)lane_id() < n ? buf[lane_id()] : make_uint2(0u, 0u), n);
+    n = 0;
+  }
+};
+
+// Push the lanes' ready vertices u with arc ranges [rb, re): light ones
+// (degree <= kHeavyDeg) staged, heavy ones as chunk entries.
+__device__ __forceinline__ void push_ranges(const ColorWs& ws, RangeStage& st, uint4* hc,
+                                            unsigned long long* hcount, bool ready, bool heavy,
+                                            uint32_t u, uint32_t rb, uint32_t re) {
+  st.add(ready && !heavy && re > rb, make_uint2(rb, re));
+  const bool hv = ready && heavy;
+  const unsigned hm = __ballot_sync(kFull, hv);
+  if (!hm) return;
+  const int lane = lane_id();
+  const uint32_t nch = hv ? chunks_of(re - rb) : 0u;
+  uint32_t inc = nch;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += t;
+  }
+  const uint32_t total = __shfl_sync(kFull, inc, 31);
+  const int leader = __ffs(hm) - 1;
+  unsigned long long old = 0;
+  if (lane == leader) old = atomicAdd(hcount, ((unsigned long long)__popc(hm) << 32) | total);
+  old = __shfl_sync(kFull, old, leader);
+  const uint32_t cbase = (uint32_t)old;
+  if (cbase + total > ws.hcap) {
+    if (lane == leader) atomicExch(ws.overflow, 1);
+    return;
+  }
+  const uint32_t first = cbase + inc - nch;
+  for (unsigned m = hm; m; m &= m - 1) {
+    const int l = __ffs(m) - 1;
+    const uint32_t v = __shfl_sync(kFull, u, l), n = __shfl_sync(kFull, nch, l);
+    const uint32_t f = __shfl_sync(kFull, first, l), b0 = __shfl_sync(kFull, rb, l),
+                   e0 = __shfl_sync(kFull, re, l);
+    for (uint32_t j = lane; j < n; j += 32)
+      hc[f + j] = make_uint4(v, b0 + j * kChunk, min(e0, b0 + (j + 1) * kChunk), j);
+  }
+}
+
 template <class Sync>
 __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const ColorWs& ws, uint32_t* smem) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
   const int lane = lane_id();
   uint32_t* my = smem + (threadIdx.x & ~31u);
-  unsigned long long arcs = 0;
+  __shared__ uint2 rstage[kMaxGraphWarps][64];
+  unsigned long long arcs = 0, coloured = 0;
   // -- superstep 0: color = -1; count the neighbours each vertex waits for
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.color[v] = -1;
@@ -282,14 +368,18 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   if (!s.sync()) return;
   // -- superstep 1: vertices that wait for nobody take colour 1
   {
-    Frontier out{pick(ws.q, 1), pick(ws.hc, 1), &ws.qcount[1], &ws.hcount[1], ws.qcap, ws.hcap,
-                 ws.overflow};
-    WarpStage qs = frontier_stage(out, 0);
+    RangeStage qs{rstage[threadIdx.x >> 5], pick(ws.q, 1), &ws.qcount[1], ws.qcap, ws.overflow};
     for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
       const uint32_t v = g * 32 + lane;
       const bool first = v < G.V && ld_cg(&ws.cnt[v]) == 0;
-      if (first) ws.color[v] = 1;
-      frontier_push_staged(G, out, qs, first, v);
+      uint32_t rb = 0, re = 0;
+      if (first) {
+        ws.color[v] = 1;
+        ++coloured;
+        rb = __ldg(&G.row[v]);
+        re = __ldg(&G.row[v + 1]);
+      }
+      push_ranges(ws, qs, pick(ws.hc, 1), &ws.hcount[1], first, re - rb > kHeavyDeg, v, rb, re);
     }
     qs.flush();
     if (leader) ws.cursor[2] = ws.hcursor[2] = 0;
@@ -298,7 +388,6 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   // -- rounds: the vertices coloured in round r (queue slot r % 3) count
   // down the neighbours waiting for them
   uint32_t r = 1;
-  unsigned long long coloured = 0;
   for (;; ++r) {
     const int cur = r % 3, nxt = (r + 1) % 3, old = (r + 2) % 3;
     const unsigned long long* sc = cta_words<2>([&](unsigned long long* w) {
@@ -314,10 +403,10 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
       ws.cursor[old] = 0;
       ws.hcursor[old] = 0;
     }
-    coloured += (leader ? n + (uint32_t)(hp >> 32) : 0);
-    Frontier out{pick(ws.q, r + 1), pick(ws.hc, r + 1), &ws.qcount[nxt], &ws.hcount[nxt],
-                 ws.qcap, ws.hcap, ws.overflow};
-    WarpStage qs = frontier_stage(out, 0);
+    RangeStage qs{rstage[threadIdx.x >> 5], pick(ws.q, r + 1), &ws.qcount[nxt], ws.qcap,
+                  ws.overflow};
+    uint4* hc_out = pick(ws.hc, r + 1);
+    unsigned long long* hcount_out = &ws.hcount[nxt];
     const int32_t next_color = (int32_t)r + 1;
     // up to four 32-arc steps at once: their column, wait-byte loads and
     // count-downs are all in flight together (a round is a chain of
@@ -331,34 +420,40 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
         wa[s4] = valid[s4] ? ws.waitarc[arc[s4]] : (uint8_t)0;
         arcs += valid[s4];
       }
-      uint32_t old4[4];
+      uint32_t old4[4], rb[4], re[4];
 #pragma unroll
-      for (int s4 = 0; s4 < 4; ++s4) old4[s4] = (wa[s4] & kWaits) ? atomicSub(&ws.cnt[u[s4]], 1u) : 0u;
+      for (int s4 = 0; s4 < 4; ++s4) {
+        const bool w = wa[s4] & kWaits;
+        old4[s4] = w ? atomicSub(&ws.cnt[u[s4]], 1u) : 0u;
+        // the rows of a vertex this count-down may complete, loaded with it
+        rb[s4] = w ? __ldg(&G.row[u[s4]]) : 0u;
+        re[s4] = w ? __ldg(&G.row[u[s4] + 1]) : 0u;
+      }
 #pragma unroll
       for (int s4 = 0; s4 < 4; ++s4) {
         const bool ready = (wa[s4] & kWaits) && old4[s4] == 1u;
-        if (ready) ws.color[u[s4]] = next_color;
-        const bool heavy = ready && (wa[s4] & kHeavyT);
-        qs.add(ready && !heavy, u[s4]);
-        frontier_push_heavy(G, out, heavy, u[s4]);
+        if (ready) {
+          ws.color[u[s4]] = next_color;
+          ++coloured;
+        }
+        push_ranges(ws, qs, hc_out, hcount_out, ready, wa[s4] & kHeavyT, u[s4], rb[s4], re[s4]);
       }
     };
-    const uint32_t* q = pick(ws.q, r);
+    const uint2* q = pick(ws.q, r);
     const uint32_t k = group_width(n, W.nwarps);
     WorkTaker lt((n + k - 1) / k, W, &ws.cursor[cur]);
     for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
       const uint32_t i = g * k + lane;
       const bool act = (uint32_t)lane < k && i < n;
-      const uint32_t v = act ? ld_cg(&q[i]) : 0u;
-      group_arcs4(G, act, v, relax4);
+      const uint2 rg = act ? __ldcg(&q[i]) : make_uint2(0u, 0u);
+      range_arcs4(rg.x, rg.y - rg.x, relax4);
     }
     const uint32_t nch = (uint32_t)hp;
     const uint4* hc = pick(ws.hc, r);
     WorkTaker ht(nch, W, &ws.hcursor[cur]);
     for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
       const uint4 ent = ld_cg(&hc[c]);
-      uint32_t b, en;
-      chunk_range(G, ent, b, en);
+      const uint32_t b = ent.y, en = ent.z;  // the entry's arc range
       // a chunk holds kChunk = 128 arcs: one four-step batch
       static_assert(kChunk == 4 * 32, "a colour chunk is one batch of four steps");
       bool valid[4];
@@ -374,12 +469,13 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
     if (!s.sync()) return;
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
-  if (lane == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
-  if (leader) {
-    ws.stats[1] = r - 1;
-    ws.stats[2] = coloured;
+  for (int o = 16; o > 0; o >>= 1) {
+    arcs += __shfl_xor_sync(kFull, arcs, o);
+    coloured += __shfl_xor_sync(kFull, coloured, o);
   }
+  if (lane == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  if (lane == 0 && coloured) atomicAdd(&ws.stats[2], coloured);
+  if (leader) ws.stats[1] = r - 1;
 }
 
 // One CTA per SM (the rounds are latency-bound; see color_run), so the
@@ -464,7 +560,7 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   const uint32_t hcap = chunk_capacity(g);
   Bump b;
   const size_t o_cnt_v = b.take((size_t)V * 4);
-  const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
+  const size_t o_q0 = b.take((size_t)V * 8), o_q1 = b.take((size_t)V * 8);
   const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
   const size_t o_wa = b.take(std::max<uint64_t>(g->E, 1));
   const size_t o_cnt = b.take(512);
@@ -475,8 +571,8 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   ws.cnt = (uint32_t*)(base + o_cnt_v);
   ws.waitarc = (uint8_t*)(base + o_wa);
   ws.prio = d_prio;
-  ws.q[0] = (uint32_t*)(base + o_q0);
-  ws.q[1] = (uint32_t*)(base + o_q1);
+  ws.q[0] = (uint2*)(base + o_q0);
+  ws.q[1] = (uint2*)(base + o_q1);
   ws.hc[0] = (uint4*)(base + o_hc0);
   ws.hc[1] = (uint4*)(base + o_hc1);
   char* cnt = base + o_cnt;

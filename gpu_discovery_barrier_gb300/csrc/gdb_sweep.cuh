@@ -163,14 +163,10 @@ __device__ __forceinline__ void group_arcs(const GraphView& G, bool active, uint
 // the arcs (and owner lanes) of up to four consecutive 32-arc steps, so
 // that the caller can issue their loads and atomics together -- one round
 // trip per four steps on latency-bound paths instead of one per step.
+// The arcs come as the lanes' ranges [beg, beg + deg) (deg = 0: none).
 template <class Fn>
-__device__ __forceinline__ void group_arcs4(const GraphView& G, bool active, uint32_t v, Fn&& fn) {
+__device__ __forceinline__ void range_arcs4(uint32_t beg, uint32_t deg, Fn&& fn) {
   const int lane = lane_id();
-  uint32_t beg = 0, deg = 0;
-  if (active) {
-    beg = __ldg(&G.row[v]);
-    deg = __ldg(&G.row[v + 1]) - beg;
-  }
   uint32_t pre = deg;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -201,6 +197,16 @@ __device__ __forceinline__ void group_arcs4(const GraphView& G, bool active, uin
     }
     fn(valid, owner, arc);
   }
+}
+
+template <class Fn>
+__device__ __forceinline__ void group_arcs4(const GraphView& G, bool active, uint32_t v, Fn&& fn) {
+  uint32_t beg = 0, deg = 0;
+  if (active) {
+    beg = __ldg(&G.row[v]);
+    deg = __ldg(&G.row[v + 1]) - beg;
+  }
+  range_arcs4(beg, deg, fn);
 }
 
 // Walk arcs [b, e) of one vertex, 32 per step, every lane present.
