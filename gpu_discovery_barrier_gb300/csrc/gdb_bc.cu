@@ -96,7 +96,7 @@ __device__ __forceinline__ void visit_level(const GraphView& G, const Warps& W, 
     __syncwarp();
     end(v, act);
   }
-  WorkTaker ht(nch, W, hcursor);
+  WorkTaker ht(nch, W, hcursor, lt.n);
   for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
     const uint4 ent = ld_cg(&ws.hc[hcb + c]);
     uint32_t b, en;

@@ -401,11 +401,7 @@ __global__ void __launch_bounds__(512, 3) k_bfs_level(GraphView G, BfsWs ws, uin
     ws.stats[1] = L + 1;
   }
   unsigned long long arcs = 0, farcs = 0;
-  Warps W;
-  W.gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  W.nwarps = (gridDim.x * blockDim.x) >> 5;
-  W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
-  W.nthreads = gridDim.x * blockDim.x;
+  const Warps W = warps_of(blockIdx.x, gridDim.x);
   bfs_top_down(G, W, ws, L, level_counts(ws, L % 3), arcs, farcs);
   unsigned long long r = arcs;
 #pragma unroll
@@ -430,11 +426,7 @@ __global__ void __launch_bounds__(512, 3) k_bfs_glevel(GraphView G, BfsWs ws, ui
     ws.hcursor[old] = 0;
   }
   unsigned long long arcs = 0, farcs = 0;
-  Warps W;
-  W.gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  W.nwarps = (gridDim.x * blockDim.x) >> 5;
-  W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
-  W.nthreads = gridDim.x * blockDim.x;
+  const Warps W = warps_of(blockIdx.x, gridDim.x);
   bfs_top_down(G, W, ws, L, level_counts(ws, L % 3), arcs, farcs);
   unsigned long long r = arcs;
 #pragma unroll

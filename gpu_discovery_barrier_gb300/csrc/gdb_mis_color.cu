@@ -390,6 +390,13 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   uint32_t r = 1;
   for (;; ++r) {
     const int cur = r % 3, nxt = (r + 1) % 3, old = (r + 2) % 3;
+    // A small round (fewer light entries than two per warp) gives each warp
+    // at most one light entry, the first of its WorkTaker: item W.spread.
+    // That entry's load is issued before the round's counts are known, so
+    // the two round trips overlap (entries past the count are never used).
+    const uint2* q = pick(ws.q, r);
+    uint2 spec = make_uint2(0u, 0u);
+    if (lane == 0 && W.spread < ws.qcap) spec = __ldcg(&q[W.spread]);
     const unsigned long long* sc = cta_words<2>([&](unsigned long long* w) {
       w[0] = ld_cg(&ws.qcount[cur]);
       w[1] = __ldcg(&ws.hcount[cur]);
@@ -439,18 +446,20 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
         push_ranges(ws, qs, hc_out, hcount_out, ready, wa[s4] & kHeavyT, u[s4], rb[s4], re[s4]);
       }
     };
-    const uint2* q = pick(ws.q, r);
     const uint32_t k = group_width(n, W.nwarps);
-    WorkTaker lt((n + k - 1) / k, W, &ws.cursor[cur]);
+    WorkTaker lt((n + k - 1) / k, W, &ws.cursor[cur], 0, true);
+    bool first = k == 1;
     for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
       const uint32_t i = g * k + lane;
       const bool act = (uint32_t)lane < k && i < n;
-      const uint2 rg = act ? __ldcg(&q[i]) : make_uint2(0u, 0u);
+      uint2 rg = make_uint2(0u, 0u);
+      if (act) rg = first && g == W.spread ? spec : __ldcg(&q[i]);
+      first = false;
       range_arcs4(rg.x, rg.y - rg.x, relax4);
     }
     const uint32_t nch = (uint32_t)hp;
     const uint4* hc = pick(ws.hc, r);
-    WorkTaker ht(nch, W, &ws.hcursor[cur]);
+    WorkTaker ht(nch, W, &ws.hcursor[cur], lt.n, true);
     for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
       const uint4 ent = ld_cg(&hc[c]);
       const uint32_t b = ent.y, en = ent.z;  // the entry's arc range

@@ -271,7 +271,7 @@ __device__ __forceinline__ void sssp_sweep(const GraphView& G, const GraphView& 
       });
     }
   }
-  WorkTaker ht(nch, W, &ws.hcursor[cur]);
+  WorkTaker ht(nch, W, &ws.hcursor[cur], lt.n);
   for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
     const uint4 ent = ld_cg(&hc[c]);
     const uint32_t du = dist_of<Keyed>(ws, ent.x);
@@ -553,11 +553,7 @@ __global__ void __launch_bounds__(512, 3) k_sssp_glevel(GraphView G, SsspWs ws, 
     ws.cursor[old] = 0;
     ws.hcursor[old] = 0;
   }
-  Warps W;
-  W.gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  W.nwarps = (gridDim.x * blockDim.x) >> 5;
-  W.gthread = blockIdx.x * blockDim.x + threadIdx.x;
-  W.nthreads = gridDim.x * blockDim.x;
+  const Warps W = warps_of(blockIdx.x, gridDim.x);
   unsigned long long arcs = 0;
   const unsigned long long* sc = step_counts(ws, L % 3, 0);
   sssp_sweep<false>(G, G, W, ws, L, 0xFFFFFFFFu, 0, pick(ws.q, L), (uint32_t)sc[0], pick(ws.hc, L),
