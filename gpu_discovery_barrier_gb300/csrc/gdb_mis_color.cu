@@ -390,13 +390,20 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   uint32_t r = 1;
   for (;; ++r) {
     const int cur = r % 3, nxt = (r + 1) % 3, old = (r + 2) % 3;
-    // A small round (fewer light entries than two per warp) gives each warp
-    // at most one light entry, the first of its WorkTaker: item W.spread.
-    // That entry's load is issued before the round's counts are known, so
-    // the two round trips overlap (entries past the count are never used).
+    // Light groups go to the warps in spread order (warp 0 of every CTA,
+    // then warp 1, ...: a small round covers every SM) and heavy chunks to
+    // the same order from its other end, so the two lists meet only when a
+    // round has more entries than the grid has warps.  In a small round
+    // (fewer light entries than two per warp) a warp's light entry is
+    // item `ls` and its heavy chunk item `hs`: both loads are issued before
+    // the round's counts are known, so they overlap the counts' round trip
+    // (entries past the counts are never used).
+    const uint32_t ls = W.spread, hs = W.nwarps - 1 - W.spread;
     const uint2* q = pick(ws.q, r);
+    const uint4* hc = pick(ws.hc, r);
     uint2 spec = make_uint2(0u, 0u);
-    if (lane == 0 && W.spread < ws.qcap) spec = __ldcg(&q[W.spread]);
+    if (lane == 0 && ls < ws.qcap) spec = __ldcg(&q[ls]);
+    const uint4 hspec = hs < ws.hcap ? ld_cg(&hc[hs]) : make_uint4(0u, 0u, 0u, 0u);
     const unsigned long long* sc = cta_words<2>([&](unsigned long long* w) {
       w[0] = ld_cg(&ws.qcount[cur]);
       w[1] = __ldcg(&ws.hcount[cur]);
@@ -447,21 +454,22 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
       }
     };
     const uint32_t k = group_width(n, W.nwarps);
-    WorkTaker lt((n + k - 1) / k, W, &ws.cursor[cur], 0, true);
-    bool first = k == 1;
+    WorkTaker lt((n + k - 1) / k, W.nwarps, ls, &ws.cursor[cur]);
+    bool first = k == 1;  // the first item taken is the warp's own, ls
     for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
       const uint32_t i = g * k + lane;
       const bool act = (uint32_t)lane < k && i < n;
       uint2 rg = make_uint2(0u, 0u);
-      if (act) rg = first && g == W.spread ? spec : __ldcg(&q[i]);
+      if (act) rg = first ? spec : __ldcg(&q[i]);
       first = false;
       range_arcs4(rg.x, rg.y - rg.x, relax4);
     }
     const uint32_t nch = (uint32_t)hp;
-    const uint4* hc = pick(ws.hc, r);
-    WorkTaker ht(nch, W, &ws.hcursor[cur], lt.n, true);
+    WorkTaker ht(nch, W.nwarps, hs, &ws.hcursor[cur]);
+    first = true;  // the first chunk taken is the warp's own, hs
     for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
-      const uint4 ent = ld_cg(&hc[c]);
+      const uint4 ent = first ? hspec : ld_cg(&hc[c]);
+      first = false;
       const uint32_t b = ent.y, en = ent.z;  // the entry's arc range
       // a chunk holds kChunk = 128 arcs: one four-step batch
       static_assert(kChunk == 4 * 32, "a colour chunk is one batch of four steps");

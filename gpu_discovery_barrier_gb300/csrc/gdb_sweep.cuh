@@ -116,21 +116,21 @@ __device__ __forceinline__ uint32_t warp_grab(uint32_t* cursor) {
 // (thousands of rounds of colouring, the tail levels of traversals) cost no
 // atomics.  `after` rotates the assignment so that a second list (heavy
 // chunks after light groups) starts on the warps the first left idle
-// instead of queueing behind it on the same warps.  With `spread` the first
-// items go to warp 0 of every CTA, then warp 1, ..., so a small frontier
-// covers all SMs (the colouring's rounds: R-MAT-22 22.4 -> 21.8 ms); without
-// it, to the warps of CTA 0 first (the SSSP supersteps: 21.1 ms against 21.9
-// spread).
+// instead of queueing behind it on the same warps.  The first items go to
+// the warps of CTA 0 first (the SSSP supersteps: 21.1 ms against 21.9 with
+// the spread order).
 struct WorkTaker {
   uint32_t n, nwarps, next;
   uint32_t* cursor;
-  __device__ __forceinline__ WorkTaker(uint32_t n_, const Warps& W, uint32_t* c, uint32_t after = 0,
-                                       bool spread = false)
+  __device__ __forceinline__ WorkTaker(uint32_t n_, const Warps& W, uint32_t* c, uint32_t after = 0)
       : n(n_), nwarps(W.nwarps), cursor(c) {
     const uint32_t off = after % nwarps;
-    const uint32_t w = spread ? W.spread : W.gwarp;
-    next = w >= off ? w - off : w + nwarps - off;
+    next = W.gwarp >= off ? W.gwarp - off : W.gwarp + nwarps - off;
   }
+  // slot: this warp's own item, any one-to-one map of the grid's warps
+  // onto [0, nwarps)
+  __device__ __forceinline__ WorkTaker(uint32_t n_, uint32_t nwarps_, uint32_t slot, uint32_t* c)
+      : n(n_), nwarps(nwarps_), next(slot), cursor(c) {}
   // next item or n when done
   __device__ __forceinline__ uint32_t take() {
     const uint32_t g = next;
