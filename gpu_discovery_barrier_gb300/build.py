@@ -93,11 +93,13 @@ def build_graphgen() -> Path:
 
 def build_oracle() -> Path:
     out = ORACLE / "_build" / "liboracle.so"
-    srcs = [ORACLE / "oracle.c", ORACLE / "oracle.h"]
+    srcs = [ORACLE / "oracle.c", ORACLE / "oracle_dmr.c", ORACLE / "oracle.h"]
     if _stale(out, srcs):
         out.parent.mkdir(parents=True, exist_ok=True)
-        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", *_openmp_flag("gcc"),
-              str(ORACLE / "oracle.c"), "-o", str(out)])
+        # no floating-point contraction: the same doubles on x86 and Arm hosts
+        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off",
+              *_openmp_flag("gcc"), str(ORACLE / "oracle.c"), str(ORACLE / "oracle_dmr.c"),
+              "-lm", "-o", str(out)])
     return out
 
 

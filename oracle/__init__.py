@@ -62,6 +62,11 @@ def lib() -> C.CDLL:
         L.orc_verify_dist.argtypes = [U32, _u32p, _u32p, P, _u32p]
         L.orc_bfs_reached_arcs.restype = C.c_uint64
         L.orc_bfs_reached_arcs.argtypes = [U32, _u32p, _u32p, U32, C.POINTER(U32)]
+        L.orc_dmr_neighbours.argtypes = [U32, _u32p, _u32p]
+        L.orc_dmr_refine.argtypes = [_f64p, _f64p, U32, _u32p, U32, U32, U32, _f64p, _f64p, _u32p,
+                                     _u32p, _u8p, _u32p]
+        L.orc_dmr_count_bad.restype = U32
+        L.orc_dmr_count_bad.argtypes = [_f64p, _f64p, U32, _u32p, _u8p]
         L.orc_par_threads.restype = C.c_int
         L.orc_par_bfs.argtypes = [U32, _u32p, _u32p, U32, _u32p]
         _ORC = L
@@ -184,6 +189,55 @@ def mst_edge_set(g, arc_flags: np.ndarray) -> set:
 # ---------------------------------------------------------------- reference
 
 
+def _dmr_out(nnodes: int, nelements: int, maxfactor: int):
+    mn, me = (maxfactor // 2) * nnodes, maxfactor * nelements
+    return (np.zeros(mn, np.float64), np.zeros(mn, np.float64), np.zeros(3 * me, np.uint32),
+            np.zeros(3 * me, np.uint32), np.zeros(me, np.uint8), np.zeros(5, np.uint32))
+
+
+def _dmr_result(x, y, el, nb, isdel, counts) -> dict:
+    nn, ne = int(counts[0]), int(counts[1])
+    return {"x": x[:nn], "y": y[:nn], "elements": el[:3 * ne].reshape(ne, 3),
+            "neighbours": nb[:3 * ne].reshape(ne, 3), "isdel": isdel[:ne],
+            "rounds": int(counts[2]), "chunks": int(counts[3]), "refined": int(counts[4])}
+
+
+def dmr_neighbours(elements: np.ndarray) -> np.ndarray:
+    """find_neighbours_cpu (dmr.h:55-104): neighbour triples per element."""
+    el = np.ascontiguousarray(elements, np.uint32).reshape(-1)
+    nb = np.zeros_like(el)
+    _check(lib().orc_dmr_neighbours(el.size // 3, el, nb), "dmr_neighbours")
+    return nb.reshape(-1, 3)
+
+
+def dmr_refine(mesh, chunk: int, maxfactor: int = 20) -> dict:
+    """Refine `mesh` (meshgen.Mesh) with `chunk` items per superstep."""
+    out = _dmr_out(mesh.nnodes, mesh.nelements, maxfactor)
+    _check(lib().orc_dmr_refine(np.ascontiguousarray(mesh.x, np.float64),
+                                np.ascontiguousarray(mesh.y, np.float64), mesh.nnodes,
+                                np.ascontiguousarray(mesh.elements, np.uint32).reshape(-1),
+                                mesh.nelements, maxfactor, chunk, *out), "dmr_refine")
+    return _dmr_result(*out)
+
+
+def dmr_count_bad(x, y, elements, isdel) -> int:
+    """Live triangles with an angle below 30 degrees (angleLT)."""
+    el = np.ascontiguousarray(elements, np.uint32).reshape(-1)
+    return int(lib().orc_dmr_count_bad(np.ascontiguousarray(x, np.float64),
+                                       np.ascontiguousarray(y, np.float64), el.size // 3, el,
+                                       np.ascontiguousarray(isdel, np.uint8)))
+
+
+def ref_dmr(mesh, maxfactor: int = 20) -> dict:
+    """The reference's check_triangles / refine (one work-item) on `mesh`."""
+    out = _dmr_out(mesh.nnodes, mesh.nelements, maxfactor)
+    _check(ref().ref_dmr_lonestar(np.ascontiguousarray(mesh.x, np.float64),
+                                  np.ascontiguousarray(mesh.y, np.float64), mesh.nnodes,
+                                  np.ascontiguousarray(mesh.elements, np.uint32).reshape(-1),
+                                  mesh.nelements, maxfactor, *out), "ref_dmr")
+    return _dmr_result(*out)
+
+
 def ref_available() -> bool:
     return (HERE / "_ref" / "libgdbref.so").exists()
 
@@ -203,6 +257,8 @@ def ref() -> C.CDLL:
         L.ref_bc_pannotia_sources.argtypes = [U32, _u32p, _u32p, _u32p, _u32p, _u32p, U32, _f32p]
         L.ref_mst_lonestar.argtypes = [U32, _u32p, _u32p, _u32p, C.POINTER(U32), C.POINTER(U32),
                                        C.POINTER(U32)]
+        L.ref_dmr_lonestar.argtypes = [_f64p, _f64p, U32, _u32p, U32, U32, _f64p, _f64p, _u32p,
+                                       _u32p, _u8p, _u32p]
         L.ref_discovery_threads.argtypes = [C.c_int, C.c_int, _i32p, C.POINTER(C.c_int),
                                             C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _REF = L

@@ -52,6 +52,17 @@ int orc_bc_f64(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
 int orc_mst(uint32_t V, const uint32_t* row_ptr, const uint32_t* col,
             const uint32_t* w, uint64_t* weight64, uint32_t* weight32,
             uint32_t* components, uint32_t* edges, uint8_t* arc_in_mst);
+/* Delaunay mesh refinement (oracle_dmr.c): elements are node triples,
+ * segments carry 1234567890 as their third node; outputs sized for
+ * (maxfactor / 2) * nnodes nodes and maxfactor * nelements elements;
+ * counts = {nodes, elements, rounds, chunks, refinements}. */
+int orc_dmr_neighbours(uint32_t ne, const uint32_t* el, uint32_t* nb);
+int orc_dmr_refine(const double* x0, const double* y0, uint32_t nnodes,
+                   const uint32_t* el0, uint32_t nelements, uint32_t maxfactor,
+                   uint32_t chunk, double* x, double* y, uint32_t* el,
+                   uint32_t* nb, uint8_t* isdel, uint32_t* counts);
+uint32_t orc_dmr_count_bad(const double* x, const double* y, uint32_t ne,
+                           const uint32_t* el, const uint8_t* isdel);
 uint64_t orc_verify_dist(uint32_t V, const uint32_t* row_ptr,
                          const uint32_t* col, const uint32_t* w,
                          const uint32_t* dist);
