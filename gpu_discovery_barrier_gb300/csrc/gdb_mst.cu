@@ -65,21 +65,31 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
       const int cur = t % 3, old = (t + 2) % 3;
       if (leader) ws.cursor[old] = ws.hcursor[old] = ws.hooks[old] = 0;
       uint32_t cv = 0;
-      sweep_light(
+      // four 32-arc steps at once: their weight, column and component
+      // loads are in flight together
+      sweep_light4(
           G, &ws.cursor[cur],
           [&](uint32_t v, bool in_range) {
             my[lane] = kNoArc;
             cv = in_range ? ld_cg(&ws.comp[v]) : 0u;
             return true;
           },
-          [&](bool valid, int owner, uint32_t arc) {
-            const uint32_t co = __shfl_sync(kFull, cv, owner);
-            if (valid) {
-              ++arcs;
-              const uint32_t wt = __ldg(&G.w[arc]);
-              if (wt < kInf && ld_cg(&ws.comp[__ldg(&G.col[arc])]) != co) {
-                const unsigned long long key = ((unsigned long long)wt << 32) | arc;
-                if (key < my[owner]) atomicMin(&my[owner], key);
+          [&](const bool* valid, const int* owner, const uint32_t* arc) {
+            uint32_t wt[4], cu[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              wt[k] = valid[k] ? __ldg(&G.w[arc[k]]) : kInf;
+              cu[k] = wt[k] < kInf ? __ldg(&G.col[arc[k]]) : 0u;
+              arcs += valid[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) cu[k] = wt[k] < kInf ? ld_cg(&ws.comp[cu[k]]) : 0u;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const uint32_t co = __shfl_sync(kFull, cv, owner[k]);
+              if (wt[k] < kInf && cu[k] != co) {
+                const unsigned long long key = ((unsigned long long)wt[k] << 32) | arc[k];
+                if (key < my[owner[k]]) atomicMin(&my[owner[k]], key);
               }
             }
           },
@@ -91,15 +101,23 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
       sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
         const uint32_t c = ld_cg(&ws.comp[v]);
         unsigned long long m = kNoArc;
-        for (uint32_t a0 = b; a0 < e; a0 += 32) {
-          const uint32_t a = a0 + lane;
-          if (a < e) {
-            ++arcs;
-            const uint32_t wt = __ldg(&G.w[a]);
-            if (wt < kInf && ld_cg(&ws.comp[__ldg(&G.col[a])]) != c) {
-              const unsigned long long key = ((unsigned long long)wt << 32) | a;
-              m = key < m ? key : m;
-            }
+        // a chunk's four 32-arc steps with their loads in flight together
+        static_assert(kChunk == 4 * 32, "an MST chunk is four steps");
+        uint32_t wt[4], cu[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const uint32_t a = b + 32 * k + lane;
+          wt[k] = a < e ? __ldg(&G.w[a]) : kInf;
+          cu[k] = wt[k] < kInf ? __ldg(&G.col[a]) : 0u;
+          arcs += a < e;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cu[k] = wt[k] < kInf ? ld_cg(&ws.comp[cu[k]]) : 0u;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (wt[k] < kInf && cu[k] != c) {
+            const unsigned long long key = ((unsigned long long)wt[k] << 32) | (b + 32 * k + lane);
+            m = key < m ? key : m;
           }
         }
         m = warp_min_u64(m);

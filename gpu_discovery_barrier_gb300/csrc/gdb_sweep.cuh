@@ -493,6 +493,29 @@ __device__ __forceinline__ void sweep_light(const GraphView& G, uint32_t* cursor
   }
 }
 
+// sweep_light with four 32-arc steps per call of edge4(valid[4],
+// owner_lane[4], arc[4]) (group_arcs4), so a step's dependent loads are in
+// flight together with the next three steps'.
+template <class Begin, class Edge4, class End>
+__device__ __forceinline__ void sweep_light4(const GraphView& G, uint32_t* cursor, Begin&& begin,
+                                             Edge4&& edge4, End&& end) {
+  const int lane = lane_id();
+  const uint32_t ngroups = (G.V + 31) / 32;
+  for (;;) {
+    const uint32_t g0 = warp_grab(cursor) * kGrab;
+    if (g0 >= ngroups) break;
+    for (uint32_t g = g0; g < min(g0 + kGrab, ngroups); ++g) {
+      const uint32_t v = g * 32 + lane;
+      const bool in_range = v < G.V && !is_heavy(G, v);
+      const bool act = begin(v, in_range) && in_range;
+      __syncwarp();
+      group_arcs4(G, act, v, edge4);
+      __syncwarp();
+      end(v, act);
+    }
+  }
+}
+
 // Sweep the heavy vertices through the static chunk table, kGrab chunks
 // per grab: fn(v, heavy_index, chunk_in_vertex, arc_begin, arc_end).
 template <class Fn>
