@@ -40,6 +40,8 @@ struct MisWs {
   unsigned long long* stats;  // [0] arcs, [1] rounds
 };
 
+constexpr uint32_t kMisNone = 0xFFFFFFFFu;  // no arc in this lane's step
+
 template <class Sync>
 __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisWs& ws, uint32_t* smem) {
   const Warps W = warps_of(s.id(), s.P());
@@ -69,7 +71,9 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
       const int cur = t % 3, old = (t + 1) % 3;
       if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
       bool undecided_seen = false;
-      sweep_light(
+      // four 32-arc steps at once: the column, state and priority loads of
+      // the four are in flight together
+      sweep_light4(
           G, &ws.cursor[cur],
           [&](uint32_t v, bool in_range) {
             const bool und = in_range && ld_cg(&ws.state[v]) == -1;
@@ -77,15 +81,21 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
             undecided_seen |= und;
             return und;
           },
-          [&](bool valid, int owner, uint32_t arc) {
-            if (valid) {
-              ++arcs;
-              const uint32_t u = __ldg(&G.col[arc]);
-              if (ld_cg(&ws.state[u]) == -1) {
-                const uint32_t k = fkey(__ldg(&ws.prio[u]));
-                if (k < my[owner]) atomicMin(&my[owner], k);
-              }
+          [&](const bool* valid, const int* owner, const uint32_t* arc) {
+            uint32_t u[4], k[4];
+            bool und[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              u[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
+              arcs += valid[j];
             }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) und[j] = valid[j] && ld_cg(&ws.state[u[j]]) == -1;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) k[j] = und[j] ? fkey(__ldg(&ws.prio[u[j]])) : big;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (und[j] && k[j] < my[owner[j]]) atomicMin(&my[owner[j]], k[j]);
           },
           [&](uint32_t v, bool act) {
             if (act) ws.mn[v] = my[lane];
@@ -100,14 +110,21 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
         if (ld_cg(&ws.state[v]) != -1) return;
         undecided_seen = true;
         uint32_t m = big;
-        for (uint32_t a0 = b; a0 < e; a0 += 32) {
-          const uint32_t a = a0 + lane;
-          if (a < e) {
-            ++arcs;
-            const uint32_t u = __ldg(&G.col[a]);
-            if (ld_cg(&ws.state[u]) == -1) m = min(m, fkey(__ldg(&ws.prio[u])));
-          }
+        // a chunk (kChunk = 128 arcs) as four steps with their loads in flight
+        uint32_t u[4];
+        bool und[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const uint32_t a = b + 32 * j + lane;
+          u[j] = a < e ? __ldg(&G.col[a]) : 0u;
+          arcs += a < e;
+          und[j] = a < e;
         }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) und[j] = und[j] && ld_cg(&ws.state[u[j]]) == -1;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (und[j]) m = min(m, fkey(__ldg(&ws.prio[u[j]])));
         m = warp_min_u32(m);
         if (lane == 0 && m < big) atomicMin(&hmn[h], m);
       });
@@ -124,7 +141,7 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
       if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
       // next round's heavy minima start from BIGNUM
       for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) pick(ws.hmn, r + 1)[h] = big;
-      sweep_light(
+      sweep_light4(
           G, &ws.cursor[cur],
           [&](uint32_t v, bool in_range) {
             bool win = false;
@@ -135,12 +152,16 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
             }
             return win;
           },
-          [&](bool valid, int, uint32_t arc) {
-            if (valid) {
-              ++arcs;
-              const uint32_t u = __ldg(&G.col[arc]);
-              if (ld_cg(&ws.state[u]) == -1) ws.state[u] = -2;
+          [&](const bool* valid, const int*, const uint32_t* arc) {
+            uint32_t u[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              u[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
+              arcs += valid[j];
             }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (valid[j] && ld_cg(&ws.state[u[j]]) == -1) ws.state[u[j]] = -2;
           },
           [](uint32_t, bool) {});
       const uint32_t* hmn = pick(ws.hmn, r);
@@ -152,14 +173,16 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
         if (ld_cg(&ws.state[v]) != -1) return;
         if (!(fkey(__ldg(&ws.prio[v])) < ld_cg(&hmn[h]))) return;
         if (lane == 0) ws.s[v] = 2;
-        for (uint32_t a0 = b; a0 < e; a0 += 32) {
-          const uint32_t a = a0 + lane;
-          if (a < e) {
-            ++arcs;
-            const uint32_t u = __ldg(&G.col[a]);
-            if (ld_cg(&ws.state[u]) == -1) ws.state[u] = -2;
-          }
+        uint32_t u[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const uint32_t a = b + 32 * j + lane;
+          u[j] = a < e ? __ldg(&G.col[a]) : kMisNone;
+          arcs += a < e;
         }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (u[j] != kMisNone && ld_cg(&ws.state[u[j]]) == -1) ws.state[u[j]] = -2;
       });
       if (!s.sync()) return;
       ++t;
