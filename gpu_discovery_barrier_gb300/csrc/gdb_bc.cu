@@ -105,6 +105,47 @@ __device__ __forceinline__ void visit_level(const GraphView& G, const Warps& W, 
   }
 }
 
+// visit_level with four 32-arc steps per call of edge4(valid[4], owner[4],
+// arc[4]) (group_arcs4): a step's dependent loads are in flight together
+// with the next three steps'.
+template <class Begin, class Edge4, class End, class Heavy>
+__device__ __forceinline__ void visit_level4(const GraphView& G, const Warps& W, const BcWs& ws,
+                                             uint32_t lb, uint32_t nl, uint32_t hcb, uint32_t hvb,
+                                             uint32_t nch, uint32_t* cursor, uint32_t* hcursor,
+                                             Begin&& begin, Edge4&& edge4, End&& end, Heavy&& heavy) {
+  const int lane = lane_id();
+  const uint32_t k = group_width(nl, W.nwarps);
+  WorkTaker lt((nl + k - 1) / k, W, cursor);
+  for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
+    const uint32_t i = g * k + lane;
+    const bool act = (uint32_t)lane < k && i < nl;
+    const uint32_t v = act ? ld_cg(&ws.order[lb + i]) : 0u;
+    begin(v, act);
+    __syncwarp();
+    group_arcs4(G, act, v, edge4);
+    __syncwarp();
+    end(v, act);
+  }
+  WorkTaker ht(nch, W, hcursor, lt.n);
+  for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
+    const uint4 ent = ld_cg(&ws.hc[hcb + c]);
+    uint32_t b, en;
+    chunk_range(G, ent, b, en);
+    heavy(ent.x, hvb + ent.z, ent.w, b, en);
+  }
+}
+
+// The four steps of a heavy chunk [b, e) (at most kChunk = 128 arcs).
+__device__ __forceinline__ void chunk_steps(uint32_t b, uint32_t e, bool* valid, uint32_t* arc) {
+  static_assert(kChunk == 4 * 32, "a chunk is four steps");
+  const uint32_t lane = lane_id();
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    arc[j] = b + 32 * j + lane;
+    valid[j] = arc[j] < e;
+  }
+}
+
 __device__ __forceinline__ int32_t level_of(const BcWs& ws, uint32_t v) {
   return (int32_t)__ldcg(reinterpret_cast<const uint32_t*>(&ws.st[v]));
 }
@@ -238,40 +279,58 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       if (!pull) {
         // push: one arc of a level-L vertex of path count rv -- claim an
         // unvisited neighbour, add rv to every level-L+1 neighbour
-        auto fwd = [&](bool valid, float rv, uint32_t arc) {
-          uint32_t u = 0;
-          bool claimed = false;
-          if (valid) {
-            ++arcs;
-            u = __ldg(&G.col[arc]);
-            const int32_t du = level_of(ws, u);
-            bool add = du == Li + 1;
-            if (du == -1) {
-              // the degree loads go out with the claim, not after it
-              const uint32_t r0 = __ldg(&G.row[u]), r1 = __ldg(&G.row[u + 1]);
-              const int old = atomicCAS(reinterpret_cast<int*>(&ws.st[u]), -1, Li + 1);
-              claimed = old == -1;
-              add = claimed || old == Li + 1;
-              if (claimed) next_arcs += r1 - r0;
-            }
-            if (add) atomicAdd(&ws.rho[u], rv);
+        // four steps of arcs of level-L vertices with path counts rv: claim
+        // unvisited neighbours, add rv to every level-L+1 neighbour; the
+        // column, level, degree and claim round trips of the four overlap
+        auto fwd4 = [&](const bool* valid, const float* rv, const uint32_t* arc) {
+          uint32_t u[4], r0[4], r1[4];
+          int32_t du[4];
+          int old[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            u[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
+            arcs += valid[j];
           }
-          frontier_push_staged(G, out, qs, claimed, u);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) du[j] = valid[j] ? level_of(ws, u[j]) : -2;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const bool cl = du[j] == -1;
+            // the degree loads go out with the claim, not after it
+            r0[j] = cl ? __ldg(&G.row[u[j]]) : 0u;
+            r1[j] = cl ? __ldg(&G.row[u[j] + 1]) : 0u;
+            old[j] = cl ? atomicCAS(reinterpret_cast<int*>(&ws.st[u[j]]), -1, Li + 1) : -2;
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const bool claimed = du[j] == -1 && old[j] == -1;
+            const bool add = du[j] == Li + 1 || claimed || (du[j] == -1 && old[j] == Li + 1);
+            if (claimed) next_arcs += r1[j] - r0[j];
+            if (add) atomicAdd(&ws.rho[u[j]], rv[j]);
+            frontier_push_staged(G, out, qs, claimed, u[j]);
+          }
         };
         float rv_lane = 0.f;
-        visit_level(
+        visit_level4(
             G, W, ws, lbase, nl, hcbase, hvbase, nch, &ws.cursor[cur], &ws.hcursor[cur],
             [&](uint32_t v, bool act) {
               rv_lane = act ? rho_of(ws, v) : 0.f;
               if (act) reached_arcs += degree(v);
             },
-            [&](bool valid, int owner, uint32_t arc) {
-              fwd(valid, __shfl_sync(kFull, rv_lane, owner), arc);
+            [&](const bool* valid, const int* owner, const uint32_t* arc) {
+              float rv[4];
+#pragma unroll
+              for (int j = 0; j < 4; ++j) rv[j] = __shfl_sync(kFull, rv_lane, owner[j]);
+              fwd4(valid, rv, arc);
             },
             [&](uint32_t, bool) {},
             [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
-              const float rv = rho_of(ws, v);
-              for (uint32_t a0 = b; a0 < e; a0 += 32) fwd(a0 + lane < e, rv, a0 + lane);
+              const float r = rho_of(ws, v);
+              const float rv[4] = {r, r, r, r};
+              bool valid[4];
+              uint32_t arc[4];
+              chunk_steps(b, e, valid, arc);
+              fwd4(valid, rv, arc);
               if (lane == 0 && b == __ldg(&G.row[v])) reached_arcs += degree(v);
             });
       } else {
@@ -282,14 +341,24 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
           const bool unv = u < G.V && level_of(ws, u) == -1;
           my[lane] = 0.0;
           __syncwarp();
-          group_arcs(G, unv, u, [&](bool valid, int owner, uint32_t arc) {
-            float a = -0.f;  // no term
-            if (valid) {
-              ++arcs;
-              const uint32_t w = __ldg(&G.col[arc]);
-              if (level_of(ws, w) == Li) a = rho_of(ws, w);
+          // four steps at once; a neighbour's path count is loaded with its
+          // level (and used only when the level is L)
+          group_arcs4(G, unv, u, [&](const bool* valid, const int* owner, const uint32_t* arc) {
+            uint32_t w[4];
+            int32_t lw[4];
+            float rw[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              w[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
+              arcs += valid[j];
             }
-            segment_add(my, owner, a);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              lw[j] = valid[j] ? level_of(ws, w[j]) : -2;
+              rw[j] = valid[j] ? rho_of(ws, w[j]) : 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) segment_add(my, owner[j], lw[j] == Li ? rw[j] : -0.f);  // -0: no term
           });
           __syncwarp();
           const double sum = my[lane];
@@ -343,29 +412,46 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       };
       if ((uint32_t)Lb < peak) {
         // pull the coefficients of the level-Lb+1 neighbours
-        auto bwd = [&](bool valid, uint32_t arc) {
-          float a = -0.f;  // no term
-          if (valid) {
-            ++arcs;
-            const uint2 su = __ldcg(&ws.st[__ldg(&G.col[arc])]);  // level and coefficient
-            if ((int32_t)su.x == Lb + 1) a = __uint_as_float(su.y);
+        // four steps at once: the successors' coefficients (-0: no term)
+        auto bwd4 = [&](const bool* valid, const uint32_t* arc, float* a) {
+          uint32_t c[4];
+          uint2 su[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            c[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
+            arcs += valid[j];
           }
-          return a;
+#pragma unroll
+          for (int j = 0; j < 4; ++j)  // level and coefficient
+            su[j] = valid[j] ? __ldcg(&ws.st[c[j]]) : make_uint2(0xFFFFFFFFu, 0u);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) a[j] = (int32_t)su[j].x == Lb + 1 ? __uint_as_float(su[j].y) : -0.f;
         };
         float rv_lane = 0.f;
-        visit_level(
+        visit_level4(
             G, W, ws, lb, le - lb, hcb, hvb, nch, &ws.cursor[cur], &ws.hcursor[cur],
             [&](uint32_t v, bool act) {
               my[lane] = -0.0;
               rv_lane = act ? rho_of(ws, v) : 0.f;
             },
-            [&](bool valid, int owner, uint32_t arc) { segment_add(my, owner, bwd(valid, arc)); },
+            [&](const bool* valid, const int* owner, const uint32_t* arc) {
+              float a[4];
+              bwd4(valid, arc, a);
+#pragma unroll
+              for (int j = 0; j < 4; ++j) segment_add(my, owner[j], a[j]);
+            },
             [&](uint32_t v, bool act) {
               if (act) finalize(v, rv_lane, my[lane]);
             },
             [&](uint32_t v, uint32_t slot, uint32_t nchunks, uint32_t b, uint32_t e) {
+              bool valid[4];
+              uint32_t arc[4];
+              float a[4];
+              chunk_steps(b, e, valid, arc);
+              bwd4(valid, arc, a);
               float part = -0.f;
-              for (uint32_t a0 = b; a0 < e; a0 += 32) part += bwd(a0 + lane < e, a0 + lane);
+#pragma unroll
+              for (int j = 0; j < 4; ++j) part += a[j];
               part = warp_sum_f32(part);
               double tot = 0.0;
               if (heavy_done(ws, slot, part, nchunks, &tot) && lane == 0) finalize(v, rho_of(ws, v), tot);
@@ -384,21 +470,32 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
       } else {
         // finalise from the pushed sum, then push the coefficient into the
         // level-Lb-1 neighbours
-        auto push = [&](bool valid, float cf, uint32_t arc) {
-          if (valid) {
-            ++arcs;
-            const uint32_t u = __ldg(&G.col[arc]);
-            if (level_of(ws, u) == Lb - 1) atomicAdd(&ws.sacc[u], (double)cf);
+        // four steps at once: add the coefficient into level-Lb-1 neighbours
+        auto push4 = [&](const bool* valid, const float* cf, const uint32_t* arc) {
+          uint32_t u[4];
+          int32_t lu[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            u[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
+            arcs += valid[j];
           }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) lu[j] = valid[j] ? level_of(ws, u[j]) : -2;
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (lu[j] == Lb - 1) atomicAdd(&ws.sacc[u[j]], (double)cf[j]);
         };
         float cf_lane = 0.f;
-        visit_level(
+        visit_level4(
             G, W, ws, lb, le - lb, hcb, hvb, nch, &ws.cursor[cur], &ws.hcursor[cur],
             [&](uint32_t v, bool act) {
               cf_lane = act ? finalize(v, rho_of(ws, v), __ldcg(&ws.sacc[v])) : 0.f;
             },
-            [&](bool valid, int owner, uint32_t arc) {
-              push(valid, __shfl_sync(kFull, cf_lane, owner), arc);
+            [&](const bool* valid, const int* owner, const uint32_t* arc) {
+              float cf[4];
+#pragma unroll
+              for (int j = 0; j < 4; ++j) cf[j] = __shfl_sync(kFull, cf_lane, owner[j]);
+              push4(valid, cf, arc);
             },
             [&](uint32_t, bool) {},
             [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
@@ -413,7 +510,11 @@ __device__ __forceinline__ void bc_body(Sync& s, const GraphView& G, const BcWs&
                 const float sg = no_terms(sum) ? 0.f : (float)((double)rv * sum);
                 cf = (1.0f + sg) / rv;
               }
-              for (uint32_t a0 = b; a0 < e; a0 += 32) push(a0 + lane < e, cf, a0 + lane);
+              const float cfs[4] = {cf, cf, cf, cf};
+              bool valid[4];
+              uint32_t arc[4];
+              chunk_steps(b, e, valid, arc);
+              push4(valid, cfs, arc);
             });
       }
       if (!s.sync()) return;
