@@ -327,13 +327,20 @@ __device__ __forceinline__ void settle_pull(const GraphView& GT, const Warps& W,
     const bool open = u < GT.V && du >= split;
     my[lane] = 0xFFFFFFFFu;
     __syncwarp();
-    group_arcs(GT, open, u, [&](bool valid, int owner, uint32_t arc) {
-      if (valid) {
-        ++arcs;
-        const uint32_t v = __ldg(&GT.col[arc]), w = __ldg(&GT.w[arc]);
-        const uint32_t dv = dist_of<true>(ws, v);
-        if (dv < split) atomicMin(&my[owner], dv + w);
+    // four steps at once: their column, weight and distance loads overlap
+    group_arcs4(GT, open, u, [&](const bool* valid, const int* owner, const uint32_t* arc) {
+      uint32_t v[4], w[4], dv[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        v[j] = valid[j] ? __ldg(&GT.col[arc[j]]) : 0u;
+        w[j] = valid[j] ? __ldg(&GT.w[arc[j]]) : 0u;
+        arcs += valid[j];
       }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) dv[j] = valid[j] ? dist_of<true>(ws, v[j]) : 0xFFFFFFFFu;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (dv[j] < split) atomicMin(&my[owner[j]], dv[j] + w[j]);
     });
     __syncwarp();
     const uint32_t nd = my[lane];
