@@ -345,7 +345,9 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
   {
     float pv_lane = 0.f;
     bool looks_lane = false;
-    sweep_light(
+    // four 32-arc steps at once: the neighbours' priority and degree loads
+    // of the four are in flight together
+    sweep_light4(
         G, &ws.cursor[0],
         [&](uint32_t v, bool in_range) {
           my[lane] = 0;
@@ -355,16 +357,28 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
           looks_lane = in_range && __ldg(&G.row[v + 1]) - __ldg(&G.row[v]) != 1;
           return in_range;
         },
-        [&](bool valid, int owner, uint32_t arc) {
-          const float pv = __shfl_sync(kFull, pv_lane, owner);
-          const bool looks = __shfl_sync(kFull, looks_lane, owner);
-          if (valid) {
-            ++arcs;
-            const uint32_t u = __ldg(&G.col[arc]);
-            const float pu = __ldg(&ws.prio[u]);
-            if (looks && pu >= pv) atomicAdd(&my[owner], 1u);
-            const uint32_t du = __ldg(&G.row[u + 1]) - __ldg(&G.row[u]);
-            ws.waitarc[arc] = (pv >= pu && du != 1 ? kWaits : 0) | (du > kHeavyDeg ? kHeavyT : 0);
+        [&](const bool* valid, const int* owner, const uint32_t* arc) {
+          uint32_t u[4], du[4];
+          float pu[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            u[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
+            arcs += valid[j];
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            pu[j] = valid[j] ? __ldg(&ws.prio[u[j]]) : 0.f;
+            du[j] = valid[j] ? __ldg(&G.row[u[j] + 1]) - __ldg(&G.row[u[j]]) : 0u;
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float pv = __shfl_sync(kFull, pv_lane, owner[j]);
+            const bool looks = __shfl_sync(kFull, looks_lane, owner[j]);
+            if (valid[j]) {
+              if (looks && pu[j] >= pv) atomicAdd(&my[owner[j]], 1u);
+              ws.waitarc[arc[j]] =
+                  (pv >= pu[j] && du[j] != 1 ? kWaits : 0) | (du[j] > kHeavyDeg ? kHeavyT : 0);
+            }
           }
         },
         [&](uint32_t v, bool) {
@@ -373,15 +387,27 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
     sweep_heavy(G, &ws.hcursor[0], [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
       const float pv = __ldg(&ws.prio[v]);
       uint32_t n = 0;
-      for (uint32_t a0 = b; a0 < e; a0 += 32) {
-        const uint32_t a = a0 + lane;
+      // a chunk (kChunk = 128 arcs) as four steps with their loads in flight
+      uint32_t u[4], du[4];
+      float pu[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t a = b + 32 * j + lane;
+        u[j] = a < e ? __ldg(&G.col[a]) : 0u;
+        arcs += a < e;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const bool ok = b + 32 * j + lane < e;
+        pu[j] = ok ? __ldg(&ws.prio[u[j]]) : 0.f;
+        du[j] = ok ? __ldg(&G.row[u[j] + 1]) - __ldg(&G.row[u[j]]) : 0u;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t a = b + 32 * j + lane;
         if (a < e) {
-          ++arcs;
-          const uint32_t u = __ldg(&G.col[a]);
-          const float pu = __ldg(&ws.prio[u]);
-          n += pu >= pv;
-          const uint32_t du = __ldg(&G.row[u + 1]) - __ldg(&G.row[u]);
-          ws.waitarc[a] = (pv >= pu && du != 1 ? kWaits : 0) | (du > kHeavyDeg ? kHeavyT : 0);
+          n += pu[j] >= pv;
+          ws.waitarc[a] = (pv >= pu[j] && du[j] != 1 ? kWaits : 0) | (du[j] > kHeavyDeg ? kHeavyT : 0);
         }
       }
       n = warp_add_u32(n);
