@@ -18,7 +18,10 @@ divided by the device time of the step.
 * cpu_baseline: the CPU oracle on a bounded sample of the same workload.
 
 ``--impl reference`` times the CPU implementation of the path on the host's
-cores instead (see the design doc for why it is the oracle port).
+cores instead: the oracle port, spread over all host threads, because the
+reference's own apps need an OpenCL runtime that neither machine has (its
+kernels compile through oracle/refshim only where its sources are, to pin
+the oracle).
 """
 from __future__ import annotations
 
