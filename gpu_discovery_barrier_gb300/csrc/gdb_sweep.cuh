@@ -469,6 +469,40 @@ __device__ __forceinline__ void visit_frontier(const GraphView& G, const Warps& 
   }
 }
 
+// visit_frontier with four 32-arc steps per call of edge4(valid[4], arc[4]):
+// light groups through group_arcs4, a heavy chunk (kChunk = 128 arcs) as
+// its four steps.
+template <class Edge4>
+__device__ __forceinline__ void visit_frontier4(const GraphView& G, const Warps& W, const uint32_t* q,
+                                                uint32_t n, const uint4* hc, unsigned long long hpacked,
+                                                uint32_t* cursor, uint32_t* hcursor, Edge4&& edge4) {
+  static_assert(kChunk == 4 * 32, "a chunk is four steps");
+  const int lane = lane_id();
+  const uint32_t k = group_width(n, W.nwarps);
+  WorkTaker lt((n + k - 1) / k, W, cursor);
+  for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
+    const uint32_t i = g * k + lane;
+    const bool act = (uint32_t)lane < k && i < n;
+    const uint32_t v = act ? ld_cg(&q[i]) : 0u;
+    group_arcs4(G, act, v, [&](const bool* valid, const int*, const uint32_t* arc) { edge4(valid, arc); });
+  }
+  const uint32_t nch = (uint32_t)hpacked;
+  WorkTaker ht(nch, W, hcursor, lt.n);
+  for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
+    const uint4 ent = ld_cg(&hc[c]);
+    uint32_t b, en;
+    chunk_range(G, ent, b, en);
+    bool valid[4];
+    uint32_t arc[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      arc[j] = b + 32 * j + lane;
+      valid[j] = arc[j] < en;
+    }
+    edge4(valid, arc);
+  }
+}
+
 // Sweep the light vertices of [0, V) in warp groups of 32 consecutive ids.
 // begin(v, in_range) -> bool active: per-lane setup (v is light and < V
 // when in_range); edge(valid, owner_lane, arc) per 32-arc step;
