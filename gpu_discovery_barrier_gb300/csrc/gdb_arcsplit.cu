@@ -128,23 +128,41 @@ __global__ void k_split_count(GraphView G, uint32_t bound, uint32_t* nl, uint32_
       nh[v] = th;
     }
   }
-  // the others: one warp each
+  // the others: 32 consecutive vertices per warp, their arcs walked together
+  // four 32-arc steps at a time; the lanes of one owner in a step are found
+  // with __match_any_sync and one of them adds the owner's counts
   const Warps W = warps_of(blockIdx.x, gridDim.x);
   const int lane = lane_id();
-  for (uint32_t v = W.gwarp; v < G.V; v += W.nwarps) {
-    if (is_heavy(G, v)) continue;
-    const uint32_t b = G.row[v], e = G.row[v + 1];
-    uint32_t cl = 0, ch = 0;
-    for (uint32_t a0 = b; a0 < e; a0 += 32) {
-      const uint32_t a = a0 + lane;
-      const uint32_t w = a < e ? __ldg(&G.w[a]) : kInf;
-      cl += __popc(__ballot_sync(kFull, a < e && is_light(w, bound)));
-      ch += __popc(__ballot_sync(kFull, a < e && is_heavy_arc(w, bound)));
+  __shared__ uint32_t scnt[2][32][32];
+  uint32_t* cl_s = scnt[0][threadIdx.x >> 5];
+  uint32_t* ch_s = scnt[1][threadIdx.x >> 5];
+  for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
+    const uint32_t v = g * 32 + lane;
+    const bool act = v < G.V && !is_heavy(G, v);
+    cl_s[lane] = ch_s[lane] = 0;
+    __syncwarp();
+    group_arcs4(G, act, v, [&](const bool* valid, const int* owner, const uint32_t* arc) {
+      uint32_t w[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) w[j] = valid[j] ? __ldg(&G.w[arc[j]]) : kInf;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const unsigned same = __match_any_sync(kFull, owner[j]);
+        const unsigned ml = __ballot_sync(kFull, valid[j] && is_light(w[j], bound)) & same;
+        const unsigned mh = __ballot_sync(kFull, valid[j] && is_heavy_arc(w[j], bound)) & same;
+        if (lane == 31 - __clz(same)) {
+          cl_s[owner[j]] += __popc(ml);
+          ch_s[owner[j]] += __popc(mh);
+        }
+        __syncwarp();
+      }
+    });
+    __syncwarp();
+    if (act) {
+      nl[v] = cl_s[lane];
+      nh[v] = ch_s[lane];
     }
-    if (lane == 0) {
-      nl[v] = cl;
-      nh[v] = ch;
-    }
+    __syncwarp();
   }
 }
 
@@ -193,31 +211,53 @@ __global__ void k_split_scatter(GraphView G, uint32_t bound, const uint32_t* rl,
       __syncthreads();
     }
   }
+  // the others: 32 consecutive vertices per warp, four 32-arc steps at a
+  // time; a lane's place in its owner's row is the owner's arcs placed so far
+  // plus its rank among the owner's lanes of the step, so every row keeps
+  // its order
   const Warps W = warps_of(blockIdx.x, gridDim.x);
-  for (uint32_t v = W.gwarp; v < G.V; v += W.nwarps) {
-    if (is_heavy(G, v)) continue;
-    const uint32_t b = G.row[v], e = G.row[v + 1];
-    uint32_t ol = rl[v], oh = rh[v];
-    for (uint32_t a0 = b; a0 < e; a0 += 32) {
-      const uint32_t a = a0 + lane;
-      const bool ok = a < e;
-      const uint32_t w = ok ? __ldg(&G.w[a]) : kInf;
-      const uint32_t c = ok ? __ldg(&G.col[a]) : 0u;
-      const bool il = ok && is_light(w, bound), ih = ok && is_heavy_arc(w, bound);
-      const unsigned ml = __ballot_sync(kFull, il), mh = __ballot_sync(kFull, ih);
-      if (il) {
-        const uint32_t p = ol + __popc(ml & lanemask_lt());
-        cl[p] = c;
-        wl[p] = w;
+  __shared__ uint32_t sput[2][32][32];
+  uint32_t* pl_s = sput[0][threadIdx.x >> 5];
+  uint32_t* ph_s = sput[1][threadIdx.x >> 5];
+  for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
+    const uint32_t v = g * 32 + lane;
+    const bool act = v < G.V && !is_heavy(G, v);
+    const uint32_t ol = act ? rl[v] : 0u, oh = act ? rh[v] : 0u;
+    pl_s[lane] = ph_s[lane] = 0;
+    __syncwarp();
+    group_arcs4(G, act, v, [&](const bool* valid, const int* owner, const uint32_t* arc) {
+      uint32_t w[4], c[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        w[j] = valid[j] ? __ldg(&G.w[arc[j]]) : kInf;
+        c[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
       }
-      if (ih) {
-        const uint32_t p = oh + __popc(mh & lanemask_lt());
-        ch[p] = c;
-        wh[p] = w;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const unsigned same = __match_any_sync(kFull, owner[j]);
+        const bool il = valid[j] && is_light(w[j], bound), ih = valid[j] && is_heavy_arc(w[j], bound);
+        const unsigned ml = __ballot_sync(kFull, il) & same, mh = __ballot_sync(kFull, ih) & same;
+        const uint32_t bl = __shfl_sync(kFull, ol, owner[j]) + pl_s[owner[j]];
+        const uint32_t bh = __shfl_sync(kFull, oh, owner[j]) + ph_s[owner[j]];
+        if (il) {
+          const uint32_t p = bl + __popc(ml & lanemask_lt());
+          cl[p] = c[j];
+          wl[p] = w[j];
+        }
+        if (ih) {
+          const uint32_t p = bh + __popc(mh & lanemask_lt());
+          ch[p] = c[j];
+          wh[p] = w[j];
+        }
+        __syncwarp();
+        if (lane == 31 - __clz(same)) {
+          pl_s[owner[j]] += __popc(ml);
+          ph_s[owner[j]] += __popc(mh);
+        }
+        __syncwarp();
       }
-      ol += __popc(ml);
-      oh += __popc(mh);
-    }
+    });
+    __syncwarp();
   }
 }
 
