@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--edge-factor", type=float, default=16)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-parity", action="store_true",
+                   help="skip the full-size output check against the CPU oracle")
     p.add_argument("--apps", default="bfs,sssp,mis,color,bc,mst")
     p.add_argument("--batch-graphs", type=int, default=512)
     p.add_argument("--schedule", choices=["plain", "adaptive", "learned"], default="learned",
@@ -94,6 +96,22 @@ def make_workload(scale: int, ef: float, path: str | None = None):
         "uw": gg.unique_weights(g, seed=3),
         "prio": gg.priorities(g.V, seed=4),
         "src": gg.sources(g, NSRC, seed=2),
+    }
+
+
+def make_workload_cpu(scale: int, ef: float):
+    """The same seeded workload from the oracle's own generator (no library
+    of the product is loaded by the CPU implementation's arm)."""
+    import oracle as O
+
+    g = O.gen_rmat(1 << scale, ef, seed=1)
+    return {
+        "g": g,
+        "w": O.gen_uniform_weights(g, 1, 255, seed=1),
+        "symmetric": True,
+        "uw": O.gen_unique_weights(g, seed=3),
+        "prio": O.gen_priorities(g.V, seed=4),
+        "src": O.gen_sources(g, NSRC, seed=2),
     }
 
 
@@ -379,9 +397,23 @@ def barrier(world: int):
         dist.barrier()
 
 
+def suite_metric(schedule: str) -> str:
+    return (f"edges/sec (persistent suite, {schedule} BFS/SSSP schedule: BFS+SSSP+BC x16 sources, "
+            "MIS, colour, MST)")
+
+
+def suite_config(args, g, world) -> dict:
+    """The workload as both arms report it (identical dicts)."""
+    return {"workload": (f"file {args.graph} suite" if args.graph
+                         else f"rmat scale {args.scale} ef {args.edge_factor:g} suite"),
+            "V": g.V, "E": g.E, "sources": NSRC, "apps": args.apps.split(","),
+            "schedule": args.schedule, "global_batch": world,
+            "parallelism": f"replicas x{world}", "l2": "inputs > L2 (no flush)"}
+
+
 def base_line(args, world, metric_value, ms_per_step, cfg):
     return {
-        "metric": "edges/sec (plain persistent suite: BFS+SSSP+BC x16 sources, MIS, colour, MST)",
+        "metric": suite_metric(args.schedule),
         "value": metric_value,
         "unit": "edges/s",
         "n_gpus": world,
@@ -397,12 +429,95 @@ def base_line(args, world, metric_value, ms_per_step, cfg):
     }
 
 
+def mst_edges(g, arc_flags) -> np.ndarray:
+    """Sorted unique undirected edges (min << 32 | max) of the flagged arcs."""
+    sel = np.nonzero(np.asarray(arc_flags)[: g.E])[0]
+    src = np.searchsorted(g.row_ptr.astype(np.int64), sel, side="right") - 1
+    a, b = src.astype(np.uint64), g.col[sel].astype(np.uint64)
+    return np.unique((np.minimum(a, b) << np.uint64(32)) | np.maximum(a, b))
+
+
+def suite_parity(suite, wl, threads: int) -> dict:
+    """Every app of the suite on the full workload, read back through the
+    host-buffer API, against the CPU oracle (spread over `threads` host
+    threads): BFS levels and SSSP distances for the 16 sources, the MIS set,
+    the colours and the MST weight, edge count, components and edge set bit
+    for bit; BC within 1e-4 relative of the FP64 Brandes oracle (the same
+    tolerance as the tests), non-finite where the oracle is."""
+    import oracle as O
+
+    c, g, src = suite.ctx, wl["g"], [int(x) for x in wl["src"]]
+    gw, gu = g.with_weights(wl["w"]), g.with_weights(wl["uw"])
+    apps = suite.apps
+    got = {}
+    if "bfs" in apps:
+        got["bfs"] = c.bfs_sources(suite.G, src)
+    if "sssp" in apps:
+        got["sssp"] = c.sssp_sources(suite.G, src)
+    if "mis" in apps:
+        got["mis"] = c.mis(suite.G, wl["prio"])
+    if "color" in apps:
+        got["color"] = c.color(suite.G, wl["prio"])
+    if "bc" in apps:
+        got["bc"] = c.bc(suite.G, src)
+    if "mst" in apps:
+        got["mst"] = c.mst(suite.Gu, with_arcs=True)
+    t0 = time.perf_counter()
+    tasks = {}
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        for i, s in enumerate(src):
+            if "bfs" in apps:
+                tasks[("bfs", i)] = ex.submit(O.bfs, g, s)
+            if "sssp" in apps:
+                tasks[("sssp", i)] = ex.submit(O.sssp_worklist, gw, s)
+            if "bc" in apps:
+                tasks[("bc", i)] = ex.submit(O.bc_f64, g, [s])
+        if "mis" in apps:
+            tasks[("mis", 0)] = ex.submit(lambda: O.mis(g, wl["prio"])[0])
+        if "color" in apps:
+            tasks[("color", 0)] = ex.submit(lambda: O.color_fast(g, wl["prio"])[0])
+        if "mst" in apps:
+            tasks[("mst", 0)] = ex.submit(O.mst, gu)
+        want = {k: f.result() for k, f in tasks.items()}
+    res: dict = {}
+    for app in ("bfs", "sssp"):
+        if app in got:
+            res[app] = all(np.array_equal(got[app][i], want[(app, i)]) for i in range(len(src)))
+    for app in ("mis", "color"):
+        if app in got:
+            res[app] = bool(np.array_equal(got[app], want[(app, 0)]))
+    detail = {}
+    if "bc" in got:
+        ref = np.sum([want[("bc", i)] for i in range(len(src))], axis=0)
+        fin = np.isfinite(ref)
+        b = got["bc"].astype(np.float64)
+        scale = np.maximum(np.abs(ref[fin]), 1e-6 * max(1.0, float(np.abs(ref[fin]).max())))
+        err = np.abs(b[fin] - ref[fin]) / scale
+        res["bc"] = bool(np.all(np.abs(b[fin] - ref[fin]) <= 1e-4 * scale + 1e-6)
+                         and not np.any(np.isfinite(b[~fin])))
+        detail["bc_max_rel_err"] = float(err.max()) if err.size else 0.0
+    if "mst" in got:
+        m, r = got["mst"], want[("mst", 0)]
+        res["mst"] = bool((m["weight64"], m["weight32"], m["edges"], m["components"])
+                          == (r["weight64"], r["weight32"], r["edges"], r["components"])
+                          and np.array_equal(mst_edges(g, m["arc_in_mst"]),
+                                             mst_edges(g, r["arc_in_mst"])))
+    detail["oracle_s"] = round(time.perf_counter() - t0, 1)
+    detail["oracle_threads"] = threads
+    res["detail"] = detail
+    return res
+
+
 def run_reference(args, rank, world):
     import oracle as O
 
     if rank != 0:
         return
-    wl = make_workload(args.scale, args.edge_factor, args.graph)
+    if args.graph:
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU implementation's arm runs "
+                          "the generated R-MAT workload only (no graph-file reader on that side)"}))
+        return
+    wl = make_workload_cpu(args.scale, args.edge_factor)
     g = wl["g"]
     er = {int(s): reach(g, O.par_bfs(g, int(s)))[1] for s in wl["src"]}
     threads = os.cpu_count() or 1
@@ -415,9 +530,7 @@ def run_reference(args, rank, world):
         units += units_of(names, srcs, er, g.E)
     total = sum(times)
     value = units / total
-    cfg = {"workload": (f"file {args.graph} suite" if args.graph else f"rmat scale {args.scale} ef {args.edge_factor:g} suite"), "V": g.V, "E": g.E,
-           "sources": NSRC, "global_batch": 1, "parallelism": "host threads", "l2": "inputs > L2"}
-    line = base_line(args, 1, value, 1e3 * total / args.steps, cfg)
+    line = base_line(args, 1, value, 1e3 * total / args.steps, suite_config(args, g, 1))
     line["impl"] = "reference"
     line["cpu_baseline"] = {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
                             "sample": "full suite per step (16 sources of BFS/SSSP/BC, MIS, "
@@ -465,18 +578,24 @@ def run_gdb(args, rank, world, local):
     value = world * units_per_step * args.steps / (ms / 1e3)
     clocks = clk.summary()
 
-    # the plain schedule on the schedule-dependent apps, for comparison
-    plain_ms = None
+    # the whole suite under the plain schedule, timed the same way, for
+    # comparison (only BFS and SSSP depend on the schedule)
+    plain = None
     if args.schedule != "plain" and any(a in apps for a in ("bfs", "sssp")):
         set_schedule(suite.ctx, "plain")
-        saved = suite.apps
-        suite.apps = [a for a in apps if a in ("bfs", "sssp")]
         suite.step_device({})
         prec: dict = {}
-        for _ in range(args.steps):
-            suite.step_device(prec)
-        plain_ms = {a: prec[a]["ms"] / args.steps for a in prec}
-        suite.apps = saved
+        torch.cuda.synchronize()
+        with torch.cuda.stream(suite.stream):
+            start.record(suite.stream)
+            for _ in range(args.steps):
+                suite.step_device(prec)
+            end.record(suite.stream)
+        torch.cuda.synchronize()
+        pms = reduce_max(start.elapsed_time(end), world)
+        plain = {"value": world * units_per_step * args.steps / (pms / 1e3),
+                 "ms_per_step": pms / args.steps,
+                 "per_app_ms": {a: prec[a]["ms"] / args.steps for a in prec}}
         set_schedule(suite.ctx, args.schedule)
 
     # roofline of every kernel, reported for the one with the largest time share
@@ -539,13 +658,15 @@ def run_gdb(args, rank, world, local):
                "kind": "port", "sample": "BFS, worklist SSSP and BC from one source plus MIS on the "
                                          f"same graph, serial CPU oracle ({dt:.1f} s)"}
 
+    # full-size parity of every app's output against the CPU oracle
+    parity = None
+    if not args.no_parity:
+        parity = suite_parity(suite, wl, os.cpu_count() or 1)
+
     if rank == 0:
-        cfg = {"workload": (f"file {args.graph} suite" if args.graph else f"rmat scale {args.scale} ef {args.edge_factor:g} suite"), "V": g.V,
-               "E": g.E, "sources": NSRC, "apps": apps, "global_batch": world,
-               "parallelism": f"replicas x{world}", "l2": "inputs > L2 (no flush)",
-               "block": suite.ctx.opt.block_size, "barrier": "xf", "lock": "lock-free poll",
-               "schedule": args.schedule}
-        line = base_line(args, world, value, ms / args.steps, cfg)
+        line = base_line(args, world, value, ms / args.steps, suite_config(args, g, world))
+        line["setup"] = {"block": suite.ctx.opt.block_size, "barrier": "xf",
+                         "lock": "lock-free poll", "schedule": args.schedule}
         line["clocks"] = clocks
         line["e2e"] = e2e
         line["roofline"] = roof
@@ -554,9 +675,13 @@ def run_gdb(args, rank, world, local):
         line["gpu_launches"] = sum(r["launches"] for r in rec.values())
         line["per_app_ms"] = {a: rec[a]["ms"] / args.steps for a in rec}
         line["schedule"] = args.schedule
-        line["plain_schedule_ms"] = plain_ms
+        line["plain_schedule"] = plain
         line["per_app_supersteps"] = {a: rec[a]["supersteps"] // args.steps for a in rec}
+        line["parity"] = parity
         print(json.dumps(line), flush=True)
+        if parity is not None and not all(v is True for k, v in parity.items() if k != "detail"):
+            print(f"PARITY FAILURE: {parity}", file=sys.stderr, flush=True)
+            sys.exit(3)
 
 
 def run_grid(args, rank, world, local):

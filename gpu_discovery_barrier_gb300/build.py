@@ -28,7 +28,10 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "lib"
 INCLUDE = ROOT / "include"
 ORACLE = ROOT / "oracle"
-REF_CHECKOUT = Path(os.environ.get("GDB_REFERENCE_DIR", "/root/reference"))
+# the reference checkout: GDB_REFERENCE_DIR, else a "reference" directory
+# beside the repository (where the development container keeps it); the
+# GPU host has neither and skips that build
+REF_CHECKOUT = Path(os.environ.get("GDB_REFERENCE_DIR") or ROOT.parent / "reference")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -93,12 +96,13 @@ def build_graphgen() -> Path:
 
 def build_oracle() -> Path:
     out = ORACLE / "_build" / "liboracle.so"
-    srcs = [ORACLE / "oracle.c", ORACLE / "oracle_dmr.c", ORACLE / "oracle.h"]
+    srcs = [ORACLE / "oracle.c", ORACLE / "oracle_dmr.c", ORACLE / "oracle_gen.c",
+            ORACLE / "oracle.h"]
     if _stale(out, srcs):
         out.parent.mkdir(parents=True, exist_ok=True)
         # no floating-point contraction: the same doubles on x86 and Arm hosts
         _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off",
-              *_openmp_flag("gcc"), str(ORACLE / "oracle.c"), str(ORACLE / "oracle_dmr.c"),
+              *_openmp_flag("gcc"), *(str(s) for s in srcs if s.suffix == ".c"),
               "-lm", "-o", str(out)])
     return out
 

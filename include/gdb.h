@@ -53,7 +53,7 @@ typedef enum {
 
 /* Inter-CTA barrier between supersteps. */
 typedef enum {
-  GDB_BARRIER_XF = 0,        /* discovery + XF master/slave flags (discovery.cl:177-238) */
+  GDB_BARRIER_XF = 0,        /* discovery + XF master/slave flags (discovery.cl:129-190) */
   GDB_BARRIER_GRID_SYNC = 1, /* cooperative launch + cooperative_groups grid.sync() */
   GDB_BARRIER_RELAUNCH = 2,  /* one launch per superstep, host reads the stop flag */
   GDB_BARRIER_XF_FIXED = 3,  /* XF over all launched CTAs, no discovery (gbar_cl.h:15-74);
@@ -161,7 +161,7 @@ int gdb_abi_version(void);
 
 /* ------------------------------------------- discovery protocol / barrier */
 /* Reset the device discovery context; replaces init_discovery_kernel_ctx
- * (code/discovery_protocol/api/discovery.h:10, kernel discovery.cl:242-250). */
+ * (code/discovery_protocol/api/discovery.h:10, kernel discovery.cl:194-202). */
 int gdb_init_discovery_kernel_ctx(gdb_ctx* ctx);
 /* Same with the skip flag (discovery.h:36): skip = 1 makes every launched CTA
  * participate without the protocol.  Only kernels capped at the occupancy
@@ -453,7 +453,9 @@ int gdb_server_destroy(gdb_server* s);
  * The first call on a device looks up that array's address and arms it, so
  * make that first call before any stream capture.  All calls share the
  * array: calls that overlap on the GPU (other streams, other threads) race
- * and must be serialised by the caller.  Synchronous. */
+ * and must be serialised by the caller.  Synchronous: every call waits
+ * for its stream and reads the run's status back to host memory before it
+ * returns. */
 #define GDB_NOALLOC_MAX_VERTICES (1u << 20)
 int gdb_bfs_noalloc(const uint32_t* d_row_ptr, const uint32_t* d_col, uint32_t V, uint64_t E,
                     uint32_t src, uint32_t* d_dist, void* cuda_stream);

@@ -76,7 +76,7 @@ struct __align__(128) DeviceCtx {
   } flat, flat_base;
 };
 
-// discovery_local_ctx (discovery.cl:67-71), in shared memory.
+// discovery_local_ctx (discovery.cl:19-23), in shared memory.
 struct LocalCtx {
   int id;             // participating_group_id
   int P;              // participating_group_size
@@ -90,7 +90,7 @@ struct LocalCtx {
 
 // XF release forms.
 enum XfRelease {
-  kXfPerSlave = 0,   // the master stores 0 into every slave's flag (discovery.cl:203-209)
+  kXfPerSlave = 0,   // the master stores 0 into every slave's flag (discovery.cl:155-161)
   kXfBroadcast = 1,  // slaves store a launch-unique epoch; one broadcast release word
   kXfCombined = 2,   // slaves add to 16 padded arrival counters; one generation word
   kXfFlat = 3,       // every CTA adds to one counter and waits for the barrier's count
@@ -209,7 +209,7 @@ __device__ __forceinline__ void lock_release(DeviceCtx* c, int kind) {
   }
 }
 
-// reset_kernel_context (discovery.cl:79-85): re-arm for the next launch.
+// reset_kernel_context (discovery.cl:31-37): re-arm for the next launch.
 // Called by the last CTA through while it holds the lock; the final release
 // of the lock words is the implicit unlock.
 __device__ __forceinline__ void reset_kernel_context(DeviceCtx* c) {
@@ -220,7 +220,7 @@ __device__ __forceinline__ void reset_kernel_context(DeviceCtx* c) {
   st_release(&c->lock_serving, 0);
 }
 
-// discovery_protocol_master (discovery.cl:90-136) with a mutex, executed by
+// discovery_protocol_master (discovery.cl:42-88) with a mutex, executed by
 // one thread per CTA.
 __device__ inline void protocol_master_locked(const DiscoveryArgs& a, LocalCtx* l) {
   DeviceCtx* c = a.ctx;
@@ -299,7 +299,7 @@ __device__ inline void protocol_master_lockfree(const DiscoveryArgs& a, LocalCtx
   }
 }
 
-// DISCOVERY_PROTOCOL (discovery.cl:261-274).  All threads of the CTA call
+// DISCOVERY_PROTOCOL (discovery.cl:213-226).  All threads of the CTA call
 // it; returns true for participating CTAs (the others must return).
 __device__ inline bool discover(const DiscoveryArgs& a, LocalCtx* l) {
   if (threadIdx.x == 0) {
@@ -332,7 +332,7 @@ __device__ inline bool discover(const DiscoveryArgs& a, LocalCtx* l) {
   return l->participating != 0;
 }
 
-// p_get_* (discovery.cl:160-174)
+// p_get_* (discovery.cl:112-126)
 __device__ __forceinline__ int p_get_group_id(const LocalCtx* l) { return l->id; }
 __device__ __forceinline__ int p_get_num_groups(const LocalCtx* l) { return l->P; }
 __device__ __forceinline__ int p_get_global_id(const LocalCtx* l) {
@@ -518,7 +518,7 @@ __device__ inline bool xf_barrier_flat(const DiscoveryArgs& a, LocalCtx* l, Hook
   return l->ok != 0;
 }
 
-// XF barrier (discovery.cl:177-238) over the participating CTAs.  Slave: one
+// XF barrier (discovery.cl:129-190) over the participating CTAs.  Slave: one
 // elected thread publishes its arrival in its own padded flag and spins
 // until released.  Master: each thread issues loads for all of its peers'
 // flags at once and retires the ones that arrived, so the wait costs one

@@ -69,8 +69,83 @@ def lib() -> C.CDLL:
         L.orc_dmr_count_bad.argtypes = [_f64p, _f64p, U32, _u32p, _u8p]
         L.orc_par_threads.restype = C.c_int
         L.orc_par_bfs.argtypes = [U32, _u32p, _u32p, U32, _u32p]
+        U64, PU32 = C.c_uint64, C.POINTER(C.POINTER(U32))
+        L.orc_gen_rmat.argtypes = [U32, C.c_double, C.c_double, C.c_double, C.c_double, U64,
+                                   PU32, PU32, C.POINTER(U64)]
+        L.orc_gen_free.argtypes = [P]
+        L.orc_gen_uniform_weights.argtypes = [U32, _u32p, _u32p, U64, U32, U32, _u32p]
+        L.orc_gen_permutation.argtypes = [U32, U64, _u32p]
+        L.orc_gen_unique_weights.restype = U64
+        L.orc_gen_unique_weights.argtypes = [U32, _u32p, _u32p, U64, _u32p]
+        L.orc_gen_sources.restype = U32
+        L.orc_gen_sources.argtypes = [U32, _u32p, U64, U32, _u32p]
         _ORC = L
     return _ORC
+
+
+class Graph:
+    """Plain CSR holder for graphs the oracle generates itself."""
+
+    def __init__(self, row_ptr: np.ndarray, col: np.ndarray, w: np.ndarray | None = None):
+        self.row_ptr, self.col, self.w = row_ptr, col, w
+
+    @property
+    def V(self) -> int:
+        return int(self.row_ptr.shape[0] - 1)
+
+    @property
+    def E(self) -> int:
+        return int(self.col.shape[0])
+
+    def degrees(self) -> np.ndarray:
+        return np.diff(self.row_ptr.astype(np.int64))
+
+    def with_weights(self, w: np.ndarray) -> "Graph":
+        return Graph(self.row_ptr, self.col, np.ascontiguousarray(w, dtype=np.uint32))
+
+
+def gen_rmat(V: int, edge_factor: float, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 1) -> Graph:
+    """The seeded R-MAT workload graph (oracle_gen.c), symmetric uint32 CSR."""
+    rp_p, col_p = C.POINTER(C.c_uint32)(), C.POINTER(C.c_uint32)()
+    E = C.c_uint64()
+    _check(lib().orc_gen_rmat(V, edge_factor, a, b, c, seed, C.byref(rp_p), C.byref(col_p),
+                              C.byref(E)), "gen_rmat")
+    try:
+        rp = np.ctypeslib.as_array(rp_p, shape=(V + 1,)).copy()
+        col = np.ctypeslib.as_array(col_p, shape=(max(E.value, 1),))[: E.value].copy()
+    finally:
+        lib().orc_gen_free(rp_p)
+        lib().orc_gen_free(col_p)
+    return Graph(rp, col)
+
+
+def gen_uniform_weights(g, lo: int, hi: int, seed: int) -> np.ndarray:
+    w = np.empty(max(g.E, 1), dtype=np.uint32)
+    lib().orc_gen_uniform_weights(g.V, g.row_ptr, _nz(g.col), seed, lo, hi, w)
+    return w[: g.E]
+
+
+def gen_unique_weights(g, seed: int) -> np.ndarray:
+    w = np.empty(max(g.E, 1), dtype=np.uint32)
+    lib().orc_gen_unique_weights(g.V, g.row_ptr, _nz(g.col), seed, w)
+    return w[: g.E]
+
+
+def gen_permutation(n: int, seed: int) -> np.ndarray:
+    out = np.empty(max(n, 1), dtype=np.uint32)
+    lib().orc_gen_permutation(n, seed, out)
+    return out[:n]
+
+
+def gen_priorities(n: int, seed: int) -> np.ndarray:
+    return gen_permutation(n, seed).astype(np.float32)
+
+
+def gen_sources(g, count: int, seed: int) -> np.ndarray:
+    out = np.empty(max(count, 1), dtype=np.uint32)
+    got = lib().orc_gen_sources(g.V, g.row_ptr, seed, count, out)
+    return out[:got]
 
 
 def _check(rc: int, what: str) -> None:

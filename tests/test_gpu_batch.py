@@ -107,3 +107,23 @@ def test_batch_rejects_bad_arguments():
         Unw = c.graph_batch(members, weights=False)
         with pytest.raises(gdb.GdbError):
             c.batch(Unw, [0], apps=gdb.BATCH_SSSP)   # SSSP without weights
+
+
+def test_full_mixed_batch_sampled_members():
+    """The benchmark's own batch at full size (512 members, V log-uniform
+    in [1e3, 1e6]): one captured replay, then every 16th member and the
+    last one against the oracle, BFS and SSSP bit-exact."""
+    members = gg.mixed_batch(512, 1000, 1_000_000, seed=1)
+    srcs = [g.meta["source"] for g in members]
+    with gdb.Ctx() as c:
+        U = c.graph_batch(members)
+        off = U.vertex_offset
+        with c.batch(U, [int(off[i]) + s for i, s in enumerate(srcs)]) as B:
+            B.run()
+            B.run()  # a replay of the captured graph
+            res = B.results()
+    sample = sorted(set(range(0, len(members), 16)) | {len(members) - 1})
+    for i in sample:
+        g, a, b = members[i], int(off[i]), int(off[i + 1])
+        assert np.array_equal(res["bfs"][a:b], oracle.bfs(g, srcs[i])), (i, g.name)
+        assert np.array_equal(res["sssp"][a:b], oracle.sssp_worklist(g, srcs[i])), (i, g.name)

@@ -30,7 +30,7 @@ def test_occupancy_test_discovers_coresident(lock):
 @pytest.mark.parametrize("lock", [gdb.LOCK_TICKET, gdb.LOCK_FREE])
 def test_protocol_self_resets(lock):
     """The last CTA re-arms the context, so launches need no re-init
-    (discovery.cl:80-84 / reset_kernel_context)."""
+    (discovery.cl:32-36 / reset_kernel_context)."""
     with gdb.Ctx(lock=lock) as c:
         fit = c.api_occupancy(128)
         for _ in range(3):

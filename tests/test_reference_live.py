@@ -40,7 +40,7 @@ def test_random_rmat(seed):
 def test_reference_discovery_on_threads(groups):
     """The reference's discovery protocol + XF barrier on host threads:
     participants get the ids 0..P-1, the barrier holds, and the last group
-    re-arms the context (discovery.cl:80-84)."""
+    re-arms the context (discovery.cl:32-36)."""
     R = O.ref()
     ids = np.empty(groups, np.int32)
     n, ok, err = C.c_int(), C.c_int(), C.c_int()
