@@ -66,7 +66,8 @@ def parse():
     p.add_argument("--graph", default=None,
                    help="rmat workload: run the suite on this .gr / DIMACS / METIS file instead "
                         "(undirected; its weights for SSSP when it has them)")
-    p.add_argument("--workload", choices=["rmat", "grid4096", "batch", "serve"], default="rmat",
+    p.add_argument("--workload", choices=["rmat", "grid4096", "batch", "serve", "relaunch"],
+                   default="rmat",
                    help="rmat: the R-MAT suite (default); grid4096: the barrier-bound "
                         "4096x4096 grid, BFS and SSSP from the corner per barrier kind")
     return p.parse_args()
@@ -616,12 +617,19 @@ def run_gdb(args, rank, world, local):
     per_app_roof = {a: round(app_roofline(a)[2] / peak, 4) for a in rec}
     dom = max(rec, key=lambda a: rec[a]["ms"])
     nbytes, launch_ms, achieved = app_roofline(dom)
-    traffic = None
+    # measured DRAM traffic per call (ncu, profiles/traffic.json) where it
+    # was captured: the HBM fraction those bytes give at the measured time
+    measured = {}
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists() and not args.graph and args.scale == 22 and args.edge_factor == 16:  # the captured workload
-        traffic = json.loads(tf.read_text()).get(dom)
-        if traffic is not None and dom in ("bfs", "sssp"):
-            traffic *= NSRC  # captured per single-source launch; a call runs NSRC of them
+        tj = json.loads(tf.read_text())
+        for a in rec:
+            if isinstance(tj.get(a), (int, float)):
+                # captured per single-source launch; a BFS / SSSP call runs NSRC of them
+                measured[a] = tj[a] * (NSRC if a in ("bfs", "sssp") else 1)
+    traffic = measured.get(dom)
+    per_app_traffic_frac = {a: round(measured[a] / (app_roofline(a)[1] / 1e3) / 1e9 / peak, 4)
+                            for a in measured}
     roof = {"bound": "hbm", "kernel": f"k_{dom}_xf", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
             "alg_bytes_per_launch": nbytes, "launch_ms": launch_ms, "traffic": traffic,
@@ -671,6 +679,7 @@ def run_gdb(args, rank, world, local):
         line["e2e"] = e2e
         line["roofline"] = roof
         line["per_app_hbm_frac"] = per_app_roof
+        line["per_app_hbm_frac_measured_traffic"] = per_app_traffic_frac
         line["cpu_baseline"] = cpu
         line["gpu_launches"] = sum(r["launches"] for r in rec.values())
         line["per_app_ms"] = {a: rec[a]["ms"] / args.steps for a in rec}
@@ -756,6 +765,80 @@ def run_grid(args, rank, world, local):
     line["plain_value"] = 2 * g.E / ((res["xf"]["bfs"]["ms"] + res["xf"]["sssp"]["ms"]) / 1e3)
     line["barrier_kinds"] = res
     if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_relaunch(args, rank, world, local):
+    """Persistent against relaunched supersteps, per app, on the R-MAT
+    suite graph: each app under the XF barrier (one persistent launch),
+    under GDB_BARRIER_RELAUNCH (one launch per superstep with the stop flag
+    read back, the reference's multi-kernel pattern) and under
+    GDB_BARRIER_RELAUNCH_GRAPH (the same launches from a CUDA-graph WHILE
+    node).  Outputs of the three forms are compared bit for bit (BC within
+    1e-4)."""
+    import torch
+
+    from gpu_discovery_barrier_gb300 import gdb
+
+    torch.cuda.set_device(local)
+    wl = make_workload(args.scale, args.edge_factor, args.graph)
+    g, src = wl["g"], [int(x) for x in wl["src"]]
+    kinds = {"xf": gdb.BARRIER_XF, "relaunch": gdb.BARRIER_RELAUNCH,
+             "relaunch_graph": gdb.BARRIER_RELAUNCH_GRAPH}
+    apps = {
+        "bfs": lambda c, G, Gu: c.bfs(G, src[0]),
+        "sssp": lambda c, G, Gu: c.sssp(G, src[0]),
+        "sssp_jacobi": lambda c, G, Gu: c.sssp_jacobi(G, src[0]),
+        "mis": lambda c, G, Gu: c.mis(G, wl["prio"]),
+        "color": lambda c, G, Gu: c.color(G, wl["prio"]),
+        "bc": lambda c, G, Gu: c.bc(G, src),
+    }
+    res, outs = {}, {}
+    for kname, kind in kinds.items():
+        with gdb.Ctx(barrier=kind) as c:
+            G = c.graph(g.row_ptr, g.col, wl["w"], symmetric=wl["symmetric"])
+            for app, fn in apps.items():
+                for _ in range(args.warmup):
+                    out = fn(c, G, None)
+                ms, st = [], None
+                for _ in range(args.steps):
+                    out = fn(c, G, None)
+                    st = c.last_stats()
+                    ms.append(st["kernel_ms"])
+                t = statistics.median(ms)
+                res.setdefault(app, {})[kname] = {"ms": t, "launches": st["launches"],
+                                                  "supersteps": st["supersteps"]}
+                outs.setdefault(app, {})[kname] = out
+    same = {}
+    for app, o in outs.items():
+        a = o["xf"]
+        if app == "bc":
+            fin = np.isfinite(a)
+            scale = np.maximum(np.abs(a[fin]), 1e-6 * max(1.0, float(np.abs(a[fin]).max())))
+            same[app] = all(bool(np.all(np.abs(o[k][fin].astype(np.float64) - a[fin]) <= 1e-4 * scale
+                                        + 1e-6)) for k in o)
+        else:
+            same[app] = all(np.array_equal(o[k], a) for k in o)
+    for app, r in res.items():
+        r["relaunch_over_xf"] = r["relaunch"]["ms"] / r["xf"]["ms"]
+        r["graph_over_xf"] = r["relaunch_graph"]["ms"] / r["xf"]["ms"]
+    total = {k: sum(res[a][k]["ms"] for a in res) for k in kinds}
+    # work units as in the suite: arcs out of the reached vertices for the
+    # traversals (BC: its 16 sources), every arc for Jacobi, MIS, colour
+    with gdb.Ctx() as c:
+        G = c.graph(g.row_ptr, g.col)
+        er = [reach(g, c.bfs(G, s))[1] for s in src]
+    units = 2 * er[0] + sum(er) + 3 * g.E
+    value = units / (total["xf"] / 1e3)
+    if rank == 0:
+        cfg = suite_config(args, g, world)
+        cfg["workload"] += " (persistent vs relaunched supersteps, per app)"
+        line = base_line(args, world, value, total["xf"], cfg)
+        line["metric"] = "edges/sec (per-app persistent XF vs relaunch vs graph relaunch)"
+        line["per_app"] = res
+        line["total_ms"] = total
+        line["identical_across_forms"] = same
+        line["gpu_launches"] = sum(res[a]["xf"]["launches"] for a in res)
         print(json.dumps(line), flush=True)
 
 
@@ -1013,6 +1096,8 @@ def main():
         run_batch(args, rank, world, local)
     elif args.workload == "serve":
         run_serve(args, rank, world, local)
+    elif args.workload == "relaunch":
+        run_relaunch(args, rank, world, local)
     else:
         run_gdb(args, rank, world, local)
     if world > 1:

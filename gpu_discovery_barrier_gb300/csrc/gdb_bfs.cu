@@ -698,6 +698,7 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
   c->last.kernel_ms = ms;
   c->last.edges_processed = hs[0];
   c->last.supersteps = (uint32_t)hs[1];
+  if (kind == GDB_BARRIER_RELAUNCH_GRAPH) c->last.launches = 1 + c->last.supersteps;  // init + levels
   return GDB_OK;
 }
 

@@ -21,6 +21,7 @@
 #include <algorithm>
 
 #include "gdb_internal.h"
+#include "gdb_relaunch.cuh"
 
 namespace {
 
@@ -42,14 +43,9 @@ struct MisWs {
 
 constexpr uint32_t kMisNone = 0xFFFFFFFFu;  // no arc in this lane's step
 
-template <class Sync>
-__device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisWs& ws, uint32_t* smem) {
-  const Warps W = warps_of(s.id(), s.P());
-  const bool leader = s.id() == 0 && threadIdx.x == 0;
-  const int lane = lane_id();
-  uint32_t* my = smem + (threadIdx.x & ~31u);
+// mis_kernel.cl:78-93 (init), run by every thread of the grid.
+__device__ __forceinline__ void mis_init(const GraphView& G, const Warps& W, const MisWs& ws, bool leader) {
   const uint32_t big = fkey(kMisBig);
-  // init kernel (mis_kernel.cl:78-93)
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.state[v] = -1;
     ws.s[v] = 0;
@@ -59,138 +55,160 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
     for (int i = 0; i < 3; ++i) ws.cursor[i] = ws.hcursor[i] = ws.flag[i] = 0;
     ws.stats[0] = ws.stats[1] = 0;
   }
+}
+
+// mis1 of round r (superstep t): every undecided vertex takes the minimum
+// priority key over its undecided neighbours; flag[t % 3] records whether
+// any vertex was still undecided.  Every thread of the grid calls it.
+__device__ __forceinline__ void mis_phase1(const GraphView& G, const MisWs& ws, uint32_t r, uint32_t t,
+                                           uint32_t* my, bool leader, unsigned long long& arcs) {
+  const int lane = lane_id();
+  const uint32_t big = fkey(kMisBig);
+  // flag[t % 3] is read after this superstep's barrier: clear the slot
+  // of superstep t - 2
+  const int cur = t % 3, old = (t + 1) % 3;
+  if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
+  bool undecided_seen = false;
+  // four 32-arc steps at once: the column, state and priority loads of
+  // the four are in flight together
+  sweep_light4(
+      G, &ws.cursor[cur],
+      [&](uint32_t v, bool in_range) {
+        const bool und = in_range && ld_cg(&ws.state[v]) == -1;
+        my[lane] = big;
+        undecided_seen |= und;
+        return und;
+      },
+      [&](const bool* valid, const int* owner, const uint32_t* arc) {
+        uint32_t u[4], k[4];
+        bool und[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          u[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
+          arcs += valid[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) und[j] = valid[j] && ld_cg(&ws.state[u[j]]) == -1;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) k[j] = und[j] ? fkey(__ldg(&ws.prio[u[j]])) : big;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (und[j] && k[j] < my[owner[j]]) atomicMin(&my[owner[j]], k[j]);
+      },
+      [&](uint32_t v, bool act) {
+        if (act) ws.mn[v] = my[lane];
+      });
+  uint32_t* hmn = pick(ws.hmn, r);
+  sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
+    // a heavy winner's own state is settled here (see mis2)
+    if (ld_cg(&ws.s[v]) == 2) {
+      if (lane == 0) ws.state[v] = -2;
+      return;
+    }
+    if (ld_cg(&ws.state[v]) != -1) return;
+    undecided_seen = true;
+    uint32_t m = big;
+    // a chunk (kChunk = 128 arcs) as four steps with their loads in flight
+    uint32_t u[4];
+    bool und[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t a = b + 32 * j + lane;
+      u[j] = a < e ? __ldg(&G.col[a]) : 0u;
+      arcs += a < e;
+      und[j] = a < e;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) und[j] = und[j] && ld_cg(&ws.state[u[j]]) == -1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (und[j]) m = min(m, fkey(__ldg(&ws.prio[u[j]])));
+    m = warp_min_u32(m);
+    if (lane == 0 && m < big) atomicMin(&hmn[h], m);
+  });
+  cta_or(undecided_seen, &ws.flag[cur], 1u);
+}
+
+// mis2 of round r (superstep t): strict local minima join the set and
+// decide their neighbours.  Every thread of the grid calls it.
+__device__ __forceinline__ void mis_phase2(const GraphView& G, const Warps& W, const MisWs& ws, uint32_t r,
+                                           uint32_t t, bool leader, unsigned long long& arcs) {
+  const int lane = lane_id();
+  const uint32_t big = fkey(kMisBig);
+  // flag[t % 3] is read after this superstep's barrier: clear the slot
+  // of superstep t - 2
+  const int cur = t % 3, old = (t + 1) % 3;
+  if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
+  // next round's heavy minima start from BIGNUM
+  for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) pick(ws.hmn, r + 1)[h] = big;
+  sweep_light4(
+      G, &ws.cursor[cur],
+      [&](uint32_t v, bool in_range) {
+        bool win = false;
+        if (in_range && ld_cg(&ws.state[v]) == -1 && fkey(__ldg(&ws.prio[v])) < ws.mn[v]) {
+          win = true;
+          ws.s[v] = 2;
+          ws.state[v] = -2;
+        }
+        return win;
+      },
+      [&](const bool* valid, const int*, const uint32_t* arc) {
+        uint32_t u[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          u[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
+          arcs += valid[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (valid[j] && ld_cg(&ws.state[u[j]]) == -1) ws.state[u[j]] = -2;
+      },
+      [](uint32_t, bool) {});
+  const uint32_t* hmn = pick(ws.hmn, r);
+  // A heavy winner is split over chunks: its own state stays -1 here so
+  // every chunk sees the same test; s = 2 marks it and mis1 of the next
+  // round settles its state (all its neighbours are decided by then, so
+  // nobody reads it in between).
+  sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
+    if (ld_cg(&ws.state[v]) != -1) return;
+    if (!(fkey(__ldg(&ws.prio[v])) < ld_cg(&hmn[h]))) return;
+    if (lane == 0) ws.s[v] = 2;
+    uint32_t u[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t a = b + 32 * j + lane;
+      u[j] = a < e ? __ldg(&G.col[a]) : kMisNone;
+      arcs += a < e;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (u[j] != kMisNone && ld_cg(&ws.state[u[j]]) == -1) ws.state[u[j]] = -2;
+  });
+}
+
+template <class Sync>
+__device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisWs& ws, uint32_t* smem) {
+  const Warps W = warps_of(s.id(), s.P());
+  const bool leader = s.id() == 0 && threadIdx.x == 0;
+  uint32_t* my = smem + (threadIdx.x & ~31u);
+  mis_init(G, W, ws, leader);
   if (!s.sync()) return;
   unsigned long long arcs = 0;
   uint32_t r = 0;
   uint32_t t = 0;  // cursor slot counter: two sweeps per round
   for (;; ++r) {
-    // ---- mis1: min over undecided neighbours
-    {
-      // flag[t % 3] is read after this superstep's barrier: clear the slot
-      // of superstep t - 2
-      const int cur = t % 3, old = (t + 1) % 3;
-      if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
-      bool undecided_seen = false;
-      // four 32-arc steps at once: the column, state and priority loads of
-      // the four are in flight together
-      sweep_light4(
-          G, &ws.cursor[cur],
-          [&](uint32_t v, bool in_range) {
-            const bool und = in_range && ld_cg(&ws.state[v]) == -1;
-            my[lane] = big;
-            undecided_seen |= und;
-            return und;
-          },
-          [&](const bool* valid, const int* owner, const uint32_t* arc) {
-            uint32_t u[4], k[4];
-            bool und[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              u[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
-              arcs += valid[j];
-            }
-#pragma unroll
-            for (int j = 0; j < 4; ++j) und[j] = valid[j] && ld_cg(&ws.state[u[j]]) == -1;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) k[j] = und[j] ? fkey(__ldg(&ws.prio[u[j]])) : big;
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-              if (und[j] && k[j] < my[owner[j]]) atomicMin(&my[owner[j]], k[j]);
-          },
-          [&](uint32_t v, bool act) {
-            if (act) ws.mn[v] = my[lane];
-          });
-      uint32_t* hmn = pick(ws.hmn, r);
-      sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
-        // a heavy winner's own state is settled here (see mis2)
-        if (ld_cg(&ws.s[v]) == 2) {
-          if (lane == 0) ws.state[v] = -2;
-          return;
-        }
-        if (ld_cg(&ws.state[v]) != -1) return;
-        undecided_seen = true;
-        uint32_t m = big;
-        // a chunk (kChunk = 128 arcs) as four steps with their loads in flight
-        uint32_t u[4];
-        bool und[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const uint32_t a = b + 32 * j + lane;
-          u[j] = a < e ? __ldg(&G.col[a]) : 0u;
-          arcs += a < e;
-          und[j] = a < e;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) und[j] = und[j] && ld_cg(&ws.state[u[j]]) == -1;
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-          if (und[j]) m = min(m, fkey(__ldg(&ws.prio[u[j]])));
-        m = warp_min_u32(m);
-        if (lane == 0 && m < big) atomicMin(&hmn[h], m);
-      });
-      cta_or(undecided_seen, &ws.flag[cur], 1u);
-      if (!s.sync()) return;
-      ++t;
-      if (cta_words<1>([&](unsigned long long* w) { w[0] = ld_cg(&ws.flag[cur]); })[0] == 0) break;
-    }
-    // ---- mis2: strict local minima join the set and decide their neighbours
-    {
-      // flag[t % 3] is read after this superstep's barrier: clear the slot
-      // of superstep t - 2
-      const int cur = t % 3, old = (t + 1) % 3;
-      if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
-      // next round's heavy minima start from BIGNUM
-      for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) pick(ws.hmn, r + 1)[h] = big;
-      sweep_light4(
-          G, &ws.cursor[cur],
-          [&](uint32_t v, bool in_range) {
-            bool win = false;
-            if (in_range && ld_cg(&ws.state[v]) == -1 && fkey(__ldg(&ws.prio[v])) < ws.mn[v]) {
-              win = true;
-              ws.s[v] = 2;
-              ws.state[v] = -2;
-            }
-            return win;
-          },
-          [&](const bool* valid, const int*, const uint32_t* arc) {
-            uint32_t u[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              u[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
-              arcs += valid[j];
-            }
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-              if (valid[j] && ld_cg(&ws.state[u[j]]) == -1) ws.state[u[j]] = -2;
-          },
-          [](uint32_t, bool) {});
-      const uint32_t* hmn = pick(ws.hmn, r);
-      // A heavy winner is split over chunks: its own state stays -1 here so
-      // every chunk sees the same test; s = 2 marks it and mis1 of the next
-      // round settles its state (all its neighbours are decided by then, so
-      // nobody reads it in between).
-      sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
-        if (ld_cg(&ws.state[v]) != -1) return;
-        if (!(fkey(__ldg(&ws.prio[v])) < ld_cg(&hmn[h]))) return;
-        if (lane == 0) ws.s[v] = 2;
-        uint32_t u[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const uint32_t a = b + 32 * j + lane;
-          u[j] = a < e ? __ldg(&G.col[a]) : kMisNone;
-          arcs += a < e;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-          if (u[j] != kMisNone && ld_cg(&ws.state[u[j]]) == -1) ws.state[u[j]] = -2;
-      });
-      if (!s.sync()) return;
-      ++t;
-    }
+    mis_phase1(G, ws, r, t, my, leader, arcs);
+    if (!s.sync()) return;
+    const int cur = t % 3;
+    ++t;
+    if (cta_words<1>([&](unsigned long long* w) { w[0] = ld_cg(&ws.flag[cur]); })[0] == 0) break;
+    mis_phase2(G, W, ws, r, t, leader, arcs);
+    if (!s.sync()) return;
+    ++t;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
-  if (lane == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
   if (leader) ws.stats[1] = r + 1;
 }
 
@@ -200,6 +218,42 @@ __global__ void __launch_bounds__(512, 3) k_mis_xf(DiscoveryArgs a, GraphView G,
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
   mis_body(s, G, ws, smem);
+}
+
+// Relaunch form (mis.cpp:314-364: one launch per phase, the stop flag read
+// back after each): control state s[0] = round, s[1] = superstep, s[2] =
+// phase (1: mis1, 2: mis2).
+__global__ void k_mis_rl_init(GraphView G, MisWs ws) {
+  mis_init(G, warps_of(blockIdx.x, gridDim.x), ws, blockIdx.x == 0 && threadIdx.x == 0);
+}
+
+__global__ void __launch_bounds__(512, 3) k_mis_rl_step(GraphView G, MisWs ws, StepCtl* ctl,
+                                                       cudaGraphConditionalHandle cond) {
+  __shared__ uint32_t smem[1024];
+  const StepCtl& st0 = step_state(ctl);
+  const uint32_t r = st0.s[0], t = st0.s[1], phase = st0.s[2];
+  const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long arcs = 0;
+  if (phase == 1)
+    mis_phase1(G, ws, r, t, smem + (threadIdx.x & ~31u), leader, arcs);
+  else
+    mis_phase2(G, warps_of(blockIdx.x, gridDim.x), ws, r, t, leader, arcs);
+  arcs = warp_add_u64(arcs);
+  if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  step_end(ctl, cond, [&](StepCtl& st) {
+    st.s[1] = t + 1;
+    if (phase == 1) {
+      if (__ldcg(&ws.flag[t % 3]) == 0) {
+        ws.stats[1] = r + 1;
+        return false;
+      }
+      st.s[2] = 2;
+    } else {
+      st.s[0] = r + 1;
+      st.s[2] = 1;
+    }
+    return true;
+  });
 }
 
 // ------------------------------------------------------------- colouring
@@ -325,20 +379,18 @@ __device__ __forceinline__ void push_ranges(const ColorWs& ws, RangeStage& st, u
   }
 }
 
-template <class Sync>
-__device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const ColorWs& ws, uint32_t* smem) {
-  const Warps W = warps_of(s.id(), s.P());
-  const bool leader = s.id() == 0 && threadIdx.x == 0;
-  const int lane = lane_id();
-  uint32_t* my = smem + (threadIdx.x & ~31u);
-  __shared__ uint2 rstage[kMaxGraphWarps][64];
-  unsigned long long arcs = 0, coloured = 0;
-  // -- superstep 0: color = -1; count the neighbours each vertex waits for
+// Superstep 0: every colour -1, the heavy vertices' counters 0.
+__device__ __forceinline__ void color_init(const GraphView& G, const Warps& W, const ColorWs& ws) {
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.color[v] = -1;
     if (is_heavy(G, v)) ws.cnt[v] = 0;
   }
-  if (!s.sync()) return;
+}
+
+// Superstep 1: count the neighbours each vertex waits for.
+__device__ __forceinline__ void color_count(const GraphView& G, const ColorWs& ws, uint32_t* my,
+                                            unsigned long long& arcs) {
+  const int lane = lane_id();
   // The same pass records, per arc v -> u, whether u waits for v, so that
   // the rounds test one byte indexed by the arc instead of loading u's
   // priority and degree after u itself.
@@ -414,8 +466,12 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
       if (lane == 0 && n) atomicAdd(&ws.cnt[v], n);
     });
   }
-  if (!s.sync()) return;
-  // -- superstep 1: vertices that wait for nobody take colour 1
+}
+
+// Superstep 2: vertices that wait for nobody take colour 1 (queue slot 1).
+__device__ __forceinline__ void color_first(const GraphView& G, const Warps& W, const ColorWs& ws, bool leader,
+                                            uint2 (*rstage)[64], unsigned long long& coloured) {
+  const int lane = lane_id();
   {
     RangeStage qs{rstage[threadIdx.x >> 5], pick(ws.q, 1), &ws.qcount[1], ws.qcap, ws.overflow};
     for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
@@ -433,105 +489,132 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
     qs.flush();
     if (leader) ws.cursor[2] = ws.hcursor[2] = 0;
   }
+}
+
+// Round r: the vertices coloured in round r (queue slot r % 3) count down
+// the neighbours waiting for them; false when the round has no entries.
+__device__ __forceinline__ bool color_round(const GraphView& G, const Warps& W, const ColorWs& ws, uint32_t r,
+                                            bool leader, uint2 (*rstage)[64], unsigned long long& arcs,
+                                            unsigned long long& coloured) {
+  const int lane = lane_id();
+  const int cur = r % 3, nxt = (r + 1) % 3, old = (r + 2) % 3;
+  // Light groups go to the warps in spread order (warp 0 of every CTA,
+  // then warp 1, ...: a small round covers every SM) and heavy chunks to
+  // the same order from its other end, so the two lists meet only when a
+  // round has more entries than the grid has warps.  In a small round
+  // (fewer light entries than two per warp) a warp's light entry is
+  // item `ls` and its heavy chunk item `hs`: both loads are issued before
+  // the round's counts are known, so they overlap the counts' round trip
+  // (entries past the counts are never used).
+  const uint32_t ls = W.spread, hs = W.nwarps - 1 - W.spread;
+  const uint2* q = pick(ws.q, r);
+  const uint4* hc = pick(ws.hc, r);
+  uint2 spec = make_uint2(0u, 0u);
+  if (lane == 0 && ls < ws.qcap) spec = __ldcg(&q[ls]);
+  const uint4 hspec = hs < ws.hcap ? ld_cg(&hc[hs]) : make_uint4(0u, 0u, 0u, 0u);
+  const unsigned long long* sc = cta_words<2>([&](unsigned long long* w) {
+    w[0] = ld_cg(&ws.qcount[cur]);
+    w[1] = __ldcg(&ws.hcount[cur]);
+  });
+  const uint32_t n = (uint32_t)sc[0];
+  const unsigned long long hp = sc[1];
+  if (n == 0 && hp == 0) return false;
+  if (leader) {
+    ws.qcount[old] = 0;
+    ws.hcount[old] = 0;
+    ws.cursor[old] = 0;
+    ws.hcursor[old] = 0;
+  }
+  RangeStage qs{rstage[threadIdx.x >> 5], pick(ws.q, r + 1), &ws.qcount[nxt], ws.qcap,
+                ws.overflow};
+  uint4* hc_out = pick(ws.hc, r + 1);
+  unsigned long long* hcount_out = &ws.hcount[nxt];
+  const int32_t next_color = (int32_t)r + 1;
+  // up to four 32-arc steps at once: their column, wait-byte loads and
+  // count-downs are all in flight together (a round is a chain of
+  // dependent round trips, and thousands of rounds run one after another)
+  auto relax4 = [&](const bool* valid, const int*, const uint32_t* arc) {
+    uint32_t u[4];
+    uint8_t wa[4];
+#pragma unroll
+    for (int s4 = 0; s4 < 4; ++s4) {
+      u[s4] = valid[s4] ? __ldg(&G.col[arc[s4]]) : 0u;
+      wa[s4] = valid[s4] ? ws.waitarc[arc[s4]] : (uint8_t)0;
+      arcs += valid[s4];
+    }
+    uint32_t old4[4], rb[4], re[4];
+#pragma unroll
+    for (int s4 = 0; s4 < 4; ++s4) {
+      const bool w = wa[s4] & kWaits;
+      old4[s4] = w ? atomicSub(&ws.cnt[u[s4]], 1u) : 0u;
+      // the rows of a vertex this count-down may complete, loaded with it
+      rb[s4] = w ? __ldg(&G.row[u[s4]]) : 0u;
+      re[s4] = w ? __ldg(&G.row[u[s4] + 1]) : 0u;
+    }
+#pragma unroll
+    for (int s4 = 0; s4 < 4; ++s4) {
+      const bool ready = (wa[s4] & kWaits) && old4[s4] == 1u;
+      if (ready) {
+        ws.color[u[s4]] = next_color;
+        ++coloured;
+      }
+      push_ranges(ws, qs, hc_out, hcount_out, ready, wa[s4] & kHeavyT, u[s4], rb[s4], re[s4]);
+    }
+  };
+  const uint32_t k = group_width(n, W.nwarps);
+  WorkTaker lt((n + k - 1) / k, W.nwarps, ls, &ws.cursor[cur]);
+  bool first = k == 1;  // the first item taken is the warp's own, ls
+  for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
+    const uint32_t i = g * k + lane;
+    const bool act = (uint32_t)lane < k && i < n;
+    uint2 rg = make_uint2(0u, 0u);
+    if (act) rg = first ? spec : __ldcg(&q[i]);
+    first = false;
+    range_arcs4(rg.x, rg.y - rg.x, relax4);
+  }
+  const uint32_t nch = (uint32_t)hp;
+  WorkTaker ht(nch, W.nwarps, hs, &ws.hcursor[cur]);
+  first = true;  // the first chunk taken is the warp's own, hs
+  for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
+    const uint4 ent = first ? hspec : ld_cg(&hc[c]);
+    first = false;
+    const uint32_t b = ent.y, en = ent.z;  // the entry's arc range
+    // a chunk holds kChunk = 128 arcs: one four-step batch
+    static_assert(kChunk == 4 * 32, "a colour chunk is one batch of four steps");
+    bool valid[4];
+    uint32_t arc[4];
+#pragma unroll
+    for (int s4 = 0; s4 < 4; ++s4) {
+      arc[s4] = b + 32 * s4 + lane;
+      valid[s4] = arc[s4] < en;
+    }
+    relax4(valid, nullptr, arc);
+  }
+  qs.flush();
+  return true;
+}
+
+template <class Sync>
+__device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const ColorWs& ws, uint32_t* smem) {
+  const Warps W = warps_of(s.id(), s.P());
+  const bool leader = s.id() == 0 && threadIdx.x == 0;
+  uint32_t* my = smem + (threadIdx.x & ~31u);
+  __shared__ uint2 rstage[kMaxGraphWarps][64];  // per-warp queue staging
+  unsigned long long arcs = 0, coloured = 0;
+  color_init(G, W, ws);
+  if (!s.sync()) return;
+  // The count pass also records, per arc v -> u, whether u waits for v, so
+  // that the rounds test one byte indexed by the arc instead of loading u's
+  // priority and degree after u itself.
+  color_count(G, ws, my, arcs);
+  if (!s.sync()) return;
+  color_first(G, W, ws, leader, rstage, coloured);
   if (!s.sync()) return;
   // -- rounds: the vertices coloured in round r (queue slot r % 3) count
   // down the neighbours waiting for them
   uint32_t r = 1;
   for (;; ++r) {
-    const int cur = r % 3, nxt = (r + 1) % 3, old = (r + 2) % 3;
-    // Light groups go to the warps in spread order (warp 0 of every CTA,
-    // then warp 1, ...: a small round covers every SM) and heavy chunks to
-    // the same order from its other end, so the two lists meet only when a
-    // round has more entries than the grid has warps.  In a small round
-    // (fewer light entries than two per warp) a warp's light entry is
-    // item `ls` and its heavy chunk item `hs`: both loads are issued before
-    // the round's counts are known, so they overlap the counts' round trip
-    // (entries past the counts are never used).
-    const uint32_t ls = W.spread, hs = W.nwarps - 1 - W.spread;
-    const uint2* q = pick(ws.q, r);
-    const uint4* hc = pick(ws.hc, r);
-    uint2 spec = make_uint2(0u, 0u);
-    if (lane == 0 && ls < ws.qcap) spec = __ldcg(&q[ls]);
-    const uint4 hspec = hs < ws.hcap ? ld_cg(&hc[hs]) : make_uint4(0u, 0u, 0u, 0u);
-    const unsigned long long* sc = cta_words<2>([&](unsigned long long* w) {
-      w[0] = ld_cg(&ws.qcount[cur]);
-      w[1] = __ldcg(&ws.hcount[cur]);
-    });
-    const uint32_t n = (uint32_t)sc[0];
-    const unsigned long long hp = sc[1];
-    if (n == 0 && hp == 0) break;
-    if (leader) {
-      ws.qcount[old] = 0;
-      ws.hcount[old] = 0;
-      ws.cursor[old] = 0;
-      ws.hcursor[old] = 0;
-    }
-    RangeStage qs{rstage[threadIdx.x >> 5], pick(ws.q, r + 1), &ws.qcount[nxt], ws.qcap,
-                  ws.overflow};
-    uint4* hc_out = pick(ws.hc, r + 1);
-    unsigned long long* hcount_out = &ws.hcount[nxt];
-    const int32_t next_color = (int32_t)r + 1;
-    // up to four 32-arc steps at once: their column, wait-byte loads and
-    // count-downs are all in flight together (a round is a chain of
-    // dependent round trips, and thousands of rounds run one after another)
-    auto relax4 = [&](const bool* valid, const int*, const uint32_t* arc) {
-      uint32_t u[4];
-      uint8_t wa[4];
-#pragma unroll
-      for (int s4 = 0; s4 < 4; ++s4) {
-        u[s4] = valid[s4] ? __ldg(&G.col[arc[s4]]) : 0u;
-        wa[s4] = valid[s4] ? ws.waitarc[arc[s4]] : (uint8_t)0;
-        arcs += valid[s4];
-      }
-      uint32_t old4[4], rb[4], re[4];
-#pragma unroll
-      for (int s4 = 0; s4 < 4; ++s4) {
-        const bool w = wa[s4] & kWaits;
-        old4[s4] = w ? atomicSub(&ws.cnt[u[s4]], 1u) : 0u;
-        // the rows of a vertex this count-down may complete, loaded with it
-        rb[s4] = w ? __ldg(&G.row[u[s4]]) : 0u;
-        re[s4] = w ? __ldg(&G.row[u[s4] + 1]) : 0u;
-      }
-#pragma unroll
-      for (int s4 = 0; s4 < 4; ++s4) {
-        const bool ready = (wa[s4] & kWaits) && old4[s4] == 1u;
-        if (ready) {
-          ws.color[u[s4]] = next_color;
-          ++coloured;
-        }
-        push_ranges(ws, qs, hc_out, hcount_out, ready, wa[s4] & kHeavyT, u[s4], rb[s4], re[s4]);
-      }
-    };
-    const uint32_t k = group_width(n, W.nwarps);
-    WorkTaker lt((n + k - 1) / k, W.nwarps, ls, &ws.cursor[cur]);
-    bool first = k == 1;  // the first item taken is the warp's own, ls
-    for (uint32_t g = lt.take(); g < lt.n; g = lt.take()) {
-      const uint32_t i = g * k + lane;
-      const bool act = (uint32_t)lane < k && i < n;
-      uint2 rg = make_uint2(0u, 0u);
-      if (act) rg = first ? spec : __ldcg(&q[i]);
-      first = false;
-      range_arcs4(rg.x, rg.y - rg.x, relax4);
-    }
-    const uint32_t nch = (uint32_t)hp;
-    WorkTaker ht(nch, W.nwarps, hs, &ws.hcursor[cur]);
-    first = true;  // the first chunk taken is the warp's own, hs
-    for (uint32_t c = ht.take(); c < nch; c = ht.take()) {
-      const uint4 ent = first ? hspec : ld_cg(&hc[c]);
-      first = false;
-      const uint32_t b = ent.y, en = ent.z;  // the entry's arc range
-      // a chunk holds kChunk = 128 arcs: one four-step batch
-      static_assert(kChunk == 4 * 32, "a colour chunk is one batch of four steps");
-      bool valid[4];
-      uint32_t arc[4];
-#pragma unroll
-      for (int s4 = 0; s4 < 4; ++s4) {
-        arc[s4] = b + 32 * s4 + lane;
-        valid[s4] = arc[s4] < en;
-      }
-      relax4(valid, nullptr, arc);
-    }
-    qs.flush();
+    if (!color_round(G, W, ws, r, leader, rstage, arcs, coloured)) break;
     if (!s.sync()) return;
   }
 #pragma unroll
@@ -539,8 +622,8 @@ __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const Co
     arcs += __shfl_xor_sync(kFull, arcs, o);
     coloured += __shfl_xor_sync(kFull, coloured, o);
   }
-  if (lane == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
-  if (lane == 0 && coloured) atomicAdd(&ws.stats[2], coloured);
+  if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  if (lane_id() == 0 && coloured) atomicAdd(&ws.stats[2], coloured);
   if (leader) ws.stats[1] = r - 1;
 }
 
@@ -553,6 +636,48 @@ __global__ void __launch_bounds__(512, 1) k_color_xf(DiscoveryArgs a, GraphView 
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
   color_body(s, G, ws, smem);
+}
+
+// Relaunch form (color.cpp:294-334: one launch per superstep, the stop
+// flag read back after each): control state s[0] = superstep kind (0:
+// count pass, 1: colour 1, 2: round s[1]).
+__global__ void k_color_rl_init(GraphView G, ColorWs ws) {
+  color_init(G, warps_of(blockIdx.x, gridDim.x), ws);
+}
+
+__global__ void __launch_bounds__(512, 1) k_color_rl_step(GraphView G, ColorWs ws, StepCtl* ctl,
+                                                         cudaGraphConditionalHandle cond) {
+  __shared__ uint32_t smem[1024];
+  __shared__ uint2 rstage[kMaxGraphWarps][64];
+  const StepCtl& st0 = step_state(ctl);
+  const uint32_t kind = st0.s[0], r = st0.s[1];
+  const Warps W = warps_of(blockIdx.x, gridDim.x);
+  const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long arcs = 0, coloured = 0;
+  if (kind == 0)
+    color_count(G, ws, smem + (threadIdx.x & ~31u), arcs);
+  else if (kind == 1)
+    color_first(G, W, ws, leader, rstage, coloured);
+  else
+    color_round(G, W, ws, r, leader, rstage, arcs, coloured);
+  arcs = warp_add_u64(arcs);
+  coloured = warp_add_u64(coloured);
+  if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  if (lane_id() == 0 && coloured) atomicAdd(&ws.stats[2], coloured);
+  step_end(ctl, cond, [&](StepCtl& st) {
+    if (kind == 0) {
+      st.s[0] = 1;
+      return true;
+    }
+    // the next round's entries (slot r + 1), filled by this superstep
+    const uint32_t nr = kind == 1 ? 1u : r + 1;
+    const int nx = nr % 3;
+    const bool more = __ldcg(&ws.qcount[nx]) != 0 || __ldcg(&ws.hcount[nx]) != 0;
+    st.s[0] = 2;
+    st.s[1] = nr;
+    if (!more) ws.stats[1] = nr - 1;
+    return more;
+  });
 }
 
 }  // namespace
@@ -597,12 +722,41 @@ static int launch_xf(gdb_ctx* c, K kernel, const GraphView& G, const Ws& ws, uns
   return GDB_OK;
 }
 
+// Relaunch forms: init once, then one step launch per superstep until the
+// step kernels stop (at most `cap` launches); d_stats as for launch_xf.
+template <class KI, class KS, class Ws>
+static int launch_steps(gdb_ctx* c, KI init, KS step, const GraphView& G, const Ws& ws,
+                        unsigned long long* d_stats, StepCtl* ctl, const StepCtl& first,
+                        unsigned long long cap, int default_ctas = 0) {
+  const int block = c->opt.block_size;
+  int grid = 0;
+  int rc = step_grid(c, (const void*)step, block, &grid);
+  if (rc) return rc;
+  if (default_ctas > 0 && c->opt.max_ctas == 0) grid = std::min(grid, default_ctas);
+  c->last = gdb_run_stats{};
+  rc = step_run(c, c->opt.barrier, (const void*)init, (const void*)step, grid, block, ctl, first, cap,
+                true, G, ws);
+  if (rc) return rc;
+  unsigned long long* hs = (unsigned long long*)pinned(c, 64);
+  if (!hs) return GDB_ERR_OOM;
+  GDB_CUDA(c, cudaMemcpyAsync(hs, d_stats, 16, cudaMemcpyDeviceToHost, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->last.edges_processed = hs[0];
+  c->last.supersteps = (uint32_t)hs[1];
+  return GDB_OK;
+}
+
+static bool relaunch_kind(const gdb_ctx* c) {
+  return c->opt.barrier == GDB_BARRIER_RELAUNCH || c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH;
+}
+
 static int mis_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_s) {
   if (!graph_ok(c, g) || !d_prio || !d_s) return GDB_ERR_INVALID;
   const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
   Bump b;
   const size_t o_state = b.take((size_t)g->V * 4), o_mn = b.take((size_t)g->V * 4);
   const size_t o_h0 = b.take(hcap * 4), o_h1 = b.take(hcap * 4), o_cnt = b.take(256);
+  const size_t o_ctl = b.take(sizeof(StepCtl));
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
   MisWs ws;
@@ -617,6 +771,13 @@ static int mis_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_s) 
   ws.cursor = (uint32_t*)(cnt + 64);
   ws.hcursor = (uint32_t*)(cnt + 80);
   ws.flag = (uint32_t*)(cnt + 96);
+  // a round decides at least one vertex: at most V rounds of two phases
+  if (relaunch_kind(c)) {
+    StepCtl first{};
+    first.s[2] = 1;  // round 0 starts with mis1
+    return launch_steps(c, k_mis_rl_init, k_mis_rl_step, g->view(), ws, ws.stats, (StepCtl*)(base + o_ctl),
+                        first, 2ull * g->V + 4);
+  }
   return launch_xf(c, k_mis_xf, g->view(), ws, ws.stats);
 }
 
@@ -630,6 +791,7 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
   const size_t o_wa = b.take(std::max<uint64_t>(g->E, 1));
   const size_t o_cnt = b.take(512);
+  const size_t o_ctl = b.take(sizeof(StepCtl));
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
   ColorWs ws;
@@ -655,7 +817,11 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   // colours (thousands of small rounds on power-law graphs): latency-bound,
   // and faster on one CTA per SM (R-MAT-22: 42.8 ms against 47.4 ms on all
   // 456 co-resident CTAs)
-  int rc = launch_xf(c, k_color_xf, g->view(), ws, ws.stats, c->sm_count);
+  // relaunched: the count pass, colour 1 and at most V rounds
+  int rc = relaunch_kind(c) ? launch_steps(c, k_color_rl_init, k_color_rl_step, g->view(), ws, ws.stats,
+                                           (StepCtl*)(base + o_ctl), StepCtl{}, (unsigned long long)V + 4,
+                                           c->sm_count)
+                            : launch_xf(c, k_color_xf, g->view(), ws, ws.stats, c->sm_count);
   if (rc) return rc;
   unsigned long long* h = (unsigned long long*)pinned(c, 4096);
   GDB_CUDA(c, cudaMemcpy(h, cnt, 192, cudaMemcpyDeviceToHost));

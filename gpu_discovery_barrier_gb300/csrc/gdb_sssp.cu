@@ -38,6 +38,7 @@
 #include <algorithm>
 
 #include "gdb_internal.h"
+#include "gdb_relaunch.cuh"
 #include "gdb_selector.cuh"
 
 namespace {
@@ -523,9 +524,11 @@ __global__ void __launch_bounds__(512, 2) k_sssp_grid(GraphView G, GraphView GH,
   sssp_body(s, G, GH, GT, ws, src, smin);
 }
 
-// Graph-relaunch mode (CUDA-graph WHILE node): an init launch, then one
-// launch per superstep; the last CTA of a superstep advances ctl[0] and
-// sets the loop condition.
+// Relaunch modes: an init launch, then one launch per superstep; the last
+// CTA of a superstep advances ctl[0] and publishes whether another
+// superstep follows -- as the loop condition of a CUDA-graph WHILE node
+// (ctl[2] == 0) or as the stop word ctl[3] that the host loop reads back
+// (ctl[2] == 1).
 __global__ void k_sssp_init(GraphView G, SsspWs ws, uint32_t src) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, n = gridDim.x * blockDim.x;
   for (uint32_t v = t; v < G.V; v += n) {
@@ -577,8 +580,9 @@ __global__ void __launch_bounds__(512, 3) k_sssp_glevel(GraphView G, SsspWs ws, 
       const bool more = ld_cg(&ws.qcount[nxt]) != 0 || __ldcg(&ws.hcount[nxt]) != 0;
       ctl[0] = L + 1;
       ctl[1] = 0;
+      ctl[3] = more ? 0u : 1u;
       ws.stats[1] = L + 1;
-      cudaGraphSetConditional(cond, more ? 1u : 0u);
+      if (ctl[2] == 0) cudaGraphSetConditional(cond, more ? 1u : 0u);
     }
   }
 }
@@ -696,6 +700,42 @@ __global__ void __launch_bounds__(512, 3) k_jacobi_xf(DiscoveryArgs a, GraphView
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
   jacobi_body(s, G, ws, src, smin);
+}
+
+// Relaunch form (sssp.cpp:290-344: one launch per iteration, the stop flag
+// read back after it): vector_init, then one jacobi_iter per launch; the
+// control block holds the iteration number k.
+__global__ void k_jacobi_rl_init(GraphView G, JacobiWs ws, uint32_t src) {
+  const Warps W = warps_of(blockIdx.x, gridDim.x);
+  for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
+    const int32_t init = v == src ? 0 : GDB_PANNOTIA_BIG;
+    ws.x[0][v] = init;
+    ws.x[1][v] = init;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    for (int i = 0; i < 3; ++i) ws.cursor[i] = ws.hcursor[i] = ws.changed[i] = 0;
+    ws.stats[0] = ws.stats[1] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(512, 3) k_jacobi_rl_step(GraphView G, JacobiWs ws, uint32_t src,
+                                                          StepCtl* ctl, cudaGraphConditionalHandle cond) {
+  __shared__ int smin[1024];
+  const uint32_t k = step_state(ctl).s[0];
+  const int cur = k % 3, old = (k + 1) % 3;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ws.cursor[old] = ws.hcursor[old] = ws.changed[old] = 0;
+  unsigned long long arcs = 0;
+  const bool ch = jacobi_iter(G, ws, k, smin, arcs);
+  cta_or(ch, &ws.changed[cur], 1u);
+  arcs = warp_add_u64(arcs);
+  if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
+  step_end(ctl, cond, [&](StepCtl& st) {
+    const uint32_t k1 = st.s[0] + 1;  // iterations run
+    st.s[0] = k1;
+    ws.stats[1] = k1;
+    // the reference's loop: k = 1 .. num_rows-1 while something changed
+    return __ldcg(&ws.changed[cur]) != 0 && k1 + 1 < G.V;
+  });
 }
 
 // Sum, count and maximum of the usable weights (< kInf), for the automatic
@@ -930,13 +970,13 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   if (!graph_ok(c, g) || !d_dist || (nsrc && !d_srcs)) return GDB_ERR_INVALID;
   if (!nsrc && src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
   if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
-  if (nsrc && c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH)
+  // relaunched supersteps run the plain worklist
+  const bool relaunched = c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH || c->opt.barrier == GDB_BARRIER_RELAUNCH;
+  if (nsrc && relaunched)
     return set_error(c, GDB_ERR_UNSUPPORTED, "multi-source SSSP needs a persistent barrier");
   uint32_t delta = 0, light = kInf;
   bool relaunch = false;
-  int rc = c->opt.barrier == GDB_BARRIER_RELAUNCH_GRAPH
-               ? GDB_OK
-               : sssp_plan(c, g, nsrc ? nsrc : 1, nsrc == 0, &delta, &relaunch, &light);
+  int rc = relaunched ? GDB_OK : sssp_plan(c, g, nsrc ? nsrc : 1, nsrc == 0, &delta, &relaunch, &light);
   if (rc) return rc;
   char* base = (char*)workspace(c, sssp_layout(g, nullptr, nullptr, nullptr, nullptr));
   if (!base) return GDB_ERR_OOM;
@@ -991,16 +1031,46 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
     GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sssp_glevel, block, 0));
     int grid = occ * c->sm_count;
     if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
-    uint32_t* ctl = (uint32_t*)(cnt + 192);  // [0] superstep, [1] CTAs done
+    uint32_t* ctl = (uint32_t*)(cnt + 192);  // [0] superstep, [1] CTAs done, [2] host loop, [3] stop
+    GDB_CUDA(c, cudaMemsetAsync(ctl, 0, 16, c->stream));
     rc = graph_while_run(c, (const void*)k_sssp_init, grid, block, G, ws, src,
                          (const void*)k_sssp_glevel, ctl);
     if (rc) return rc;
     c->last.participating = grid;
     c->last.launched = grid;
+  } else if (kind == GDB_BARRIER_RELAUNCH) {
+    // the reference's host loop: one launch per superstep, the stop word
+    // read back after each
+    int occ = 0;
+    GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sssp_glevel, block, 0));
+    int grid = occ * c->sm_count;
+    if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
+    uint32_t* ctl = (uint32_t*)(cnt + 192);
+    uint32_t* h = (uint32_t*)pinned(c, 64);
+    if (!h) return GDB_ERR_OOM;
+    GDB_CUDA(c, cudaMemsetAsync(ctl, 0, 16, c->stream));
+    GDB_CUDA(c, cudaMemsetAsync(ctl + 2, 1, 1, c->stream));  // ctl[2] = 1: host loop
+    GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    k_sssp_init<<<grid, block, 0, c->stream>>>(G, ws, src);
+    GDB_CUDA(c, cudaGetLastError());
+    uint32_t launches = 1;
+    for (;;) {
+      k_sssp_glevel<<<grid, block, 0, c->stream>>>(G, ws, ctl, 0);
+      ++launches;
+      GDB_CUDA(c, cudaMemcpyAsync(h, ctl + 3, 4, cudaMemcpyDeviceToHost, c->stream));
+      GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (h[0]) break;
+    }
+    GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->last.participating = grid;
+    c->last.launched = grid;
+    c->last.launches = launches;
   } else {
     return set_error(c, GDB_ERR_UNSUPPORTED, "barrier kind not available for SSSP");
   }
-  c->last.launches = 1;
+  if (kind == GDB_BARRIER_XF || kind == GDB_BARRIER_XF_FIXED || kind == GDB_BARRIER_GRID_SYNC)
+    c->last.launches = 1;
   unsigned long long* hs = (unsigned long long*)pinned(c, 512);
   if (!hs) return GDB_ERR_OOM;
   GDB_CUDA(c, cudaMemcpyAsync(hs, cnt, 512, cudaMemcpyDeviceToHost, c->stream));
@@ -1011,6 +1081,7 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   c->last.kernel_ms = ms;
   c->last.edges_processed = hs[0];
   c->last.supersteps = (uint32_t)hs[1];
+  if (kind == GDB_BARRIER_RELAUNCH_GRAPH) c->last.launches = 1 + c->last.supersteps;  // init + supersteps
   c->last.phases = (uint32_t)hs[2];
   c->last.sssp_delta = delta;
   c->last.sssp_light = ws.light < kInf ? ws.light : 0u;
@@ -1021,11 +1092,14 @@ static int jacobi_run(gdb_ctx* c, gdb_graph* g, uint32_t src, int32_t* d_cost) {
   if (!graph_ok(c, g) || !d_cost) return GDB_ERR_INVALID;
   if (src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
   if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
-  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED)
-    return set_error(c, GDB_ERR_UNSUPPORTED, "Jacobi SSSP runs on the XF barrier");
+  const int kind = c->opt.barrier;
+  const bool relaunch = kind == GDB_BARRIER_RELAUNCH || kind == GDB_BARRIER_RELAUNCH_GRAPH;
+  if (kind != GDB_BARRIER_XF && kind != GDB_BARRIER_XF_FIXED && !relaunch)
+    return set_error(c, GDB_ERR_UNSUPPORTED, "Jacobi SSSP runs on the XF barrier or relaunched");
   Bump b;
   const size_t o_x = b.take((size_t)g->V * 4);
   const size_t o_cnt = b.take(256);
+  const size_t o_ctl = b.take(sizeof(StepCtl));
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
   JacobiWs ws;
@@ -1040,16 +1114,28 @@ static int jacobi_run(gdb_ctx* c, gdb_graph* g, uint32_t src, int32_t* d_cost) {
   const int block = c->opt.block_size;
   c->last = gdb_run_stats{};
   Shape s;
-  int rc = persistent_shape(c, (const void*)k_jacobi_xf, block, 0, &s,
-                            c->opt.barrier == GDB_BARRIER_XF);
-  if (rc) return rc;
-  DiscoveryArgs a = discovery_args(c, s);
-  GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-  k_jacobi_xf<<<s.grid, block, 0, c->stream>>>(a, G, ws, src);
-  GDB_CUDA(c, cudaGetLastError());
-  GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
-  rc = finish_run(c);
-  if (rc) return rc;
+  int rc = GDB_OK;
+  if (relaunch) {
+    int grid = 0;
+    if ((rc = step_grid(c, (const void*)k_jacobi_rl_step, block, &grid))) return rc;
+    StepCtl first{};
+    // at most num_rows - 1 iterations (sssp_kernel.cl:185)
+    rc = step_run(c, kind, (const void*)k_jacobi_rl_init, (const void*)k_jacobi_rl_step, grid, block,
+                  (StepCtl*)(base + o_ctl), first, (unsigned long long)g->V + 1, g->V >= 2, G, ws, src);
+    if (rc) return rc;
+    s.grid = grid;
+  } else {
+    rc = persistent_shape(c, (const void*)k_jacobi_xf, block, 0, &s, kind == GDB_BARRIER_XF);
+    if (rc) return rc;
+    DiscoveryArgs a = discovery_args(c, s);
+    GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    k_jacobi_xf<<<s.grid, block, 0, c->stream>>>(a, G, ws, src);
+    GDB_CUDA(c, cudaGetLastError());
+    GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    rc = finish_run(c);
+    if (rc) return rc;
+  }
+  const uint32_t launches = relaunch ? c->last.launches : 1;
   unsigned long long* hs = (unsigned long long*)pinned(c, 256);
   if (!hs) return GDB_ERR_OOM;
   GDB_CUDA(c, cudaMemcpyAsync(hs, cnt, 64, cudaMemcpyDeviceToHost, c->stream));
@@ -1062,11 +1148,11 @@ static int jacobi_run(gdb_ctx* c, gdb_graph* g, uint32_t src, int32_t* d_cost) {
   GDB_CUDA(c, cudaStreamSynchronize(c->stream));
   float ms = 0;
   GDB_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-  int n = 0;
-  read_participating(c, &n);
+  int n = s.grid;
+  if (!relaunch) read_participating(c, &n);
   c->last.participating = n;
   c->last.launched = s.grid;
-  c->last.launches = 1;
+  c->last.launches = launches;
   c->last.kernel_ms = ms;
   c->last.edges_processed = hs[0];
   c->last.supersteps = k;

@@ -74,7 +74,7 @@ def test_sssp_worklist(ctx, name, g):
         assert np.array_equal(got, oracle.sssp_worklist(gw, int(src))), (name, src)
 
 
-@pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC,
+@pytest.mark.parametrize("barrier", [gdb.BARRIER_XF, gdb.BARRIER_GRID_SYNC, gdb.BARRIER_RELAUNCH,
                                      gdb.BARRIER_RELAUNCH_GRAPH])
 def test_sssp_barrier_kinds(barrier):
     g = gg.grid(64, 64)
