@@ -391,6 +391,29 @@ def reduce_max(x: float, world: int) -> float:
     return float(t.item())
 
 
+def reduce_sum(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def my_members(n: int, rank: int, world: int, seed: int):
+    """This rank's members of the n-graph mixed batch: all of them on one
+    GPU; on several, a placement of whole graphs balanced by arcs."""
+    if world == 1:
+        return None
+    from gpu_discovery_barrier_gb300 import graphgen as gg, placement
+
+    spec = gg.mixed_batch_spec(n, 1000, 1_000_000, seed=seed)
+    return placement.place([m["arcs"] for m in spec], world)[rank]
+
+
 def barrier(world: int):
     if world > 1:
         import torch.distributed as dist
@@ -855,7 +878,9 @@ def run_batch(args, rank, world, local):
 
     torch.cuda.set_device(local)
     t0 = time.perf_counter()
-    members = gg.mixed_batch(args.batch_graphs, 1000, 1_000_000, seed=1 + rank)
+    # the same batch on every rank count: whole graphs placed over the GPUs
+    mine = my_members(args.batch_graphs, rank, world, seed=1)
+    members = gg.mixed_batch(args.batch_graphs, 1000, 1_000_000, seed=1, members=mine)
     gen_s = time.perf_counter() - t0
     srcs = [m.meta["source"] for m in members]
     V = sum(m.V for m in members)
@@ -925,8 +950,11 @@ def run_batch(args, rank, world, local):
             er = int(deg[reached].sum())
             vr = int(reached.sum())
             units = 2 * er
-            value = world * units * args.steps / (ms / 1e3)
-            plain_value = units / (plain_ms / 1e3)
+            # whole job: every rank's units over the slowest rank's time
+            units_all = reduce_sum(units, world)
+            value = units_all * args.steps / (ms / 1e3)
+            plain_value = units_all / (reduce_max(plain_ms, world) / 1e3)
+            identical = reduce_sum(0.0 if identical else 1.0, world) == 0.0
             # end to end through the host-buffer API: sources in, both
             # result arrays out, every step
             e2e = None
@@ -941,8 +969,9 @@ def run_batch(args, rank, world, local):
                     B.run()
                     B.results()
                 dt = reduce_max(time.perf_counter() - t1, world)
-                e2e = {"value": world * units * args.steps / dt, "unit": "edges/s",
-                       "h2d_bytes_per_step": 4 * len(usrc), "d2h_bytes_per_step": 8 * V}
+                e2e = {"value": units_all * args.steps / dt, "unit": "edges/s",
+                       "h2d_bytes_per_step": int(reduce_sum(4 * len(usrc), world)),
+                       "d2h_bytes_per_step": int(reduce_sum(8 * V, world))}
     # algorithmic bytes of one replay: BFS + SSSP over the reached part
     nbytes = (8 * er + 12 * vr + 4 * V) + (12 * er + 12 * vr + 4 * V)
     peak, peak_kind = peaks()
@@ -952,12 +981,15 @@ def run_batch(args, rank, world, local):
             "alg_bytes_per_launch": nbytes, "launch_ms": ms / args.steps, "traffic": None}
     cfg = {"workload": f"mixed batch: {len(members)} graphs (V log-uniform 1e3..1e6, half R-MAT "
                        "ef 8..32, half grids aspect 1..64), BFS + SSSP per graph",
-           "V": V, "E": E, "graphs": len(members), "global_batch": world,
-           "parallelism": f"replicas x{world}", "l2": "inputs > L2 (no flush)",
+           "V": int(reduce_sum(V, world)), "E": int(reduce_sum(E, world)),
+           "graphs": args.batch_graphs, "global_batch": 1,
+           "parallelism": (f"graph placement over {world} GPUs (balanced by arcs)" if world > 1
+                           else "one GPU"), "l2": "inputs > L2 (no flush)",
            "tuned": tune["options"] if tune else None, "generation_s": round(gen_s, 1)}
     if rank == 0:
         line = base_line(args, world, value, ms / args.steps, cfg)
         line["metric"] = "edges/sec (batched BFS + SSSP over the mixed batch)"
+        line["scaling"] = "strong"  # the same 512 graphs at every GPU count
         line["clocks"] = clocks
         line["e2e"] = e2e
         line["roofline"] = roof
@@ -965,7 +997,7 @@ def run_batch(args, rank, world, local):
         line["gpu_launches"] = 2 * args.steps
         line["plain"] = {"value": plain_value, "ms": plain_ms, "kernel_ms_sum": plain_kernel_ms,
                          "launches": 2 * len(members)}
-        line["speedup_vs_plain"] = value / world / plain_value
+        line["speedup_vs_plain"] = value / plain_value
         line["bit_identical"] = bool(identical)
         line["supersteps"] = {"bfs": steps_bfs, "sssp": steps_sssp}
         line["arcs_inspected"] = {"bfs": arcs_bfs, "sssp": arcs_sssp}
@@ -980,16 +1012,22 @@ def run_serve(args, rank, world, local):
     the same requests run alone."""
     import torch
 
-    from gpu_discovery_barrier_gb300 import gdb, graphgen as gg, selector
+    from gpu_discovery_barrier_gb300 import gdb, graphgen as gg, placement, selector
 
     torch.cuda.set_device(local)
-    members = gg.mixed_batch(64, 1000, 1_000_000, seed=3 + rank)
-    rng = np.random.default_rng(17 + rank)
+    # the same 64 graphs and request stream at every GPU count: each GPU
+    # keeps the graphs placed on it and serves the requests for them
+    ngraphs = 64
+    spec = gg.mixed_batch_spec(ngraphs, 1000, 1_000_000, seed=3)
+    mine = my_members(ngraphs, rank, world, seed=3) or list(range(ngraphs))
+    members = gg.mixed_batch(ngraphs, 1000, 1_000_000, seed=3, members=mine)
+    local_of = {gi: j for j, gi in enumerate(mine)}
+    rng = np.random.default_rng(17)
     n = args.requests
     gaps = rng.exponential(1.0 / args.rate, n)
-    graph_of = rng.integers(0, len(members), n)
+    graph_of = rng.integers(0, ngraphs, n)
     app_of = rng.integers(1, 4, n)
-    src_of = [int(rng.integers(members[i].V)) for i in graph_of]
+    src_of = [int(rng.integers(spec[i]["V"])) for i in graph_of]
     with gdb.Ctx() as c:
         set_schedule(c, args.schedule)
         Gs = [c.graph(m.row_ptr, m.col, m.w) for m in members]
@@ -1009,13 +1047,15 @@ def run_serve(args, rank, world, local):
                 sub = {}
                 for k in range(n):
                     due += gaps[k]
+                    if graph_of[k] not in local_of:
+                        continue  # another GPU's graph
                     while True:
                         now = time.perf_counter()
                         if now >= due:
                             break
                         if due - now > 2e-4:
                             time.sleep(due - now - 1e-4)
-                    rid, out = srv.submit(ids[graph_of[k]], int(app_of[k]), src_of[k])
+                    rid, out = srv.submit(ids[local_of[graph_of[k]]], int(app_of[k]), src_of[k])
                     sub[rid] = (k, out)
                 srv.drain(0)
                 wall = time.perf_counter() - t0
@@ -1045,7 +1085,7 @@ def run_serve(args, rank, world, local):
         set_schedule(c2, args.schedule)
         for d in done[:: max(1, len(done) // 24)]:
             k, out = sub[d["id"]]
-            m = members[graph_of[k]]
+            m = members[local_of[graph_of[k]]]
             G = c2.graph(m.row_ptr, m.col, m.w)
             app, src = d["app"], d["src"]
             if app == 1:
@@ -1061,27 +1101,43 @@ def run_serve(args, rank, world, local):
                     scale = np.maximum(np.abs(w), 1e-6 * max(1.0, float(np.abs(w).max())))
                     identical &= bool(np.all(np.abs(out[fin] - w) <= 1e-4 * scale + 1e-6))
             G.close()
-    cfg = {"workload": f"serving: {len(members)} resident graphs (mixed-batch distribution), "
+    # whole job: every rank's requests, the slowest rank's wall time, the
+    # latency percentiles over all requests
+    per_rank = placement.gather_results({rank: {
+        "lat": lat.tolist(), "run": run.tolist(), "queue": qms.tolist(), "ok": ok,
+        "identical": identical, "units": units,
+        "d2h": int(sum(members[local_of[graph_of[sub[d['id']][0]]]].V for d in done)) * 4}}, world)
+    wall = reduce_max(wall, world)
+    cfg = {"workload": f"serving: {ngraphs} resident graphs (mixed-batch distribution), "
                        f"BFS/SSSP/BC-single-source, Poisson {args.rate:g} req/s",
-           "requests": n, "slots": args.slots, "global_batch": world, "parallelism": f"replicas x{world}",
+           "requests": n, "slots": args.slots, "global_batch": 1,
+           "parallelism": (f"graph placement over {world} GPUs (balanced by arcs)" if world > 1
+                           else "one GPU"),
            "l2": "inputs > L2 (no flush)", "schedule": args.schedule}
-    value = world * units / wall
     if rank == 0:
+        parts = list(per_rank.values())
+        lat = np.concatenate([np.array(p["lat"]) for p in parts])
+        run = np.concatenate([np.array(p["run"]) for p in parts])
+        qms = np.concatenate([np.array(p["queue"]) for p in parts])
+        units = sum(p["units"] for p in parts)
+        value = units / wall
         line = base_line(args, world, value, 1e3 * wall / max(args.steps, 1), cfg)
         line["metric"] = "edges/sec (request loop, continuous batching)"
+        line["scaling"] = "strong"  # the same request stream at every GPU count
         line["steps"] = 1
         line["clocks"] = clocks
         line["e2e"] = {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 4 * n,
-                       "d2h_bytes_per_step": int(sum(members[graph_of[sub[d['id']][0]]].V for d in done)) * 4}
+                       "d2h_bytes_per_step": sum(p["d2h"] for p in parts)}
         line["roofline"] = None
         line["cpu_baseline"] = None
-        line["gpu_launches"] = len(done)
+        line["gpu_launches"] = int(lat.size)
         line["serving"] = {
-            "offered_rps": args.rate, "achieved_rps": len(done) / wall, "wall_s": wall,
+            "offered_rps": args.rate, "achieved_rps": lat.size / wall, "wall_s": wall,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "run_p50_ms": float(np.percentile(run, 50)),
             "run_p99_ms": float(np.percentile(run, 99)), "queue_p99_ms": float(np.percentile(qms, 99)),
-            "all_ok": ok, "alone_equals_mix_sample": identical}
+            "all_ok": all(p["ok"] for p in parts),
+            "alone_equals_mix_sample": all(p["identical"] for p in parts)}
         print(json.dumps(line), flush=True)
 
 

@@ -540,13 +540,25 @@ size_t gdbi::bfs_workspace_bytes(const gdb_graph* g) {
   return bfs_layout(g, nullptr, nullptr, nullptr, nullptr);
 }
 
-// BfsWs::adaptive for c's schedule; the learned one needs a loaded selector.
-static int bfs_mode(gdb_ctx* c, int* mode) {
+// Graphs whose vertices all have at most this many arcs run the
+// direction-optimising schedules as plain push.  A pull level scans every
+// unvisited vertex, a push level the frontier's arcs: with d <= 8 arcs per
+// vertex a pull can only pay once the unvisited vertices are fewer than
+// 8x the frontier, i.e. in the last few levels of a traversal, while the
+// per-level cost of the hooked kernel (the next frontier's degree loads,
+// the decision inside every barrier, the four-step batches) is paid on
+// every level: on the 4096^2 grid (8,191 levels) the learned BFS took
+// 91.9 ms against 51.0 ms push-only.
+constexpr uint32_t kPushOnlyMaxDeg = 8;
+
+// BfsWs::adaptive for c's schedule on g; the learned one needs a loaded
+// selector.
+static int bfs_mode(gdb_ctx* c, const gdb_graph* g, int* mode) {
   switch (c->opt.schedule) {
-    case GDB_SCHED_ADAPTIVE: *mode = kBfsHeuristic; return GDB_OK;
+    case GDB_SCHED_ADAPTIVE: *mode = g->maxdeg <= kPushOnlyMaxDeg ? kBfsPlain : kBfsHeuristic; return GDB_OK;
     case GDB_SCHED_LEARNED:
       if (!c->d_mlp) return set_error(c, GDB_ERR_INVALID, "learned schedule without a selector");
-      *mode = kBfsLearned;
+      *mode = g->maxdeg <= kPushOnlyMaxDeg ? kBfsPlain : kBfsLearned;
       return GDB_OK;
     default: *mode = kBfsPlain; return GDB_OK;
   }
@@ -562,7 +574,7 @@ int gdbi::bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_
   bfs_layout(g, (char*)wsbase, d_dist, &ws, &cnt);
   ws.srcs = d_srcs;
   ws.nsrc = nsrc;
-  int rc = bfs_mode(c, &ws.adaptive);
+  int rc = bfs_mode(c, g, &ws.adaptive);
   if (rc) return rc;
   ws.mlp = c->d_mlp;
   if (c->opt.pull_alpha) ws.alpha = c->opt.pull_alpha;
@@ -594,7 +606,7 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
   if (force >= 0) {
     ws.adaptive = force;
   } else {
-    int rc0 = bfs_mode(c, &ws.adaptive);
+    int rc0 = bfs_mode(c, g, &ws.adaptive);
     if (rc0) return rc0;
   }
   ws.mlp = c->d_mlp;
@@ -747,7 +759,7 @@ int gdb_bfs_sources_device(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, 
     return GDB_OK;
   }
   int mode = 0;
-  int rc = bfs_mode(c, &mode);
+  int rc = bfs_mode(c, g, &mode);
   if (rc) return rc;
   const int fit = traversal_occupancy(c, c->opt.block_size) * c->sm_count;
   return run_on_lanes(c, n, bfs_workspace_bytes(g), fit, [&](gdb_lane& L, uint32_t i) {

@@ -193,32 +193,52 @@ def _unit(seed: int, i: int, k: int) -> float:
     return (_splitmix64((seed << 40) ^ (i << 8) ^ k) >> 11) / float(1 << 53)
 
 
+def mixed_batch_spec(n: int, vmin: int = 1000, vmax: int = 1_000_000, seed: int = 1,
+                     max_aspect: float = 64.0) -> list[dict]:
+    """The shape of every member of mixed_batch(n, ...) without building it:
+    kind, V, edge factor (R-MAT) or rows x cols (grid), and the arcs the
+    member will hold (grids exactly, R-MAT the 2 x ef x V pairs before
+    de-duplication)."""
+    out = []
+    lo, hi = np.log(vmin), np.log(vmax)
+    for i in range(n):
+        V = int(round(np.exp(lo + _unit(seed, i, 0) * (hi - lo))))
+        if i % 2 == 0:
+            ef = 8 + int(_unit(seed, i, 1) * 25)
+            out.append({"i": i, "kind": "rmat", "V": V, "ef": ef, "arcs": 2 * ef * V})
+        else:
+            aspect = float(np.exp(_unit(seed, i, 2) * np.log(max_aspect)))
+            rows = max(1, int(round(np.sqrt(V / aspect))))
+            cols = max(1, int(round(V / rows)))
+            out.append({"i": i, "kind": "grid", "V": rows * cols, "rows": rows, "cols": cols,
+                        "arcs": 2 * (rows * (cols - 1) + cols * (rows - 1))})
+    return out
+
+
 def mixed_batch(n: int, vmin: int = 1000, vmax: int = 1_000_000, seed: int = 1,
-                max_aspect: float = 64.0) -> list[CSR]:
+                max_aspect: float = 64.0, members=None) -> list[CSR]:
     """The mixed batch workload: n graphs with vertex counts log-uniform in
     [vmin, vmax]; even members are R-MAT (edge factor uniform in 8..32,
     (a,b,c,d) = (0.57,0.19,0.19,0.05)), odd members 2-D grids whose aspect
     ratio is log-uniform in [1, max_aspect].  Each member carries weights
     (R-MAT uniform [1,255], grid uniform [1,1000]) and meta["source"], one
-    seeded non-isolated vertex."""
+    seeded non-isolated vertex.  `members`: build only these member indices
+    (in the order given), each identical to its copy in the full batch."""
     out = []
-    lo, hi = np.log(vmin), np.log(vmax)
-    for i in range(n):
-        V = int(round(np.exp(lo + _unit(seed, i, 0) * (hi - lo))))
+    spec = mixed_batch_spec(n, vmin, vmax, seed, max_aspect)
+    for i in (range(n) if members is None else members):
+        m = spec[i]
         gseed = (seed << 20) + i
-        if i % 2 == 0:
-            ef = 8 + int(_unit(seed, i, 1) * 25)
-            g = rmat(V, ef, seed=gseed)
+        if m["kind"] == "rmat":
+            g = rmat(m["V"], m["ef"], seed=gseed)
             w = uniform_weights(g, 1, 255, gseed)
         else:
-            aspect = float(np.exp(_unit(seed, i, 2) * np.log(max_aspect)))
-            rows = max(1, int(round(np.sqrt(V / aspect))))
-            cols = max(1, int(round(V / rows)))
-            g = grid(rows, cols)
+            g = grid(m["rows"], m["cols"])
             w = uniform_weights(g, 1, 1000, gseed)
         g = g.with_weights(w)
         s = sources(g, 1, gseed)
         g.meta["source"] = int(s[0]) if len(s) else 0
-        g.meta["kind"] = "rmat" if i % 2 == 0 else "grid"
+        g.meta["kind"] = m["kind"]
+        g.meta["member"] = i
         out.append(g)
     return out

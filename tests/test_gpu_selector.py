@@ -170,3 +170,23 @@ def test_learned_bfs_inspects_fewer_arcs():
         learned = c.last_stats()["edges_processed"]
     assert np.array_equal(got, oracle.bfs(g, 1))
     assert learned < 0.7 * plain, (learned, plain)
+
+
+@pytest.mark.parametrize("schedule", [gdb.SCHED_ADAPTIVE, gdb.SCHED_LEARNED])
+def test_bounded_degree_graphs_run_push_only(schedule):
+    """On a graph whose vertices have at most 8 arcs the direction-optimising
+    schedules run the plain push kernel (a pull level can pay only in the
+    last few levels, while the hooked kernel costs extra on every level):
+    the same arcs inspected as the plain schedule, the same levels."""
+    p = selector.load()
+    assert p is not None, "selector_weights.json missing"
+    g = gg.grid(300, 200)
+    with gdb.Ctx() as c:
+        c.selector_set(p)
+        G = c.graph(g.row_ptr, g.col)
+        want = c.bfs(G, 0)
+        plain = c.last_stats()["edges_processed"]
+        c.set_options(schedule=schedule)
+        got = c.bfs(G, 0)
+        assert c.last_stats()["edges_processed"] == plain
+    assert np.array_equal(got, want)
