@@ -48,7 +48,11 @@ CUDA_SOURCES = [
     "gdb_mlp.cu",
     "gdb_server.cu",
     "gdb_io.cu",
+    "gdb_dmr.cu",
 ]
+# per-file flags: the mesh refinement's double arithmetic must round as the
+# reference's does, operation for operation (no contraction into FMAs)
+CUDA_EXTRA = {"gdb_dmr.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -132,7 +136,7 @@ def build_cuda(jobs: int | None = None) -> Path:
         src = CSRC / name
         obj = objdir / (name + ".o")
         if _stale(obj, [src, *headers]):
-            _run([nvcc, *flags, "-c", str(src), "-o", str(obj)])
+            _run([nvcc, *flags, *CUDA_EXTRA.get(name, []), "-c", str(src), "-o", str(obj)])
         return obj
 
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:

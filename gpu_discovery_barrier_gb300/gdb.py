@@ -178,6 +178,8 @@ SIGNATURES = [
     ("gdb_server_drain", C.c_int, [_P, C.c_double]),
     ("gdb_server_destroy", C.c_int, [_P]),
     ("gdb_bfs_noalloc", C.c_int, [_P, _P, C.c_uint32, C.c_uint64, C.c_uint32, _P, _P]),
+    ("gdb_dmr_refine", C.c_int, [_P, _P, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, C.c_uint32,
+                                 _P, _P, _P, _P, _P, _P]),
 ]
 
 APP_BFS, APP_SSSP, APP_BC = 1, 2, 3
@@ -424,6 +426,25 @@ class Ctx:
         if with_arcs:
             out["arc_in_mst"] = flags[: g.E]
         return out
+
+    def dmr_refine(self, mesh, chunk: int, maxfactor: int = 20) -> dict:
+        """Delaunay mesh refinement of `mesh` (meshgen.Mesh: x, y, elements)
+        with `chunk` items per superstep; the refined mesh and its counts."""
+        x = np.ascontiguousarray(mesh.x, np.float64)
+        y = np.ascontiguousarray(mesh.y, np.float64)
+        el = np.ascontiguousarray(mesh.elements, np.uint32).reshape(-1)
+        nn, ne = x.size, el.size // 3
+        mn, me = (maxfactor // 2) * nn, maxfactor * ne
+        xo, yo = np.zeros(mn, np.float64), np.zeros(mn, np.float64)
+        elo, nbo = np.zeros(3 * me, np.uint32), np.zeros(3 * me, np.uint32)
+        delo, counts = np.zeros(me, np.uint8), np.zeros(5, np.uint32)
+        self.check(self._lib.gdb_dmr_refine(self.h, _ptr(x), _ptr(y), nn, _ptr(el), ne, maxfactor, chunk,
+                                            _ptr(xo), _ptr(yo), _ptr(elo), _ptr(nbo), _ptr(delo),
+                                            _ptr(counts)), "gdb_dmr_refine")
+        n, e = int(counts[0]), int(counts[1])
+        return {"x": xo[:n], "y": yo[:n], "elements": elo[:3 * e].reshape(e, 3),
+                "neighbours": nbo[:3 * e].reshape(e, 3), "isdel": delo[:e], "rounds": int(counts[2]),
+                "chunks": int(counts[3]), "refined": int(counts[4])}
 
     # -- schedule selector (no reference counterpart)
     def selector_set(self, params: np.ndarray | None) -> None:

@@ -440,6 +440,29 @@ int gdb_server_poll(gdb_server* s, gdb_request_info* info, uint32_t max, uint32_
 int gdb_server_drain(gdb_server* s, double timeout_s);
 int gdb_server_destroy(gdb_server* s);
 
+/* ---------------------------------------------- Delaunay mesh refinement */
+/* LonestarGPU DMR (lonestar_gpu_opencl/apps/dmr/dmr_port.cpp:160-316 host
+ * loop over the refine kernel, dmr_port_kernel.cl:37-188, and
+ * check_triangles, dmr_common.cl:144-187) as one persistent kernel over the
+ * XF barrier.  Input: nnodes coordinates, nelements triples (triangles
+ * counter-clockwise; a boundary segment's third node is GDB_DMR_SEGMENT).
+ * Refines until no triangle has an angle below 30 degrees, with capacity
+ * (maxfactor / 2) x nnodes nodes and maxfactor x nelements elements (the
+ * reference's meshfiles.h:27,67).  A round's worklist is processed in chunks
+ * of `chunk` items (1 .. GDB_DMR_MAX_CHUNK); the lowest item claiming an
+ * element owns it and the winners take slots in item order, so the result
+ * is deterministic and equals the same schedule run serially.  Outputs
+ * (host, sized to the capacities): node coordinates, elements, neighbour
+ * triples (GDB_DMR_SEGMENT = none), deleted flags; counts[5] = nodes,
+ * elements, rounds, chunks, refinements.  GDB_ERR_CAPACITY when the mesh
+ * outgrows the capacity or a cavity its slot. */
+#define GDB_DMR_SEGMENT 1234567890u
+#define GDB_DMR_MAX_CHUNK (1u << 16)
+int gdb_dmr_refine(gdb_ctx* ctx, const double* x, const double* y, uint32_t nnodes,
+                   const uint32_t* elements, uint32_t nelements, uint32_t maxfactor, uint32_t chunk,
+                   double* x_out, double* y_out, uint32_t* elements_out, uint32_t* neighbours_out,
+                   uint8_t* deleted_out, uint32_t* counts);
+
 /* -------------------------------------------- allocation-free BFS variant */
 /* No counterpart in the reference: an extra entry point for callers that
  * cannot allocate device memory (a host whose own pool owns the GPU's

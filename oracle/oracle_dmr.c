@@ -90,6 +90,14 @@ static void shared_edge(const uint32_t* e1, const uint32_t* e2, uint32_t* se) {
   if (!is_seg(e1) && has_node(e2, e1[2]) && sc < 2) se[sc++] = e1[2];
 }
 
+/* does neighbour n of triangle e share the edge facing node ob */
+static int faces(const Mesh* m, const uint32_t* e, uint32_t n, uint32_t ob) {
+  if (n == NONE) return 0;
+  uint32_t se[2];
+  shared_edge(e, m->el + 3 * (size_t)n, se);
+  return se[0] == ob || se[1] == ob;
+}
+
 /* opposite, dmr_common.cl:214-256: a triangle obtuse at some node hands its
  * refinement to the neighbour across the edge facing that node */
 static uint32_t opposite(const Mesh* m, uint32_t t) {
@@ -101,12 +109,13 @@ static uint32_t opposite(const Mesh* m, uint32_t t) {
   else if (angle_ob(m, e[1], e[2], e[0])) ob = e[0];
   else return t;
   const uint32_t* nb = m->nb + 3 * (size_t)t;
-  uint32_t se[2], cand = nb[0];
-  shared_edge(e, m->el + 3 * (size_t)nb[0], se);
-  if (se[0] == ob || se[1] == ob) {
+  uint32_t cand = nb[0];
+  /* a missing neighbour (NONE) shares no edge; the reference would read
+   * element NONE here, past its arrays, and the caller rejects a NONE
+   * hand-off instead */
+  if (faces(m, e, nb[0], ob)) {
     cand = nb[1];
-    shared_edge(e, m->el + 3 * (size_t)nb[1], se);
-    if (se[0] == ob || se[1] == ob) cand = nb[2];
+    if (faces(m, e, nb[1], ob)) cand = nb[2];
   }
   return cand;
 }
@@ -425,6 +434,7 @@ int orc_dmr_refine(const double* x0, const double* y0, uint32_t nnodes, const ui
         k->nc = 1;
         k->bc = 0;
         k->cav[0] = opposite(&m, ele);
+        if (k->cav[0] == NONE) { rc = -6; goto out; } /* an obtuse triangle facing no neighbour */
         int r = build_cavity(&m, k);
         if (r == 0) r = build_cavity(&m, k);
         if (r < 0) { rc = -5; goto out; }

@@ -3,9 +3,9 @@
 The restatement (oracle/oracle_dmr.c) is pinned against the reference's own
 kernels (dmr_port_kernel.cl, run through oracle/refshim) on meshes where the
 reference's refinement terminates, and shown to stop with a capacity error
-where the reference's runs past its arrays.  No GPU form is built: the
-reference refinement does not terminate on the synthetic meshes available
-here (see the DMR entry of the design notes).
+where the reference's runs past its arrays.  The GPU kernel
+(gdb_dmr_refine) is held to this restatement bit for bit in
+tests/test_gpu_dmr.py.
 """
 import numpy as np
 import pytest
