@@ -81,7 +81,63 @@ struct SsspWs {
   uint32_t* sqcount;
   unsigned long long* shcount;
   unsigned long long* sarcs;   // heavy arcs of the settle list's vertices
+  // direction of the settle supersteps (split only): kSettleRule -- the
+  // side with fewer heavy arcs; kSettleLearned -- the selector, evaluated
+  // at the start of each settle superstep; forced push / pull (settle
+  // traces)
+  int settle;
+  const float* mlp;
+  gdb_level_trace* trace;      // one record per settle superstep (nullable)
+  uint32_t trace_cap;
+  uint32_t maxdeg;
 };
+
+enum { kSettleRule = 0, kSettleLearned = 1, kSettlePush = 2, kSettlePull = 3 };
+
+// CTA 0's settle trace bookkeeping, in its shared memory.
+struct SettleState {
+  unsigned long long t0;  // start of the settle superstep of the open record
+  uint32_t k;             // settle supersteps recorded so far
+  uint32_t open;          // a record waits for its duration
+};
+
+__device__ __forceinline__ unsigned long long sssp_clock() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Direction of a settle superstep (1 = pull), chosen at its start by warp
+// 0 of every CTA from the counters every CTA has just read after the
+// barrier -- identical inputs and operations, so every CTA reaches the same
+// decision and no barrier waits for it: the network's cheaper output of
+// push / pull on the settle's features (decision kind 3), or the forced
+// mode of a trace run.  CTA 0 opens the trace record.
+__device__ __noinline__ uint32_t settle_choose(const GraphView& GH, const SsspWs& ws, const float* smlp,
+                                               SettleState* st, uint32_t phase, uint32_t sn, uint32_t hn,
+                                               unsigned long long an, uint32_t sdone, uint32_t hdone,
+                                               unsigned long long adone, uint32_t nwarps, bool master) {
+  const unsigned long long mf = an - adone;
+  const unsigned long long mu = GH.E > an ? GH.E - an : 0ull;
+  const float nf = (float)(sn - sdone) + (float)(hn - hdone);
+  float x[kFeat];
+  bfs_features(x, nf, (float)mf, (float)mu, (float)GH.V, (float)GH.E,
+               (float)(GH.V > sn ? GH.V - sn : 0u), phase, 3u, (float)ws.maxdeg, (float)nwarps);
+  uint32_t mode = ws.settle == kSettlePull ? 1u : 0u;
+  if (ws.settle == kSettleLearned) {
+    float out[kOut];
+    mlp_warp(smlp, x, out);
+    mode = out[kOutPull] < out[kOutPush] ? 1u : 0u;
+  }
+  if (master && threadIdx.x == 0 && ws.trace && st->k < ws.trace_cap) {
+    for (int i = 0; i < kFeat; ++i) ws.trace[st->k].x[i] = x[i];
+    ws.trace[st->k].mode = mode;
+    ws.trace[st->k].us = 0.f;
+    st->t0 = sssp_clock();
+    st->open = 1;
+  }
+  return mode;
+}
 
 // Warp-aggregated append of the lanes' `want` vertices to the far pile of
 // `phase` (each vertex at most once per pile, so V entries suffice).
@@ -390,13 +446,20 @@ __device__ __forceinline__ void far_filter(const GraphView& G, const Warps& W, c
 // G: the arcs near supersteps relax (all arcs, or the light half under
 // the split); GH: the heavy half the settle supersteps relax, GT the same
 // transposed (split only).
-template <class Sync>
+// Hooked: the settle direction comes from settle_choose (learned and trace
+// schedules); a separate instantiation keeps the plain kernels' registers.
+template <bool Hooked, class Sync>
 __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const GraphView& GH,
                                           const GraphView& GT, const SsspWs& ws, uint32_t src,
-                                          uint32_t* smin) {
+                                          uint32_t* smin, float* smlp, SettleState* sst) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
   const bool split_arcs = ws.light < kInf;
+  if constexpr (Hooked) {
+    if (ws.settle == kSettleLearned)
+      for (int i = threadIdx.x; i < kParams; i += blockDim.x) smlp[i] = __ldg(&ws.mlp[i]);
+    if (threadIdx.x == 0) *sst = SettleState{0, 0, 0};  // read after the first barrier
+  }
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.key[v] = (unsigned long long)kInf << 32;
     if (ws.delta) ws.farmark[v] = 0;
@@ -451,6 +514,14 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Gra
   for (;; ++L) {
     const int cur = L % 3, old = (L + 2) % 3;
     const unsigned long long* sc = step_counts(ws, cur, phase);
+    if constexpr (Hooked) {
+      // a settle superstep ended at the barrier just passed: its duration
+      if (s.id() == 0 && threadIdx.x == 0 && sst->open) {
+        if (sst->k < ws.trace_cap) ws.trace[sst->k].us = (float)(sssp_clock() - sst->t0) * 1e-3f;
+        sst->open = 0;
+        ++sst->k;
+      }
+    }
     const bool dry = sc[0] == 0 && sc[1] == 0;
     const uint32_t sn = (uint32_t)sc[4], hn = (uint32_t)sc[5];
     const bool unsettled = sn > sdone || hn > hdone;
@@ -467,7 +538,18 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Gra
       // every vertex's distance once)
       const unsigned long long an = sc[6];
       const unsigned long long open_arcs = GH.E > an ? GH.E - an : 0ull;
-      if (open_arcs + GH.V < an - adone) {
+      bool pull = open_arcs + GH.V < an - adone;
+      if constexpr (Hooked) {
+        __shared__ uint32_t sdir;
+        if (threadIdx.x < 32) {
+          const uint32_t d = settle_choose(GH, ws, smlp, sst, phase, sn, hn, an, sdone, hdone, adone,
+                                           W.nwarps, s.id() == 0);
+          if (threadIdx.x == 0) sdir = d;
+        }
+        __syncthreads();
+        pull = sdir != 0;
+      }
+      if (pull) {
         settle_pull(GT, W, ws, split, phase, smin, arcs);
       } else {
         sssp_sweep<true>(GH, GH, W, ws, L, split, phase, ws.sq + sdone, sn - sdone, ws.shc + hdone,
@@ -514,14 +596,25 @@ __global__ void __launch_bounds__(512, 2) k_sssp_xf(DiscoveryArgs a, GraphView G
   __shared__ uint32_t smin[512];
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
-  sssp_body(s, G, GH, GT, ws, src, smin);
+  sssp_body<false>(s, G, GH, GT, ws, src, smin, nullptr, nullptr);
+}
+
+__global__ void __launch_bounds__(512, 2) k_sssp_xf_sel(DiscoveryArgs a, GraphView G, GraphView GH,
+                                                         GraphView GT, SsspWs ws, uint32_t src) {
+  __shared__ LocalCtx l;
+  __shared__ uint32_t smin[512];
+  __shared__ float smlp[kParams];
+  __shared__ SettleState sst;
+  if (!discover(a, &l)) return;
+  XfSync s{&a, &l};
+  sssp_body<true>(s, G, GH, GT, ws, src, smin, smlp, &sst);
 }
 
 __global__ void __launch_bounds__(512, 2) k_sssp_grid(GraphView G, GraphView GH, GraphView GT,
                                                        SsspWs ws, uint32_t src) {
   __shared__ uint32_t smin[512];
   GridSync s;
-  sssp_body(s, G, GH, GT, ws, src, smin);
+  sssp_body<false>(s, G, GH, GT, ws, src, smin, nullptr, nullptr);
 }
 
 // Relaunch modes: an init launch, then one launch per superstep; the last
@@ -809,6 +902,11 @@ static size_t sssp_layout(const gdb_graph* g, char* base, uint32_t* d_dist, Sssp
   ws->sarcs = (unsigned long long*)(cnt + 272);
   ws->sq = (uint32_t*)(base + o_sq);
   ws->shc = (uint4*)(base + o_shc);
+  ws->settle = kSettleRule;
+  ws->mlp = nullptr;
+  ws->trace = nullptr;
+  ws->trace_cap = 0;
+  ws->maxdeg = g->maxdeg;
   ws->light = kInf;
   ws->qcap = V;
   ws->hcap = hcap;
@@ -940,6 +1038,14 @@ int gdbi::sssp_plan(gdb_ctx* c, gdb_graph* g, uint32_t nsrc, bool allow_relaunch
   return sssp_light_bound(c, g, *delta, light);
 }
 
+// Settle direction of a run (see SsspWs::settle): only the split has
+// settle supersteps; the learned schedule hands them to the selector.
+static int settle_of(const gdb_ctx* c, uint32_t light, int force) {
+  if (light >= kInf) return kSettleRule;
+  if (force >= 0) return force;
+  return c->opt.schedule == GDB_SCHED_LEARNED && c->d_mlp ? kSettleLearned : kSettleRule;
+}
+
 int gdbi::sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
                        uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto,
                        uint32_t delta, uint32_t light) {
@@ -954,19 +1060,25 @@ int gdbi::sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d
   ws.light = delta && light < kInf && g->split_l && g->split_bound == light ? light : kInf;
   GraphView GN, GH, GT;
   split_views(g, ws.light, &GN, &GH, &GT);
+  ws.settle = settle_of(c, ws.light, -1);
+  ws.mlp = c->d_mlp;
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, stream));
   Shape s;
-  int rc = persistent_shape(c, (const void*)k_sssp_xf, c->opt.block_size, 0, &s, false);
+  auto kx = ws.settle == kSettleRule ? k_sssp_xf : k_sssp_xf_sel;
+  int rc = persistent_shape(c, (const void*)kx, c->opt.block_size, 0, &s, false);
   if (rc) return rc;
   DiscoveryArgs a = proto;
   a.expected = std::min(s.grid, s.fit);
-  k_sssp_xf<<<s.grid, c->opt.block_size, 0, stream>>>(a, GN, GH, GT, ws, 0u);
+  kx<<<s.grid, c->opt.block_size, 0, stream>>>(a, GN, GH, GT, ws, 0u);
   GDB_CUDA(c, cudaGetLastError());
   return GDB_OK;
 }
 
+// force_settle >= 0: a fixed settle direction (trace runs), recording up to
+// trace_cap settle supersteps in d_trace.
 static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_srcs, uint32_t nsrc,
-                    uint32_t* d_dist) {
+                    uint32_t* d_dist, int force_settle = -1, gdb_level_trace* d_trace = nullptr,
+                    uint32_t trace_cap = 0) {
   if (!graph_ok(c, g) || !d_dist || (nsrc && !d_srcs)) return GDB_ERR_INVALID;
   if (!nsrc && src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
   if (!g->w) return set_error(c, GDB_ERR_INVALID, "SSSP needs weights");
@@ -989,20 +1101,26 @@ static int sssp_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_sr
   // the split lives in the persistent kernels only (graph relaunch runs
   // the plain worklist)
   ws.light = relaunch ? kInf : light;
+  const int kind = relaunch ? GDB_BARRIER_RELAUNCH_GRAPH : c->opt.barrier;
+  const bool xf = kind == GDB_BARRIER_XF || kind == GDB_BARRIER_XF_FIXED;
+  ws.settle = xf ? settle_of(c, ws.light, force_settle) : kSettleRule;
+  ws.mlp = c->d_mlp;
+  ws.trace = d_trace;
+  ws.trace_cap = trace_cap;
   const GraphView G = g->view();
   GraphView GN, GH, GT;
   split_views(g, ws.light, &GN, &GH, &GT);
   GDB_CUDA(c, cudaMemsetAsync(cnt, 0, 512, c->stream));
   const int block = c->opt.block_size;
-  const int kind = relaunch ? GDB_BARRIER_RELAUNCH_GRAPH : c->opt.barrier;
   c->last = gdb_run_stats{};
-  if (kind == GDB_BARRIER_XF || kind == GDB_BARRIER_XF_FIXED) {
+  if (xf) {
     Shape s;
-    rc = persistent_shape(c, (const void*)k_sssp_xf, block, 0, &s, kind == GDB_BARRIER_XF);
+    auto kx = ws.settle == kSettleRule ? k_sssp_xf : k_sssp_xf_sel;
+    rc = persistent_shape(c, (const void*)kx, block, 0, &s, kind == GDB_BARRIER_XF);
     if (rc) return rc;
     DiscoveryArgs a = discovery_args(c, s);
     GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    k_sssp_xf<<<s.grid, block, 0, c->stream>>>(a, GN, GH, GT, ws, src);
+    kx<<<s.grid, block, 0, c->stream>>>(a, GN, GH, GT, ws, src);
     GDB_CUDA(c, cudaGetLastError());
     GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     rc = finish_run(c);
@@ -1252,6 +1370,37 @@ int gdb_sssp_sources(gdb_ctx* c, gdb_graph* g, const uint32_t* sources, uint32_t
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) rc = set_cuda_error(c, e, "dist read-back");
   }
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
+int gdb_sssp_trace(gdb_ctx* c, gdb_graph* g, uint32_t src, int mode, uint32_t* dist,
+                   gdb_level_trace* trace, uint32_t cap, uint32_t* settles) {
+  if (!graph_ok(c, g) || mode < 0 || mode > 2 || (cap && !trace)) return GDB_ERR_INVALID;
+  if (src >= g->V) return set_error(c, GDB_ERR_INVALID, "source out of range");
+  if (c->opt.barrier != GDB_BARRIER_XF && c->opt.barrier != GDB_BARRIER_XF_FIXED)
+    return set_error(c, GDB_ERR_UNSUPPORTED, "settle traces need the XF barrier");
+  if (mode == 2 && !c->d_mlp) return set_error(c, GDB_ERR_INVALID, "no selector loaded");
+  const int force = mode == 0 ? kSettlePush : mode == 1 ? kSettlePull : kSettleLearned;
+  const size_t nb = (size_t)g->V * 4, tb = (size_t)std::max<uint32_t>(cap, 1) * sizeof(gdb_level_trace);
+  char* d = nullptr;
+  GDB_CUDA(c, cudaMallocAsync((void**)&d, nb + tb, c->stream));
+  cudaError_t e = cudaMemsetAsync(d + nb, 0, tb, c->stream);
+  int rc = e == cudaSuccess ? sssp_run(c, g, src, nullptr, 0, (uint32_t*)d, force, (gdb_level_trace*)(d + nb), cap)
+                            : set_cuda_error(c, e, "trace buffer");
+  uint32_t n = 0;
+  if (rc == GDB_OK) {
+    if (dist) e = cudaMemcpyAsync(dist, d, nb, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && cap)
+      e = cudaMemcpyAsync(trace, d + nb, (size_t)cap * sizeof(gdb_level_trace), cudaMemcpyDeviceToHost,
+                          c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = set_cuda_error(c, e, "trace read-back");
+    // settle records: those with a duration (the trace may be shorter than the run)
+    for (uint32_t i = 0; rc == GDB_OK && i < cap && trace[i].us > 0.f; ++i) ++n;
+  }
+  if (settles) *settles = n;
   cudaFreeAsync(d, c->stream);
   cudaStreamSynchronize(c->stream);
   return rc;

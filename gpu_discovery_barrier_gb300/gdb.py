@@ -149,6 +149,8 @@ SIGNATURES = [
     ("gdb_bfs_trace", C.c_int, [_P, _P, C.c_uint32, C.c_int, _P, _P, C.c_uint32,
                                 C.POINTER(C.c_uint32)]),
     ("gdb_sssp_features", C.c_int, [_P, _P, C.c_uint32, _P]),
+    ("gdb_sssp_trace", C.c_int, [_P, _P, C.c_uint32, C.c_int, _P, _P, C.c_uint32,
+                                 C.POINTER(C.c_uint32)]),
     ("gdb_mlp_forward", C.c_int, [_P, _P, _P, C.c_uint32, _P]),
     ("gdb_mlp_loss_grad", C.c_int, [_P, _P, _P, _P, _P, C.c_uint32, _P, C.POINTER(C.c_double)]),
     ("gdb_mlp_train", C.c_int, [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_float, C.c_float,
@@ -465,6 +467,20 @@ class Ctx:
         L = min(n.value, cap)
         arr = np.frombuffer(rec, dtype=np.float32, count=14 * max(cap, 1)).reshape(-1, 14)[:L]
         modes = np.frombuffer(rec, dtype=np.uint32, count=14 * max(cap, 1)).reshape(-1, 14)[:L, 12]
+        return dist, arr[:, :12].copy(), modes.copy(), arr[:, 13].copy()
+
+    def sssp_trace(self, g: "Graph", src: int, mode: int, cap: int = 1 << 14):
+        """SSSP with every settle superstep pushed (0), pulled (1) or chosen
+        by the selector (2); returns (dist, features[S, 12], modes[S], us[S])
+        over the S settle supersteps."""
+        rec = (LevelTrace * max(cap, 1))()
+        dist = np.empty(g.V, dtype=np.uint32)
+        n = C.c_uint32()
+        self.check(self._lib.gdb_sssp_trace(self.h, g.h, src, mode, _ptr(dist), rec, cap, C.byref(n)),
+                   "gdb_sssp_trace")
+        S = min(n.value, cap)
+        arr = np.frombuffer(rec, dtype=np.float32, count=14 * max(cap, 1)).reshape(-1, 14)[:S]
+        modes = np.frombuffer(rec, dtype=np.uint32, count=14 * max(cap, 1)).reshape(-1, 14)[:S, 12]
         return dist, arr[:, :12].copy(), modes.copy(), arr[:, 13].copy()
 
     def sssp_features(self, g: "Graph", nsrc: int = 1) -> np.ndarray:

@@ -13,6 +13,13 @@ decisions:
 * SSSP, per run: label-correcting worklist, near-far at the automatic
   bucket width, near-far at 4x that width, or the worklist under graph
   relaunch.  Each option is timed on every training graph.
+* SSSP, per settle superstep of the light/heavy split, taken inside the
+  kernel at the start of the superstep: push (the bucket's vertices relax
+  their heavy arcs) or pull (every vertex beyond the split takes the
+  minimum over its heavy in-arcs), the same push / pull outputs as a BFS
+  level with decision kind 3.  Both directions give the same distances, so
+  the run's supersteps are the same under any choice: an all-push and an
+  all-pull run time both options at every settle, as for BFS levels.
 
 Training runs on the GPU through the library's own CUDA kernels
 (gdb_mlp_train: forward, backward and Adam); the gradient of those kernels
@@ -116,6 +123,45 @@ def sssp_sample(ctx: gdb.Ctx, G: gdb.Graph, src: int, name: str = "", reps: int 
     return SsspSample(name, x, np.asarray(ms))
 
 
+@dataclass
+class SettleTrace:
+    name: str
+    x: np.ndarray        # [S, 12] features of each settle superstep (kind 3)
+    us_push: np.ndarray  # [S]
+    us_pull: np.ndarray  # [S]
+
+
+def settle_trace(ctx: gdb.Ctx, G: gdb.Graph, src: int, name: str = "", reps: int = 2) -> SettleTrace:
+    """Per-settle durations of the all-push and all-pull settle directions
+    under the near-far schedule with the light/heavy split at the automatic
+    width (the median over `reps` runs of each)."""
+    base = {f: getattr(ctx.opt, f) for f in ("schedule", "sssp_delta", "sssp_split")}
+    ctx.set_options(schedule=gdb.SCHED_ADAPTIVE, sssp_delta=0, sssp_split=0)
+    runs, feats = {}, np.zeros((0, F), np.float32)
+    for mode in (0, 1):
+        us = []
+        for _ in range(reps):
+            _, x, _, t = ctx.sssp_trace(G, src, mode)
+            us.append(t)
+            if mode == 0:
+                feats = x
+        n = min(len(u) for u in us)
+        runs[mode] = np.median(np.stack([u[:n] for u in us]), axis=0)
+    ctx.set_options(**base)
+    S = min(len(runs[0]), len(runs[1]), len(feats))
+    return SettleTrace(name, feats[:S], runs[0][:S], runs[1][:S])
+
+
+def settle_rule(x: np.ndarray) -> np.ndarray:
+    """The fixed settle direction (1 = pull) from the features: pull when
+    the unsettled vertices' heavy arcs plus one look at every vertex are
+    fewer than the bucket's heavy arcs."""
+    mf = np.exp2(x[:, 1]) - 1
+    mu = np.exp2(x[:, 2]) - 1
+    V = np.exp2(x[:, 3]) - 1
+    return (mu + V < mf).astype(np.int64)
+
+
 def training_graphs(small: bool = False):
     """Synthetic graphs spanning the workloads' shapes: R-MAT of several
     scales and edge factors, square and elongated grids, mixed-batch
@@ -156,14 +202,42 @@ def collect(ctx: gdb.Ctx, graphs, reps: int = 2, ctas=(0,)):
     return bfs, sssp
 
 
+def collect_settle(ctx: gdb.Ctx, graphs, reps: int = 2, ctas=(0,)):
+    """Settle traces of every graph and source at every launch shape; runs
+    without settle supersteps (no split) give no rows."""
+    out = []
+    base = ctx.opt.max_ctas
+    for name, g, srcs in graphs:
+        G = ctx.graph(g.row_ptr, g.col, g.w)
+        for k in ctas:
+            ctx.set_options(max_ctas=k)
+            for s in srcs:
+                tr = settle_trace(ctx, G, s, f"{name}@{k}", reps)
+                if len(tr.x):
+                    out.append(tr)
+        G.close()
+    ctx.set_options(max_ctas=base)
+    return out
+
+
 # --------------------------------------------------------------- training
 
 
-def dataset(bfs: list[BfsTrace], sssp: list[SsspSample]):
+def dataset(bfs: list[BfsTrace], sssp: list[SsspSample], settle: list[SettleTrace] = ()):
     """Rows (x, target, mask).  A BFS level yields one row per mode, its
     previous-mode feature set both ways (the implementation keeps the queue
-    in both modes, so switching costs nothing); targets are log2 us."""
+    in both modes, so switching costs nothing); a settle superstep one row
+    with its push and pull targets; targets are log2 us."""
     X, T, M = [], [], []
+    for tr in settle:
+        for i in range(len(tr.x)):
+            t = np.zeros(OUT)
+            m = np.zeros(OUT)
+            t[PUSH], t[PULL] = math.log2(max(tr.us_push[i], 0.05)), math.log2(max(tr.us_pull[i], 0.05))
+            m[PUSH] = m[PULL] = 1.0
+            X.append(tr.x[i])
+            T.append(t)
+            M.append(m)
     for tr in bfs:
         for l in range(len(tr.x)):
             for prev in (0.0, 1.0):
@@ -216,6 +290,30 @@ def bfs_choices(ctx: gdb.Ctx, p: np.ndarray, tr: BfsTrace) -> np.ndarray:
     return modes
 
 
+def settle_choices(ctx: gdb.Ctx, p: np.ndarray, tr: SettleTrace) -> np.ndarray:
+    """The selector's direction (1 = pull) per settle superstep of a trace."""
+    if not len(tr.x):
+        return np.zeros(0, np.int64)
+    y = ctx.mlp_forward(p, tr.x)
+    return (y[:, PULL] < y[:, PUSH]).astype(np.int64)
+
+
+def settle_regret(ctx: gdb.Ctx, p: np.ndarray, settle: list[SettleTrace]) -> dict:
+    """Settle supersteps: the selector's choices against the per-superstep
+    optimum, the fixed rule and all-push."""
+    opt = sel = rule = push = 0.0
+    for tr in settle:
+        ch = settle_choices(ctx, p, tr)
+        r = settle_rule(tr.x)
+        opt += float(np.minimum(tr.us_push, tr.us_pull).sum())
+        sel += float(np.where(ch == 1, tr.us_pull, tr.us_push).sum())
+        rule += float(np.where(r == 1, tr.us_pull, tr.us_push).sum())
+        push += float(tr.us_push.sum())
+    return {"optimal_us": opt, "selector_us": sel, "rule_us": rule, "push_us": push,
+            "regret": sel / opt - 1 if opt else 0.0, "gain_vs_rule": rule / sel if sel else 0.0,
+            "supersteps": int(sum(len(t.x) for t in settle))}
+
+
 def regret(ctx: gdb.Ctx, p: np.ndarray, bfs: list[BfsTrace], sssp: list[SsspSample]) -> dict:
     b_opt = b_sel = b_plain = 0.0
     for tr in bfs:
@@ -254,10 +352,14 @@ def main(argv=None) -> None:
     with gdb.Ctx() as ctx:
         bfs_fit, sssp_fit = collect(ctx, fit, ctas=ctas)
         bfs_held, sssp_held = collect(ctx, held, ctas=ctas)
-        X, T, M = dataset(bfs_fit, sssp_fit)
+        settle_fit = collect_settle(ctx, fit, ctas=ctas)
+        settle_held = collect_settle(ctx, held, ctas=ctas)
+        X, T, M = dataset(bfs_fit, sssp_fit, settle_fit)
         p, info = train(ctx, X, T, M, epochs=args.epochs)
         info["regret_fit"] = regret(ctx, p, bfs_fit, sssp_fit)
         info["regret_held_out"] = regret(ctx, p, bfs_held, sssp_held)
+        info["regret_fit"]["settle"] = settle_regret(ctx, p, settle_fit)
+        info["regret_held_out"]["settle"] = settle_regret(ctx, p, settle_held)
         info["fit_graphs"] = [n for n, _, _ in fit]
         info["held_out_graphs"] = [n for n, _, _ in held]
         info["launch_shapes"] = list(ctas)

@@ -297,8 +297,9 @@ const char* gdb_io_last_error(void);
 /* No reference counterpart.  A 12-32-32-6 ReLU MLP in FP32 (GDB_MLP_PARAMS
  * floats: feature shift[12], scale[12], W1[12][32], b1[32], W2[32][32],
  * b2[32], W3[32][6], b3[6]); its outputs are predicted log2 costs of the
- * options of a decision (0 push level, 1 pull level, 2 SSSP worklist,
- * 3 SSSP near-far, 4 SSSP near-far 4x width, 5 SSSP graph relaunch). */
+ * options of a decision (0 push / 1 pull: a BFS level or an SSSP settle
+ * superstep; 2 SSSP worklist, 3 SSSP near-far, 4 SSSP near-far 4x width,
+ * 5 SSSP graph relaunch). */
 #define GDB_MLP_FEATURES 12
 #define GDB_MLP_OUTPUTS 6
 #define GDB_MLP_PARAMS 1694
@@ -318,6 +319,13 @@ int gdb_selector_set(gdb_ctx* ctx, const float* params);
  * run.  Levels (dist) are the same for every mode. */
 int gdb_bfs_trace(gdb_ctx* ctx, gdb_graph* g, uint32_t src, int mode, uint32_t* dist,
                   gdb_level_trace* trace, uint32_t cap, uint32_t* levels);
+/* SSSP with the light/heavy split from src, the direction of every settle
+ * superstep fixed (0 push, 1 pull) or chosen by the loaded network (2),
+ * recording up to cap settle supersteps (features with decision kind 3, the
+ * direction, the duration from the superstep's start to the next one's);
+ * *settles = records written.  Distances are the same for every mode. */
+int gdb_sssp_trace(gdb_ctx* ctx, gdb_graph* g, uint32_t src, int mode, uint32_t* dist,
+                   gdb_level_trace* trace, uint32_t cap, uint32_t* settles);
 /* Features of an SSSP run-level decision for g from nsrc sources. */
 int gdb_sssp_features(gdb_ctx* ctx, gdb_graph* g, uint32_t nsrc, float* x);
 /* Network outputs for n feature rows x[n][12] (host arrays). */
