@@ -113,8 +113,7 @@ __device__ __forceinline__ unsigned long long sssp_clock() {
 // decision and no barrier waits for it: the network's cheaper output of
 // push / pull on the settle's features (decision kind 3), or the forced
 // mode of a trace run.  CTA 0 opens the trace record.
-__device__ __noinline__ uint32_t settle_choose(const GraphView& GH, const SsspWs& ws, const float* smlp,
-                                               SettleState* st, uint32_t phase, uint32_t sn, uint32_t hn,
+__device__ __noinline__ uint32_t settle_choose(const GraphView& GH, const SsspWs& ws, SettleState* st, uint32_t phase, uint32_t sn, uint32_t hn,
                                                unsigned long long an, uint32_t sdone, uint32_t hdone,
                                                unsigned long long adone, uint32_t nwarps, bool master) {
   const unsigned long long mf = an - adone;
@@ -125,9 +124,25 @@ __device__ __noinline__ uint32_t settle_choose(const GraphView& GH, const SsspWs
                (float)(GH.V > sn ? GH.V - sn : 0u), phase, 3u, (float)ws.maxdeg, (float)nwarps);
   uint32_t mode = ws.settle == kSettlePull ? 1u : 0u;
   if (ws.settle == kSettleLearned) {
-    float out[kOut];
-    mlp_warp(smlp, x, out);
-    mode = out[kOutPull] < out[kOutPush] ? 1u : 0u;
+    // where one side holds over 16x the other's work (the push's heavy
+    // arcs against the pull's open heavy arcs plus one look at every
+    // vertex) the choice is plain and the network, a few microseconds on
+    // the superstep's critical path, is not asked (on R-MAT-22 it agrees
+    // with this on every such settle; evaluated on all ten it made the
+    // 16-source SSSP 0.8 ms slower)
+    const double push_work = (double)mf, pull_work = (double)mu + GH.V;
+    if (push_work > 16.0 * pull_work) {
+      mode = 1;
+    } else if (pull_work > 16.0 * push_work) {
+      mode = 0;
+    } else {
+      // parameters straight from global memory: asked a few times per run,
+      // they would cost the kernel 6.8 KB of shared memory per CTA, and the
+      // smaller L1 that leaves made the whole SSSP 2-4 % slower
+      float out[kOut];
+      mlp_warp(ws.mlp, x, out);
+      mode = out[kOutPull] < out[kOutPush] ? 1u : 0u;
+    }
   }
   if (master && threadIdx.x == 0 && ws.trace && st->k < ws.trace_cap) {
     for (int i = 0; i < kFeat; ++i) ws.trace[st->k].x[i] = x[i];
@@ -451,13 +466,11 @@ __device__ __forceinline__ void far_filter(const GraphView& G, const Warps& W, c
 template <bool Hooked, class Sync>
 __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const GraphView& GH,
                                           const GraphView& GT, const SsspWs& ws, uint32_t src,
-                                          uint32_t* smin, float* smlp, SettleState* sst) {
+                                          uint32_t* smin, SettleState* sst) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
   const bool split_arcs = ws.light < kInf;
   if constexpr (Hooked) {
-    if (ws.settle == kSettleLearned)
-      for (int i = threadIdx.x; i < kParams; i += blockDim.x) smlp[i] = __ldg(&ws.mlp[i]);
     if (threadIdx.x == 0) *sst = SettleState{0, 0, 0};  // read after the first barrier
   }
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
@@ -542,8 +555,8 @@ __device__ __forceinline__ void sssp_body(Sync& s, const GraphView& G, const Gra
       if constexpr (Hooked) {
         __shared__ uint32_t sdir;
         if (threadIdx.x < 32) {
-          const uint32_t d = settle_choose(GH, ws, smlp, sst, phase, sn, hn, an, sdone, hdone, adone,
-                                           W.nwarps, s.id() == 0);
+          const uint32_t d = settle_choose(GH, ws, sst, phase, sn, hn, an, sdone, hdone, adone, W.nwarps,
+                                           s.id() == 0);
           if (threadIdx.x == 0) sdir = d;
         }
         __syncthreads();
@@ -596,25 +609,24 @@ __global__ void __launch_bounds__(512, 2) k_sssp_xf(DiscoveryArgs a, GraphView G
   __shared__ uint32_t smin[512];
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
-  sssp_body<false>(s, G, GH, GT, ws, src, smin, nullptr, nullptr);
+  sssp_body<false>(s, G, GH, GT, ws, src, smin, nullptr);
 }
 
 __global__ void __launch_bounds__(512, 2) k_sssp_xf_sel(DiscoveryArgs a, GraphView G, GraphView GH,
                                                          GraphView GT, SsspWs ws, uint32_t src) {
   __shared__ LocalCtx l;
   __shared__ uint32_t smin[512];
-  __shared__ float smlp[kParams];
   __shared__ SettleState sst;
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
-  sssp_body<true>(s, G, GH, GT, ws, src, smin, smlp, &sst);
+  sssp_body<true>(s, G, GH, GT, ws, src, smin, &sst);
 }
 
 __global__ void __launch_bounds__(512, 2) k_sssp_grid(GraphView G, GraphView GH, GraphView GT,
                                                        SsspWs ws, uint32_t src) {
   __shared__ uint32_t smin[512];
   GridSync s;
-  sssp_body<false>(s, G, GH, GT, ws, src, smin, nullptr, nullptr);
+  sssp_body<false>(s, G, GH, GT, ws, src, smin, nullptr);
 }
 
 // Relaunch modes: an init launch, then one launch per superstep; the last
