@@ -60,6 +60,9 @@ def parse():
     p.add_argument("--schedule", choices=["plain", "adaptive", "learned"], default="learned",
                    help="BFS/SSSP schedule of the suite (learned = the trained selector)")
     p.add_argument("--no-tune", action="store_true")
+    p.add_argument("--pull-bitmap-kb", type=int, default=0,
+                   help="BFS pull levels' frontier bitmap stage (gdb_options.pull_bitmap_kb: "
+                        "0 automatic, -1 none, 1..64 KB)")
     p.add_argument("--requests", type=int, default=4000, help="serve: requests submitted")
     p.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (req/s)")
     p.add_argument("--slots", type=int, default=64, help="serve: concurrent slots")
@@ -228,7 +231,7 @@ def set_schedule(ctx, name: str) -> None:
 
 
 class GpuSuite:
-    def __init__(self, wl, apps, device, schedule="plain"):
+    def __init__(self, wl, apps, device, schedule="plain", bitmap_kb=0):
         import torch
 
         from gpu_discovery_barrier_gb300 import gdb
@@ -239,7 +242,7 @@ class GpuSuite:
         self.apps = apps
         self.device = device
         g = wl["g"]
-        self.ctx = gdb.Ctx(device=device)
+        self.ctx = gdb.Ctx(device=device, pull_bitmap_kb=bitmap_kb)
         set_schedule(self.ctx, schedule)
         self.G = self.ctx.graph(g.row_ptr, g.col, wl["w"], symmetric=wl["symmetric"])
         self.Gu = self.ctx.graph(g.row_ptr, g.col, wl["uw"])
@@ -640,10 +643,11 @@ def run_gdb(args, rank, world, local):
     apps = args.apps.split(",")
     wl = make_workload(args.scale, args.edge_factor, args.graph)
     g = wl["g"]
-    suite = GpuSuite(wl, apps, local, args.schedule)
-    er_by_src, reached = {}, []
+    suite = GpuSuite(wl, apps, local, args.schedule, args.pull_bitmap_kb)
+    er_by_src, reached, one_ms = {}, [], []
     for s in wl["src"]:
         vr, erv = reach(g, suite.ctx.bfs(suite.G, int(s)))
+        one_ms.append(suite.ctx.last_stats()["kernel_ms"])  # one traversal alone on the GPU
         er_by_src[int(s)] = erv
         reached.append((vr, erv))
     sum_er = sum(er_by_src.values())
@@ -783,6 +787,9 @@ def run_gdb(args, rank, world, local):
         line["schedule"] = args.schedule
         line["plain_schedule"] = plain
         line["per_app_supersteps"] = {a: rec[a]["supersteps"] // args.steps for a in rec}
+        # the reach runs: one source per call, the traversal alone on the GPU
+        line["bfs_one_source_ms"] = {"median": float(np.median(one_ms)), "min": float(np.min(one_ms)),
+                                     "pull_bitmap_kb": args.pull_bitmap_kb}
         line["parity"] = parity
         print(json.dumps(line), flush=True)
         if parity is not None and not all(v is True for k, v in parity.items() if k != "detail"):

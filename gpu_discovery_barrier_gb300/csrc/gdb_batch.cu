@@ -168,7 +168,7 @@ int gdb_batch_create(gdb_ctx* c, gdb_graph* g, uint32_t apps, const uint32_t* so
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "capture stream"));
   e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    if (apps & GDB_BATCH_BFS) rc = bfs_enqueue(c, g, b->ws_bfs, b->d_srcs, nsrc, b->d_bfs, cs, proto);
+    if (apps & GDB_BATCH_BFS) rc = bfs_enqueue(c, g, b->ws_bfs, b->d_srcs, nsrc, b->d_bfs, cs, proto, true);
     if (rc == GDB_OK && (apps & GDB_BATCH_SSSP))
       rc = sssp_enqueue(c, g, b->ws_sssp, b->d_srcs, nsrc, b->d_sssp, cs, proto, b->delta, b->light);
     cudaError_t e2 = cudaStreamEndCapture(cs, &b->graph);

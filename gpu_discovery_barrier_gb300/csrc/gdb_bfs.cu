@@ -49,7 +49,32 @@ struct BfsWs {
   uint32_t maxdeg;
   const uint32_t* srcs;        // multi-source run when nsrc > 0
   uint32_t nsrc;
+  // frontier bitmaps of the pull levels (nullptr: none): two slots of
+  // fwords words, slot L & 1 holding bit v iff dist[v] == L while a pull
+  // level L reads it; the level stages its first swords words in shared
+  // memory
+  uint32_t* fbm;
+  uint32_t fwords;             // ceil(V / 32) rounded up to a multiple of 4
+  uint32_t swords;             // multiple of 4, <= fwords
 };
+
+// Frontier bitmap slot of level L (nullptr without bitmaps).
+__device__ __forceinline__ uint32_t* fbm_slot(const BfsWs& ws, uint32_t L) {
+  return ws.fbm ? ws.fbm + (size_t)(L & 1) * ws.fwords : nullptr;
+}
+
+// Level L's bitmap from the level array, one ballot per 32-vertex group
+// (every word written, so the slot needs no clearing): run over the grid
+// before a pull level that follows a push level.
+__device__ __forceinline__ void fbm_build(const GraphView& G, const BfsWs& ws, uint32_t L, const Warps& W) {
+  uint32_t* F = fbm_slot(ws, L);
+  const uint32_t ngroups = (G.V + 31) / 32;
+  for (uint32_t g = W.gwarp; g < ngroups; g += W.nwarps) {
+    const uint32_t v = g * 32 + lane_id();
+    const unsigned m = __ballot_sync(kFull, v < G.V && ld_cg(&ws.dist[v]) == L);
+    if (lane_id() == 0) F[g] = m;
+  }
+}
 
 // BfsWs::adaptive: plain push, the threshold heuristic, the learned
 // selector, and the two fixed modes of trace generation.
@@ -227,22 +252,52 @@ __device__ __forceinline__ void bfs_top_down(const GraphView& G, const Warps& W,
 // go on are then scanned by the whole warp, 32 arcs per step, one vertex
 // after another, leaving at the first step with a hit (so a long list
 // costs its length / 32 round trips instead of its length).
+//
+// With frontier bitmaps a probe tests the neighbour's bit in level L's
+// bitmap instead of loading its level.  The bitmap's first swords words
+// (the lowest vertex ids: on R-MAT-22 80 % of the vertices' first arcs
+// land below id 393,216, a 48 KB prefix, because rows are sorted and
+// R-MAT concentrates hubs there) are copied into the CTA's shared memory
+// at the level's start with 16-byte loads, so most probes are one
+// shared-memory read after the column load instead of a second L2 round
+// trip; the rest read the bitmap word from L2.  The level writes level
+// L + 1's bitmap whole, one ballot per 32-vertex group, for a following
+// pull level; push levels keep no bitmap (fbm_build makes one when a pull
+// level follows them).
 constexpr uint32_t kPullProbe = 8;
 
 __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& ws, uint32_t L,
-                                              const Warps& W, unsigned long long& arcs,
+                                              const Warps& W, uint32_t* sbits, unsigned long long& arcs,
                                               unsigned long long& farcs) {
   const int nxt = (L + 1) % 3;
   Frontier out{pick(ws.q, L + 1), pick(ws.hc, L + 1), &ws.qcount[nxt], &ws.hcount[nxt],
                ws.qcap, ws.hcap, ws.overflow};
   WarpStage qs = frontier_stage(out, 0);
   const int lane = lane_id();
+  const uint32_t* F = fbm_slot(ws, L);
+  uint32_t* Fn = fbm_slot(ws, L + 1);
+  const uint32_t sw = F ? ws.swords : 0u;
+  if (sw) {
+    const uint4* f4 = reinterpret_cast<const uint4*>(F);
+    uint4* s4 = reinterpret_cast<uint4*>(sbits);
+    for (uint32_t i = threadIdx.x; i < sw / 4; i += blockDim.x) s4[i] = ld_cg(&f4[i]);
+    __syncthreads();
+  }
+  // u in level L's frontier (F written before this level's barrier)
+  auto in_frontier = [&](uint32_t u) -> bool {
+    if (!F) return ld_cg(&ws.dist[u]) == L;
+    const uint32_t wd = u >> 5;
+    const uint32_t word = wd < sw ? sbits[wd] : ld_cg(&F[wd]);
+    return (word >> (u & 31)) & 1u;
+  };
   const uint32_t ngroups = (G.V + 31) / 32;
   for (uint32_t g = W.gwarp; g < ngroups; g += W.nwarps) {
     const uint32_t v = g * 32 + lane;
     bool want = false, open = false;
     uint32_t b = 0, e = 0, deg = 0;
-    if (v < G.V && ws.dist[v] == kInf) {
+    // an L2 read: another SM's claim in an earlier push level may have
+    // changed dist[v] after this SM cached it
+    if (v < G.V && ld_cg(&ws.dist[v]) == kInf) {
       b = __ldg(&G.row[v]);
       e = __ldg(&G.row[v + 1]);
       deg = e - b;
@@ -251,11 +306,29 @@ __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& w
         uint32_t u[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) u[k] = a + k < stop ? __ldg(&G.col[a + k]) : kInf;
+        if (F) {
+          // the four probes' L2 words first (all in flight together), then
+          // the staged ones
+          uint32_t word[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          if (u[k] != kInf) {
-            ++arcs;
-            if (ld_cg(&ws.dist[u[k]]) == L) want = true;
+          for (int k = 0; k < 4; ++k) word[k] = u[k] != kInf && (u[k] >> 5) >= sw ? ld_cg(&F[u[k] >> 5]) : 0u;
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (u[k] != kInf && (u[k] >> 5) < sw) word[k] = sbits[u[k] >> 5];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            if (u[k] != kInf) {
+              ++arcs;
+              if ((word[k] >> (u[k] & 31)) & 1u) want = true;
+            }
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            if (u[k] != kInf) {
+              ++arcs;
+              if (ld_cg(&ws.dist[u[k]]) == L) want = true;
+            }
           }
         }
       }
@@ -270,7 +343,7 @@ __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& w
         bool hit = false;
         if (a + lane < ee) {
           ++arcs;
-          hit = ld_cg(&ws.dist[__ldg(&G.col[a + lane])]) == L;
+          hit = in_frontier(__ldg(&G.col[a + lane]));
         }
         if (__any_sync(kFull, hit)) {
           found = true;
@@ -283,6 +356,8 @@ __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& w
       ws.dist[v] = L + 1;  // only this lane writes v
       farcs += deg;
     }
+    const unsigned found = __ballot_sync(kFull, want);
+    if (Fn && lane == 0) Fn[g] = found;
     frontier_push_staged(G, out, qs, want, v);
   }
   qs.flush();
@@ -292,7 +367,7 @@ __device__ __forceinline__ void bfs_bottom_up(const GraphView& G, const BfsWs& w
 // barrier); a separate instantiation keeps the plain kernels' registers.
 template <bool Hooked, class Sync>
 __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsWs& ws, uint32_t src,
-                                         float* smlp, DecideState* dst) {
+                                         float* smlp, DecideState* dst, uint32_t* sbits) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
   constexpr bool hooked = Hooked;
@@ -334,7 +409,7 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
   if (!level_sync(0)) return;
   unsigned long long arcs = 0;
   uint32_t L = 0;
-  bool bottom_up = false;
+  bool bottom_up = false, prev_bottom_up = false;
   // direction-choice inputs, identical in every CTA: arcs of the frontier
   // (mf) and of the still-unvisited vertices (mu).  acc[k % 3] (stats[4..6])
   // collects the arcs of level k while level k-1 runs.
@@ -364,8 +439,15 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
       ws.hcursor[old] = 0;
       ws.stats[4 + old] = 0;
     }
+    if (bottom_up && ws.fbm && !prev_bottom_up) {
+      // a pull level after a push level (or the first level): its
+      // frontier's bitmap from the level array, complete before any probe
+      fbm_build(G, ws, L, W);
+      if (!s.sync()) return;
+    }
+    prev_bottom_up = bottom_up;
     unsigned long long farcs = 0;
-    if (bottom_up) bfs_bottom_up(G, ws, L, W, arcs, farcs);
+    if (bottom_up) bfs_bottom_up(G, ws, L, W, sbits, arcs, farcs);
     else bfs_top_down<Hooked>(G, W, ws, L, sc, arcs, farcs);
     if (ws.adaptive) {
 #pragma unroll
@@ -381,16 +463,20 @@ __device__ __forceinline__ void bfs_body(Sync& s, const GraphView& G, const BfsW
   if (leader) ws.stats[1] = L;
 }
 
+// Dynamic shared memory of the traversal kernels: ws.swords words of the
+// frontier bitmap staged by pull levels (none when ws.swords is 0).
 __global__ void __launch_bounds__(512, 3) k_bfs_xf(DiscoveryArgs a, GraphView G, BfsWs ws, uint32_t src) {
   __shared__ LocalCtx l;
+  extern __shared__ uint4 bfs_stage[];
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
-  bfs_body<false>(s, G, ws, src, nullptr, nullptr);
+  bfs_body<false>(s, G, ws, src, nullptr, nullptr, reinterpret_cast<uint32_t*>(bfs_stage));
 }
 
 __global__ void __launch_bounds__(512, 3) k_bfs_grid(GraphView G, BfsWs ws, uint32_t src) {
+  extern __shared__ uint4 bfs_stage[];
   GridSync s;
-  bfs_body<false>(s, G, ws, src, nullptr, nullptr);
+  bfs_body<false>(s, G, ws, src, nullptr, nullptr, reinterpret_cast<uint32_t*>(bfs_stage));
 }
 
 __global__ void __launch_bounds__(512, 3) k_bfs_xf_sel(DiscoveryArgs a, GraphView G, BfsWs ws,
@@ -398,16 +484,18 @@ __global__ void __launch_bounds__(512, 3) k_bfs_xf_sel(DiscoveryArgs a, GraphVie
   __shared__ LocalCtx l;
   __shared__ float smlp[kParams];
   __shared__ DecideState dst;
+  extern __shared__ uint4 bfs_stage[];
   if (!discover(a, &l)) return;
   XfSync s{&a, &l};
-  bfs_body<true>(s, G, ws, src, smlp, &dst);
+  bfs_body<true>(s, G, ws, src, smlp, &dst, reinterpret_cast<uint32_t*>(bfs_stage));
 }
 
 __global__ void __launch_bounds__(512, 3) k_bfs_grid_sel(GraphView G, BfsWs ws, uint32_t src) {
   __shared__ float smlp[kParams];
   __shared__ DecideState dst;
+  extern __shared__ uint4 bfs_stage[];
   GridSync s;
-  bfs_body<true>(s, G, ws, src, smlp, &dst);
+  bfs_body<true>(s, G, ws, src, smlp, &dst, reinterpret_cast<uint32_t*>(bfs_stage));
 }
 
 // Relaunch mode: init kernel, then one launch per level (no in-kernel barrier).
@@ -489,14 +577,20 @@ __global__ void __launch_bounds__(512, 3) k_bfs_glevel(GraphView G, BfsWs ws, ui
 
 using namespace gdbi;
 
+// Words of one frontier bitmap slot of a graph of V vertices.
+static uint32_t bitmap_words(uint32_t V) { return ((V + 31) / 32 + 3) & ~3u; }
+
 // Workspace of one BFS run: two light queues, two chunk-entry queues, the
-// 512-byte counter block.
+// two frontier bitmap slots, the 512-byte counter block (last: the
+// lanes read their statistics at its fixed offset from the end).
 static size_t bfs_layout(const gdb_graph* g, char* base, uint32_t* d_dist, BfsWs* ws, char** cnt_out) {
   const uint32_t V = g->V;
   const uint32_t hcap = chunk_capacity(g);
+  const uint32_t fwords = bitmap_words(V);
   Bump b;
   const size_t o_q0 = b.take((size_t)V * 4), o_q1 = b.take((size_t)V * 4);
   const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
+  const size_t o_fbm = b.take((size_t)fwords * 8);
   const size_t o_cnt = b.take(512);
   if (!base) return b.off;
   ws->dist = d_dist;
@@ -523,8 +617,47 @@ static size_t bfs_layout(const gdb_graph* g, char* base, uint32_t* d_dist, BfsWs
   ws->maxdeg = g->maxdeg;
   ws->srcs = nullptr;
   ws->nsrc = 0;
+  ws->fbm = (uint32_t*)(base + o_fbm);
+  ws->fwords = fwords;
+  ws->swords = 0;
   *cnt_out = cnt;
   return b.off;
+}
+
+// The automatic frontier bitmap (pull_bitmap_kb 0): a 16 KB stage
+// (131,072 vertex ids) for a traversal that has the GPU to itself; none
+// for traversals that share it.  Measured on R-MAT-22 (learned schedule):
+// one source 0.380 -> 0.354 ms with the bitmap (threshold schedule 0.352
+// -> 0.314 ms), while 16 sources on four concurrent lanes go 2.93 ->
+// 3.02 ms -- their pull levels are bandwidth-bound, and the bitmap's
+// build pass costs more than its shared-memory probes save.  Stages of
+// 48 KB and more cost occupancy and L1 (one source 0.40 / 0.46 ms).
+constexpr uint32_t kStageKbAuto = 16;
+constexpr uint32_t kStageKbMax = 64;
+
+// Words of the bitmap a pull level stages for schedule `mode` on a graph
+// of V vertices (0: no bitmap).
+static uint32_t bitmap_stage_words(gdb_ctx* c, int mode, uint32_t V, bool alone) {
+  if (mode == kBfsPlain || c->opt.pull_bitmap_kb < 0) return 0;
+  const uint32_t kb = c->opt.pull_bitmap_kb ? (uint32_t)c->opt.pull_bitmap_kb : (alone ? kStageKbAuto : 0u);
+  return std::min<uint32_t>(kb * 256u, bitmap_words(V));  // both multiples of 4
+}
+
+// Frontier bitmaps of ws's schedule (none for plain push, when
+// pull_bitmap_kb is -1, or automatically for a traversal sharing the GPU);
+// returns the dynamic shared memory, in bytes, the traversal kernel takes.
+static void bfs_bitmap(gdb_ctx* c, const gdb_graph* g, BfsWs* ws, bool alone, size_t* smem) {
+  ws->swords = bitmap_stage_words(c, ws->adaptive, g->V, alone);
+  if (!ws->swords) ws->fbm = nullptr;
+  *smem = (size_t)ws->swords * 4;
+}
+
+int gdbi::bfs_prepare(gdb_ctx* c) {
+  // static + dynamic shared memory above 48 KB needs each kernel's opt-in
+  for (const void* k : {(const void*)k_bfs_xf, (const void*)k_bfs_xf_sel, (const void*)k_bfs_grid,
+                        (const void*)k_bfs_grid_sel})
+    GDB_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageKbMax * 1024));
+  return GDB_OK;
 }
 
 int gdbi::traversal_occupancy(gdb_ctx* c, int block) {
@@ -568,7 +701,7 @@ static int bfs_mode(gdb_ctx* c, const gdb_graph* g, int* mode) {
 // `stream` without waiting, so that it can be stream-captured.  `proto`
 // carries the discovery context and flags the launch synchronises through.
 int gdbi::bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
-                      uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto) {
+                      uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto, bool alone) {
   BfsWs ws;
   char* cnt = nullptr;
   bfs_layout(g, (char*)wsbase, d_dist, &ws, &cnt);
@@ -583,11 +716,13 @@ int gdbi::bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_
   Shape s;
   const bool sel = ws.adaptive >= kBfsLearned;
   auto kx = sel ? k_bfs_xf_sel : k_bfs_xf;
-  rc = persistent_shape(c, (const void*)kx, c->opt.block_size, 0, &s, false);
+  size_t smem = 0;
+  bfs_bitmap(c, g, &ws, alone, &smem);
+  rc = persistent_shape(c, (const void*)kx, c->opt.block_size, smem, &s, false);
   if (rc) return rc;
   DiscoveryArgs a = proto;
   a.expected = std::min(s.grid, s.fit);
-  kx<<<s.grid, c->opt.block_size, 0, stream>>>(a, g->view(), ws, 0u);
+  kx<<<s.grid, c->opt.block_size, smem, stream>>>(a, g->view(), ws, 0u);
   GDB_CUDA(c, cudaGetLastError());
   return GDB_OK;
 }
@@ -628,11 +763,13 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
   if (kind == GDB_BARRIER_XF || kind == GDB_BARRIER_XF_FIXED) {
     Shape s;
     auto kx = ws.adaptive >= kBfsLearned ? k_bfs_xf_sel : k_bfs_xf;
-    rc = persistent_shape(c, (const void*)kx, block, 0, &s, kind == GDB_BARRIER_XF);
+    size_t smem = 0;
+    bfs_bitmap(c, g, &ws, true, &smem);
+    rc = persistent_shape(c, (const void*)kx, block, smem, &s, kind == GDB_BARRIER_XF);
     if (rc) return rc;
     DiscoveryArgs a = discovery_args(c, s);
     GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    kx<<<s.grid, block, 0, c->stream>>>(a, G, ws, src);
+    kx<<<s.grid, block, smem, c->stream>>>(a, G, ws, src);
     GDB_CUDA(c, cudaGetLastError());
     GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     rc = finish_run(c);
@@ -645,7 +782,9 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
   } else if (kind == GDB_BARRIER_GRID_SYNC) {
     int occ = 0;
     auto kg = ws.adaptive >= kBfsLearned ? k_bfs_grid_sel : k_bfs_grid;
-    GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kg, block, 0));
+    size_t smem = 0;
+    bfs_bitmap(c, g, &ws, true, &smem);
+    GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kg, block, smem));
     int grid = occ * c->sm_count;
     if (c->opt.max_ctas > 0) grid = std::min(grid, c->opt.max_ctas);
     GraphView Gc = G;
@@ -653,7 +792,7 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
     uint32_t srcc = src;
     void* args[] = {(void*)&Gc, (void*)&wsc, (void*)&srcc};
     GDB_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    GDB_CUDA(c, cudaLaunchCooperativeKernel((const void*)kg, grid, block, args, 0, c->stream));
+    GDB_CUDA(c, cudaLaunchCooperativeKernel((const void*)kg, grid, block, args, smem, c->stream));
     GDB_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     GDB_CUDA(c, cudaStreamSynchronize(c->stream));
     c->last.participating = grid;
@@ -661,6 +800,7 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
     c->last.launches = 1;
   } else if (kind == GDB_BARRIER_RELAUNCH) {
     if (ws.adaptive) return set_error(c, GDB_ERR_UNSUPPORTED, "adaptive schedule needs a persistent barrier");
+    ws.fbm = nullptr;
     int occ = 0;
     GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs_level, block, 0));
     int grid = occ * c->sm_count;
@@ -687,6 +827,7 @@ static int bfs_run(gdb_ctx* c, gdb_graph* g, uint32_t src, const uint32_t* d_src
     c->last.launches = launches;
   } else if (kind == GDB_BARRIER_RELAUNCH_GRAPH) {
     if (ws.adaptive) return set_error(c, GDB_ERR_UNSUPPORTED, "adaptive schedule needs a persistent barrier");
+    ws.fbm = nullptr;
     int occ = 0;
     GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs_glevel, block, 0));
     int grid = occ * c->sm_count;
@@ -761,9 +902,13 @@ int gdb_bfs_sources_device(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, 
   int mode = 0;
   int rc = bfs_mode(c, g, &mode);
   if (rc) return rc;
-  const int fit = traversal_occupancy(c, c->opt.block_size) * c->sm_count;
+  int occ = 0;
+  const void* kx = mode >= kBfsLearned ? (const void*)k_bfs_xf_sel : (const void*)k_bfs_xf;
+  const size_t smem = (size_t)bitmap_stage_words(c, mode, g->V, false) * 4;
+  GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kx, c->opt.block_size, smem));
+  const int fit = occ * c->sm_count;
   return run_on_lanes(c, n, bfs_workspace_bytes(g), fit, [&](gdb_lane& L, uint32_t i) {
-    return bfs_enqueue(c, g, L.ws, d_sources + i, 1, d_dist + i * V, L.stream, lane_args(c, L));
+    return bfs_enqueue(c, g, L.ws, d_sources + i, 1, d_dist + i * V, L.stream, lane_args(c, L), false);
   });
 }
 
@@ -975,6 +1120,9 @@ extern "C" int gdb_bfs_noalloc(const uint32_t* d_row_ptr, const uint32_t* d_col,
   ws.maxdeg = 0;
   ws.srcs = nullptr;
   ws.nsrc = 0;
+  ws.fbm = nullptr;  // plain push: no frontier bitmaps
+  ws.fwords = 0;
+  ws.swords = 0;
   DiscoveryArgs a;
   a.ctx = (gdb::DeviceCtx*)(base + kNaCtx);
   a.flags = (int*)(base + kNaFlags);

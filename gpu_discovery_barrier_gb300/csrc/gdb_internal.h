@@ -172,8 +172,14 @@ void dev_free(gdb_ctx* c, void* p);
 int traversal_occupancy(gdb_ctx* c, int block);
 size_t bfs_workspace_bytes(const gdb_graph* g);
 size_t sssp_workspace_bytes(const gdb_graph* g);
+// `alone`: the traversal has the GPU to itself while it runs (the batch's
+// one launch), not one of several sharing it (lanes, serving slots); it
+// decides the automatic frontier bitmap.
 int bfs_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
-                uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto);
+                uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto, bool alone);
+// Allows the traversal kernels their largest shared-memory stage (once per
+// context, outside any stream capture).
+int bfs_prepare(gdb_ctx* c);
 int sssp_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_srcs, uint32_t nsrc,
                  uint32_t* d_dist, cudaStream_t stream, const gdb::DiscoveryArgs& proto,
                  uint32_t delta, uint32_t light);

@@ -337,6 +337,7 @@ static int check_options(const gdb_options* o) {
   if (o->max_ctas < 0 || o->oversubscribe < 0) return GDB_ERR_INVALID;
   if (o->xf_release < 0 || o->xf_release > 4) return GDB_ERR_INVALID;
   if (o->sssp_split < -1 || o->sssp_split > 1) return GDB_ERR_INVALID;
+  if (o->pull_bitmap_kb < -1 || o->pull_bitmap_kb > 64) return GDB_ERR_INVALID;
   return GDB_OK;
 }
 
@@ -383,7 +384,7 @@ int gdb_ctx_create(const gdb_options* opt, gdb_ctx** out) {
             cudaEventCreate(&c->ev0) == cudaSuccess && cudaEventCreate(&c->ev1) == cudaSuccess &&
             cudaMalloc(&c->dctx, sizeof(gdb::DeviceCtx)) == cudaSuccess &&
             cudaMalloc(&c->flags, (size_t)c->flag_cap * gdb::kLineInts * sizeof(int)) == cudaSuccess;
-  if (!ok || reset_device_ctx(c, 0) != GDB_OK) {
+  if (!ok || reset_device_ctx(c, 0) != GDB_OK || bfs_prepare(c) != GDB_OK) {
     cudaGetLastError();
     gdb_ctx_destroy(c);
     return GDB_ERR_CUDA;

@@ -186,7 +186,7 @@ int launch(gdb_server* s, Slot& sl, Req& r) {
   GDB_CUDA(c, cudaEventRecord(sl.ev0, sl.stream));
   int rc;
   if (r.app == GDB_APP_BFS)
-    rc = bfs_enqueue(c, g, ws, d_src, 1, (uint32_t*)out, sl.stream, proto);
+    rc = bfs_enqueue(c, g, ws, d_src, 1, (uint32_t*)out, sl.stream, proto, false);
   else if (r.app == GDB_APP_SSSP)
     rc = sssp_enqueue(c, g, ws, d_src, 1, (uint32_t*)out, sl.stream, proto, ge.delta, ge.light);
   else

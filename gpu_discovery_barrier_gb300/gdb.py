@@ -23,7 +23,7 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libgdb.so"
 
-ABI_VERSION = 9  # GDB_ABI_VERSION of include/gdb.h
+ABI_VERSION = 10  # GDB_ABI_VERSION of include/gdb.h
 LONESTAR_INF = 1_000_000_000
 PANNOTIA_BIG = 99_999_999
 
@@ -48,7 +48,7 @@ class Options(C.Structure):
                 ("oversubscribe", C.c_int), ("lock", C.c_int), ("barrier", C.c_int),
                 ("schedule", C.c_int), ("xf_release", C.c_int), ("timeout_ns", C.c_uint64),
                 ("pull_alpha", C.c_uint32), ("push_beta", C.c_uint32), ("sssp_delta", C.c_uint32),
-                ("sssp_split", C.c_int)]
+                ("sssp_split", C.c_int), ("pull_bitmap_kb", C.c_int)]
 
 
 class RunStats(C.Structure):

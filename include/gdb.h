@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GDB_ABI_VERSION 9
+#define GDB_ABI_VERSION 10
 
 /* Sentinels of the reference kernels. */
 #define GDB_LONESTAR_INF 1000000000u /* lonestar/apps/bfs/kernel/bfs_common.cl:35 */
@@ -110,6 +110,16 @@ typedef struct {
      bucket's heavy arcs are relaxed once when it runs dry.  0 = automatic
      (split when some weight >= the width), 1 = always, -1 = never. */
   int sssp_split;
+  /* frontier bitmap of the direction-optimising BFS: a bottom-up (pull)
+     level tests a neighbour's bit in its frontier's V-bit bitmap instead of
+     loading the neighbour's level, and writes the next level's bitmap; the
+     bitmap's first pull_bitmap_kb KB (the lowest vertex ids) are staged in
+     every CTA's shared memory for the level.  1..64 = that stage everywhere,
+     -1 = no bitmap (pull levels test the level array), 0 = automatic: 16 KB
+     for a traversal that has the GPU to itself (gdb_bfs, gdb_bfs_multi,
+     batches, traces), no bitmap for traversals that share it
+     (gdb_bfs_sources, serving slots). */
+  int pull_bitmap_kb;
 } gdb_options;
 
 typedef struct {

@@ -74,3 +74,15 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for f, _ in py._fields_:
             assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+@pytest.mark.parametrize("field,value", [("pull_bitmap_kb", 65), ("pull_bitmap_kb", -2),
+                                         ("sssp_split", 2), ("xf_release", 5)])
+def test_out_of_range_options_are_rejected_before_any_cuda_call(field, value):
+    """gdb_ctx_create checks the options first: no device is touched."""
+    from gpu_discovery_barrier_gb300 import gdb
+
+    o = gdb.default_options(**{field: value})
+    h = ctypes.c_void_p()
+    assert gdb.lib().gdb_ctx_create(ctypes.byref(o), ctypes.byref(h)) == -1
+    assert not h.value
