@@ -69,7 +69,7 @@ def parse():
     p.add_argument("--graph", default=None,
                    help="rmat workload: run the suite on this .gr / DIMACS / METIS file instead "
                         "(undirected; its weights for SSSP when it has them)")
-    p.add_argument("--workload", choices=["rmat", "grid4096", "batch", "serve", "relaunch"],
+    p.add_argument("--workload", choices=["rmat", "grid4096", "batch", "serve", "relaunch", "barrier"],
                    default="rmat",
                    help="rmat: the R-MAT suite (default); grid4096: the barrier-bound "
                         "4096x4096 grid, BFS and SSSP from the corner per barrier kind")
@@ -946,6 +946,52 @@ def run_relaunch(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def run_barrier(args, rank, world, local):
+    """The barrier alone: nanoseconds per barrier of every kind at 1, 2, 3
+    and 4 CTAs of 512 threads per SM (gdb_barrier_bench: empty supersteps;
+    the persistent kinds run 20,000 barriers in one launch, the relaunch
+    kinds one launch per superstep), the median of `steps` runs after
+    `warmup` unrecorded ones.  The headline is the XF barrier at 4 CTAs per
+    SM, the reference's full co-residency."""
+    import torch
+
+    from gpu_discovery_barrier_gb300 import gdb
+
+    torch.cuda.set_device(local)
+    kinds = {"xf": gdb.BARRIER_XF, "xf_fixed": gdb.BARRIER_XF_FIXED,
+             "grid_sync": gdb.BARRIER_GRID_SYNC, "relaunch": gdb.BARRIER_RELAUNCH,
+             "relaunch_graph": gdb.BARRIER_RELAUNCH_GRAPH}
+    res = {}
+    with gdb.Ctx() as c:
+        sms = c.device_info()["sm_count"]
+        for per in (1, 2, 3, 4):
+            c.set_options(max_ctas=per * sms)
+            row = {}
+            for name, kind in kinds.items():
+                iters = 2000 if name.startswith("relaunch") else 20000
+                for _ in range(args.warmup):
+                    c.barrier_bench(kind, 512, iters)
+                runs = [c.barrier_bench(kind, 512, iters) for _ in range(args.steps)]
+                row[name] = {"ns": statistics.median(r[0] for r in runs), "ctas": runs[0][1]}
+            row["xf_over_grid_sync"] = row["xf"]["ns"] / row["grid_sync"]["ns"]
+            res[str(per * sms)] = row
+    if rank == 0:
+        full = res[str(4 * sms)]
+        line = {
+            "metric": "ns per barrier (XF barrier, 4 CTAs of 512 threads per SM)",
+            "value": full["xf"]["ns"], "unit": "ns", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": full["xf"]["ns"] * 20000 / 1e6,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "none (empty supersteps)",
+            "config": {"workload": "barrier alone, 1-4 CTAs of 512 threads per SM", "block": 512,
+                       "sms": sms, "parallelism": f"replicas x{world}",
+                       "l2": "no data (barrier words only)"},
+            "per_ctas": res,
+            "gpu_launches": args.steps,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def run_batch(args, rank, world, local):
     """Mixed batch: n graphs (V log-uniform in [1e3, 1e6], half R-MAT with
     edge factor 8..32, half grids with aspect ratio log-uniform in [1, 64]),
@@ -1235,6 +1281,8 @@ def main():
         run_serve(args, rank, world, local)
     elif args.workload == "relaunch":
         run_relaunch(args, rank, world, local)
+    elif args.workload == "barrier":
+        run_barrier(args, rank, world, local)
     else:
         run_gdb(args, rank, world, local)
     if world > 1:
