@@ -967,15 +967,21 @@ static int sssp_auto_delta(gdb_ctx* c, gdb_graph* g, uint32_t* delta) {
   return GDB_OK;
 }
 
-// Automatic width: the Davidson et al. width, halved when the light/heavy
-// split is allowed and some arc weighs at least half of it (with heavy arcs
-// relaxed once per vertex, narrower buckets pay: on R-MAT-22 with U[1,255]
-// weights the split run takes 3.0 ms per source at widths 48-64 against 3.7
-// ms at the full width 128 and 4.2 ms for the worklist).
+// Automatic width: the Davidson et al. width, a quarter of it when the
+// light/heavy split is allowed and some arc weighs at least half of it.
+// With heavy arcs relaxed once per vertex, narrow buckets pay: a bucket's
+// near supersteps re-expand a vertex each time its distance improves, and
+// on a power-law graph the first bucket holds most hubs.  R-MAT-22 with
+// U[1,255] weights (the rule's width 134), 16 sources on lanes:
+//   width 24: 16.4 ms, 28: 15.4, 32: 15.6, 40: 17.3, 48: 18.2, 67: 20.6,
+//   96: 25.3, 134: 31.9 ms.
+// Graphs whose weights stay below half the width (the 4096^2 grid: width
+// 1,024, no split) keep the full width, where narrower buckets only add
+// supersteps (grid SSSP 108 ms at 1,024, 131 at 512, 157 at 256).
 static int sssp_auto_width(gdb_ctx* c, gdb_graph* g, uint32_t* delta) {
   int rc = sssp_auto_delta(c, g, delta);
   if (rc || c->opt.sssp_split < 0 || *delta < 2) return rc;
-  if (c->opt.sssp_split == 1 || g->wmax >= *delta / 2) *delta /= 2;
+  if (c->opt.sssp_split == 1 || g->wmax >= *delta / 2) *delta = std::max<uint32_t>(*delta / 4, 1u);
   return GDB_OK;
 }
 
