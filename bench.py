@@ -290,9 +290,10 @@ class GpuSuite:
             note("mst")
 
     def e2e_buffers(self):
-        """Page-locked host arrays (inputs and results) and the device
-        buffers the end-to-end step copies them to and from; allocated once,
-        reused every step, as a serving loop would."""
+        """Page-locked host arrays (inputs and results) and two sets of
+        device buffers the end-to-end steps copy them to and from (one
+        step's inputs land in one set while the other set's step runs);
+        allocated once, reused every step, as a serving loop would."""
         torch, wl = self.torch, self.wl
         g = wl["g"]
         dev = torch.device("cuda", self.device)
@@ -301,23 +302,21 @@ class GpuSuite:
         outs = {"bfs": np.zeros((NSRC, g.V), np.uint32), "sssp": np.zeros((NSRC, g.V), np.uint32),
                 "mis": np.zeros(g.V, np.int32), "color": np.zeros(g.V, np.int32),
                 "bc": np.zeros(g.V, np.float32)}
-        h, d = {}, {}
+        h, d, d2 = {}, {}, {}
         for k, a in {**ins, **outs}.items():
             h[k] = pinned_tensor(torch, a)
             d[k] = torch.empty_like(h[k], device=dev)
+            d2[k] = torch.empty_like(h[k], device=dev) if k in ins else d[k]
         h["mst"] = torch.zeros(4, dtype=torch.int64, pin_memory=True)
-        d["mst"] = torch.zeros(4, dtype=torch.int64, device=dev)
-        return h, d
+        d["mst"] = d2["mst"] = torch.zeros(4, dtype=torch.int64, device=dev)
+        return h, (d, d2)
 
-    def step_e2e(self, h, d, cs):
-        """The suite from page-locked host inputs to page-locked host
-        results through the library's device-pointer entry points: every
-        input goes up on the copy stream `cs` at the start (BFS waits only
-        for the row and column arrays), every app's result comes back on
-        `cs` while the next app runs, the MST weights arrive under the
-        earlier apps.  Returns the bytes read back."""
-        torch, gdb = self.torch, self.gdb
-        c, g = self.ctx, self.wl["g"]
+    def upload(self, h, d, cs):
+        """Issue one step's input copies (page-locked host -> device) on the
+        copy stream `cs`; returns the events the apps wait for: row, column
+        and sources first, then the weights, the priorities, the MST
+        weights."""
+        torch = self.torch
         ev = {k: torch.cuda.Event() for k in ("rc", "w", "p", "uw")}
         with torch.cuda.stream(cs):
             for k in ("row", "col", "src"):
@@ -329,6 +328,22 @@ class GpuSuite:
             ev["p"].record(cs)
             d["uw"].copy_(h["uw"], non_blocking=True)
             ev["uw"].record(cs)
+        return ev
+
+    def step_e2e(self, h, d, cs, ev=None, d_next=None, us=None):
+        """The suite from page-locked host inputs to page-locked host
+        results through the library's device-pointer entry points.  The
+        step's inputs are on their way (`ev`, from upload(); issued here on
+        `cs` when None); every app's result comes back on the copy stream
+        `cs` while the next app runs.  With `d_next` (the other buffer set),
+        the next step's inputs go up on the upload stream `us` under this
+        step's kernels, in the other direction of the link.  Returns (bytes
+        read back, the next step's upload events or None)."""
+        torch, gdb = self.torch, self.gdb
+        c, g = self.ctx, self.wl["g"]
+        if ev is None:
+            ev = self.upload(h, d, cs)
+        ev_next = self.upload(h, d_next, us) if d_next is not None else None
         outs = 0
 
         def back(k):
@@ -371,7 +386,7 @@ class GpuSuite:
         G.close()
         if Gu is not None:
             Gu.close()
-        return outs
+        return outs, ev_next
 
 
 def pinned_tensor(torch, a: np.ndarray):
@@ -736,22 +751,27 @@ def run_gdb(args, rank, world, local):
     # with the kernels of earlier apps, see GpuSuite.step_e2e)
     e2e = None
     if not args.no_e2e:
-        h, dbuf = suite.e2e_buffers()
+        h, dbufs = suite.e2e_buffers()
         h2d = sum(h[k].numel() * h[k].element_size() for k in ("row", "col", "w", "uw", "prio", "src"))
-        cs = torch.cuda.Stream()
-        suite.step_e2e(h, dbuf, cs)
+        cs, us = torch.cuda.Stream(), torch.cuda.Stream()
+        suite.step_e2e(h, dbufs[0], cs)
         barrier(world)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        d2h = 0
-        for _ in range(args.steps):
-            d2h = suite.step_e2e(h, dbuf, cs)
+        d2h, ev = 0, None
+        # exactly one upload and one read-back per timed step: step 1 sends
+        # its own inputs, each step sends the next one's under its kernels,
+        # the last step sends none
+        for k in range(args.steps):
+            d2h, ev = suite.step_e2e(h, dbufs[k % 2], cs, ev,
+                                     dbufs[(k + 1) % 2] if k + 1 < args.steps else None, us)
         torch.cuda.synchronize()
         dt = reduce_max(time.perf_counter() - t0, world)
         e2e = {"value": world * units_per_step * args.steps / dt, "unit": "edges/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "path": "device-pointer entry points; inputs up on a copy stream, each app's "
-                       "result down while the next app runs"}
+               "path": "device-pointer entry points; each step's inputs up on a copy stream "
+                       "under the previous step's kernels (the first step's at its start), each "
+                       "app's result down while the next app runs"}
         # the last step's results, read back through the host copies, equal
         # the device-resident run's (a check of the end-to-end path)
         # (the device-resident step leaves SSSP's distances and the colours
