@@ -108,31 +108,37 @@ __device__ __forceinline__ bool is_heavy_arc(uint32_t w, uint32_t bound) {
   return w >= bound && w < kInf;
 }
 
-// Light and heavy arc counts of every vertex.
-__global__ void k_split_count(GraphView G, uint32_t bound, uint32_t* nl, uint32_t* nh) {
-  // vertices of degree > kHeavyDeg: one CTA each
-  for (uint32_t h = blockIdx.x; h < G.nheavy; h += gridDim.x) {
-    const uint32_t v = G.heavy_v[h];
-    const uint32_t b = G.row[v], e = G.row[v + 1];
+// Light and heavy arc counts of every vertex (nl, nh zeroed first: a heavy
+// vertex's chunks add theirs) and of every heavy chunk (cl_c, ch_c).
+__global__ void k_split_count(GraphView G, uint32_t bound, uint32_t* nl, uint32_t* nh, uint32_t* cl_c,
+                              uint32_t* ch_c) {
+  const Warps W = warps_of(blockIdx.x, gridDim.x);
+  const int lane = lane_id();
+  // heavy vertices: one warp per 128-arc chunk, its four 32-arc steps'
+  // weight loads in flight together
+  for (uint32_t c = W.gwarp; c < G.nheavy_chunks; c += W.nwarps) {
+    const uint4 ent = __ldg(&G.heavy_chunk[c]);
+    uint32_t b, e;
+    chunk_range(G, ent, b, e);
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) w[j] = b + 32 * j + lane < e ? __ldg(&G.w[b + 32 * j + lane]) : kInf;
     uint32_t cl = 0, ch = 0;
-    for (uint32_t a = b + threadIdx.x; a < e; a += blockDim.x) {
-      const uint32_t w = __ldg(&G.w[a]);
-      cl += is_light(w, bound);
-      ch += is_heavy_arc(w, bound);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      cl += __popc(__ballot_sync(kFull, is_light(w[j], bound)));
+      ch += __popc(__ballot_sync(kFull, is_heavy_arc(w[j], bound)));
     }
-    uint32_t tl, th;
-    cta_exclusive(cl, &tl);
-    cta_exclusive(ch, &th);
-    if (threadIdx.x == 0) {
-      nl[v] = tl;
-      nh[v] = th;
+    if (lane == 0) {
+      cl_c[c] = cl;
+      ch_c[c] = ch;
+      if (cl) atomicAdd(&nl[ent.x], cl);
+      if (ch) atomicAdd(&nh[ent.x], ch);
     }
   }
   // the others: 32 consecutive vertices per warp, their arcs walked together
   // four 32-arc steps at a time; the lanes of one owner in a step are found
   // with __match_any_sync and one of them adds the owner's counts
-  const Warps W = warps_of(blockIdx.x, gridDim.x);
-  const int lane = lane_id();
   __shared__ uint32_t scnt[2][32][32];
   uint32_t* cl_s = scnt[0][threadIdx.x >> 5];
   uint32_t* ch_s = scnt[1][threadIdx.x >> 5];
@@ -168,47 +174,45 @@ __global__ void k_split_count(GraphView G, uint32_t bound, uint32_t* nl, uint32_
 
 // Order-preserving scatter of every vertex's arcs into the two halves.
 __global__ void k_split_scatter(GraphView G, uint32_t bound, const uint32_t* rl, const uint32_t* rh,
-                                uint32_t* cl, uint32_t* wl, uint32_t* ch, uint32_t* wh) {
-  __shared__ uint32_t wsum[2][32];
-  const int lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (uint32_t h = blockIdx.x; h < G.nheavy; h += gridDim.x) {
-    const uint32_t v = G.heavy_v[h];
-    const uint32_t b = G.row[v], e = G.row[v + 1];
-    uint32_t ol = rl[v], oh = rh[v];
-    for (uint32_t a0 = b; a0 < e; a0 += blockDim.x) {
-      const uint32_t a = a0 + threadIdx.x;
-      const bool ok = a < e;
-      const uint32_t w = ok ? __ldg(&G.w[a]) : kInf;
-      const uint32_t c = ok ? __ldg(&G.col[a]) : 0u;
-      const bool il = ok && is_light(w, bound), ih = ok && is_heavy_arc(w, bound);
-      const unsigned ml = __ballot_sync(kFull, il), mh = __ballot_sync(kFull, ih);
-      if (lane == 0) {
-        wsum[0][warp] = __popc(ml);
-        wsum[1][warp] = __popc(mh);
+                                const uint32_t* pl_c, const uint32_t* ph_c, uint32_t* cl, uint32_t* wl,
+                                uint32_t* ch, uint32_t* wh) {
+  const int lane = lane_id();
+  // heavy vertices: one warp per 128-arc chunk; the chunk's arcs start in
+  // the vertex's halves after the arcs of its earlier chunks (pl_c, ph_c:
+  // exclusive scans of the per-chunk counts over the chunk table, where a
+  // vertex's chunks are consecutive), so every row keeps its order
+  {
+    const Warps W = warps_of(blockIdx.x, gridDim.x);
+    for (uint32_t c = W.gwarp; c < G.nheavy_chunks; c += W.nwarps) {
+      const uint4 ent = __ldg(&G.heavy_chunk[c]);
+      uint32_t b, e;
+      chunk_range(G, ent, b, e);
+      const uint32_t c0 = c - ent.y;  // the vertex's first chunk
+      uint32_t ol = rl[ent.x] + (pl_c[c] - pl_c[c0]), oh = rh[ent.x] + (ph_c[c] - ph_c[c0]);
+      uint32_t w[4], u[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t a = b + 32 * j + lane;
+        w[j] = a < e ? __ldg(&G.w[a]) : kInf;
+        u[j] = a < e ? __ldg(&G.col[a]) : 0u;
       }
-      __syncthreads();
-      uint32_t pl = 0, ph = 0, tl = 0, th = 0;
-      for (int k = 0; k < nw; ++k) {
-        if (k < warp) {
-          pl += wsum[0][k];
-          ph += wsum[1][k];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const bool il = is_light(w[j], bound), ih = is_heavy_arc(w[j], bound);
+        const unsigned ml = __ballot_sync(kFull, il), mh = __ballot_sync(kFull, ih);
+        if (il) {
+          const uint32_t p = ol + __popc(ml & lanemask_lt());
+          cl[p] = u[j];
+          wl[p] = w[j];
         }
-        tl += wsum[0][k];
-        th += wsum[1][k];
+        if (ih) {
+          const uint32_t p = oh + __popc(mh & lanemask_lt());
+          ch[p] = u[j];
+          wh[p] = w[j];
+        }
+        ol += __popc(ml);
+        oh += __popc(mh);
       }
-      if (il) {
-        const uint32_t p = ol + pl + __popc(ml & lanemask_lt());
-        cl[p] = c;
-        wl[p] = w;
-      }
-      if (ih) {
-        const uint32_t p = oh + ph + __popc(mh & lanemask_lt());
-        ch[p] = c;
-        wh[p] = w;
-      }
-      ol += tl;
-      oh += th;
-      __syncthreads();
     }
   }
   // the others: 32 consecutive vertices per warp, four 32-arc steps at a
@@ -417,10 +421,13 @@ int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
   gdb_graph* L = new_half(c, V);
   gdb_graph* H = new_half(c, V);
   gdb_graph* T = nullptr;  // transpose of H, built last
-  // scratch: four V + 1 word arrays, the scan's tile sums, totals
+  // scratch: four V + 1 word arrays, the scan's tile sums, totals, and
+  // four arrays over the heavy chunks (counts and their scans)
   const size_t vw = (size_t)V + 1;
+  const uint32_t nch = g->nheavy_chunks;
+  const size_t cw = (size_t)nch + 1;
   uint32_t* scratch = nullptr;
-  const size_t words = 4 * vw + scan_tmp_words(V) + 8;
+  const size_t words = 4 * vw + std::max(scan_tmp_words(V), scan_tmp_words(nch)) + 8 + 4 * cw;
   int rc = GDB_OK;
   auto fail = [&](int r) {
     if (scratch) cudaFreeAsync(scratch, st);
@@ -433,16 +440,23 @@ int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
   cudaError_t e = cudaMallocAsync((void**)&scratch, words * 4, st);
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split scratch"));
   uint32_t *t0 = scratch, *t1 = t0 + vw, *t2 = t1 + vw, *t3 = t2 + vw, *tmp = t3 + vw,
-           *hs = tmp + scan_tmp_words(V);
+           *hs = tmp + std::max(scan_tmp_words(V), scan_tmp_words(nch)), *cl_c = hs + 8, *ch_c = cl_c + cw,
+           *pl_c = ch_c + cw, *ph_c = pl_c + cw;
   e = dev_alloc(c, (void**)&L->row, vw * 4);
   if (e == cudaSuccess) e = dev_alloc(c, (void**)&H->row, vw * 4);
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split rows"));
   const GraphView G = g->view();
   const int grid = 8 * c->sm_count;  // every 256-thread CTA resident: the loops are latency-bound
-  k_split_count<<<grid, 256, 0, st>>>(G, bound, t0, t1);
-  e = cudaGetLastError();
+  // a heavy vertex's counts are added up over its chunks
+  e = cudaMemsetAsync(t0, 0, 2 * vw * 4, st);
+  if (e == cudaSuccess) {
+    k_split_count<<<grid, 256, 0, st>>>(G, bound, t0, t1, cl_c, ch_c);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess) e = exclusive_scan(t0, V, L->row, tmp, st);
   if (e == cudaSuccess) e = exclusive_scan(t1, V, H->row, tmp, st);
+  if (e == cudaSuccess && nch) e = exclusive_scan(cl_c, nch, pl_c, tmp, st);
+  if (e == cudaSuccess && nch) e = exclusive_scan(ch_c, nch, ph_c, tmp, st);
   uint32_t* hh = (uint32_t*)pinned(c, 64);
   if (!hh) return fail(GDB_ERR_OOM);
   if (e == cudaSuccess) e = cudaMemcpyAsync(hh, L->row + V, 4, cudaMemcpyDeviceToHost, st);
@@ -456,7 +470,7 @@ int arc_split(gdb_ctx* c, gdb_graph* g, uint32_t bound) {
   if (e == cudaSuccess) e = dev_alloc(c, (void**)&H->col, std::max<uint64_t>(H->E, 1) * 4);
   if (e == cudaSuccess) e = dev_alloc(c, (void**)&H->w, std::max<uint64_t>(H->E, 1) * 4);
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split arcs"));
-  k_split_scatter<<<grid, 256, 0, st>>>(G, bound, L->row, H->row, L->col, L->w, H->col, H->w);
+  k_split_scatter<<<grid, 256, 0, st>>>(G, bound, L->row, H->row, pl_c, ph_c, L->col, L->w, H->col, H->w);
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(set_cuda_error(c, e, "arc split scatter"));
   if ((rc = heavy_table_device(c, L, t0, t1, t2, t3, tmp, hs))) return fail(rc);
