@@ -721,7 +721,7 @@ __global__ void __launch_bounds__(512, 3) k_bc_rl_step(GraphView G, BcWs ws, Ste
 
 // out[v] = the lanes' partial sums, in lane order (deterministic).
 struct LaneParts {
-  const float* p[gdbi::kLanes];
+  const float* p[gdbi::kMaxLanes];
   int k;
 };
 __global__ void k_bc_sum(float* out, LaneParts parts, uint32_t V) {
@@ -817,7 +817,7 @@ static int bc_lanes(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_
   int occ = 0;
   GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bc_xf, c->opt.block_size, 0));
   std::vector<unsigned long long> st((size_t)k * 4);
-  int rc = run_on_lanes(c, k, vb + bc_workspace_bytes(g), occ * c->sm_count,
+  int rc = run_on_lanes(c, k, (int)k, vb + bc_workspace_bytes(g), occ * c->sm_count,
                         [&](gdb_lane& L, uint32_t j) {
                           const uint32_t b = j * nsrc / k, e = (j + 1) * nsrc / k;
                           return bc_enqueue(c, g, L.ws + vb, d_sources + b, e - b, (float*)L.ws,

@@ -137,15 +137,20 @@ cudaError_t arm_device_ctx(gdb_ctx* c, gdb::DeviceCtx* d, int* flags, cudaStream
 // in c->last.kernel_ms.
 // stats_out (optional, n x 4): the first four statistics words of each
 // run's counter block (the last 512 bytes of its workspace).
-int run_on_lanes(gdb_ctx* c, uint32_t n, size_t ws_bytes, int fit,
+// `lanes`: how many concurrent lanes (at most kMaxLanes) the n runs share.
+int run_on_lanes(gdb_ctx* c, uint32_t n, int lanes, size_t ws_bytes, int fit,
                  const std::function<int(gdb_lane&, uint32_t)>& run,
                  unsigned long long* stats_out = nullptr);
 // Discovery arguments of a launch on lane L.
 gdb::DiscoveryArgs lane_args(gdb_ctx* c, const gdb_lane& L);
 void lanes_destroy(gdb_ctx* c);
-// Lanes of a many-source call (R-MAT-22, 16 sources: BFS 3.6 / 2.8 / 3.0 /
-// 4.2 ms and SSSP 24.0 / 21.0 / 22.2 / 21.8 ms on 2 / 4 / 6 / 8 lanes).
-constexpr int kLanes = 4;
+// Lanes of a many-source call.  R-MAT-22, 16 sources, learned schedule:
+//   BFS  3.44 / 2.97 / 2.90 / 2.85 / 6.87 ms on 3 / 4 / 6 / 8 / 16 lanes,
+//   SSSP 18.37 / 16.20 / 16.65 / 15.57 / 15.26 ms on the same counts
+// (16 sources over 6 lanes leave two lanes short).  BC runs on 2 (gdb_bc.cu).
+constexpr int kMaxLanes = 16;
+constexpr int kBfsLanes = 8;
+constexpr int kSsspLanes = 16;
 int read_participating(gdb_ctx* c, int* n);
 
 // Light (weight < bound) and heavy (bound <= weight < infinity) halves of

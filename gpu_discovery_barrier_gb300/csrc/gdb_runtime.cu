@@ -131,10 +131,11 @@ gdb::DiscoveryArgs lane_args(gdb_ctx* c, const gdb_lane& L) {
   return a;
 }
 
-int run_on_lanes(gdb_ctx* c, uint32_t n, size_t ws_bytes, int fit,
+int run_on_lanes(gdb_ctx* c, uint32_t n, int lanes, size_t ws_bytes, int fit,
                  const std::function<int(gdb_lane&, uint32_t)>& run,
                  unsigned long long* stats_out) {
-  const int k = (int)std::min<uint32_t>(kLanes, std::max<uint32_t>(n, 1u));
+  const int k = (int)std::min<uint32_t>((uint32_t)std::min(std::max(lanes, 1), kMaxLanes),
+                                        std::max<uint32_t>(n, 1u));
   while ((int)c->lanes.size() < k) {
     gdb_lane L;
     cudaError_t e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking);

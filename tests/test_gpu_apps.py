@@ -233,11 +233,12 @@ def test_bc(ctx, name, g):
     assert not np.any(np.isfinite(got[~fin])), name
 
 
-@pytest.mark.parametrize("n", [1, 3, 7])
+@pytest.mark.parametrize("n", [1, 3, 7, 17])
 @pytest.mark.parametrize("schedule", [gdb.SCHED_PLAIN, gdb.SCHED_ADAPTIVE])
 def test_many_sources_on_lanes(n, schedule):
     """Independent runs of several sources on concurrent lanes: row i is the
-    single-source answer of sources[i]."""
+    single-source answer of sources[i] (17 sources: more than the 8 lanes of
+    BFS and the 16 of SSSP, so lanes run several sources in turn)."""
     g = gg.rmat(1 << 13, 16, seed=41)
     w = gg.uniform_weights(g, 1, 255, seed=7)
     gw = g.with_weights(w)
