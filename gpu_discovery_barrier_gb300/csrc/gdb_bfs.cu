@@ -626,12 +626,13 @@ static size_t bfs_layout(const gdb_graph* g, char* base, uint32_t* d_dist, BfsWs
 
 // The automatic frontier bitmap (pull_bitmap_kb 0): a 16 KB stage
 // (131,072 vertex ids) for a traversal that has the GPU to itself; none
-// for traversals that share it.  Measured on R-MAT-22 (learned schedule):
-// one source 0.380 -> 0.354 ms with the bitmap (threshold schedule 0.352
-// -> 0.314 ms), while 16 sources on four concurrent lanes go 2.93 ->
-// 3.02 ms -- their pull levels are bandwidth-bound, and the bitmap's
-// build pass costs more than its shared-memory probes save.  Stages of
-// 48 KB and more cost occupancy and L1 (one source 0.40 / 0.46 ms).
+// for traversals that share it.  Measured on R-MAT-22, one source per
+// call, mean over 16 sources: learned schedule 0.349 -> 0.333 ms with the
+// bitmap, threshold schedule 0.324 -> 0.302 ms; 16 sources on four
+// concurrent lanes go 2.93 -> 3.02 ms -- their pull levels are
+// bandwidth-bound, and the bitmap's build pass costs more than its
+// shared-memory probes save.  Stages of 48 KB and more cost occupancy and
+// L1 (one source 0.40 / 0.46 ms against 0.36 at 16 KB).
 constexpr uint32_t kStageKbAuto = 16;
 constexpr uint32_t kStageKbMax = 64;
 

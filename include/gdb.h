@@ -491,8 +491,8 @@ int gdb_dmr_refine(gdb_ctx* ctx, const double* x, const double* y, uint32_t nnod
  * and barrier state live in one fixed device array inside the library
  * (about 8.6 MB, kept by every GPU that loads the library until the process
  * exits).  V above GDB_NOALLOC_MAX_VERTICES returns GDB_ERR_INVALID.
- * The first call on a device looks up that array's address and arms it, so
- * make that first call before any stream capture.  All calls share the
+ * The first call on a device looks up that array's address and arms it.
+ * All calls share the
  * array: calls that overlap on the GPU (other streams, other threads) race
  * and must be serialised by the caller.  Synchronous: every call waits
  * for its stream and reads the run's status back to host memory before it

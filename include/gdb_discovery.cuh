@@ -99,12 +99,12 @@ enum XfRelease {
 };
 
 // Participants up to which the flat form is used.  In isolation (empty
-// supersteps, every CTA arriving at once) it beats the combining form up
-// to 456 CTAs of 512 threads (flat 1.36 / 1.54 / 1.80 / 2.30 us at 152 /
-// 304 / 456 / 608, combining 2.02-2.05 us at every count), but inside real
-// kernels, whose arrivals spread out, it also wins at 608 (4096^2 grid BFS,
-// 8,191 levels: 46.4 ms flat, 53.3 ms combining); the one counter every
-// CTA polls is its limit beyond a GPU's worth of CTAs.
+// supersteps, every CTA arriving at once) it beats the combining form at
+// every co-resident count of 512-thread CTAs (flat 1.21 / 1.26 / 1.39 /
+// 1.53 us at 152 / 304 / 456 / 608, combining 2.02-2.05 us), and inside
+// real kernels too (4096^2 grid BFS, 8,191 levels: 46.4 ms flat, 53.3 ms
+// combining, with the earlier flat form); the one counter every CTA polls
+// is its limit beyond a GPU's worth of CTAs.
 constexpr int kXfFlatMax = 1024;
 
 // The form a launch's barriers take (uniform: P is the same in every CTA).
