@@ -806,10 +806,10 @@ int gdbi::bc_enqueue(gdb_ctx* c, gdb_graph* g, void* wsbase, const uint32_t* d_s
 
 // Several sources: contiguous groups of them on concurrent lanes, each
 // lane summing into its own array, then one pass adds the lanes' arrays.
-// Two lanes: BC's launches are longer and fuller than BFS's and SSSP's
-// (R-MAT-22, 16 sources: 20.9 ms on one launch, 17.7 ms on two lanes, 19.9
-// on four, 25.7 on six).
-constexpr uint32_t kBcLanes = 2;
+// Four lanes: BC's launches are longer and fuller than BFS's and SSSP's
+// (R-MAT-22, 16 sources: 16.7 ms on two lanes, 16.2 on four, 18.2 on
+// eight, 27.3 on sixteen; on one launch, an earlier build took 20.9 ms).
+constexpr uint32_t kBcLanes = 4;
 
 static int bc_lanes(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc, float* d_bc) {
   const uint32_t k = std::min<uint32_t>(kBcLanes, nsrc);

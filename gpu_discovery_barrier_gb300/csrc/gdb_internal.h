@@ -147,7 +147,7 @@ void lanes_destroy(gdb_ctx* c);
 // Lanes of a many-source call.  R-MAT-22, 16 sources, learned schedule:
 //   BFS  3.44 / 2.97 / 2.90 / 2.85 / 6.87 ms on 3 / 4 / 6 / 8 / 16 lanes,
 //   SSSP 18.37 / 16.20 / 16.65 / 15.57 / 15.26 ms on the same counts
-// (16 sources over 6 lanes leave two lanes short).  BC runs on 2 (gdb_bc.cu).
+// (16 sources over 6 lanes leave two lanes short).  BC runs on 4 (gdb_bc.cu).
 constexpr int kMaxLanes = 16;
 constexpr int kBfsLanes = 8;
 constexpr int kSsspLanes = 16;
