@@ -330,20 +330,21 @@ class GpuSuite:
             ev["uw"].record(cs)
         return ev
 
-    def step_e2e(self, h, d, cs, ev=None, d_next=None, us=None):
+    def step_e2e(self, h, d, cs, ev=None, d_next=None, us=None, h_next=None):
         """The suite from page-locked host inputs to page-locked host
         results through the library's device-pointer entry points.  The
         step's inputs are on their way (`ev`, from upload(); issued here on
         `cs` when None); every app's result comes back on the copy stream
         `cs` while the next app runs.  With `d_next` (the other buffer set),
-        the next step's inputs go up on the upload stream `us` under this
-        step's kernels, in the other direction of the link.  Returns (bytes
-        read back, the next step's upload events or None)."""
+        the next step's inputs (`h_next`, default `h`) go up on the upload
+        stream `us` under this step's kernels, in the other direction of the
+        link.  Returns (bytes read back, the next step's upload events or
+        None)."""
         torch, gdb = self.torch, self.gdb
         c, g = self.ctx, self.wl["g"]
         if ev is None:
             ev = self.upload(h, d, cs)
-        ev_next = self.upload(h, d_next, us) if d_next is not None else None
+        ev_next = self.upload(h if h_next is None else h_next, d_next, us) if d_next is not None else None
         outs = 0
 
         def back(k):
