@@ -817,7 +817,8 @@ static int bc_lanes(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, uint32_
   int occ = 0;
   GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bc_xf, c->opt.block_size, 0));
   std::vector<unsigned long long> st((size_t)k * 4);
-  int rc = run_on_lanes(c, k, (int)k, vb + bc_workspace_bytes(g), occ * c->sm_count,
+  // every lane sums its group into its own array: exactly k lanes
+  int rc = run_on_lanes(c, k, (int)k, false, vb + bc_workspace_bytes(g), occ * c->sm_count,
                         [&](gdb_lane& L, uint32_t j) {
                           const uint32_t b = j * nsrc / k, e = (j + 1) * nsrc / k;
                           return bc_enqueue(c, g, L.ws + vb, d_sources + b, e - b, (float*)L.ws,

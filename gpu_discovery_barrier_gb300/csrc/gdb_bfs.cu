@@ -908,7 +908,7 @@ int gdb_bfs_sources_device(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources, 
   const size_t smem = (size_t)bitmap_stage_words(c, mode, g->V, false) * 4;
   GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kx, c->opt.block_size, smem));
   const int fit = occ * c->sm_count;
-  return run_on_lanes(c, n, kBfsLanes, bfs_workspace_bytes(g), fit, [&](gdb_lane& L, uint32_t i) {
+  return run_on_lanes(c, n, kBfsLanes, true, bfs_workspace_bytes(g), fit, [&](gdb_lane& L, uint32_t i) {
     return bfs_enqueue(c, g, L.ws, d_sources + i, 1, d_dist + i * V, L.stream, lane_args(c, L), false);
   });
 }

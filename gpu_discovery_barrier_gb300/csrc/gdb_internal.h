@@ -137,8 +137,11 @@ cudaError_t arm_device_ctx(gdb_ctx* c, gdb::DeviceCtx* d, int* flags, cudaStream
 // in c->last.kernel_ms.
 // stats_out (optional, n x 4): the first four statistics words of each
 // run's counter block (the last 512 bytes of its workspace).
-// `lanes`: how many concurrent lanes (at most kMaxLanes) the n runs share.
-int run_on_lanes(gdb_ctx* c, uint32_t n, int lanes, size_t ws_bytes, int fit,
+// `lanes`: how many concurrent lanes (at most kMaxLanes) the n runs share;
+// with `fit_memory`, fewer when the free device memory does not hold a
+// workspace for each (runs whose results do not depend on the lane they
+// run on: any lane count gives the same output).
+int run_on_lanes(gdb_ctx* c, uint32_t n, int lanes, bool fit_memory, size_t ws_bytes, int fit,
                  const std::function<int(gdb_lane&, uint32_t)>& run,
                  unsigned long long* stats_out = nullptr);
 // Discovery arguments of a launch on lane L.

@@ -131,11 +131,24 @@ gdb::DiscoveryArgs lane_args(gdb_ctx* c, const gdb_lane& L) {
   return a;
 }
 
-int run_on_lanes(gdb_ctx* c, uint32_t n, int lanes, size_t ws_bytes, int fit,
+int run_on_lanes(gdb_ctx* c, uint32_t n, int lanes, bool fit_memory, size_t ws_bytes, int fit,
                  const std::function<int(gdb_lane&, uint32_t)>& run,
                  unsigned long long* stats_out) {
-  const int k = (int)std::min<uint32_t>((uint32_t)std::min(std::max(lanes, 1), kMaxLanes),
-                                        std::max<uint32_t>(n, 1u));
+  int k = (int)std::min<uint32_t>((uint32_t)std::min(std::max(lanes, 1), kMaxLanes),
+                                  std::max<uint32_t>(n, 1u));
+  if (fit_memory && k > 1) {
+    // lanes that already hold a large enough workspace, plus as many new
+    // ones as half of the free device memory holds (at least one lane)
+    int ready = 0;
+    for (int i = 0; i < (int)c->lanes.size() && i < k; ++i) ready += c->lanes[i].ws_bytes >= ws_bytes;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && ws_bytes > 0) {
+      const size_t more = free_b / 2 / ws_bytes;
+      k = std::max(1, (int)std::min<size_t>((size_t)k, (size_t)ready + more));
+    } else {
+      cudaGetLastError();
+    }
+  }
   while ((int)c->lanes.size() < k) {
     gdb_lane L;
     cudaError_t e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking);

@@ -1391,7 +1391,8 @@ int gdb_sssp_sources_device(gdb_ctx* c, gdb_graph* g, const uint32_t* d_sources,
   if (rc) return rc;
   int occ = 0;
   GDB_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sssp_xf, c->opt.block_size, 0));
-  rc = run_on_lanes(c, n, kSsspLanes, sssp_workspace_bytes(g), occ * c->sm_count, [&](gdb_lane& L, uint32_t i) {
+  rc = run_on_lanes(c, n, kSsspLanes, true, sssp_workspace_bytes(g), occ * c->sm_count,
+                    [&](gdb_lane& L, uint32_t i) {
     return sssp_enqueue(c, g, L.ws, d_sources + i, 1, d_dist + i * V, L.stream, lane_args(c, L),
                         delta, light);
   });
