@@ -271,14 +271,11 @@ __global__ void __launch_bounds__(512, 3) k_mis_rl_step(GraphView G, MisWs ws, S
 // -- as in the reference, which never terminates then -- they stay
 // uncoloured; the host reports that as an error.
 
-// waitarc bits of arc v -> u
-constexpr uint8_t kWaits = 1;   // u waits for v
-constexpr uint8_t kHeavyT = 2;  // u has degree > kHeavyDeg (a chunked frontier entry)
-
 struct ColorWs {
   int32_t* color;
   uint32_t* cnt;       // neighbours still to be coloured before this vertex
-  uint8_t* waitarc;    // per arc v -> u: kWaits | kHeavyT (set by the count pass)
+  uint32_t* wcol;      // from row[v]: the wcnt[v] neighbours that wait for v (the count pass)
+  uint32_t* wcnt;
   const float* prio;
   uint2* q[2];                 // light vertices as their arc ranges {begin, end}
   uint4* hc[2];                // heavy chunks as {vertex, first arc, end arc, chunk}
@@ -292,7 +289,12 @@ struct ColorWs {
 };
 
 // u waits for v when u looks at its neighbours (degree != 1) and v's
-// priority is not below u's (the count pass stores it per arc v -> u).
+// priority is not below u's.  The count pass packs, for every vertex v,
+// the neighbours waiting for v at the start of v's arc range (wcol from
+// row[v], wcnt[v] of them), so a round walks only arcs that count down:
+// half of the arcs, one load each, and a hub's entry is cut into chunks of
+// its waiting arcs.  A vertex is a heavy (chunked) entry when more than
+// kHeavyDeg neighbours wait for it.
 
 // The colouring's frontier entries carry arc ranges, so a round's consumer
 // needs no row load: the producer loads the rows of every vertex it counts
@@ -383,30 +385,31 @@ __device__ __forceinline__ void push_ranges(const ColorWs& ws, RangeStage& st, u
 __device__ __forceinline__ void color_init(const GraphView& G, const Warps& W, const ColorWs& ws) {
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.color[v] = -1;
-    if (is_heavy(G, v)) ws.cnt[v] = 0;
+    if (is_heavy(G, v)) ws.cnt[v] = ws.wcnt[v] = 0;
   }
 }
 
-// Superstep 1: count the neighbours each vertex waits for.
+// Superstep 1: count the neighbours each vertex waits for, and pack the
+// neighbours that wait for it (my / wmy: per-lane counters of a warp).
 __device__ __forceinline__ void color_count(const GraphView& G, const ColorWs& ws, uint32_t* my,
-                                            unsigned long long& arcs) {
+                                            uint32_t* wmy, unsigned long long& arcs) {
   const int lane = lane_id();
-  // The same pass records, per arc v -> u, whether u waits for v, so that
-  // the rounds test one byte indexed by the arc instead of loading u's
-  // priority and degree after u itself.
   {
     float pv_lane = 0.f;
     bool looks_lane = false;
+    uint32_t rv_lane = 0;
     // four 32-arc steps at once: the neighbours' priority and degree loads
     // of the four are in flight together
     sweep_light4(
         G, &ws.cursor[0],
         [&](uint32_t v, bool in_range) {
           my[lane] = 0;
+          wmy[lane] = 0;
           pv_lane = in_range ? __ldg(&ws.prio[v]) : 0.f;
-          // a degree-1 vertex never looks at its neighbour (but its arc
-          // still needs its waits-for byte)
-          looks_lane = in_range && __ldg(&G.row[v + 1]) - __ldg(&G.row[v]) != 1;
+          rv_lane = in_range ? __ldg(&G.row[v]) : 0u;
+          // a degree-1 vertex never looks at its neighbour (but its
+          // neighbour may wait for it)
+          looks_lane = in_range && __ldg(&G.row[v + 1]) - rv_lane != 1;
           return in_range;
         },
         [&](const bool* valid, const int* owner, const uint32_t* arc) {
@@ -426,18 +429,22 @@ __device__ __forceinline__ void color_count(const GraphView& G, const ColorWs& w
           for (int j = 0; j < 4; ++j) {
             const float pv = __shfl_sync(kFull, pv_lane, owner[j]);
             const bool looks = __shfl_sync(kFull, looks_lane, owner[j]);
+            const uint32_t rv = __shfl_sync(kFull, rv_lane, owner[j]);
             if (valid[j]) {
               if (looks && pu[j] >= pv) atomicAdd(&my[owner[j]], 1u);
-              ws.waitarc[arc[j]] =
-                  (pv >= pu[j] && du[j] != 1 ? kWaits : 0) | (du[j] > kHeavyDeg ? kHeavyT : 0);
+              if (pv >= pu[j] && du[j] != 1) ws.wcol[rv + atomicAdd(&wmy[owner[j]], 1u)] = u[j];
             }
           }
         },
         [&](uint32_t v, bool) {
-          if (v < G.V && !is_heavy(G, v)) ws.cnt[v] = my[lane];
+          if (v < G.V && !is_heavy(G, v)) {
+            ws.cnt[v] = my[lane];
+            ws.wcnt[v] = wmy[lane];
+          }
         });
     sweep_heavy(G, &ws.hcursor[0], [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
       const float pv = __ldg(&ws.prio[v]);
+      const uint32_t rv = __ldg(&G.row[v]);
       uint32_t n = 0;
       // a chunk (kChunk = 128 arcs) as four steps with their loads in flight
       uint32_t u[4], du[4];
@@ -454,16 +461,26 @@ __device__ __forceinline__ void color_count(const GraphView& G, const ColorWs& w
         pu[j] = ok ? __ldg(&ws.prio[u[j]]) : 0.f;
         du[j] = ok ? __ldg(&G.row[u[j] + 1]) - __ldg(&G.row[u[j]]) : 0u;
       }
+      unsigned wm[4];
+      uint32_t nw = 0;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        const uint32_t a = b + 32 * j + lane;
-        if (a < e) {
-          n += pu[j] >= pv;
-          ws.waitarc[a] = (pv >= pu[j] && du[j] != 1 ? kWaits : 0) | (du[j] > kHeavyDeg ? kHeavyT : 0);
-        }
+        const bool ok = b + 32 * j + lane < e;
+        n += ok && pu[j] >= pv;
+        wm[j] = __ballot_sync(kFull, ok && pv >= pu[j] && du[j] != 1);
+        nw += __popc(wm[j]);
       }
       n = warp_add_u32(n);
       if (lane == 0 && n) atomicAdd(&ws.cnt[v], n);
+      // the chunk's waiting neighbours: one reservation in v's packed run
+      uint32_t at = 0;
+      if (lane == 0 && nw) at = atomicAdd(&ws.wcnt[v], nw);
+      at = rv + __shfl_sync(kFull, at, 0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if ((wm[j] >> lane) & 1u) ws.wcol[at + __popc(wm[j] & lanemask_lt())] = u[j];
+        at += __popc(wm[j]);
+      }
     });
   }
 }
@@ -477,14 +494,14 @@ __device__ __forceinline__ void color_first(const GraphView& G, const Warps& W, 
     for (uint32_t g = W.gwarp; g * 32 < G.V; g += W.nwarps) {
       const uint32_t v = g * 32 + lane;
       const bool first = v < G.V && ld_cg(&ws.cnt[v]) == 0;
-      uint32_t rb = 0, re = 0;
+      uint32_t rb = 0, wn = 0;
       if (first) {
         ws.color[v] = 1;
         ++coloured;
         rb = __ldg(&G.row[v]);
-        re = __ldg(&G.row[v + 1]);
+        wn = ld_cg(&ws.wcnt[v]);
       }
-      push_ranges(ws, qs, pick(ws.hc, 1), &ws.hcount[1], first, re - rb > kHeavyDeg, v, rb, re);
+      push_ranges(ws, qs, pick(ws.hc, 1), &ws.hcount[1], first, wn > kHeavyDeg, v, rb, rb + wn);
     }
     qs.flush();
     if (leader) ws.cursor[2] = ws.hcursor[2] = 0;
@@ -530,35 +547,34 @@ __device__ __forceinline__ bool color_round(const GraphView& G, const Warps& W, 
   uint4* hc_out = pick(ws.hc, r + 1);
   unsigned long long* hcount_out = &ws.hcount[nxt];
   const int32_t next_color = (int32_t)r + 1;
-  // up to four 32-arc steps at once: their column, wait-byte loads and
+  // up to four 32-arc steps at once: their neighbour loads and
   // count-downs are all in flight together (a round is a chain of
-  // dependent round trips, and thousands of rounds run one after another)
+  // dependent round trips, and thousands of rounds run one after another).
+  // Every packed arc leads to a neighbour waiting for this vertex.
   auto relax4 = [&](const bool* valid, const int*, const uint32_t* arc) {
     uint32_t u[4];
-    uint8_t wa[4];
 #pragma unroll
     for (int s4 = 0; s4 < 4; ++s4) {
-      u[s4] = valid[s4] ? __ldg(&G.col[arc[s4]]) : 0u;
-      wa[s4] = valid[s4] ? ws.waitarc[arc[s4]] : (uint8_t)0;
+      u[s4] = valid[s4] ? __ldcg(&ws.wcol[arc[s4]]) : 0u;
       arcs += valid[s4];
     }
-    uint32_t old4[4], rb[4], re[4];
+    uint32_t old4[4], rb[4], wn[4];
 #pragma unroll
     for (int s4 = 0; s4 < 4; ++s4) {
-      const bool w = wa[s4] & kWaits;
-      old4[s4] = w ? atomicSub(&ws.cnt[u[s4]], 1u) : 0u;
-      // the rows of a vertex this count-down may complete, loaded with it
-      rb[s4] = w ? __ldg(&G.row[u[s4]]) : 0u;
-      re[s4] = w ? __ldg(&G.row[u[s4] + 1]) : 0u;
+      old4[s4] = valid[s4] ? atomicSub(&ws.cnt[u[s4]], 1u) : 0u;
+      // the packed run of a vertex this count-down may complete, loaded
+      // with it
+      rb[s4] = valid[s4] ? __ldg(&G.row[u[s4]]) : 0u;
+      wn[s4] = valid[s4] ? ld_cg(&ws.wcnt[u[s4]]) : 0u;
     }
 #pragma unroll
     for (int s4 = 0; s4 < 4; ++s4) {
-      const bool ready = (wa[s4] & kWaits) && old4[s4] == 1u;
+      const bool ready = valid[s4] && old4[s4] == 1u;
       if (ready) {
         ws.color[u[s4]] = next_color;
         ++coloured;
       }
-      push_ranges(ws, qs, hc_out, hcount_out, ready, wa[s4] & kHeavyT, u[s4], rb[s4], re[s4]);
+      push_ranges(ws, qs, hc_out, hcount_out, ready, wn[s4] > kHeavyDeg, u[s4], rb[s4], rb[s4] + wn[s4]);
     }
   };
   const uint32_t k = group_width(n, W.nwarps);
@@ -598,15 +614,12 @@ template <class Sync>
 __device__ __forceinline__ void color_body(Sync& s, const GraphView& G, const ColorWs& ws, uint32_t* smem) {
   const Warps W = warps_of(s.id(), s.P());
   const bool leader = s.id() == 0 && threadIdx.x == 0;
-  uint32_t* my = smem + (threadIdx.x & ~31u);
+  uint32_t* my = smem + (threadIdx.x & ~31u);  // smem: 2 x 512 words
   __shared__ uint2 rstage[kMaxGraphWarps][64];  // per-warp queue staging
   unsigned long long arcs = 0, coloured = 0;
   color_init(G, W, ws);
   if (!s.sync()) return;
-  // The count pass also records, per arc v -> u, whether u waits for v, so
-  // that the rounds test one byte indexed by the arc instead of loading u's
-  // priority and degree after u itself.
-  color_count(G, ws, my, arcs);
+  color_count(G, ws, my, my + 512, arcs);
   if (!s.sync()) return;
   color_first(G, W, ws, leader, rstage, coloured);
   if (!s.sync()) return;
@@ -655,7 +668,7 @@ __global__ void __launch_bounds__(512, 1) k_color_rl_step(GraphView G, ColorWs w
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
   unsigned long long arcs = 0, coloured = 0;
   if (kind == 0)
-    color_count(G, ws, smem + (threadIdx.x & ~31u), arcs);
+    color_count(G, ws, smem + (threadIdx.x & ~31u), smem + 512 + (threadIdx.x & ~31u), arcs);
   else if (kind == 1)
     color_first(G, W, ws, leader, rstage, coloured);
   else
@@ -789,7 +802,8 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   const size_t o_cnt_v = b.take((size_t)V * 4);
   const size_t o_q0 = b.take((size_t)V * 8), o_q1 = b.take((size_t)V * 8);
   const size_t o_hc0 = b.take((size_t)hcap * 16), o_hc1 = b.take((size_t)hcap * 16);
-  const size_t o_wa = b.take(std::max<uint64_t>(g->E, 1));
+  const size_t o_wcol = b.take(std::max<uint64_t>(g->E, 1) * 4);
+  const size_t o_wcnt = b.take((size_t)V * 4);
   const size_t o_cnt = b.take(512);
   const size_t o_ctl = b.take(sizeof(StepCtl));
   char* base = (char*)workspace(c, b.off);
@@ -797,7 +811,8 @@ static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_c
   ColorWs ws;
   ws.color = d_color;
   ws.cnt = (uint32_t*)(base + o_cnt_v);
-  ws.waitarc = (uint8_t*)(base + o_wa);
+  ws.wcol = (uint32_t*)(base + o_wcol);
+  ws.wcnt = (uint32_t*)(base + o_wcnt);
   ws.prio = d_prio;
   ws.q[0] = (uint2*)(base + o_q0);
   ws.q[1] = (uint2*)(base + o_q1);
