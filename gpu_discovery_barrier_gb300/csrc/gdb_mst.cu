@@ -8,7 +8,14 @@
 // the device behind the XF barrier.  A round:
 //   A. every vertex finds its lightest arc to another component and
 //      atomicMin's the key (weight << 32 | arc) into its component's slot
-//      (dfindelemin + dfindelemin2 in one step: the arc index breaks ties);
+//      (dfindelemin + dfindelemin2 in one step: the arc index breaks ties).
+//      Components only merge, so the arcs of a unit (a light vertex, or a
+//      128-arc chunk of a heavy one) that leave its component only become
+//      fewer: while the lightest of them found by the unit's last scan
+//      still leaves the component, it is still the lightest, and a unit
+//      that found none never finds one.  A unit scans its arcs again only
+//      when its kept arc has turned internal (R-MAT-22: 0.38 G arcs
+//      scanned over the seven rounds instead of 0.90 G);
 //   B1. every component root records the root its lightest arc reaches;
 //   B2. roots hook onto that root, except the smaller id of a mutual pair,
 //      which stays a root (cs_unify breaks cycles by id too,
@@ -27,10 +34,17 @@ namespace {
 using namespace gdb;
 
 constexpr unsigned long long kNoArc = ~0ull;
+// A unit's kept arc (vcand per light vertex, hcand per heavy chunk): a key,
+// kScan (scan the unit's arcs) or kNone (no arc leaves its component, for
+// good).  Keys stay below 2^62 (weights below kInf).
+constexpr unsigned long long kScan = ~0ull;
+constexpr unsigned long long kNone = ~0ull - 1;
 
 struct MstWs {
   uint32_t* comp;
   unsigned long long* best;
+  unsigned long long* vcand;     // per vertex (light vertices)
+  unsigned long long* hcand;     // per heavy chunk
   uint32_t* partner;
   uint8_t* arc_flag;             // nullable
   uint32_t* cursor;              // [3]
@@ -49,7 +63,9 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.comp[v] = v;
     ws.best[v] = kNoArc;
+    ws.vcand[v] = kScan;
   }
+  for (uint32_t c = W.gthread; c < G.nheavy_chunks; c += W.nthreads) ws.hcand[c] = kScan;
   if (ws.arc_flag)
     for (uint32_t a = W.gthread; a < G.E; a += W.nthreads) ws.arc_flag[a] = 0;
   if (leader) {
@@ -72,6 +88,14 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
           [&](uint32_t v, bool in_range) {
             my[lane] = kNoArc;
             cv = in_range ? ld_cg(&ws.comp[v]) : 0u;
+            if (!in_range) return false;
+            const unsigned long long k = ld_cg(&ws.vcand[v]);
+            if (k == kNone) return false;
+            if (k != kScan && ld_cg(&ws.comp[__ldg(&G.col[(uint32_t)k])]) != cv) {
+              // the kept arc still leaves the component
+              if (k < ld_cg(&ws.best[cv])) atomicMin(&ws.best[cv], k);
+              return false;
+            }
             return true;
           },
           [&](const bool* valid, const int* owner, const uint32_t* arc) {
@@ -93,13 +117,20 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
               }
             }
           },
-          [&](uint32_t, bool act) {
-            if (act && my[lane] != kNoArc) {
-              if (my[lane] < ld_cg(&ws.best[cv])) atomicMin(&ws.best[cv], my[lane]);
-            }
+          [&](uint32_t v, bool act) {
+            if (!act) return;
+            ws.vcand[v] = my[lane] == kNoArc ? kNone : my[lane];
+            if (my[lane] != kNoArc && my[lane] < ld_cg(&ws.best[cv])) atomicMin(&ws.best[cv], my[lane]);
           });
-      sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t, uint32_t, uint32_t b, uint32_t e) {
+      sweep_heavy_indexed(G, &ws.hcursor[cur], [&](uint32_t ci, uint32_t v, uint32_t, uint32_t, uint32_t b,
+                                                    uint32_t e) {
         const uint32_t c = ld_cg(&ws.comp[v]);
+        const unsigned long long kept = ld_cg(&ws.hcand[ci]);
+        if (kept == kNone) return;
+        if (kept != kScan && ld_cg(&ws.comp[__ldg(&G.col[(uint32_t)kept])]) != c) {
+          if (lane == 0 && kept < ld_cg(&ws.best[c])) atomicMin(&ws.best[c], kept);
+          return;
+        }
         unsigned long long m = kNoArc;
         // a chunk's four 32-arc steps with their loads in flight together
         static_assert(kChunk == 4 * 32, "an MST chunk is four steps");
@@ -121,7 +152,10 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
           }
         }
         m = warp_min_u64(m);
-        if (lane == 0 && m != kNoArc) atomicMin(&ws.best[c], m);
+        if (lane == 0) {
+          ws.hcand[ci] = m == kNoArc ? kNone : m;
+          if (m != kNoArc) atomicMin(&ws.best[c], m);
+        }
       });
       if (!s.sync()) return;
       ++t;
@@ -205,12 +239,15 @@ static int mst_run(gdb_ctx* c, gdb_graph* g, gdb_mst_result* h_res, gdb_mst_resu
   Bump b;
   const size_t o_comp = b.take((size_t)V * 4), o_best = b.take((size_t)V * 8),
                o_part = b.take((size_t)V * 4), o_cnt = b.take(256);
+  const size_t o_vc = b.take((size_t)V * 8), o_hc = b.take((size_t)std::max<uint32_t>(g->nheavy_chunks, 1) * 8);
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
   MstWs ws;
   ws.comp = (uint32_t*)(base + o_comp);
   ws.best = (unsigned long long*)(base + o_best);
   ws.partner = (uint32_t*)(base + o_part);
+  ws.vcand = (unsigned long long*)(base + o_vc);
+  ws.hcand = (unsigned long long*)(base + o_hc);
   ws.arc_flag = d_flags;
   char* cnt = base + o_cnt;
   ws.acc = (unsigned long long*)cnt;

@@ -551,9 +551,10 @@ __device__ __forceinline__ void sweep_light4(const GraphView& G, uint32_t* curso
 }
 
 // Sweep the heavy vertices through the static chunk table, kGrab chunks
-// per grab: fn(v, heavy_index, chunk_in_vertex, arc_begin, arc_end).
+// per grab: fn(chunk, v, heavy_index, chunk_in_vertex, arc_begin, arc_end),
+// chunk = the entry's index in the table.
 template <class Fn>
-__device__ __forceinline__ void sweep_heavy(const GraphView& G, uint32_t* hcursor, Fn&& fn) {
+__device__ __forceinline__ void sweep_heavy_indexed(const GraphView& G, uint32_t* hcursor, Fn&& fn) {
   for (;;) {
     const uint32_t c0 = warp_grab(hcursor) * kGrab;
     if (c0 >= G.nheavy_chunks) break;
@@ -561,9 +562,18 @@ __device__ __forceinline__ void sweep_heavy(const GraphView& G, uint32_t* hcurso
       const uint4 ent = __ldg(&G.heavy_chunk[c]);
       uint32_t b, en;
       chunk_range(G, ent, b, en);
-      fn(ent.x, ent.z, ent.y, b, en);
+      fn(c, ent.x, ent.z, ent.y, b, en);
     }
   }
+}
+
+// sweep_heavy_indexed without the chunk index:
+// fn(v, heavy_index, chunk_in_vertex, arc_begin, arc_end).
+template <class Fn>
+__device__ __forceinline__ void sweep_heavy(const GraphView& G, uint32_t* hcursor, Fn&& fn) {
+  sweep_heavy_indexed(G, hcursor, [&](uint32_t, uint32_t v, uint32_t h, uint32_t j, uint32_t b, uint32_t e) {
+    fn(v, h, j, b, e);
+  });
 }
 
 // Warp reductions.
