@@ -13,9 +13,10 @@
 //      128-arc chunk of a heavy one) that leave its component only become
 //      fewer: while the lightest of them found by the unit's last scan
 //      still leaves the component, it is still the lightest, and a unit
-//      that found none never finds one.  A unit scans its arcs again only
-//      when its kept arc has turned internal (R-MAT-22: 0.38 G arcs
-//      scanned over the seven rounds instead of 0.90 G);
+//      that found none never finds one.  A heavy chunk also keeps its
+//      second lightest such arc, which takes over when the first turns
+//      internal.  A unit scans its arcs again only when its kept arcs have
+//      turned internal;
 //   B1. every component root records the root its lightest arc reaches;
 //   B2. roots hook onto that root, except the smaller id of a mutual pair,
 //      which stays a root (cs_unify breaks cycles by id too,
@@ -34,9 +35,10 @@ namespace {
 using namespace gdb;
 
 constexpr unsigned long long kNoArc = ~0ull;
-// A unit's kept arc (vcand per light vertex, hcand per heavy chunk): a key,
-// kScan (scan the unit's arcs) or kNone (no arc leaves its component, for
-// good).  Keys stay below 2^62 (weights below kInf).
+// A unit's kept arc (vcand per light vertex; hcand.x per heavy chunk, with
+// the second lightest in hcand.y): a key, kScan (scan the unit's arcs; for
+// hcand.y: not known) or kNone (no arc leaves its component, for good; for
+// hcand.y: no second one).  Keys stay below 2^62 (weights below kInf).
 constexpr unsigned long long kScan = ~0ull;
 constexpr unsigned long long kNone = ~0ull - 1;
 
@@ -44,7 +46,7 @@ struct MstWs {
   uint32_t* comp;
   unsigned long long* best;
   unsigned long long* vcand;     // per vertex (light vertices)
-  unsigned long long* hcand;     // per heavy chunk
+  ulonglong2* hcand;             // per heavy chunk: the two lightest
   uint32_t* partner;
   uint8_t* arc_flag;             // nullable
   uint32_t* cursor;              // [3]
@@ -65,7 +67,7 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
     ws.best[v] = kNoArc;
     ws.vcand[v] = kScan;
   }
-  for (uint32_t c = W.gthread; c < G.nheavy_chunks; c += W.nthreads) ws.hcand[c] = kScan;
+  for (uint32_t c = W.gthread; c < G.nheavy_chunks; c += W.nthreads) ws.hcand[c] = make_ulonglong2(kScan, kScan);
   if (ws.arc_flag)
     for (uint32_t a = W.gthread; a < G.E; a += W.nthreads) ws.arc_flag[a] = 0;
   if (leader) {
@@ -125,13 +127,32 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
       sweep_heavy_indexed(G, &ws.hcursor[cur], [&](uint32_t ci, uint32_t v, uint32_t, uint32_t, uint32_t b,
                                                     uint32_t e) {
         const uint32_t c = ld_cg(&ws.comp[v]);
-        const unsigned long long kept = ld_cg(&ws.hcand[ci]);
-        if (kept == kNone) return;
-        if (kept != kScan && ld_cg(&ws.comp[__ldg(&G.col[(uint32_t)kept])]) != c) {
-          if (lane == 0 && kept < ld_cg(&ws.best[c])) atomicMin(&ws.best[c], kept);
-          return;
+        const ulonglong2 kept = __ldcg(&ws.hcand[ci]);
+        if (kept.x == kNone) return;
+        if (kept.x != kScan) {
+          // both kept arcs checked at once
+          const bool two = kept.y != kScan && kept.y != kNone;
+          const uint32_t u1 = __ldg(&G.col[(uint32_t)kept.x]);
+          const uint32_t u2 = two ? __ldg(&G.col[(uint32_t)kept.y]) : 0u;
+          const bool out1 = ld_cg(&ws.comp[u1]) != c;
+          const bool out2 = two && ld_cg(&ws.comp[u2]) != c;
+          unsigned long long use = kNoArc;
+          if (out1) {
+            use = kept.x;
+          } else if (kept.y == kNone) {
+            // the only arc that left the chunk's component is internal now
+            if (lane == 0) ws.hcand[ci].x = kNone;
+            return;
+          } else if (out2) {
+            use = kept.y;
+            if (lane == 0) ws.hcand[ci] = make_ulonglong2(kept.y, kScan);
+          }
+          if (use != kNoArc) {
+            if (lane == 0 && use < ld_cg(&ws.best[c])) atomicMin(&ws.best[c], use);
+            return;
+          }
         }
-        unsigned long long m = kNoArc;
+        unsigned long long m = kNoArc, m2 = kNoArc;  // this lane's two lightest
         // a chunk's four 32-arc steps with their loads in flight together
         static_assert(kChunk == 4 * 32, "an MST chunk is four steps");
         uint32_t wt[4], cu[4];
@@ -148,13 +169,21 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
         for (int k = 0; k < 4; ++k) {
           if (wt[k] < kInf && cu[k] != c) {
             const unsigned long long key = ((unsigned long long)wt[k] << 32) | (b + 32 * k + lane);
-            m = key < m ? key : m;
+            if (key < m) {
+              m2 = m;
+              m = key;
+            } else if (key < m2) {
+              m2 = key;
+            }
           }
         }
-        m = warp_min_u64(m);
+        // the chunk's lightest, then the lightest of the rest (keys are
+        // unique: one lane holds the lightest)
+        const unsigned long long lo = warp_min_u64(m);
+        const unsigned long long lo2 = warp_min_u64(m == lo ? m2 : m);
         if (lane == 0) {
-          ws.hcand[ci] = m == kNoArc ? kNone : m;
-          if (m != kNoArc) atomicMin(&ws.best[c], m);
+          ws.hcand[ci] = make_ulonglong2(lo == kNoArc ? kNone : lo, lo2 == kNoArc ? kNone : lo2);
+          if (lo != kNoArc) atomicMin(&ws.best[c], lo);
         }
       });
       if (!s.sync()) return;
@@ -239,7 +268,7 @@ static int mst_run(gdb_ctx* c, gdb_graph* g, gdb_mst_result* h_res, gdb_mst_resu
   Bump b;
   const size_t o_comp = b.take((size_t)V * 4), o_best = b.take((size_t)V * 8),
                o_part = b.take((size_t)V * 4), o_cnt = b.take(256);
-  const size_t o_vc = b.take((size_t)V * 8), o_hc = b.take((size_t)std::max<uint32_t>(g->nheavy_chunks, 1) * 8);
+  const size_t o_vc = b.take((size_t)V * 8), o_hc = b.take((size_t)std::max<uint32_t>(g->nheavy_chunks, 1) * 16);
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
   MstWs ws;
@@ -247,7 +276,7 @@ static int mst_run(gdb_ctx* c, gdb_graph* g, gdb_mst_result* h_res, gdb_mst_resu
   ws.best = (unsigned long long*)(base + o_best);
   ws.partner = (uint32_t*)(base + o_part);
   ws.vcand = (unsigned long long*)(base + o_vc);
-  ws.hcand = (unsigned long long*)(base + o_hc);
+  ws.hcand = (ulonglong2*)(base + o_hc);
   ws.arc_flag = d_flags;
   char* cnt = base + o_cnt;
   ws.acc = (unsigned long long*)cnt;
