@@ -31,6 +31,7 @@ constexpr float kMisBig = 99999999.0f;  // BIGNUM, mis_kernel.cl:68
 
 struct MisWs {
   int32_t* state;       // -1 undecided, -2 decided
+  uint32_t* ukey;       // the priority key while undecided, kMisGone once decided
   int32_t* s;           // output: 2 in the set, 0 otherwise
   uint32_t* mn;         // light vertices: key of the min undecided neighbour priority
   uint32_t* hmn[2];     // heavy vertices, by heavy index, double-buffered by round
@@ -42,6 +43,11 @@ struct MisWs {
 };
 
 constexpr uint32_t kMisNone = 0xFFFFFFFFu;  // no arc in this lane's step
+// ukey of a decided vertex: above every key mis1 can take as a minimum
+// (BIGNUM's key and all finite priorities), so a decided neighbour never
+// lowers one, and mis1 needs one load per neighbour instead of the state
+// and then the priority
+constexpr uint32_t kMisGone = 0xFFFFFFFFu;
 
 // mis_kernel.cl:78-93 (init), run by every thread of the grid.
 __device__ __forceinline__ void mis_init(const GraphView& G, const Warps& W, const MisWs& ws, bool leader) {
@@ -49,6 +55,7 @@ __device__ __forceinline__ void mis_init(const GraphView& G, const Warps& W, con
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.state[v] = -1;
     ws.s[v] = 0;
+    ws.ukey[v] = fkey(__ldg(&ws.prio[v]));
   }
   for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) ws.hmn[0][h] = ws.hmn[1][h] = big;
   if (leader) {
@@ -69,8 +76,8 @@ __device__ __forceinline__ void mis_phase1(const GraphView& G, const MisWs& ws, 
   const int cur = t % 3, old = (t + 1) % 3;
   if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
   bool undecided_seen = false;
-  // four 32-arc steps at once: the column, state and priority loads of
-  // the four are in flight together
+  // four 32-arc steps at once: the column and key loads of the four are
+  // in flight together
   sweep_light4(
       G, &ws.cursor[cur],
       [&](uint32_t v, bool in_range) {
@@ -81,19 +88,16 @@ __device__ __forceinline__ void mis_phase1(const GraphView& G, const MisWs& ws, 
       },
       [&](const bool* valid, const int* owner, const uint32_t* arc) {
         uint32_t u[4], k[4];
-        bool und[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           u[j] = valid[j] ? __ldg(&G.col[arc[j]]) : 0u;
           arcs += valid[j];
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) und[j] = valid[j] && ld_cg(&ws.state[u[j]]) == -1;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) k[j] = und[j] ? fkey(__ldg(&ws.prio[u[j]])) : big;
+        for (int j = 0; j < 4; ++j) k[j] = valid[j] ? ld_cg(&ws.ukey[u[j]]) : kMisGone;
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-          if (und[j] && k[j] < my[owner[j]]) atomicMin(&my[owner[j]], k[j]);
+          if (k[j] < my[owner[j]]) atomicMin(&my[owner[j]], k[j]);
       },
       [&](uint32_t v, bool act) {
         if (act) ws.mn[v] = my[lane];
@@ -102,27 +106,27 @@ __device__ __forceinline__ void mis_phase1(const GraphView& G, const MisWs& ws, 
   sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
     // a heavy winner's own state is settled here (see mis2)
     if (ld_cg(&ws.s[v]) == 2) {
-      if (lane == 0) ws.state[v] = -2;
+      if (lane == 0) {
+        ws.state[v] = -2;
+        ws.ukey[v] = kMisGone;
+      }
       return;
     }
     if (ld_cg(&ws.state[v]) != -1) return;
     undecided_seen = true;
     uint32_t m = big;
     // a chunk (kChunk = 128 arcs) as four steps with their loads in flight
-    uint32_t u[4];
-    bool und[4];
+    uint32_t u[4], k[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const uint32_t a = b + 32 * j + lane;
-      u[j] = a < e ? __ldg(&G.col[a]) : 0u;
+      u[j] = a < e ? __ldg(&G.col[a]) : kMisNone;
       arcs += a < e;
-      und[j] = a < e;
     }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) und[j] = und[j] && ld_cg(&ws.state[u[j]]) == -1;
+    for (int j = 0; j < 4; ++j) k[j] = u[j] != kMisNone ? ld_cg(&ws.ukey[u[j]]) : kMisGone;
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
-      if (und[j]) m = min(m, fkey(__ldg(&ws.prio[u[j]])));
+    for (int j = 0; j < 4; ++j) m = min(m, k[j]);
     m = warp_min_u32(m);
     if (lane == 0 && m < big) atomicMin(&hmn[h], m);
   });
@@ -149,6 +153,7 @@ __device__ __forceinline__ void mis_phase2(const GraphView& G, const Warps& W, c
           win = true;
           ws.s[v] = 2;
           ws.state[v] = -2;
+          ws.ukey[v] = kMisGone;
         }
         return win;
       },
@@ -161,7 +166,10 @@ __device__ __forceinline__ void mis_phase2(const GraphView& G, const Warps& W, c
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-          if (valid[j] && ld_cg(&ws.state[u[j]]) == -1) ws.state[u[j]] = -2;
+          if (valid[j] && ld_cg(&ws.state[u[j]]) == -1) {
+            ws.state[u[j]] = -2;
+            ws.ukey[u[j]] = kMisGone;
+          }
       },
       [](uint32_t, bool) {});
   const uint32_t* hmn = pick(ws.hmn, r);
@@ -182,7 +190,10 @@ __device__ __forceinline__ void mis_phase2(const GraphView& G, const Warps& W, c
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      if (u[j] != kMisNone && ld_cg(&ws.state[u[j]]) == -1) ws.state[u[j]] = -2;
+      if (u[j] != kMisNone && ld_cg(&ws.state[u[j]]) == -1) {
+        ws.state[u[j]] = -2;
+        ws.ukey[u[j]] = kMisGone;
+      }
   });
 }
 
@@ -768,12 +779,14 @@ static int mis_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_s) 
   const uint32_t hcap = std::max<uint32_t>(g->nheavy, 1);
   Bump b;
   const size_t o_state = b.take((size_t)g->V * 4), o_mn = b.take((size_t)g->V * 4);
+  const size_t o_ukey = b.take((size_t)g->V * 4);
   const size_t o_h0 = b.take(hcap * 4), o_h1 = b.take(hcap * 4), o_cnt = b.take(256);
   const size_t o_ctl = b.take(sizeof(StepCtl));
   char* base = (char*)workspace(c, b.off);
   if (!base) return GDB_ERR_OOM;
   MisWs ws;
   ws.state = (int32_t*)(base + o_state);
+  ws.ukey = (uint32_t*)(base + o_ukey);
   ws.s = d_s;
   ws.mn = (uint32_t*)(base + o_mn);
   ws.hmn[0] = (uint32_t*)(base + o_h0);
