@@ -285,3 +285,25 @@ def test_mst(ctx, name, g):
     assert got["weight32"] == want["weight32"], name
     assert got["edges"] == want["edges"] and got["components"] == want["components"], name
     assert oracle.mst_edge_set(g, got["arc_in_mst"]) == oracle.mst_edge_set(g, want["arc_in_mst"])
+
+
+@pytest.mark.parametrize("name", ["rmat14_hubs", "star_isolated", "grid256x256"])
+def test_mst_never_chosen_weights(ctx, name):
+    """Arcs of weight >= 1e9 are never chosen (mst_common.cl:84-88): lift
+    the heavier half of the unique weights past 1e9, so that components
+    whose remaining arcs are all of that kind stop hooking while others
+    still do, and every light vertex and heavy chunk meets arcs it must
+    skip in every round."""
+    g = dict(GRAPHS)[name]
+    uw = gg.unique_weights(g, seed=11).astype(np.uint64)
+    half = uw > (uw.max() // 2 if len(uw) else 0)
+    uw = np.where(half, uw + 1_000_000_000, uw).astype(np.uint32)
+    gu = g.with_weights(uw)
+    G = ctx.graph(g.row_ptr, g.col, uw)
+    got = ctx.mst(G, with_arcs=True)
+    want = oracle.mst(gu)
+    assert got["weight64"] == want["weight64"], name
+    assert got["weight32"] == want["weight32"], name
+    assert got["edges"] == want["edges"] and got["components"] == want["components"], name
+    assert oracle.mst_edge_set(g, got["arc_in_mst"]) == oracle.mst_edge_set(g, want["arc_in_mst"])
+    assert want["edges"] < g.V - 1, "some components must stay apart"
