@@ -20,6 +20,7 @@ import os
 import shutil
 import subprocess
 import sys
+import tempfile
 from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
@@ -76,15 +77,14 @@ def _stale(out: Path, deps: list[Path]) -> bool:
 
 
 def _openmp_flag(cc: str) -> list[str]:
-    """-fopenmp when the host compiler has libgomp, else nothing."""
-    probe = LIBDIR / "_omp_probe.c"
-    probe.parent.mkdir(parents=True, exist_ok=True)
-    probe.write_text("#include <omp.h>\nint main(void){return omp_get_max_threads()<1;}\n")
-    res = subprocess.run([cc, "-fopenmp", str(probe), "-o", str(probe.with_suffix(".bin"))],
-                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
-    for p in (probe, probe.with_suffix(".bin")):
-        if p.exists():
-            p.unlink()
+    """-fopenmp when the host compiler has libgomp, else nothing.  Each call
+    probes in a directory of its own: build_all runs the library builds in
+    parallel threads, and two probes sharing a file race on it."""
+    with tempfile.TemporaryDirectory(prefix="gdb_omp_") as d:
+        probe = Path(d) / "probe.c"
+        probe.write_text("#include <omp.h>\nint main(void){return omp_get_max_threads()<1;}\n")
+        res = subprocess.run([cc, "-fopenmp", str(probe), "-o", str(Path(d) / "probe.bin")],
+                             stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     return ["-fopenmp"] if res.returncode == 0 else []
 
 
