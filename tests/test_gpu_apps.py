@@ -215,6 +215,39 @@ def test_color(ctx, name, g):
     assert np.array_equal(got, want), name
 
 
+def test_color_waiting_counts_around_chunk_size(ctx):
+    """The colouring enters a coloured vertex as chunks (kChunk = 128
+    arcs) when more than 128 neighbours wait for it, else as one light
+    entry.  Hubs of degree 300 whose waiting neighbours number 1, 127, 128,
+    129, 255, 256, 257 and 299 (each neighbour also has a second arc, to a
+    shared anchor, so that it looks at its neighbours)."""
+    ks = [1, 127, 128, 129, 255, 256, 257, 299]
+    deg = 300
+    rng = np.random.default_rng(3)
+    V = 1 + len(ks) * (deg + 1)
+    pairs, prio = [], np.zeros(V, np.float32)
+    # distinct even integers below 2**24 for every vertex, so that each
+    # hub's priority can sit strictly between two of its neighbours'
+    vals = 2 * rng.permutation(V).astype(np.int64)
+    prio[:] = vals
+    for i, k in enumerate(ks):
+        h = 1 + i * (deg + 1)
+        us = np.arange(h + 1, h + 1 + deg)
+        pairs += [(h, int(u)) for u in us] + [(int(u), 0) for u in us]
+        pu = np.sort(vals[us])
+        prio[h] = np.float32(pu[k - 1] + 1) if k < deg else np.float32(pu[-1] + 1)
+    assert len(np.unique(prio)) == V
+    g = gg.from_edges(V, pairs)
+    G = ctx.graph(g.row_ptr, g.col)
+    got = ctx.color(G, prio)
+    want, _ = oracle.color(g, prio)
+    assert np.array_equal(got, want)
+    for i, k in enumerate(ks):
+        h = 1 + i * (deg + 1)
+        us = np.arange(h + 1, h + 1 + deg)
+        assert int((prio[us] <= prio[h]).sum()) == k
+
+
 @pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
 def test_bc(ctx, name, g):
     """Path counts are float32 as in the reference (bc_kernel.cl rho); on
