@@ -39,6 +39,8 @@ struct MisWs {
   uint32_t* cursor;     // [3]
   uint32_t* hcursor;    // [3]
   uint32_t* flag;       // [3] some vertex undecided
+  uint32_t* won;        // [3] some vertex joined the set (mis2 supersteps)
+  int* stuck;           // set when a round chose no vertex (see mis_body)
   unsigned long long* stats;  // [0] arcs, [1] rounds
 };
 
@@ -49,17 +51,25 @@ constexpr uint32_t kMisNone = 0xFFFFFFFFu;  // no arc in this lane's step
 // and then the priority
 constexpr uint32_t kMisGone = 0xFFFFFFFFu;
 
+// A priority's key: fkey's order, with every NaN, of either sign, at
+// kMisGone -- above all numbers, so that a NaN priority never wins and
+// never lowers a neighbour's minimum, as the reference's comparisons with
+// NaN are all false (fkey alone would put a NaN with its sign bit set
+// below every number).
+__device__ __forceinline__ uint32_t mis_key(float f) { return isnan(f) ? kMisGone : fkey(f); }
+
 // mis_kernel.cl:78-93 (init), run by every thread of the grid.
 __device__ __forceinline__ void mis_init(const GraphView& G, const Warps& W, const MisWs& ws, bool leader) {
   const uint32_t big = fkey(kMisBig);
   for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
     ws.state[v] = -1;
     ws.s[v] = 0;
-    ws.ukey[v] = fkey(__ldg(&ws.prio[v]));
+    ws.ukey[v] = mis_key(__ldg(&ws.prio[v]));
   }
   for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) ws.hmn[0][h] = ws.hmn[1][h] = big;
   if (leader) {
-    for (int i = 0; i < 3; ++i) ws.cursor[i] = ws.hcursor[i] = ws.flag[i] = 0;
+    for (int i = 0; i < 3; ++i) ws.cursor[i] = ws.hcursor[i] = ws.flag[i] = ws.won[i] = 0;
+    *ws.stuck = 0;
     ws.stats[0] = ws.stats[1] = 0;
   }
 }
@@ -139,18 +149,20 @@ __device__ __forceinline__ void mis_phase2(const GraphView& G, const Warps& W, c
                                            uint32_t t, bool leader, unsigned long long& arcs) {
   const int lane = lane_id();
   const uint32_t big = fkey(kMisBig);
-  // flag[t % 3] is read after this superstep's barrier: clear the slot
-  // of superstep t - 2
+  // flag[t % 3] and won[t % 3] are read after this superstep's barrier:
+  // clear the slots of superstep t - 2
   const int cur = t % 3, old = (t + 1) % 3;
-  if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = 0;
+  if (leader) ws.cursor[old] = ws.hcursor[old] = ws.flag[old] = ws.won[old] = 0;
+  bool any_win = false;
   // next round's heavy minima start from BIGNUM
   for (uint32_t h = W.gthread; h < G.nheavy; h += W.nthreads) pick(ws.hmn, r + 1)[h] = big;
   sweep_light4(
       G, &ws.cursor[cur],
       [&](uint32_t v, bool in_range) {
         bool win = false;
-        if (in_range && ld_cg(&ws.state[v]) == -1 && fkey(__ldg(&ws.prio[v])) < ws.mn[v]) {
+        if (in_range && ld_cg(&ws.state[v]) == -1 && mis_key(__ldg(&ws.prio[v])) < ws.mn[v]) {
           win = true;
+          any_win = true;
           ws.s[v] = 2;
           ws.state[v] = -2;
           ws.ukey[v] = kMisGone;
@@ -179,7 +191,8 @@ __device__ __forceinline__ void mis_phase2(const GraphView& G, const Warps& W, c
   // nobody reads it in between).
   sweep_heavy(G, &ws.hcursor[cur], [&](uint32_t v, uint32_t h, uint32_t, uint32_t b, uint32_t e) {
     if (ld_cg(&ws.state[v]) != -1) return;
-    if (!(fkey(__ldg(&ws.prio[v])) < ld_cg(&hmn[h]))) return;
+    if (!(mis_key(__ldg(&ws.prio[v])) < ld_cg(&hmn[h]))) return;
+    any_win = true;
     if (lane == 0) ws.s[v] = 2;
     uint32_t u[4];
 #pragma unroll
@@ -195,6 +208,7 @@ __device__ __forceinline__ void mis_phase2(const GraphView& G, const Warps& W, c
         ws.ukey[u[j]] = kMisGone;
       }
   });
+  cta_or(any_win, &ws.won[cur], 1u);
 }
 
 template <class Sync>
@@ -207,7 +221,14 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
   unsigned long long arcs = 0;
   uint32_t r = 0;
   uint32_t t = 0;  // cursor slot counter: two sweeps per round
-  for (;; ++r) {
+  // A round in which no vertex joins the set changes nothing, so every
+  // later round would repeat it: adjacent vertices of equal priority, NaN
+  // priorities and priorities of BIGNUM and above never win.  The
+  // reference loops forever then; here the kernel stops at that round and
+  // the host reports it.  A round that does choose a vertex decides at
+  // least that one, so V rounds always suffice: the bound below holds the
+  // loop to them whatever happens.
+  for (; r <= G.V; ++r) {
     mis_phase1(G, ws, r, t, my, leader, arcs);
     if (!s.sync()) return;
     const int cur = t % 3;
@@ -215,8 +236,14 @@ __device__ __forceinline__ void mis_body(Sync& s, const GraphView& G, const MisW
     if (cta_words<1>([&](unsigned long long* w) { w[0] = ld_cg(&ws.flag[cur]); })[0] == 0) break;
     mis_phase2(G, W, ws, r, t, leader, arcs);
     if (!s.sync()) return;
+    const int cur2 = t % 3;
     ++t;
+    if (cta_words<1>([&](unsigned long long* w) { w[0] = ld_cg(&ws.won[cur2]); })[0] == 0) {
+      if (leader) *ws.stuck = 1;
+      break;
+    }
   }
+  if (r > G.V && leader) *ws.stuck = 1;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) arcs += __shfl_xor_sync(kFull, arcs, o);
   if (lane_id() == 0 && arcs) atomicAdd(&ws.stats[0], arcs);
@@ -260,6 +287,12 @@ __global__ void __launch_bounds__(512, 3) k_mis_rl_step(GraphView G, MisWs ws, S
       }
       st.s[2] = 2;
     } else {
+      if (__ldcg(&ws.won[t % 3]) == 0) {
+        // no vertex joined the set: every later round would repeat this one
+        *ws.stuck = 1;
+        ws.stats[1] = r + 1;
+        return false;
+      }
       st.s[0] = r + 1;
       st.s[2] = 1;
     }
@@ -797,14 +830,29 @@ static int mis_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_s) 
   ws.cursor = (uint32_t*)(cnt + 64);
   ws.hcursor = (uint32_t*)(cnt + 80);
   ws.flag = (uint32_t*)(cnt + 96);
-  // a round decides at least one vertex: at most V rounds of two phases
+  ws.won = (uint32_t*)(cnt + 112);
+  ws.stuck = (int*)(cnt + 128);
+  // a round that chooses a vertex decides at least that one: at most V
+  // rounds of two phases (a round that chooses none stops the run)
+  int rc;
   if (relaunch_kind(c)) {
     StepCtl first{};
     first.s[2] = 1;  // round 0 starts with mis1
-    return launch_steps(c, k_mis_rl_init, k_mis_rl_step, g->view(), ws, ws.stats, (StepCtl*)(base + o_ctl),
-                        first, 2ull * g->V + 4);
+    rc = launch_steps(c, k_mis_rl_init, k_mis_rl_step, g->view(), ws, ws.stats, (StepCtl*)(base + o_ctl),
+                      first, 2ull * g->V + 4);
+  } else {
+    rc = launch_xf(c, k_mis_xf, g->view(), ws, ws.stats);
   }
-  return launch_xf(c, k_mis_xf, g->view(), ws, ws.stats);
+  if (rc) return rc;
+  int stuck = 0;
+  GDB_CUDA(c, cudaMemcpyAsync(&stuck, ws.stuck, sizeof stuck, cudaMemcpyDeviceToHost, c->stream));
+  GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (stuck)
+    return set_error(c, GDB_ERR_INVALID,
+                     "MIS: a round chose no vertex (adjacent vertices of equal priority, or a NaN "
+                     "priority or one of 99999999 and above, never win; the reference never "
+                     "terminates then)");
+  return GDB_OK;
 }
 
 static int color_run(gdb_ctx* c, gdb_graph* g, const float* d_prio, int32_t* d_color) {

@@ -243,9 +243,11 @@ int gdb_sssp_jacobi(gdb_ctx* ctx, gdb_graph* g, uint32_t src, int32_t* cost);
 int gdb_sssp_jacobi_device(gdb_ctx* ctx, gdb_graph* g, uint32_t src, int32_t* d_cost);
 
 /* Maximal independent set: s_array[v] = 2 in the set, 0 otherwise, for
- * float priorities node_value (equal priorities on adjacent vertices never
- * terminate in the reference; this call returns GDB_ERR_TIMEOUT).  Replaces
- * mega_kernel (pannotia/graph_app/mis/kernel/mis_kernel.cl:220-337). */
+ * float priorities node_value.  Where a round lets no vertex join the set
+ * (adjacent vertices of equal priority; a NaN priority, or one of 99999999
+ * and above, never wins), the reference never terminates; this call stops
+ * at that round and returns GDB_ERR_INVALID.  Replaces mega_kernel
+ * (pannotia/graph_app/mis/kernel/mis_kernel.cl:220-337). */
 int gdb_mis(gdb_ctx* ctx, gdb_graph* g, const float* node_value, int32_t* s_array);
 int gdb_mis_device(gdb_ctx* ctx, gdb_graph* g, const float* d_node_value, int32_t* d_s_array);
 

@@ -206,6 +206,42 @@ def test_mis(ctx, name, g):
     assert np.array_equal(got, want), name
 
 
+STUCK_MIS = [
+    # adjacent vertices of equal priority: neither is below the other
+    ("equal_pair", gg.from_edges(2, [(0, 1)]), [0.5, 0.5]),
+    # equal priorities in a triangle, next to a path that does finish
+    ("equal_triangle", gg.from_edges(6, [(0, 1), (1, 2), (2, 0), (3, 4), (4, 5)]),
+     [0.25, 0.25, 0.25, 0.1, 0.2, 0.3]),
+    # a NaN priority, of either sign, never wins: an isolated vertex with
+    # one stays undecided (a neighbour's win would decide it)
+    ("nan", gg.from_edges(3, [(1, 2)]), np.array([0x7FC00000, 0x3E99999A, 0x3E4CCCCD], np.uint32).view(np.float32)),
+    ("negative_nan", gg.from_edges(3, [(1, 2)]),
+     np.array([0xFFC00000, 0x3E99999A, 0x3E4CCCCD], np.uint32).view(np.float32)),
+    # a priority of BIGNUM (99999999) or above never wins
+    ("bignum", gg.from_edges(3, [(0, 1), (1, 2)]), [5e8, 99999999.0, 2e8]),
+]
+
+
+@pytest.mark.parametrize("kind", [gdb.BARRIER_XF, gdb.BARRIER_RELAUNCH, gdb.BARRIER_RELAUNCH_GRAPH],
+                         ids=["xf", "relaunch", "relaunch_graph"])
+@pytest.mark.parametrize("name,g,prio", STUCK_MIS, ids=[n for n, _, _ in STUCK_MIS])
+def test_mis_stops_when_a_round_chooses_nobody(ctx, kind, name, g, prio):
+    """Inputs on which the reference's MIS loops forever (no vertex of some
+    round is below all of its undecided neighbours) end the call with
+    GDB_ERR_INVALID at that round, on every barrier form; the context stays
+    usable."""
+    ctx.set_options(barrier=kind)
+    try:
+        G = ctx.graph(g.row_ptr, g.col)
+        with pytest.raises(gdb.GdbError) as e:
+            ctx.mis(G, np.asarray(prio, np.float32))
+        assert e.value.status == -1, str(e.value)
+        ok = gg.priorities(g.V, seed=4)
+        assert np.array_equal(ctx.mis(G, ok), oracle.mis(g, ok)[0])
+    finally:
+        ctx.set_options(barrier=gdb.BARRIER_XF)
+
+
 @pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
 def test_color(ctx, name, g):
     prio = gg.priorities(g.V, seed=5)
