@@ -18,9 +18,16 @@
 //      internal.  A unit scans its arcs again only when its kept arcs have
 //      turned internal;
 //   B1. every component root records the root its lightest arc reaches;
-//   B2. roots hook onto that root, except the smaller id of a mutual pair,
-//      which stays a root (cs_unify breaks cycles by id too,
-//      component_cl.h:58-64); each hook adds its arc's weight once;
+//   B2. roots hook onto that root, except a root whose arc weighs the same
+//      as the target root's arc and whose id is the smaller, which stays a
+//      root (cs_unify breaks cycles by id too, component_cl.h:58-64); each
+//      hook adds its arc's weight once.  With unique weights an equal
+//      weight means the same edge, so this is the smaller id of a mutual
+//      pair.  With equal weights on different edges, ties between arc
+//      indices differ by direction and could close a cycle of hooks;
+//      (weight, id) falls strictly along every hook instead, so no cycle
+//      forms, and each round still hooks at least one root that has an
+//      arc leaving its component;
 //   C. pointer jumping flattens every vertex onto its root.
 // With unique weights the forest is unique, so weight, edge count and edge
 // set equal the reference's.  The weight is kept exactly (uint64) and also
@@ -52,6 +59,7 @@ struct MstWs {
   uint32_t* cursor;              // [3]
   uint32_t* hcursor;             // [3]
   uint32_t* hooks;               // [3]
+  int* stuck;                    // set if pointer jumping ever meets a cycle (see C)
   unsigned long long* acc;       // [0] weight, [1] edges, [2] rounds, [3] arcs inspected
 };
 
@@ -73,11 +81,14 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
   if (leader) {
     for (int i = 0; i < 3; ++i) ws.cursor[i] = ws.hcursor[i] = ws.hooks[i] = 0;
     for (int i = 0; i < 4; ++i) ws.acc[i] = 0;
+    *ws.stuck = 0;
   }
   if (!s.sync()) return;
   unsigned long long arcs = 0, wsum = 0, nedges = 0;
   uint32_t t = 0, round = 0;
-  for (;; ++round) {
+  // a round with a hook merges two components at least: V rounds bound
+  // the loop
+  for (; round <= G.V; ++round) {
     // ---- A: lightest arc leaving each vertex's component
     {
       const int cur = t % 3, old = (t + 2) % 3;
@@ -198,7 +209,9 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
     }
     if (!s.sync()) return;
     ++t;
-    // ---- B2: hook; the smaller root of a mutual pair stays a root
+    // ---- B2: hook; of two roots whose arcs weigh the same, the smaller
+    // stays a root (best[] stays untouched until C, so every root reads
+    // its target's key)
     {
       const int cur = t % 3, old = (t + 2) % 3;
       if (leader) ws.cursor[old] = ws.hcursor[old] = ws.hooks[old] = 0;
@@ -208,9 +221,9 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
         const unsigned long long key = ws.best[v];
         if (key == kNoArc) continue;
         const uint32_t d = ws.partner[v];
-        ws.best[v] = kNoArc;  // next round starts empty
-        const bool mutual = ws.partner[d] == v;  // partner[] is settled since B1
-        if (mutual && v < d) continue;
+        // d is a root with an arc leaving its component (the one v chose,
+        // at least), so best[d] holds a key of weight <= v's
+        if ((ws.best[d] >> 32) == (key >> 32) && v < d) continue;
         ws.comp[v] = d;
         wsum += key >> 32;
         ++nedges;
@@ -223,14 +236,26 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
       ++t;
       if (cta_words<1>([&](unsigned long long* w) { w[0] = ld_cg(&ws.hooks[cur]); })[0] == 0) break;
     }
-    // ---- C: pointer jumping onto the roots
+    // ---- C: pointer jumping onto the roots; every slot starts the next
+    // round empty.  Hooks form no cycle (B2), so each chase ends at a root
+    // within V steps; the bound keeps the loop finite whatever happens.
+    bool cycle = false;
     for (uint32_t v = W.gthread; v < G.V; v += W.nthreads) {
-      uint32_t r = ld_cg(&ws.comp[v]);
-      for (uint32_t p = ld_cg(&ws.comp[r]); p != r; p = ld_cg(&ws.comp[r])) r = p;
+      ws.best[v] = kNoArc;
+      uint32_t r = ld_cg(&ws.comp[v]), steps = 0;
+      for (uint32_t p = ld_cg(&ws.comp[r]); p != r; p = ld_cg(&ws.comp[r])) {
+        r = p;
+        if (++steps > G.V) {
+          cycle = true;
+          break;
+        }
+      }
       ws.comp[v] = r;
     }
+    if (cycle) atomicExch(ws.stuck, 1);
     if (!s.sync()) return;
     ++t;
+    if (cta_words<1>([&](unsigned long long* w) { w[0] = (unsigned)ld_cg(ws.stuck); })[0] != 0) break;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -243,6 +268,7 @@ __device__ __forceinline__ void mst_body(Sync& s, const GraphView& G, const MstW
     if (nedges) atomicAdd(&ws.acc[1], nedges);
     if (arcs) atomicAdd(&ws.acc[3], arcs);
   }
+  if (round > G.V && leader) *ws.stuck = 1;
   if (leader) ws.acc[2] = round + 1;
 }
 
@@ -283,6 +309,7 @@ static int mst_run(gdb_ctx* c, gdb_graph* g, gdb_mst_result* h_res, gdb_mst_resu
   ws.cursor = (uint32_t*)(cnt + 64);
   ws.hcursor = (uint32_t*)(cnt + 80);
   ws.hooks = (uint32_t*)(cnt + 96);
+  ws.stuck = (int*)(cnt + 112);
   const int block = c->opt.block_size;
   Shape s;
   int rc = persistent_shape(c, (const void*)k_mst_xf, block, 0, &s, c->opt.barrier == GDB_BARRIER_XF);
@@ -297,8 +324,10 @@ static int mst_run(gdb_ctx* c, gdb_graph* g, gdb_mst_result* h_res, gdb_mst_resu
   if (rc) return rc;
   unsigned long long* hs = (unsigned long long*)pinned(c, 256);
   if (!hs) return GDB_ERR_OOM;
-  GDB_CUDA(c, cudaMemcpyAsync(hs, cnt, 32, cudaMemcpyDeviceToHost, c->stream));
+  GDB_CUDA(c, cudaMemcpyAsync(hs, cnt, 128, cudaMemcpyDeviceToHost, c->stream));
   GDB_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (*(const int*)((const char*)hs + 112))
+    return set_error(c, GDB_ERR_INVALID, "MST: component pointers formed a cycle");
   gdb_mst_result r;
   r.weight64 = hs[0];
   r.weight32 = (uint32_t)hs[0];

@@ -356,6 +356,75 @@ def test_mst(ctx, name, g):
     assert oracle.mst_edge_set(g, got["arc_in_mst"]) == oracle.mst_edge_set(g, want["arc_in_mst"])
 
 
+def _forest(g, arc_in_mst) -> tuple[int, bool]:
+    """(undirected edges chosen, whether they form a forest)."""
+    edges = oracle.mst_edge_set(g, arc_in_mst)
+    parent = list(range(g.V))
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+
+    for u, v in edges:
+        ru, rv = find(u), find(v)
+        if ru == rv:
+            return len(edges), False
+        parent[ru] = rv
+    return len(edges), True
+
+
+def _csr(V, adj):
+    """CSR from adjacency lists kept in the given order."""
+    row = np.zeros(V + 1, np.uint32)
+    row[1:] = np.cumsum([len(a) for a in adj])
+    return row, np.array([u for a in adj for u in a], np.uint32)
+
+
+TIED_MST = [
+    ("rmat12_ones", gg.rmat(1 << 12, 16, seed=5), "ones"),
+    ("rmat14_hubs_1to3", gg.rmat(1 << 14, 32, seed=6), "1to3"),
+    ("grid64_ones", gg.grid(64, 64), "ones"),
+    ("grid64_1to3", gg.grid(64, 64), "1to3"),
+    ("star_isolated_ones", dict(GRAPHS)["star_isolated"], "ones"),
+]
+
+
+@pytest.mark.parametrize("name,g,kind", TIED_MST, ids=[n for n, _, _ in TIED_MST])
+def test_mst_tied_weights(ctx, name, g, kind):
+    """Equal weights on different edges: the forest is not unique, so the
+    call must give one of the minimum forests -- the oracle's weight, edge
+    and component counts, and chosen edges that form a forest."""
+    if kind == "ones":
+        w = np.ones(g.E, np.uint32)
+    else:
+        w = (gg.unique_weights(g, seed=13) % 3 + 1).astype(np.uint32)  # one per edge
+    G = ctx.graph(g.row_ptr, g.col, w)
+    got = ctx.mst(G, with_arcs=True)
+    want = oracle.mst(g.with_weights(w))
+    assert got["weight64"] == want["weight64"], name
+    assert got["edges"] == want["edges"] and got["components"] == want["components"], name
+    n, forest = _forest(g, got["arc_in_mst"])
+    assert forest and n == got["edges"], name
+
+
+@pytest.mark.parametrize("adj", [
+    [[1, 2], [2, 0], [0, 1]],                       # triangle, each vertex's first arc goes round
+    [[1, 3], [2, 0], [3, 1], [0, 2]],               # square, the same way round
+], ids=["triangle", "square"])
+def test_mst_equal_weights_in_a_ring_order(ctx, adj):
+    """Every vertex's lowest arc index points the same way round the ring:
+    with equal weights, hooks by arc index alone would close the ring."""
+    V = len(adj)
+    row, col = _csr(V, adj)
+    w = np.full(len(col), 7, np.uint32)
+    G = ctx.graph(row, col, w)
+    got = ctx.mst(G, with_arcs=True)
+    assert got["edges"] == V - 1 and got["components"] == 1
+    assert got["weight64"] == 7 * (V - 1)
+
+
 @pytest.mark.parametrize("name", ["rmat14_hubs", "star_isolated", "grid256x256"])
 def test_mst_never_chosen_weights(ctx, name):
     """Arcs of weight >= 1e9 are never chosen (mst_common.cl:84-88): lift
