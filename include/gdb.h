@@ -265,10 +265,14 @@ int gdb_bc(gdb_ctx* ctx, gdb_graph* g, const uint32_t* sources, uint32_t nsrc, f
 int gdb_bc_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc,
                   float* d_bc);
 
-/* Minimum spanning forest (Boruvka) over the graph's weights; arc_in_mst
- * (nullable, E bytes) marks one arc of every forest edge.  Replaces the
- * LonestarGPU MST host loop and kernels (lonestar/apps/mst/mst_port.cpp:202-312,
- * mst_common.cl:41-194, mst_port_kernel.cl:35-82). */
+/* Minimum spanning forest (Boruvka) over the graph's weights (one weight
+ * per edge, the same on both arcs; arcs of weight 1e9 and above are never
+ * chosen); arc_in_mst (nullable, E bytes) marks one arc of every forest
+ * edge.  With unique weights the forest is the reference's; with equal
+ * weights it is a minimum forest of the same weight, whose edges may
+ * differ.  Replaces the LonestarGPU MST host loop and kernels
+ * (lonestar/apps/mst/mst_port.cpp:202-312, mst_common.cl:41-194,
+ * mst_port_kernel.cl:35-82). */
 int gdb_mst(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* result, uint8_t* arc_in_mst);
 int gdb_mst_device(gdb_ctx* ctx, gdb_graph* g, gdb_mst_result* d_result, uint8_t* d_arc_in_mst);
 
