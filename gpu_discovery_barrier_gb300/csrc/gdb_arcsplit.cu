@@ -387,9 +387,24 @@ static int heavy_table_device(gdb_ctx* c, gdb_graph* x, uint32_t* t0, uint32_t* 
   return GDB_OK;
 }
 
+// One pass over a CSR's arrays: bit 0 when a row pointer decreases, bit 1
+// when a column names a vertex >= V -- a graph every kernel would read or
+// write out of bounds.
+__global__ void k_check_csr(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col, uint32_t V,
+                            uint64_t E, uint32_t* bad) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t b = 0;
+  for (uint64_t i = t0; i < V; i += stride) b |= __ldg(&row[i + 1]) < __ldg(&row[i]) ? 1u : 0u;
+  for (uint64_t e = t0; e < E; e += stride) b |= __ldg(&col[e]) >= V ? 2u : 0u;
+  b = __reduce_or_sync(0xffffffffu, b);
+  if ((threadIdx.x & 31) == 0 && b) atomicOr(bad, b);
+}
+
 // The heavy table of a graph whose row array is on the device (every graph
 // the library creates): scratch of its own, one synchronisation for the
-// totals.
+// CSR check and one for the totals.  The check runs first: the table's
+// degrees come from the row array.
 int build_heavy_table(gdb_graph* g) {
   gdb_ctx* c = g->ctx;
   const uint32_t V = g->V;
@@ -398,6 +413,20 @@ int build_heavy_table(gdb_graph* g) {
   GDB_CUDA(c, cudaMallocAsync((void**)&scratch, (4 * vw + scan_tmp_words(V) + 8) * 4, c->stream));
   uint32_t *t0 = scratch, *t1 = t0 + vw, *t2 = t1 + vw, *t3 = t2 + vw, *tmp = t3 + vw,
            *hs = tmp + scan_tmp_words(V);
+  uint32_t bad = 0;
+  cudaError_t ce = cudaMemsetAsync(hs + 7, 0, 4, c->stream);
+  if (ce == cudaSuccess) {
+    k_check_csr<<<4 * std::max(c->sm_count, 1), 256, 0, c->stream>>>(g->row, g->col, V, g->E, hs + 7);
+    ce = cudaGetLastError();
+  }
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(&bad, hs + 7, 4, cudaMemcpyDeviceToHost, c->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
+  if (ce != cudaSuccess || bad) {
+    cudaFreeAsync(scratch, c->stream);
+    cudaStreamSynchronize(c->stream);
+    if (ce != cudaSuccess) return set_cuda_error(c, ce, "CSR check");
+    return set_error(c, GDB_ERR_INVALID, (bad & 1) ? "row_ptr decreases" : "a column names a vertex >= V");
+  }
   const int rc = heavy_table_device(c, g, t0, t1, t2, t3, tmp, hs);
   cudaFreeAsync(scratch, c->stream);
   const cudaError_t e = cudaStreamSynchronize(c->stream);

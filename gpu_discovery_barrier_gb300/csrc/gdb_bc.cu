@@ -231,6 +231,13 @@ __device__ __forceinline__ void bc_seed(const GraphView& G, const BcWs& ws, uint
   auto degree = [&](uint32_t v) { return bc_degree(G, v); };
   // -- superstep: seed the source into slot (t+1)
   bc_reset_slot(ws, t, leader);
+  if (leader && src >= G.V) {
+    // an out-of-range source (only the device-pointer entry points can
+    // pass one) seeds nothing: its forward pass finds level 0 empty and it
+    // adds nothing, as BFS and SSSP ignore such sources
+    ws.lev_arcs[0] = ws.lev_arcs[1] = 0;
+    return;
+  }
   if (leader) {
     ws.st[src] = make_uint2(0u, 0u);
     ws.rho[src] = 1.f;

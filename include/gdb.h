@@ -204,7 +204,9 @@ int gdb_debug_stall_master(gdb_ctx* ctx, int after_barriers);
 
 /* ---------------------------------------------------------------- graphs */
 /* Symmetric or directed CSR: row_ptr[V+1], col[E], optional w[E] (uint32).
- * Host arrays are copied to HBM.  Requires E < 2^32 and V < 2^31. */
+ * Host arrays are copied to HBM.  Requires E < 2^32 and V < 2^31.  One
+ * pass on the device checks the CSR (row_ptr[0] = 0, row_ptr[V] = E,
+ * row_ptr non-decreasing, every column < V); GDB_ERR_INVALID otherwise. */
 int gdb_graph_create(gdb_ctx* ctx, uint32_t V, uint64_t E, const uint32_t* row_ptr,
                      const uint32_t* col, const uint32_t* w, gdb_graph** out);
 /* Same with device arrays, borrowed (not freed by gdb_graph_destroy). */
@@ -260,7 +262,8 @@ int gdb_color_device(gdb_ctx* ctx, gdb_graph* g, const float* d_node_value, int3
 /* Betweenness centrality (float32) summed over the given sources, no halving
  * for undirected graphs.  Replaces mega_bc_kernel
  * (pannotia/graph_app/bc/kernel/bc_kernel.cl:431-513) restricted to a source
- * list; bc is overwritten. */
+ * list; bc is overwritten.  gdb_bc checks the sources; gdb_bc_device
+ * ignores sources >= V (they add nothing). */
 int gdb_bc(gdb_ctx* ctx, gdb_graph* g, const uint32_t* sources, uint32_t nsrc, float* bc);
 int gdb_bc_device(gdb_ctx* ctx, gdb_graph* g, const uint32_t* d_sources, uint32_t nsrc,
                   float* d_bc);

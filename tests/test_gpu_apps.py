@@ -343,6 +343,51 @@ def test_many_sources_device_form_ignores_out_of_range():
             c.sssp_sources(G, [0, g.V])
 
 
+def test_bc_device_form_ignores_out_of_range_sources(ctx):
+    """gdb_bc_device skips a source >= V (it adds nothing), as the BFS and
+    SSSP device forms do; gdb_bc refuses one."""
+    import torch
+
+    g = gg.rmat(1 << 12, 16, seed=5)
+    G = ctx.graph(g.row_ptr, g.col)
+    want = ctx.bc(G, [0, 3, 77])
+    for srcs in ([0, g.V + 5, 3, 77], [g.V, 0, 3, 77, 0xFFFFFFFF]):
+        d_src = torch.tensor(np.array(srcs, np.uint32).view(np.int32), device="cuda")
+        out = torch.zeros(g.V, dtype=torch.float32, device="cuda")
+        ctx.bc_device(G, d_src.data_ptr(), len(srcs), out.data_ptr())
+        torch.cuda.synchronize()
+        assert bc_close(out.cpu().numpy(), want.astype(np.float64)), srcs
+    with pytest.raises(gdb.GdbError):
+        ctx.bc(G, [0, g.V])
+
+
+@pytest.mark.parametrize("case", ["column_out_of_range", "row_decreases"])
+@pytest.mark.parametrize("device", [False, True], ids=["host_arrays", "device_arrays"])
+def test_graph_refuses_a_malformed_csr(ctx, case, device):
+    """A CSR that the kernels would read or write out of bounds -- a column
+    naming a vertex >= V, or a row pointer that decreases (row_ptr[0] = 0
+    and row_ptr[V] = E still hold) -- is refused at creation with
+    GDB_ERR_INVALID; the context stays usable."""
+    import torch
+
+    if case == "column_out_of_range":
+        row = np.array([0, 2, 3, 4], np.uint32)
+        col = np.array([1, 2, 0, 3], np.uint32)   # vertex 3 of V = 3
+    else:
+        row = np.array([0, 3, 1, 4], np.uint32)   # 3 > 1
+        col = np.array([1, 2, 0, 0], np.uint32)
+    with pytest.raises(gdb.GdbError) as e:
+        if device:
+            d_row = torch.tensor(row.view(np.int32), device="cuda")
+            d_col = torch.tensor(col.view(np.int32), device="cuda")
+            gdb.Graph(ctx, (d_row.data_ptr(), len(row)), (d_col.data_ptr(), len(col)), device=True)
+        else:
+            ctx.graph(row, col)
+    assert e.value.status == -1, str(e.value)
+    g = gg.grid(8, 8)
+    assert np.array_equal(ctx.bfs(ctx.graph(g.row_ptr, g.col), 0), oracle.bfs(g, 0))
+
+
 @pytest.mark.parametrize("name,g", GRAPHS, ids=IDS)
 def test_mst(ctx, name, g):
     uw = gg.unique_weights(g, seed=9)
