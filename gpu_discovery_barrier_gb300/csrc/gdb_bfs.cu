@@ -661,7 +661,7 @@ int gdbi::bfs_prepare(gdb_ctx* c) {
   return GDB_OK;
 }
 
-int gdbi::traversal_occupancy(gdb_ctx* c, int block) {
+int gdbi::traversal_occupancy(gdb_ctx*, int block) {
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs_xf, block, 0) != cudaSuccess) {
     cudaGetLastError();

@@ -13,7 +13,7 @@
  * Reference interfaces replaced (paths relative to the reference project):
  *   code/discovery_protocol/api/discovery.h          host discovery API
  *   code/discovery_protocol/api/discovery.cl         device protocol + XF barrier
- *   code/experiments/occupancy_tests/src/*.c         occupancy / protocol timing
+ *   code/experiments/occupancy_tests/src (C files)   occupancy / protocol timing
  *   code/experiments/pannotia/graph_app/{sssp,mis,color,bc}/   mega-kernels
  *   code/experiments/lonestar_gpu_opencl/apps/{bfs,sssp,mst}/  port kernels
  */
